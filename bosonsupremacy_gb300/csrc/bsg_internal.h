@@ -1,0 +1,127 @@
+// Internal declarations shared by the libbsg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "bsg.h"
+
+namespace bsg {
+
+// ---- error state (per host thread) ---------------------------------------
+void set_error(const char* fmt, ...);
+
+#define BSG_CHECK_ARG(cond, ...)           \
+  do {                                     \
+    if (!(cond)) {                         \
+      ::bsg::set_error(__VA_ARGS__);       \
+      return BSG_ERR_INVALID;              \
+    }                                      \
+  } while (0)
+
+#define BSG_CUDA(call)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) {                                                                  \
+      ::bsg::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return BSG_ERR_CUDA;                                                                    \
+    }                                                                                         \
+  } while (0)
+
+#define BSG_TRY(call)             \
+  do {                            \
+    int s_ = (call);              \
+    if (s_ != BSG_OK) return s_;  \
+  } while (0)
+
+// ---- partition programs ------------------------------------------------------
+// A hafnian of a matrix whose rows/columns repeat class c m_c times equals
+// prod_c m_c! * [x^m] exp(x^T A x / 2), A the k x k matrix between classes.
+// The power-series coefficients F_r (r <= m componentwise) satisfy
+//   F_r = (1 / r_a) * sum_{b >= a, r_b > 0 (r_a >= 2 if b == a)} A_ab F_{r - e_a - e_b},
+// a = the first class with r_a > 0 (classes in ascending multiplicity), F_0 = 1.
+// A "program" lists the reachable states of one multiplicity partition in
+// topological order with their transitions; every item whose target has that
+// multiplicity partition runs the same program, which makes warps uniform.
+struct ProgramSet {
+  // host mirror
+  std::vector<uint64_t> keys;          // partition key per program
+  std::vector<int32_t> k;              // classes per program
+  std::vector<int32_t> nstates;        // states per program (>= 1)
+  std::vector<int32_t> state_off;      // first state (global index) per program
+  std::vector<int32_t> mult;           // [prog * BSG_MAX_CLASSES + c] ascending multiplicities
+  std::vector<int32_t> st_trans_off;   // per global state: first transition
+  std::vector<int32_t> st_trans_cnt;   // per global state: number of transitions
+  std::vector<int32_t> st_ra;          // per global state: r_a (0 for the empty state)
+  std::vector<uint32_t> trans;         // packed (src_local << 12) | pair(a, b)
+  std::unordered_map<uint64_t, int32_t> index;
+  // device copies (valid when dev_valid)
+  int32_t* d_k = nullptr;
+  int32_t* d_nstates = nullptr;
+  int32_t* d_state_off = nullptr;
+  int32_t* d_st_trans_off = nullptr;
+  int32_t* d_st_trans_cnt = nullptr;
+  int32_t* d_st_ra = nullptr;
+  uint32_t* d_trans = nullptr;
+  size_t dev_states_cap = 0, dev_trans_cap = 0, dev_prog_cap = 0;
+  bool dev_valid = false;
+  int max_states = 1;
+  int max_k = 0;
+};
+
+// Key of a multiplicity multiset: 6 bits per multiplicity value 1..10.
+constexpr int kKeyBits = 6;
+constexpr int kKeyMaxMult = 10;
+inline uint64_t key_add_class(uint64_t key, int mult) {
+  return mult <= 0 ? key : key + (uint64_t(1) << (kKeyBits * (mult - 1)));
+}
+int key_order(uint64_t key);            // sum of multiplicities (hafnian order n)
+int key_classes(uint64_t key);          // number of classes
+
+// Returns the program index for `key` (generating it on first use), or a
+// negative status.
+int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out);
+int programs_upload(ProgramSet& ps, cudaStream_t stream);
+void programs_free(ProgramSet& ps);
+
+// pair index of classes a <= b in the packed upper triangle
+__host__ __device__ inline int pair_index(int a, int b) { return b * (b + 1) / 2 + a; }
+
+// ---- device buffer helper ---------------------------------------------------
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need);  // grows (never shrinks); contents not preserved
+  void release();
+};
+
+struct HostBuf {  // pinned host staging
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need);
+  void release();
+};
+
+}  // namespace bsg
+
+struct bsg_handle_s {
+  int device = 0;
+  int num_sms = 0;
+  bsg::ProgramSet programs;
+  // scratch reused across calls
+  bsg::DevBuf warp_scratch;   // per-warp A/F tables of the DP kernel
+  bsg::DevBuf items;          // bucketed item ids
+  bsg::DevBuf plan;           // per-call plan tables
+  bsg::DevBuf keys;           // per-row / per-item partition keys
+  bsg::DevBuf misc;           // small counters
+  bsg::DevBuf sigma_ws;       // Sigma construction workspace
+  bsg::DevBuf cut_ws;         // cut spectra workspace
+  bsg::DevBuf contract_ws;    // contraction workspace
+  bsg::HostBuf host_stage;    // pinned staging for plans
+  bsg::HostBuf host_stage2;
+};

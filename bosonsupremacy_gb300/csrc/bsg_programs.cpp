@@ -1,0 +1,165 @@
+// Host-side generation of partition programs for the repetition-aware
+// hafnian (see bsg_internal.h for the recurrence).
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+
+#include "bsg_internal.h"
+
+namespace bsg {
+
+int key_order(uint64_t key) {
+  int n = 0;
+  for (int v = 1; v <= kKeyMaxMult; ++v) n += v * int((key >> (kKeyBits * (v - 1))) & 63);
+  return n;
+}
+
+int key_classes(uint64_t key) {
+  int k = 0;
+  for (int v = 1; v <= kKeyMaxMult; ++v) k += int((key >> (kKeyBits * (v - 1))) & 63);
+  return k;
+}
+
+int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
+  auto it = ps.index.find(key);
+  if (it != ps.index.end()) {
+    *prog_out = it->second;
+    return BSG_OK;
+  }
+  if (key >> (kKeyBits * kKeyMaxMult)) {
+    set_error("partition key 0x%llx uses a multiplicity above %d", (unsigned long long)key, kKeyMaxMult);
+    return BSG_ERR_LIMIT;
+  }
+  std::vector<int> mult;
+  for (int v = 1; v <= kKeyMaxMult; ++v) {
+    int c = int((key >> (kKeyBits * (v - 1))) & 63);
+    for (int i = 0; i < c; ++i) mult.push_back(v);
+  }
+  const int k = int(mult.size());
+  if (k > BSG_MAX_CLASSES) {
+    set_error("hafnian with %d distinct indices exceeds BSG_MAX_CLASSES=%d", k, BSG_MAX_CLASSES);
+    return BSG_ERR_LIMIT;
+  }
+  // Enumerate the states reachable from the full multiset.
+  std::unordered_map<std::string, int> seen;
+  std::vector<std::string> states;
+  std::vector<std::string> stack;
+  std::string full(k, '\0');
+  for (int c = 0; c < k; ++c) full[c] = char(mult[c]);
+  stack.push_back(full);
+  while (!stack.empty()) {
+    std::string s = std::move(stack.back());
+    stack.pop_back();
+    if (seen.count(s)) continue;
+    seen.emplace(s, int(states.size()));
+    states.push_back(s);
+    if (int(states.size()) > BSG_MAX_STATES) {
+      set_error("partition with %d classes (n=%d) needs more than BSG_MAX_STATES=%d DP states", k,
+                key_order(key), BSG_MAX_STATES);
+      return BSG_ERR_LIMIT;
+    }
+    int a = 0;
+    while (a < k && s[a] == 0) ++a;
+    if (a == k) continue;
+    for (int b = a; b < k; ++b) {
+      if (s[b] == 0 || (b == a && s[a] < 2)) continue;
+      std::string t = s;
+      t[a]--;
+      t[b]--;
+      if (!seen.count(t)) stack.push_back(t);
+    }
+  }
+  // Topological order: ascending total (every transition removes two units).
+  auto total = [](const std::string& s) {
+    int t = 0;
+    for (char c : s) t += c;
+    return t;
+  };
+  std::vector<int> order(states.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return total(states[x]) < total(states[y]); });
+  std::vector<int> local(states.size());
+  for (size_t i = 0; i < order.size(); ++i) local[order[i]] = int(i);
+
+  const int prog = int(ps.keys.size());
+  const int base = int(ps.st_trans_off.size());
+  ps.keys.push_back(key);
+  ps.k.push_back(k);
+  ps.nstates.push_back(int(states.size()));
+  ps.state_off.push_back(base);
+  for (int c = 0; c < BSG_MAX_CLASSES; ++c) ps.mult.push_back(c < k ? mult[c] : 0);
+  for (size_t i = 0; i < order.size(); ++i) {
+    const std::string& s = states[order[i]];
+    ps.st_trans_off.push_back(int(ps.trans.size()));
+    int a = 0;
+    while (a < k && s[a] == 0) ++a;
+    int cnt = 0;
+    if (a < k) {
+      for (int b = a; b < k; ++b) {
+        if (s[b] == 0 || (b == a && s[a] < 2)) continue;
+        std::string t = s;
+        t[a]--;
+        t[b]--;
+        uint32_t src = uint32_t(local[seen.at(t)]);
+        ps.trans.push_back((src << 12) | uint32_t(pair_index(a, b)));
+        ++cnt;
+      }
+    }
+    ps.st_trans_cnt.push_back(cnt);
+    ps.st_ra.push_back(a < k ? int(s[a]) : 0);
+  }
+  ps.index.emplace(key, prog);
+  ps.max_states = std::max(ps.max_states, int(states.size()));
+  ps.max_k = std::max(ps.max_k, k);
+  ps.dev_valid = false;
+  *prog_out = prog;
+  return BSG_OK;
+}
+
+template <class T>
+static int upload(T*& dptr, size_t& cap, const std::vector<T>& v, cudaStream_t stream) {
+  size_t need = std::max<size_t>(v.size(), 1);
+  if (need > cap) {
+    if (dptr) cudaFree(dptr);
+    dptr = nullptr;
+    size_t c = std::max(need, cap * 2);
+    BSG_CUDA(cudaMalloc(&dptr, c * sizeof(T)));
+    cap = c;
+  }
+  if (!v.empty()) BSG_CUDA(cudaMemcpyAsync(dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+  return BSG_OK;
+}
+
+int programs_upload(ProgramSet& ps, cudaStream_t stream) {
+  if (ps.dev_valid) return BSG_OK;
+  size_t pc = ps.dev_prog_cap, pc2 = ps.dev_prog_cap, pc3 = ps.dev_prog_cap;
+  BSG_TRY(upload(ps.d_k, pc, ps.k, stream));
+  BSG_TRY(upload(ps.d_nstates, pc2, ps.nstates, stream));
+  BSG_TRY(upload(ps.d_state_off, pc3, ps.state_off, stream));
+  ps.dev_prog_cap = pc;
+  size_t sc = ps.dev_states_cap, sc2 = ps.dev_states_cap, sc3 = ps.dev_states_cap;
+  BSG_TRY(upload(ps.d_st_trans_off, sc, ps.st_trans_off, stream));
+  BSG_TRY(upload(ps.d_st_trans_cnt, sc2, ps.st_trans_cnt, stream));
+  BSG_TRY(upload(ps.d_st_ra, sc3, ps.st_ra, stream));
+  ps.dev_states_cap = sc;
+  BSG_TRY(upload(ps.d_trans, ps.dev_trans_cap, ps.trans, stream));
+  // The host vectors stay alive in `ps`; the stream must finish the copies
+  // before they are modified again -- callers synchronise after planning.
+  ps.dev_valid = true;
+  return BSG_OK;
+}
+
+void programs_free(ProgramSet& ps) {
+  cudaFree(ps.d_k);
+  cudaFree(ps.d_nstates);
+  cudaFree(ps.d_state_off);
+  cudaFree(ps.d_st_trans_off);
+  cudaFree(ps.d_st_trans_cnt);
+  cudaFree(ps.d_st_ra);
+  cudaFree(ps.d_trans);
+  ps = ProgramSet();
+}
+
+}  // namespace bsg

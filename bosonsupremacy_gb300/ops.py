@@ -1,0 +1,120 @@
+"""Device-side operators of the MPS construction (thin wrappers over libbsg).
+
+Every function takes and returns torch CUDA tensors; torch only supplies the
+device buffers and the current stream.  All arithmetic runs in libbsg's
+sm_103a kernels.
+"""
+from __future__ import annotations
+
+from typing import Optional, Sequence, Tuple
+
+import torch
+
+from . import _lib
+from ._lib import Handle, check, ptr, stream_ptr
+
+C128 = torch.complex128
+
+
+def _prec(precision) -> int:
+    if isinstance(precision, int):
+        return precision
+    return _lib.PRECISIONS[precision]
+
+
+def _dev(x, dtype, device):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.as_tensor(x, dtype=dtype, device=device).contiguous()
+
+
+def hafnian_batched(Sigma, targets, denominator=None, precision="fp64", device: int = 0) -> torch.Tensor:
+    """out[b] = haf(Sigma[t_b][:, t_b]) / denominator[b]  (the A_elem seam,
+    MPS_cpu.py:334-355).  Sigma [n_len, n_len] complex, targets [B, n] int."""
+    dev = torch.device("cuda", device)
+    Sig = _dev(Sigma, C128, dev)
+    tgt = _dev(targets, torch.int32, dev)
+    if tgt.dim() != 2:
+        raise ValueError("targets must be [B, n]")
+    B, n = tgt.shape
+    den = None if denominator is None else _dev(denominator, torch.float64, dev)
+    out = torch.empty(B, dtype=C128, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_hafnian_batched(h.h, ptr(Sig), Sig.shape[0], ptr(tgt) if B * n else None, n, B, ptr(den),
+                                          _prec(precision), ptr(out), stream_ptr()), "bsg_hafnian_batched")
+    return out
+
+
+def hafnian(A, precision="fp64", device: int = 0) -> torch.Tensor:
+    """Hafnians of a batch [B, n, n] of symmetric matrices (MPS_cpu.py:117-140)."""
+    dev = torch.device("cuda", device)
+    At = _dev(A, C128, dev)
+    B, n, _ = At.shape
+    out = torch.empty(B, dtype=C128, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_hafnian_matrices(h.h, ptr(At), n, B, _prec(precision), ptr(out), stream_ptr()),
+          "bsg_hafnian_matrices")
+    return out
+
+
+def site_sigma(S_l, S_r, device: int = 0) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Sigma and Z of a middle or last site from the Williamson symplectics of
+    cuts site (S_l, empty for the last site) and site-1 (S_r)."""
+    dev = torch.device("cuda", device)
+    Sr = _dev(S_r, torch.float64, dev)
+    Mr = Sr.shape[0] // 2
+    Sl = None
+    ml = 0
+    if S_l is not None and (S_l.numel() if isinstance(S_l, torch.Tensor) else len(S_l)) > 0:
+        Sl = _dev(S_l, torch.float64, dev)
+        ml = Sl.shape[0] // 2
+    Sigma = torch.empty(2 * Mr, 2 * Mr, dtype=C128, device=dev)
+    Z = torch.empty(1, dtype=torch.float64, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_site_sigma(h.h, ptr(Sl), ml, ptr(Sr), Mr, ptr(Sigma), ptr(Z), stream_ptr()),
+          "bsg_site_sigma")
+    return Sigma, Z
+
+
+def first_sigma(S_0, sq_cov, device: int = 0) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Sigma (output block) and Z of site 0 from cut 0's symplectic and the pure covariance."""
+    dev = torch.device("cuda", device)
+    sq = _dev(sq_cov, torch.float64, dev)
+    M = sq.shape[0] // 2
+    S0 = _dev(S_0, torch.float64, dev) if M > 1 else None
+    Sigma = torch.empty(2 * M, 2 * M, dtype=C128, device=dev)
+    Z = torch.empty(1, dtype=torch.float64, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_first_sigma(h.h, ptr(S0), M, ptr(sq), ptr(Sigma), ptr(Z), stream_ptr()),
+          "bsg_first_sigma")
+    return Sigma, Z
+
+
+def build_site(kind: int, Sigma, num_l, lambda_l, num_r, Z, d: int, chi: int, precision="fp64",
+               out_dtype=torch.complex64, device: int = 0, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Gamma [chi, chi, d] of one site (MPS_cpu.py:402-520).  ``num_l`` are the
+    kept labels of cut ``site`` (rows with res > err_tol), ``num_r`` all labels
+    of cut ``site-1``; ``lambda_l`` = sqrt(res) of the kept rows."""
+    dev = torch.device("cuda", device)
+    Sig = _dev(Sigma, C128, dev)
+    Mr = Sig.shape[0] // 2
+    if kind != _lib.SITE_LAST:
+        nl = _dev(num_l, torch.int8, dev).reshape(len(num_l), -1).contiguous()
+        kl, ml = nl.shape
+        lam = _dev(lambda_l, torch.float64, dev)
+    else:
+        nl, kl, ml, lam = None, 0, 0, None
+    if kind != _lib.SITE_FIRST:
+        nr = _dev(num_r, torch.int8, dev).reshape(len(num_r), -1).contiguous()
+        kr, mr = nr.shape
+    else:
+        nr, kr, mr = None, 0, 0
+    Zt = _dev(Z, torch.float64, dev).reshape(-1)
+    if out is None:
+        out = torch.empty(chi, chi, d, dtype=out_dtype, device=dev)
+    odt = _lib.OUT_C128 if out.dtype == torch.complex128 else _lib.OUT_C64
+    h = Handle.get(device)
+    check(_lib.load().bsg_build_site(h.h, kind, ptr(Sig), Mr, ptr(nl) if kl * ml else None, kl, ml, ptr(lam),
+                                     ptr(nr) if kr * mr else None, kr, mr, ptr(Zt), d, chi, _prec(precision), odt,
+                                     ptr(out), stream_ptr()), "bsg_build_site")
+    return out

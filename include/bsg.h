@@ -1,0 +1,161 @@
+/*
+ * bsg.h -- C ABI of libbsg.so, the GB300 (sm_103a) MPS-construction path for
+ * lossy Gaussian boson sampling.  Drop-in for the per-cut truncation
+ * (kron_cpu.py) and the per-site Gamma/Lambda build (MPS_cpu.py) of
+ * sss441803/BosonSupremacy, plus the transfer contraction that consumes
+ * Gamma/Lambda (sampling_cpu.py:75-90).
+ *
+ * Conventions
+ *  - Every entry point returns 0 on success and a negative BSG_ERR_* code on
+ *    failure; bsg_last_error() returns a message for the calling thread.
+ *  - Pointers are DEVICE pointers unless the parameter name ends in _host.
+ *    The caller owns every buffer it passes; the library never frees them.
+ *  - Complex numbers are interleaved (re, im) pairs: "c128" = 2 doubles,
+ *    "c64" = 2 floats.  Matrices are row-major (C order), as numpy saves them.
+ *  - Work space (plans, partition programs, per-warp scratch) lives in the
+ *    handle.  One handle per stream; a handle is not re-entrant.
+ *  - Every kernel is launched on the given stream.  Entry points that must
+ *    plan on the host (they read small arrays back) synchronise that stream;
+ *    this is stated per function.
+ *  - Spin-free: no kernel waits on a flag written by another block.
+ */
+#ifndef BSG_H_
+#define BSG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct bsg_handle_s* bsg_handle_t;
+typedef struct CUstream_st* bsg_stream_t; /* == cudaStream_t */
+
+/* status codes */
+#define BSG_OK 0
+#define BSG_ERR_INVALID (-1)     /* bad argument (shape, pointer, range)      */
+#define BSG_ERR_CUDA (-2)        /* a CUDA runtime call failed                 */
+#define BSG_ERR_NOT_PD (-3)      /* covariance not symmetric positive definite */
+#define BSG_ERR_NO_CONVERGE (-4) /* an iterative factorisation hit its limit   */
+#define BSG_ERR_LIMIT (-5)       /* a size exceeds a documented maximum        */
+#define BSG_ERR_ALLOC (-6)       /* device or host allocation failed           */
+
+/* arithmetic of the hafnian evaluation */
+#define BSG_PREC_FP64 0  /* complex128 throughout (plain FP64 path)                      */
+#define BSG_PREC_SPLIT 1 /* split: FP32 products with exact error terms, sums kept as    */
+                         /* FP32 pairs (~48-bit significand) -- FP32 pipe, FP64-class     */
+#define BSG_PREC_FP32 2  /* complex64 throughout (the reference's own working precision)  */
+
+/* site kinds (MPS_cpu.py:402, 430, 461) */
+#define BSG_SITE_FIRST 0
+#define BSG_SITE_MIDDLE 1
+#define BSG_SITE_LAST 2
+
+/* output element type of Gamma */
+#define BSG_OUT_C64 0  /* complex64, the reference's Gamma_i.npy dtype (MPS_cpu.py:397) */
+#define BSG_OUT_C128 1 /* complex128 (FP64-promoted layout)                             */
+
+/* documented limits */
+#define BSG_MAX_CLASSES 24     /* distinct Sigma indices in one hafnian            */
+#define BSG_MAX_ORDER 63       /* hafnian order n                                   */
+#define BSG_MAX_STATES 16384   /* states of one partition program                   */
+#define BSG_MAX_LABEL_NNZ 32   /* non-zero Fock entries in one Schmidt label row    */
+
+/* ---- handle ------------------------------------------------------------ */
+/* No reference counterpart (the reference keeps module-level CuPy state,
+ * MPS_utils.py:13-19). */
+int bsg_create(int device, bsg_handle_t* out);
+int bsg_destroy(bsg_handle_t h);
+const char* bsg_last_error(void);
+int bsg_version(void);
+
+/* ---- batched hafnian / A_elem seam -------------------------------------
+ * Replaces A_elem + Sigma_select + hafnian (MPS_cpu.py:19-37, 117-187,
+ * 334-355; GPU twin MPS_utils.py:21-47, 127-197, 273-297;
+ * direct_mps_kernels.cu:3-39).
+ *   out[b] = haf(Sigma[t_b][:, t_b]) / denominator[b]
+ * Sigma: c128 [n_len, n_len] symmetric; targets: int32 [B, n] (indices may
+ * repeat, as the reference's targets do); denominator: float64 [B] or NULL
+ * (= 1); out: c128 [B].  Odd n gives 0, n = 0 gives 1/denominator.
+ * Synchronises `stream` (plans the partition programs on the host). */
+int bsg_hafnian_batched(bsg_handle_t h, const double* Sigma, int n_len, const int32_t* targets, int n,
+                        int64_t B, const double* denominator, int precision, double* out,
+                        bsg_stream_t stream);
+
+/* Same, taking explicit matrices: A c128 [B, n, n] (the reference's
+ * hafnian(A) input, MPS_cpu.py:117).  Synchronises `stream`. */
+int bsg_hafnian_matrices(bsg_handle_t h, const double* A, int n, int64_t B, int precision, double* out,
+                         bsg_stream_t stream);
+
+/* ---- Sigma of a site ------------------------------------------------------
+ * Replaces get_U2_sq_U1 + blochmessiah + get_Sigma (MPS_cpu.py:189-229,
+ * 305-312, 357-372).  With S = (1 (+) S_l)^{-1} S_r (xxpp, 2M_r x 2M_r) and
+ * its complex form [[A, B], [conj B, conj A]], Sigma = [[B X, X^T], [X, -X conj B]]
+ * with X = conj(A)^{-1}, and Z = sqrt|det A| -- the same matrix the
+ * reference reaches through Bloch-Messiah, without the SVDs.
+ * S_l: float64 [2 m_l, 2 m_l] with m_l = M_r - 1 (ignored when m_l == 0, the
+ * last site); S_r: float64 [2 M_r, 2 M_r]; Sigma: c128 [2 M_r, 2 M_r];
+ * Z: float64 [1].  Asynchronous. */
+int bsg_site_sigma(bsg_handle_t h, const double* S_l, int m_l, const double* S_r, int M_r, double* Sigma,
+                   double* Z, bsg_stream_t stream);
+
+/* Site 0 from the pure covariance itself (MPS_cpu.py:395, 409-414): the
+ * output-output block of Sigma for V' = (1 (+) S_0^{-1}) sq_cov (1 (+) S_0^{-1})^T,
+ * Sigma11 = Mc (conj(Nc) + I)^{-1} with [[Nc, Mc], ...] = R V' R^dag, and
+ * Z = det((Nc + I)/2)^{1/4}.  Only Sigma[:M, :M] is written (the other blocks
+ * are zero): site 0 has no input labels.  Asynchronous. */
+int bsg_first_sigma(bsg_handle_t h, const double* S_0, int M, const double* sq_cov, double* Sigma, double* Z,
+                    bsg_stream_t stream);
+
+/* ---- Gamma of a site -------------------------------------------------------
+ * Replaces the site loop body of MPS_cpu.py:402-520 (GPU twin
+ * distributed_MPS.py:88-258):
+ *   Gamma[a, b, j] = haf(Sigma[T(j, b, a)]) / (sqrt(j!) sqrt(prod num_l[b]!)
+ *                     sqrt(prod num_r[a]!)) / Z / lambda_l[b]
+ * with T = j copies of index 0, mode q of label num_l[b] at index 1 + q, mode
+ * q of label num_r[a] at index M_r + q.  Every (a, b, j) of the bond grid is
+ * one work item of one persistent launch; items are bucketed by the
+ * multiplicity partition of T so that a warp runs one program.
+ *   kind FIRST : num_r ignored (one empty right label), Gamma[0, b, j]
+ *   kind MIDDLE: Gamma[a, b, j]
+ *   kind LAST  : num_l ignored (one empty left label), lambda_l ignored, Gamma[a, 0, j]
+ * num_l: int8 [k_l, m_l] (cut `site`, rows with res > err_tol only);
+ * num_r: int8 [k_r, m_r] (cut `site-1`, all rows); lambda_l: float64 [k_l];
+ * Z: float64 [1] (device); Gamma: [chi, chi, d] of out_dtype, fully written
+ * (zeros outside the computed grid).  Synchronises `stream` once (reads the
+ * label partition keys back to plan). */
+int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int M_r, const int8_t* num_l, int k_l, int m_l,
+                   const double* lambda_l, const int8_t* num_r, int k_r, int m_r, const double* Z, int d, int chi,
+                   int precision, int out_dtype, void* Gamma, bsg_stream_t stream);
+
+/* ---- per-cut spectra (truncation to chi) ---------------------------------
+ * Replaces williamson + get_cumsum_kron (kron_cpu.py:46-127; CuPy twin
+ * distributed_kron.py:105-137) for cuts L = L0 .. L0+n_cuts-1 at once.
+ * For each cut: symplectic eigenvalues nu and a Williamson symplectic S of
+ * the sub-covariance of modes L..M-1 (FP64 Cholesky + Jacobi), thermal
+ * occupations nbar = max(0, (nu-1)/2), then the chi largest products of
+ * the per-mode geometric distributions truncated at d photons with weights
+ * > err_tol, in descending order, with their Fock labels.
+ * sq_cov: float64 [2M, 2M]; res: float64 [n_cuts, chi] (zero padded);
+ * num: int8 [n_cuts, chi, M-1] (cut c uses the first M-1-L columns);
+ * S: float64 [n_cuts, 2(M-1), 2(M-1)] (cut c uses the leading 2(M-L) block);
+ * kept: int32 [n_cuts].  Asynchronous. */
+int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
+                    double* res, int8_t* num, double* S, int32_t* kept, bsg_stream_t stream);
+
+/* ---- transfer contraction (pattern amplitudes) ---------------------------
+ * The bond contraction that consumes Gamma/Lambda (sampling_cpu.py:75-90):
+ * amp[p] = (... ((Gamma_0[0, :, n_0] * Lambda_0) @ Gamma_1[:, :, n_1]) * Lambda_1 ...) @ Gamma_{M-1}[:, 0, n_{M-1}]
+ * for P photon patterns (int32 [P, M]).  Gammas: array (device) of M device
+ * pointers to c64 [chi, chi, d]; Lambdas: float64 [M-1, chi]; amp: c128 [P].
+ * precision: BSG_PREC_FP64 (FP64 CUDA cores) or BSG_PREC_SPLIT (3-way split
+ * TF32 products on the tcgen05 tensor cores, FP32 accumulation).
+ * Synchronises `stream` (plans the shared-prefix tree on the host). */
+int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
+                           const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BSG_H_ */

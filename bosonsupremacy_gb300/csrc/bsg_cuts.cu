@@ -1,0 +1,594 @@
+// Per-cut Schmidt spectra: Williamson decomposition of the right block of each
+// cut and the top-chi product-thermal weights with their Fock labels.
+//
+// Reference: williamson + get_cumsum_kron (kron_cpu.py:46-127; the CuPy twin
+// distributed_kron.py:105-137).  All cuts of one call run in one launch, one
+// CTA per cut.
+//
+// Williamson (FP64):  V = L L^T (Cholesky);  G = L^{-1} Omega L^{-T} is
+// antisymmetric with eigenvalues +-i/nu;  H = G^T G has eigenvalues 1/nu^2
+// (each twice).  Cyclic Jacobi (round-robin parallel order, one 2x2 block per
+// thread) diagonalises H; eigenvectors x are paired with y = G x/|G x| by
+// Gram-Schmidt so that y^T G x = 1/nu.  Then S = L [y_i | x_i] nu_i^{-1/2}
+// satisfies V = S diag(nu, nu) S^T and S Omega S^T = Omega -- a Williamson
+// symplectic like the reference's (it differs from scipy's Schur-based one by
+// a symplectic-orthogonal gauge per mode, which no physical output sees).
+// Modes are ordered by nu descending.
+//
+// Truncation: the reference keeps the 1e5 largest products per step and the
+// chi largest at the end.  Every factor is <= 1, so a product outside the top
+// chi at some step has >= chi products above it whose best extensions
+// dominate all of its extensions: keeping the top chi per step gives the same
+// final set (up to exact ties).  Candidates res[i] * t[n] form a matrix sorted
+// along both axes; each candidate's rank is found with d binary searches, so
+// the top chi come out already sorted (ties broken by the flattened index
+// i*d + n, the outer-product order of the reference).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bsg_internal.h"
+
+namespace bsg {
+
+constexpr int kMaxCutModes = 256;  // modes in one cut's right block
+
+struct CutArgs {
+  const double* sq_cov;
+  int M, L0, n_cuts, d, chi;
+  double err_tol;
+  double* ws;          // per cut: 4 * nmax^2 doubles
+  size_t ws_stride;    // doubles per cut
+  double* S;           // [n_cuts, 2(M-1), 2(M-1)]
+  int ldS;
+  double* nbar;        // [n_cuts, kmax]
+  int kmax;
+  double* res;         // [n_cuts, chi]
+  int8_t* num;         // [n_cuts, chi, M-1]
+  int32_t* kept;       // [n_cuts]
+  uint32_t* rec;       // per cut: kmax * chi records (parent << 8 | digit)
+  int* status;         // [n_cuts]
+  int max_sweeps;
+};
+
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) s += red[i];
+    red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+__global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
+  const int c = blockIdx.x;
+  const int L = a.L0 + c, M = a.M;
+  const int k = M - L, n = 2 * k;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double* A = a.ws + (size_t)c * a.ws_stride;  // V -> L (lower)
+  const size_t nn = (size_t)n * n;
+  double* W = A + nn;    // L^{-1}, later Q^T (rows = eigenvectors)
+  double* Gm = W + nn;   // G
+  double* H = Gm + nn;   // H, later accepted vectors (rows)
+  extern __shared__ double sm[];
+  double* red = sm;                   // 33
+  double* cs = red + 40;              // n/2
+  double* sn = cs + kMaxCutModes;     // n/2
+  int* pos = reinterpret_cast<int*>(sn + kMaxCutModes);  // n
+  int* order = pos + 2 * kMaxCutModes;                   // n
+  double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n
+  double* vec = dots + 2 * kMaxCutModes;                               // n
+  double* vec2 = vec + 2 * kMaxCutModes;                               // n
+  __shared__ int s_flag;
+  __shared__ double s_scalar;
+
+  auto gidx = [&](int i) { return i < k ? L + i : M + L + (i - k); };
+  // 1. V and the symmetry check of the reference (norm(V - V^T) < 1e-11)
+  double asym = 0.0;
+  for (size_t i = tid; i < nn; i += nt) {
+    int r = int(i / n), q = int(i % n);
+    double v = a.sq_cov[(size_t)gidx(r) * (2 * M) + gidx(q)];
+    double vt = a.sq_cov[(size_t)gidx(q) * (2 * M) + gidx(r)];
+    A[i] = v;
+    asym += (v - vt) * (v - vt);
+  }
+  asym = block_sum(asym, red);
+  if (asym >= 1e-22) {
+    if (tid == 0) a.status[c] = 1;
+    return;
+  }
+  // 2. Cholesky, right-looking, in place (lower triangle)
+  if (tid == 0) s_flag = 0;
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (tid == 0) {
+      double djj = A[(size_t)j * n + j];
+      if (!(djj > 0.0)) s_flag = 1;
+      s_scalar = djj > 0.0 ? sqrt(djj) : 1.0;
+      A[(size_t)j * n + j] = s_scalar;
+    }
+    __syncthreads();
+    if (s_flag) break;
+    const double dj = s_scalar;
+    for (int i = j + 1 + tid; i < n; i += nt) A[(size_t)i * n + j] /= dj;
+    __syncthreads();
+    const int m = n - j - 1;
+    for (size_t t = tid; t < (size_t)m * m; t += nt) {
+      int i = j + 1 + int(t / m), l = j + 1 + int(t % m);
+      if (l > i) continue;
+      A[(size_t)i * n + l] -= A[(size_t)i * n + j] * A[(size_t)l * n + j];
+    }
+    __syncthreads();
+  }
+  if (s_flag) {
+    if (tid == 0) a.status[c] = 2;
+    return;
+  }
+  for (size_t i = tid; i < nn; i += nt) {
+    int r = int(i / n), q = int(i % n);
+    if (q > r) A[i] = 0.0;
+  }
+  // 3. W = L^{-1}: forward substitution on all columns, row by row
+  for (size_t i = tid; i < nn; i += nt) W[i] = (i / n == i % n) ? 1.0 : 0.0;
+  __syncthreads();
+  for (int r = 0; r < n; ++r) {
+    const double inv = 1.0 / A[(size_t)r * n + r];
+    for (int q = tid; q <= r; q += nt) W[(size_t)r * n + q] *= inv;
+    __syncthreads();
+    const int m = n - r - 1;
+    for (size_t t = tid; t < (size_t)m * (r + 1); t += nt) {
+      int i = r + 1 + int(t / (r + 1)), q = int(t % (r + 1));
+      W[(size_t)i * n + q] -= A[(size_t)i * n + r] * W[(size_t)r * n + q];
+    }
+    __syncthreads();
+  }
+  // 4. G = W Omega W^T: G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r]
+  for (size_t t = tid; t < nn; t += nt) {
+    int i = int(t / n), j = int(t % n);
+    double s = 0.0;
+    for (int r = 0; r < k; ++r) s += W[(size_t)i * n + r] * W[(size_t)j * n + r + k] - W[(size_t)i * n + r + k] * W[(size_t)j * n + r];
+    Gm[t] = s;
+  }
+  __syncthreads();
+  // 5. H = G^T G, Q^T = I
+  for (size_t t = tid; t < nn; t += nt) {
+    int i = int(t / n), j = int(t % n);
+    double s = 0.0;
+    for (int r = 0; r < n; ++r) s += Gm[(size_t)r * n + i] * Gm[(size_t)r * n + j];
+    H[t] = s;
+  }
+  __syncthreads();
+  for (size_t t = tid; t < nn; t += nt) W[t] = (t / n == t % n) ? 1.0 : 0.0;
+  __syncthreads();
+  // 6. cyclic Jacobi, round-robin pairs, two-sided update per 2x2 block
+  const int P = n / 2;
+  int sweep = 0;
+  bool converged = false;
+  for (; sweep < a.max_sweeps; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (size_t t = tid; t < nn; t += nt) {
+      int i = int(t / n), j = int(t % n);
+      double h = H[t];
+      if (i < j) off += h * h;
+      else if (i == j) dia += h * h;
+    }
+    off = block_sum(off, red);
+    dia = block_sum(dia, red);
+    if (off <= 1e-26 * dia) {
+      converged = true;
+      break;
+    }
+    for (int step = 0; step < n - 1; ++step) {
+      for (int i = tid; i < n; i += nt) pos[i] = i == 0 ? 0 : ((i - 1 + step) % (n - 1)) + 1;
+      __syncthreads();
+      for (int m = tid; m < P; m += nt) {
+        int p = pos[m], q = pos[n - 1 - m];
+        if (p > q) {
+          int tmp = p;
+          p = q;
+          q = tmp;
+        }
+        double hpq = H[(size_t)p * n + q];
+        double c_ = 1.0, s_ = 0.0;
+        if (fabs(hpq) > 1e-300 && fabs(hpq) > 1e-17 * sqrt(fabs(H[(size_t)p * n + p] * H[(size_t)q * n + q]))) {
+          double th = (H[(size_t)q * n + q] - H[(size_t)p * n + p]) / (2.0 * hpq);
+          double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+          c_ = 1.0 / sqrt(tt * tt + 1.0);
+          s_ = tt * c_;
+        }
+        cs[m] = c_;
+        sn[m] = s_;
+      }
+      __syncthreads();
+      for (int t = tid; t < P * P; t += nt) {
+        int m1 = t / P, m2 = t % P;
+        if (m1 > m2) continue;
+        int p1 = pos[m1], q1 = pos[n - 1 - m1], p2 = pos[m2], q2 = pos[n - 1 - m2];
+        if (p1 > q1) { int x = p1; p1 = q1; q1 = x; }
+        if (p2 > q2) { int x = p2; p2 = q2; q2 = x; }
+        double c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
+        double b00 = H[(size_t)p1 * n + p2], b01 = H[(size_t)p1 * n + q2];
+        double b10 = H[(size_t)q1 * n + p2], b11 = H[(size_t)q1 * n + q2];
+        // J1^T B
+        double r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
+        double r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
+        // (J1^T B) J2
+        double o00 = c2 * r00 - s2 * r01, o01 = s2 * r00 + c2 * r01;
+        double o10 = c2 * r10 - s2 * r11, o11 = s2 * r10 + c2 * r11;
+        if (m1 == m2) {
+          o01 = 0.0;
+          o10 = 0.0;
+        }
+        H[(size_t)p1 * n + p2] = o00;
+        H[(size_t)p1 * n + q2] = o01;
+        H[(size_t)q1 * n + p2] = o10;
+        H[(size_t)q1 * n + q2] = o11;
+        if (m1 != m2) {
+          H[(size_t)p2 * n + p1] = o00;
+          H[(size_t)q2 * n + p1] = o01;
+          H[(size_t)p2 * n + q1] = o10;
+          H[(size_t)q2 * n + q1] = o11;
+        }
+      }
+      // Q^T <- J^T Q^T (rows p, q)
+      for (int t = tid; t < P * n; t += nt) {
+        int m = t / n, j = t % n;
+        int p = pos[m], q = pos[n - 1 - m];
+        if (p > q) { int x = p; p = q; q = x; }
+        double c_ = cs[m], s_ = sn[m];
+        double hp = W[(size_t)p * n + j], hq = W[(size_t)q * n + j];
+        W[(size_t)p * n + j] = c_ * hp - s_ * hq;
+        W[(size_t)q * n + j] = s_ * hp + c_ * hq;
+      }
+      __syncthreads();
+    }
+  }
+  if (!converged) {
+    if (tid == 0) a.status[c] = 3;
+    return;
+  }
+  // 7. eigenvalues mu_i = H_ii; order ascending (nu descending), ties by index
+  for (int i = tid; i < n; i += nt) {
+    double mi = H[(size_t)i * n + i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      double mj = H[(size_t)j * n + j];
+      r += (mj < mi) || (mj == mi && j < i);
+    }
+    order[r] = i;
+  }
+  __syncthreads();
+  // 8. pair eigenvectors x with y = G x / |G x|.  Candidates are grouped in
+  // even-sized clusters of (nearly) equal mu; inside a cluster the next x is
+  // the candidate with the largest residual after projecting out the pairs
+  // already taken (pivoted Gram-Schmidt), so a degenerate eigenspace of any
+  // dimension (e.g. the nu = 1 vacuum modes) is always completed.
+  double* Xacc = H;  // accepted vectors as rows (H's diagonal was read above)
+  for (int i = tid; i < n; i += nt) vec2[i] = H[(size_t)order[i] * n + order[i]];
+  __syncthreads();
+  int* used = reinterpret_cast<int*>(vec);  // n flags (vec reused as int storage)
+  for (int i = tid; i < n; i += nt) used[i] = 0;
+  __syncthreads();
+  int acc = 0;
+  int cb = 0;
+  while (cb < n) {
+    int ce = cb + 2;
+    while (ce < n && !(vec2[ce] - vec2[ce - 1] > 1e-9 * fmax(fabs(vec2[ce]), 1e-300))) ce += 2;
+    if (ce > n) ce = n;
+    const int acc0 = acc;
+    for (int pi = 0; pi < (ce - cb) / 2; ++pi) {
+      // residual norms of the unused candidates of the cluster
+      for (int r = cb + (tid >> 5); r < ce; r += nt >> 5) {
+        const double* w = W + (size_t)order[r] * n;
+        double s = 0.0;
+        for (int i = tid & 31; i < n; i += 32) s += w[i] * w[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) dots[r] = used[r] ? -1.0 : s;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int best = -1;
+        double bv = -1.0;
+        for (int r = cb; r < ce; ++r)
+          if (dots[r] > bv) {
+            bv = dots[r];
+            best = r;
+          }
+        s_flag = best;
+        s_scalar = bv;
+        if (best >= 0) used[best] = 1;
+      }
+      __syncthreads();
+      const int best = s_flag;
+      const double bn = s_scalar;
+      if (best < 0 || !(bn > 0.0)) {
+        if (tid == 0) a.status[c] = 4;
+        return;
+      }
+      const double inv = 1.0 / sqrt(bn);
+      double* x = Xacc + (size_t)acc * n;
+      double* y = Xacc + (size_t)(acc + 1) * n;
+      for (int i = tid; i < n; i += nt) x[i] = W[(size_t)order[best] * n + i] * inv;
+      __syncthreads();
+      for (int i = tid; i < n; i += nt) {
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) s += Gm[(size_t)i * n + j] * x[j];
+        y[i] = s;
+      }
+      __syncthreads();
+      // y against x and the cluster's earlier pairs
+      for (int t = tid; t < (acc + 1 - acc0) * 32; t += nt) {
+        const int av = acc0 + (t >> 5);
+        double s = 0.0;
+        for (int i = t & 31; i < n; i += 32) s += Xacc[(size_t)av * n + i] * y[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((t & 31) == 0) dots[av - acc0] = s;
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += nt) {
+        double s = y[i];
+        for (int av = acc0; av <= acc; ++av) s -= dots[av - acc0] * Xacc[(size_t)av * n + i];
+        y[i] = s;
+      }
+      __syncthreads();
+      double ny = 0.0;
+      for (int i = tid; i < n; i += nt) ny += y[i] * y[i];
+      ny = block_sum(ny, red);
+      const double iy = ny > 0.0 ? 1.0 / sqrt(ny) : 0.0;
+      for (int i = tid; i < n; i += nt) y[i] *= iy;
+      __syncthreads();
+      // project x and y out of the remaining candidates of the cluster
+      for (int r = cb + (tid >> 5); r < ce; r += nt >> 5) {
+        if (used[r]) continue;
+        double* w = W + (size_t)order[r] * n;
+        double sx = 0.0, sy = 0.0;
+        for (int i = tid & 31; i < n; i += 32) {
+          sx += x[i] * w[i];
+          sy += y[i] * w[i];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, o);
+          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        }
+        for (int i = tid & 31; i < n; i += 32) w[i] -= sx * x[i] + sy * y[i];
+      }
+      __syncthreads();
+      acc += 2;
+    }
+    cb = ce;
+  }
+  if (acc != n) {
+    if (tid == 0) a.status[c] = 4;
+    return;
+  }
+  // 9. nu from y^T G x (Rayleigh quotient; equals 1/nu), S = L [y | x] nu^{-1/2}
+  for (int pi = 0; pi < k; ++pi) {
+    const double* x = Xacc + (size_t)(2 * pi) * n;
+    const double* y = Xacc + (size_t)(2 * pi + 1) * n;
+    double s = 0.0;
+    for (int i = tid; i < n; i += nt) {
+      double gx = 0.0;
+      for (int j = 0; j < n; ++j) gx += Gm[(size_t)i * n + j] * x[j];
+      s += y[i] * gx;
+    }
+    s = block_sum(s, red);  // = 1/nu
+    const double nu = 1.0 / s;
+    const double sc = sqrt(s);  // nu^{-1/2}
+    for (int i = tid; i < n; i += nt) {
+      double ly = 0.0, lx = 0.0;
+      for (int j = 0; j <= i; ++j) {
+        double l = A[(size_t)i * n + j];
+        ly += l * y[j];
+        lx += l * x[j];
+      }
+      a.S[(size_t)c * a.ldS * a.ldS + (size_t)i * a.ldS + pi] = ly * sc;
+      a.S[(size_t)c * a.ldS * a.ldS + (size_t)i * a.ldS + pi + k] = lx * sc;
+    }
+    if (tid == 0) {
+      double nb = (nu - 1.0) / 2.0;
+      a.nbar[(size_t)c * a.kmax + pi] = nb > 0.0 ? nb : 0.0;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) a.status[c] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Top-chi product-thermal weights (one CTA per cut).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+
+__global__ void __launch_bounds__(1024) thermal_kernel(CutArgs a) {
+  const int c = blockIdx.x;
+  if (a.status[c] != 0) return;
+  const int L = a.L0 + c, k = a.M - L, d = a.d, chi = a.chi;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  extern __shared__ unsigned long long smu[];
+  unsigned long long* prod = smu;                     // [d][chi] bit patterns
+  double* cur = reinterpret_cast<double*>(prod + (size_t)d * chi);  // [chi]
+  double* nxt = cur + chi;                             // [chi]
+  double* t = nxt + chi;                               // [d]
+  __shared__ int s_K, s_valid;
+  uint32_t* rec = a.rec + (size_t)c * a.kmax * chi;
+  const double* nb = a.nbar + (size_t)c * a.kmax;
+  // step 0: the first mode, unfiltered (kron_cpu.py:106)
+  for (int n = tid; n < d; n += nt) {
+    double x = nb[0];
+    cur[n] = 1.0 / (x + 1.0) * pow(x / (x + 1.0), (double)n);
+    rec[n] = (uint32_t)n;
+  }
+  if (tid == 0) s_K = d;
+  __syncthreads();
+  for (int s = 1; s < k; ++s) {
+    const int K = s_K;
+    for (int n = tid; n < d; n += nt) {
+      double x = nb[s];
+      t[n] = 1.0 / (x + 1.0) * pow(x / (x + 1.0), (double)n);
+    }
+    __syncthreads();
+    for (int u = tid; u < d * K; u += nt) {
+      int n = u / K, i = u % K;
+      prod[(size_t)n * chi + i] = dbits(cur[i] * t[n]);
+    }
+    if (tid == 0) s_valid = 0;
+    __syncthreads();
+    // number of valid (> err_tol) candidates
+    const unsigned long long tol = dbits(a.err_tol);
+    for (int n = tid; n < d; n += nt) {
+      const unsigned long long* col = prod + (size_t)n * chi;
+      int lo = 0, hi = K;  // first index with prod <= tol
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (col[mid] > tol) lo = mid + 1;
+        else hi = mid;
+      }
+      atomicAdd(&s_valid, lo);
+    }
+    __syncthreads();
+    const int Kn = min(chi, s_valid);
+    uint32_t* rs = rec + (size_t)s * chi;
+    for (int u = tid; u < d * K; u += nt) {
+      const int n = u / K, i = u % K;
+      const unsigned long long v = prod[(size_t)n * chi + i];
+      if (v <= tol) continue;
+      int rank = 0;
+      for (int n2 = 0; n2 < d && rank < Kn; ++n2) {
+        const unsigned long long* col = prod + (size_t)n2 * chi;
+        int lo = 0, hi = K;  // count of > v
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (col[mid] > v) lo = mid + 1;
+          else hi = mid;
+        }
+        int gt = lo;
+        hi = K;  // count of >= v
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (col[mid] >= v) lo = mid + 1;
+          else hi = mid;
+        }
+        int ge = lo;
+        int lim = i + (n2 < n ? 1 : 0);
+        int ties = min(ge, lim) - gt;
+        rank += gt + (ties > 0 ? ties : 0);
+      }
+      if (rank < Kn) {
+        nxt[rank] = __longlong_as_double((long long)v);
+        rs[rank] = ((uint32_t)i << 8) | (uint32_t)n;
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < Kn; i += nt) cur[i] = nxt[i];
+    if (tid == 0) s_K = Kn;
+    __syncthreads();
+  }
+  const int K = s_K;
+  const int Kout = min(chi, K);
+  // single-mode cuts keep the thermal row as is (already descending)
+  for (int r = tid; r < Kout; r += nt) {
+    a.res[(size_t)c * chi + r] = cur[r];
+    int p = r;
+    int8_t* row = a.num + ((size_t)c * chi + r) * (a.M - 1);
+    for (int s = k - 1; s >= 1; --s) {
+      uint32_t w = rec[(size_t)s * chi + p];
+      row[s] = (int8_t)(w & 0xff);
+      p = (int)(w >> 8);
+    }
+    row[0] = (int8_t)(rec[p] & 0xff);
+  }
+  if (tid == 0) a.kept[c] = Kout;
+}
+
+}  // namespace bsg
+
+using namespace bsg;
+
+extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
+                               double err_tol, double* res, int8_t* num, double* S, int32_t* kept,
+                               bsg_stream_t stream) {
+  BSG_CHECK_ARG(h, "bsg_cut_spectra: null handle");
+  BSG_CHECK_ARG(sq_cov && res && num && S && kept, "bsg_cut_spectra: null pointer");
+  BSG_CHECK_ARG(M >= 2 && L0 >= 1 && n_cuts >= 1 && L0 + n_cuts <= M, "bsg_cut_spectra: cuts [%d, %d) outside [1, M=%d)",
+                L0, L0 + n_cuts, M);
+  BSG_CHECK_ARG(M - L0 <= kMaxCutModes, "bsg_cut_spectra: %d modes in a cut exceeds %d", M - L0, kMaxCutModes);
+  BSG_CHECK_ARG(d >= 1 && d <= 64 && chi >= d && chi <= 4096, "bsg_cut_spectra: need 1 <= d <= chi <= 4096, d <= 64");
+  BSG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int kmax = M - L0, nmax = 2 * kmax;
+  CutArgs a{};
+  a.sq_cov = sq_cov;
+  a.M = M;
+  a.L0 = L0;
+  a.n_cuts = n_cuts;
+  a.d = d;
+  a.chi = chi;
+  a.err_tol = err_tol;
+  a.ws_stride = (size_t)4 * nmax * nmax;
+  a.S = S;
+  a.ldS = 2 * (M - 1);
+  a.kmax = kmax;
+  a.res = res;
+  a.num = num;
+  a.kept = kept;
+  a.max_sweeps = 40;
+  const size_t ws_bytes = a.ws_stride * 8 * n_cuts;
+  const size_t nbar_bytes = (size_t)n_cuts * kmax * 8;
+  const size_t rec_bytes = (size_t)n_cuts * kmax * chi * 4;
+  const size_t st_bytes = (size_t)n_cuts * 4;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes)));
+  char* base = reinterpret_cast<char*>(h->cut_ws.ptr);
+  a.ws = reinterpret_cast<double*>(base);
+  a.nbar = reinterpret_cast<double*>(base + al(ws_bytes));
+  a.rec = reinterpret_cast<uint32_t*>(base + al(ws_bytes) + al(nbar_bytes));
+  a.status = reinterpret_cast<int*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes));
+  BSG_CUDA(cudaMemsetAsync(a.status, 0xff, st_bytes, st));
+  BSG_CUDA(cudaMemsetAsync(res, 0, (size_t)n_cuts * chi * 8, st));
+  BSG_CUDA(cudaMemsetAsync(num, 0, (size_t)n_cuts * chi * (M - 1), st));
+  BSG_CUDA(cudaMemsetAsync(S, 0, (size_t)n_cuts * a.ldS * a.ldS * 8, st));
+  BSG_CUDA(cudaMemsetAsync(kept, 0, (size_t)n_cuts * 4, st));
+  const size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
+  BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+  williamson_kernel<<<n_cuts, 1024, wsm, st>>>(a);
+  BSG_CUDA(cudaGetLastError());
+  const size_t tsm = (size_t)d * chi * 8 + 2 * (size_t)chi * 8 + 64 * 8;
+  if (tsm > 227 * 1024) {
+    set_error("bsg_cut_spectra: d*chi=%d needs %zu bytes of shared memory", d * chi, tsm);
+    return BSG_ERR_LIMIT;
+  }
+  BSG_CUDA(cudaFuncSetAttribute(thermal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  thermal_kernel<<<n_cuts, 1024, tsm, st>>>(a);
+  BSG_CUDA(cudaGetLastError());
+  std::vector<int> status(n_cuts);
+  BSG_CUDA(cudaMemcpyAsync(status.data(), a.status, st_bytes, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaStreamSynchronize(st));
+  for (int c = 0; c < n_cuts; ++c) {
+    if (status[c] == 1) {
+      set_error("cut %d: the input matrix is not symmetric", L0 + c);
+      return BSG_ERR_NOT_PD;
+    }
+    if (status[c] == 2) {
+      set_error("cut %d: input matrix is not positive definite", L0 + c);
+      return BSG_ERR_NOT_PD;
+    }
+    if (status[c] == 3) {
+      set_error("cut %d: Jacobi eigen-solver did not converge", L0 + c);
+      return BSG_ERR_NO_CONVERGE;
+    }
+    if (status[c] == 4) {
+      set_error("cut %d: symplectic eigenvector pairing failed", L0 + c);
+      return BSG_ERR_NO_CONVERGE;
+    }
+    if (status[c] != 0) {
+      set_error("cut %d: Williamson kernel did not finish (status %d)", L0 + c, status[c]);
+      return BSG_ERR_CUDA;
+    }
+  }
+  return BSG_OK;
+}

@@ -393,7 +393,7 @@ static size_t prec_bytes(int precision) {
 // Converts Sigma (c128) into the precision's storage type inside `buf`.
 static int convert_sigma(bsg_handle_t h, const double* src, int64_t n, int precision, bsg::DevBuf& buf,
                          const void** out, cudaStream_t st) {
-  if (precision == BSG_PREC_FP64) {
+  if (precision == BSG_PREC_FP64 || n == 0) {
     *out = src;
     return BSG_OK;
   }

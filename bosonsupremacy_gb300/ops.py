@@ -118,3 +118,25 @@ def build_site(kind: int, Sigma, num_l, lambda_l, num_r, Z, d: int, chi: int, pr
                                      ptr(nr) if kr * mr else None, kr, mr, ptr(Zt), d, chi, _prec(precision), odt,
                                      ptr(out), stream_ptr()), "bsg_build_site")
     return out
+
+
+def cut_spectra(sq_cov, d: int, chi: int, L0: int = 1, n_cuts: Optional[int] = None, err_tol: float = 1e-12,
+                device: int = 0):
+    """Schmidt weights, Fock labels and Williamson symplectics of cuts
+    L0 .. L0+n_cuts-1 (kron_cpu.py:95-127 for each).  Returns device tensors
+    res [n, chi] f64, num [n, chi, M-1] int8, S [n, 2(M-1), 2(M-1)] f64 and
+    kept [n] int32; cut c uses the leading (M-L) label columns and the
+    leading 2(M-L) block of S."""
+    dev = torch.device("cuda", device)
+    sq = _dev(sq_cov, torch.float64, dev)
+    M = sq.shape[0] // 2
+    if n_cuts is None:
+        n_cuts = M - L0
+    res = torch.empty(n_cuts, chi, dtype=torch.float64, device=dev)
+    num = torch.empty(n_cuts, chi, M - 1, dtype=torch.int8, device=dev)
+    S = torch.empty(n_cuts, 2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device=dev)
+    kept = torch.empty(n_cuts, dtype=torch.int32, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_cut_spectra(h.h, ptr(sq), M, L0, n_cuts, d, chi, float(err_tol), ptr(res), ptr(num),
+                                      ptr(S), ptr(kept), stream_ptr()), "bsg_cut_spectra")
+    return res, num, S, kept

@@ -1,0 +1,334 @@
+#!/usr/bin/env python
+"""Benchmark: full-MPS construction throughput on GB300 (one JSON line).
+
+Workload (default): the large single instance -- M=144 modes, Haar-random
+interferometer, r_i ~ U[1.2, 1.6], eta = 0.45, d = 8, chi = 1024 -- built
+end to end: all 143 cut spectra (truncation to chi) and all 144 site
+tensors Gamma_i [chi, chi, d] (complex64, the reference's layout) with
+split-precision hafnians.  A step is one full build; `value` is sites/s with
+the covariance resident in HBM; `e2e` is the same through the public host
+API (covariance H2D, every Gamma/Lambda D2H into pinned host memory).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+  torchrun --nproc-per-node N bench.py --gpus N ...   (independent instances per rank)
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "full-MPS build throughput (sites/s), split-precision batched kernels"
+UNIT = "sites/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="M144_d8_chi1024")
+    p.add_argument("--precision", default="split", choices=["split", "fp64", "fp32"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-budget", type=float, default=20.0)
+    return p.parse_args()
+
+
+def dist_init():
+    import torch
+    import torch.distributed as dist
+
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        with open(self.tmp.name) as f:
+            rows = [ln.strip().split(",") for ln in f if ln.strip()]
+        os.unlink(self.tmp.name)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1].split()[0]))
+                mx.append(float(r[2].split()[0]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def profile_read(lib, h):
+    from bosonsupremacy_gb300 import _lib
+
+    out = {}
+    for k, name in _lib.KERNEL_CLASSES.items():
+        ms, n, w = C.c_double(), C.c_int64(), C.c_double()
+        _lib.check(lib.bsg_profile_read(h, k, C.byref(ms), C.byref(n), C.byref(w)), "bsg_profile_read")
+        out[name] = {"ms": ms.value, "launches": n.value, "work": w.value}
+    return out
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+def run_reference(args, ws, rank):
+    """The reference's own CPU MPS construction (oracle port of kron_cpu.py +
+    MPS_cpu.py), each step a bounded timed sample extrapolated to the full
+    build of the same workload on this host."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    from bosonsupremacy_gb300 import synthetic
+    from oracle import cpu_baseline, reference_mps as R
+
+    cfg = synthetic.NAMED[args.workload]
+    _, sq = synthetic.lossy_covariances(cfg)
+    # cut data for the group sizes (pruning to chi per step selects the same
+    # top-chi set as the reference's max_dim = 1e5, at a fraction of the cost)
+    cuts = [R.get_cumsum_kron(sq, c + 1, chi=cfg.chi, max_dim=cfg.chi, cutoff=cfg.d) for c in range(cfg.M - 1)]
+    vals = []
+    est = None
+    for i in range(args.warmup + args.steps):
+        est = cpu_baseline.estimate_full_build(sq, cfg.d, cfg.chi, cuts, budget_s=args.cpu_budget / 2, seed=i)
+        if i >= args.warmup:
+            vals.append(est["sites_per_s"])
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * cfg.M / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128/f64", "data": "synthetic",
+        "config": {"workload": cfg.label(), "M": cfg.M, "d": cfg.d, "chi": cfg.chi},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": (f"oracle (FP64 restatement of kron_cpu.py + MPS_cpu.py): one middle cut at "
+                                    f"max_dim=1e5, one williamson(sq_cov) + Bloch-Messiah, ~20 timed A_elem batches "
+                                    f"(n=6..12) fitted to the per-group cost model and applied to the workload's "
+                                    f"{est['groups']} exact (j, size) groups; extrapolated, not a full run"),
+                         "extrapolated_build_s": est["build_s"], "parts_s": {k: est[k] for k in
+                                                                            ("kron_s", "dense_s", "hafnian_s")}},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import numpy as np
+    import torch
+
+    from bosonsupremacy_gb300 import _lib, synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps, build_mps_host
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    lib = _lib.load()
+    handle = _lib.Handle.get(local)
+    cfg = synthetic.NAMED[args.workload]
+    _, sq = synthetic.lossy_covariances(cfg, seed=cfg.seed + rank)  # independent instance per rank
+    sq_dev = torch.as_tensor(sq).to(dev)
+    M, d, chi = cfg.M, cfg.d, cfg.chi
+    outs = [torch.empty(chi, chi, d, dtype=torch.complex64, device=dev) for _ in range(M)]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
+    torch.cuda.synchronize()
+    lib.bsg_profile_reset(handle.h)
+    lib.bsg_profile_enable(handle.h, 1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    stream = torch.cuda.current_stream()
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # evict L2 between steps (outside the timed region)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    lib.bsg_profile_enable(handle.h, 0)
+    prof = profile_read(lib, handle.h)
+    ms = statistics.mean(times)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * M / (ms / 1e3)
+
+    # plain-FP64 path of the same kernels, one build
+    fp64 = None
+    if not args.no_fp64 and args.precision != "fp64":
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        build_mps(sq_dev, d, chi, precision="fp64", out=outs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1)
+        fp64 = {"build_ms": t64, "sites_per_s": M / (t64 / 1e3), "split_speedup": t64 / ms}
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)  # restore outputs
+
+    # end to end through the public host API
+    e2e = None
+    if not args.no_e2e:
+        host_sq = torch.as_tensor(sq).pin_memory()
+        host_out = [torch.empty(chi, chi, d, dtype=torch.complex64, pin_memory=True) for _ in range(M)]
+        host_lam = torch.empty(M - 1, chi, dtype=torch.float64, pin_memory=True)
+        build_mps_host(host_sq, d, chi, host_out, host_lam, precision=args.precision, device_out=outs)
+        torch.cuda.synchronize()
+        et = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            barrier()
+            t0 = time.perf_counter()
+            build_mps_host(host_sq, d, chi, host_out, host_lam, precision=args.precision, device_out=outs)
+            torch.cuda.synchronize()
+            et.append(time.perf_counter() - t0)
+        es = statistics.mean(et)
+        if ws > 1:
+            t = torch.tensor([es], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            es = float(t.item())
+        e2e = {"value": ws * M / es, "unit": UNIT, "h2d_bytes_per_step": int(host_sq.numel() * 8),
+               "d2h_bytes_per_step": int(sum(o.numel() * 8 for o in host_out) + host_lam.numel() * 8),
+               "ms_per_step": es * 1e3}
+
+    # roofline of the dominant kernel class (live CUDA-event timing)
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    peaks = measured_peaks()
+    pk = C.c_double()
+    roof = None
+    if dom == "hafnian_dp":
+        prec_code = _lib.PREC_FP64 if args.precision == "fp64" else _lib.PREC_FP32
+        _lib.check(lib.bsg_fma_peak(handle.h, prec_code, C.byref(pk), None), "bsg_fma_peak")
+        achieved = 8.0 * prof[dom]["work"] / (prof[dom]["ms"] / 1e3)  # 8 real flops per complex multiply-add
+        roof = {"kernel": "dp_kernel (hafnian DP)", "bound": "fp64-pipe" if args.precision == "fp64" else "fp32-pipe",
+                "achieved": achieved / 1e12, "peak": pk.value / 1e12, "unit": "TFLOP/s",
+                "frac": achieved / pk.value, "traffic": None,
+                "peak_source": "measured on this GPU by bsg_fma_peak (register FMA loop on every SM)",
+                "work": "8 flops per complex multiply-add of the partition programs; the split arithmetic issues "
+                        "~48 FP32 instructions per complex multiply-add"}
+    elif dom == "williamson":
+        _lib.check(lib.bsg_fma_peak(handle.h, _lib.PREC_FP64, C.byref(pk), None), "bsg_fma_peak")
+        achieved = 2.0 * prof[dom]["work"] / (prof[dom]["ms"] / 1e3)
+        roof = {"kernel": "williamson_kernel (Cholesky + Jacobi)", "bound": "fp64-pipe", "achieved": achieved / 1e12,
+                "peak": pk.value / 1e12, "unit": "TFLOP/s", "frac": achieved / pk.value, "traffic": None,
+                "peak_source": "measured on this GPU by bsg_fma_peak (register FMA loop on every SM)"}
+    else:
+        roof = {"kernel": dom, "bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None}
+    roof["hbm_peak_gbs_measured"] = peaks.get("hbm_gbs")
+    launches = int(sum(v["launches"] for v in prof.values()))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import cpu_baseline
+
+        mps = build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
+        kept = mps.kept
+        rs, nm, Ss = mps.res.cpu().numpy(), mps.num.cpu().numpy(), mps.S.cpu().numpy()
+        cuts = []
+        for c in range(M - 1):
+            k = M - 1 - c
+            cuts.append((rs[c, : kept[c]], nm[c, : kept[c], :k], Ss[c, : 2 * k, : 2 * k]))
+        est = cpu_baseline.estimate_full_build(np.asarray(sq), d, chi, cuts, budget_s=args.cpu_budget)
+        cpu = {"value": est["sites_per_s"], "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": (f"oracle FP64 restatement of kron_cpu.py + MPS_cpu.py on this host: one middle cut at "
+                          f"max_dim=1e5, one williamson(sq_cov) + Bloch-Messiah, ~20 timed A_elem batches fitted "
+                          f"to a per-group cost model, applied to the workload's {est['groups']} (j, size) groups "
+                          f"({est['items']} items); extrapolated full build {est['build_s']:.0f} s"),
+               "extrapolated_build_s": est["build_s"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"split": "fp32x2 (split) hafnian, f64 factorisations",
+                                           "fp64": "f64", "fp32": "f32 hafnian, f64 factorisations"}[args.precision],
+            "data": "synthetic (seeded lossy GBS covariance; independent instance per rank)",
+            "config": {"workload": cfg.label(), "M": M, "d": d, "chi": chi, "precision": args.precision,
+                       "gamma_dtype": "complex64", "l2": "flushed between steps (512 MiB write)"},
+            "clocks": clk, "gpu_launches": launches, "kernels": {k: {"ms": v["ms"], "launches": v["launches"]}
+                                                                 for k, v in prof.items()},
+            "roofline": roof, "fp64_path": fp64, "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

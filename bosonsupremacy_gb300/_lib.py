@@ -17,6 +17,9 @@ LIB_PATH = os.path.join(HERE, "libbsg.so")
 PREC_FP64, PREC_SPLIT, PREC_FP32 = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "split": PREC_SPLIT, "fp32": PREC_FP32}
 SITE_FIRST, SITE_MIDDLE, SITE_LAST = 0, 1, 2
+K_DP, K_WILLIAMSON, K_THERMAL, K_SIGMA, K_PREP, K_CONTRACT = range(6)
+KERNEL_CLASSES = {K_DP: "hafnian_dp", K_WILLIAMSON: "williamson", K_THERMAL: "thermal_topk", K_SIGMA: "site_sigma",
+                  K_PREP: "prep", K_CONTRACT: "contract"}
 OUT_C64, OUT_C128 = 0, 1
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "input not positive definite",
@@ -39,6 +42,11 @@ SIGNATURES = {
     "bsg_build_site": (_I, [_P, _I, _P, _I, _P, _I, _I, _P, _P, _I, _I, _P, _I, _I, _I, _I, _P, _P]),
     "bsg_cut_spectra": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _P, _P, _P, _P, _P]),
     "bsg_pattern_amplitudes": (_I, [_P, _P, _P, _I, _I, _I, _P, _L, _I, _P, _P]),
+    "bsg_build_mps": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "bsg_profile_enable": (_I, [_P, _I]),
+    "bsg_profile_read": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_L), C.POINTER(_D)]),
+    "bsg_profile_reset": (_I, [_P]),
+    "bsg_fma_peak": (_I, [_P, _I, C.POINTER(_D), _P]),
 }
 
 

@@ -60,9 +60,94 @@ void HostBuf::release() {
   bytes = 0;
 }
 
+cudaEvent_t Profiler::get() {
+  if (!pool.empty()) {
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+int Profiler::begin(int cls, cudaStream_t st, cudaEvent_t* ev) {
+  (void)cls;
+  *ev = get();
+  if (!*ev) {
+    set_error("cudaEventCreate failed");
+    return BSG_ERR_CUDA;
+  }
+  BSG_CUDA(cudaEventRecord(*ev, st));
+  return BSG_OK;
+}
+
+int Profiler::end(int cls, cudaStream_t st, cudaEvent_t ev, double w) {
+  cudaEvent_t e2 = get();
+  if (!e2) {
+    set_error("cudaEventCreate failed");
+    return BSG_ERR_CUDA;
+  }
+  BSG_CUDA(cudaEventRecord(e2, st));
+  pending.push_back(Rec{cls, ev, e2, w});
+  return BSG_OK;
+}
+
+int Profiler::flush() {
+  for (auto& r : pending) {
+    BSG_CUDA(cudaEventSynchronize(r.b));
+    float ms = 0.f;
+    BSG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+    total_ms[r.cls] += ms;
+    launches[r.cls] += 1;
+    work[r.cls] += r.work;
+    pool.push_back(r.a);
+    pool.push_back(r.b);
+  }
+  pending.clear();
+  return BSG_OK;
+}
+
+void Profiler::release() {
+  for (auto& r : pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  pending.clear();
+  for (auto e : pool) cudaEventDestroy(e);
+  pool.clear();
+}
+
 }  // namespace bsg
 
 extern "C" {
+
+int bsg_profile_enable(bsg_handle_t h, int on) {
+  BSG_CHECK_ARG(h, "bsg_profile_enable: null handle");
+  h->prof.on = on != 0;
+  return BSG_OK;
+}
+
+int bsg_profile_reset(bsg_handle_t h) {
+  BSG_CHECK_ARG(h, "bsg_profile_reset: null handle");
+  BSG_TRY(h->prof.flush());
+  for (int i = 0; i < BSG_K_COUNT; ++i) {
+    h->prof.total_ms[i] = 0;
+    h->prof.launches[i] = 0;
+    h->prof.work[i] = 0;
+  }
+  return BSG_OK;
+}
+
+int bsg_profile_read(bsg_handle_t h, int cls, double* total_ms, int64_t* launches, double* work) {
+  BSG_CHECK_ARG(h, "bsg_profile_read: null handle");
+  BSG_CHECK_ARG(cls >= 0 && cls < BSG_K_COUNT, "bsg_profile_read: bad kernel class %d", cls);
+  BSG_TRY(h->prof.flush());
+  if (total_ms) *total_ms = h->prof.total_ms[cls];
+  if (launches) *launches = h->prof.launches[cls];
+  if (work) *work = h->prof.work[cls];
+  return BSG_OK;
+}
 
 const char* bsg_last_error(void) { return bsg::g_err; }
 
@@ -101,6 +186,7 @@ int bsg_destroy(bsg_handle_t h) {
   h->contract_ws.release();
   h->host_stage.release();
   h->host_stage2.release();
+  h->prof.release();
   delete h;
   return BSG_OK;
 }

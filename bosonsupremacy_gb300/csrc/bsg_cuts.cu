@@ -23,6 +23,7 @@
 // along both axes; each candidate's rank is found with d binary searches, so
 // the top chi come out already sorted (ties broken by the flattened index
 // i*d + n, the outer-product order of the reference).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -48,6 +49,7 @@ struct CutArgs {
   int32_t* kept;       // [n_cuts]
   uint32_t* rec;       // per cut: kmax * chi records (parent << 8 | digit)
   int* status;         // [n_cuts]
+  int* sweeps;         // [n_cuts] Jacobi sweeps used
   int max_sweeps;
 };
 
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       __syncthreads();
     }
   }
+  if (tid == 0) a.sweeps[c] = sweep;
   if (!converged) {
     if (tid == 0) a.status[c] = 3;
     return;
@@ -540,7 +543,7 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   const size_t ws_bytes = a.ws_stride * 8 * n_cuts;
   const size_t nbar_bytes = (size_t)n_cuts * kmax * 8;
   const size_t rec_bytes = (size_t)n_cuts * kmax * chi * 4;
-  const size_t st_bytes = (size_t)n_cuts * 4;
+  const size_t st_bytes = (size_t)n_cuts * 8;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes)));
   char* base = reinterpret_cast<char*>(h->cut_ws.ptr);
@@ -548,6 +551,7 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   a.nbar = reinterpret_cast<double*>(base + al(ws_bytes));
   a.rec = reinterpret_cast<uint32_t*>(base + al(ws_bytes) + al(nbar_bytes));
   a.status = reinterpret_cast<int*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes));
+  a.sweeps = a.status + n_cuts;
   BSG_CUDA(cudaMemsetAsync(a.status, 0xff, st_bytes, st));
   BSG_CUDA(cudaMemsetAsync(res, 0, (size_t)n_cuts * chi * 8, st));
   BSG_CUDA(cudaMemsetAsync(num, 0, (size_t)n_cuts * chi * (M - 1), st));
@@ -555,19 +559,27 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   BSG_CUDA(cudaMemsetAsync(kept, 0, (size_t)n_cuts * 4, st));
   const size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-  williamson_kernel<<<n_cuts, 1024, wsm, st>>>(a);
-  BSG_CUDA(cudaGetLastError());
+  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0, (williamson_kernel<<<n_cuts, 1024, wsm, st>>>(a)));
   const size_t tsm = (size_t)d * chi * 8 + 2 * (size_t)chi * 8 + 64 * 8;
   if (tsm > 227 * 1024) {
     set_error("bsg_cut_spectra: d*chi=%d needs %zu bytes of shared memory", d * chi, tsm);
     return BSG_ERR_LIMIT;
   }
   BSG_CUDA(cudaFuncSetAttribute(thermal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-  thermal_kernel<<<n_cuts, 1024, tsm, st>>>(a);
-  BSG_CUDA(cudaGetLastError());
-  std::vector<int> status(n_cuts);
+  double ranked = 0.0;
+  for (int c = 0; c < n_cuts; ++c) ranked += (double)(M - L0 - c) * chi * d;
+  BSG_PROFILED(h, BSG_K_THERMAL, st, ranked, (thermal_kernel<<<n_cuts, 1024, tsm, st>>>(a)));
+  std::vector<int> status(2 * n_cuts);
   BSG_CUDA(cudaMemcpyAsync(status.data(), a.status, st_bytes, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaStreamSynchronize(st));
+  // FP64 FMAs of the Williamson step: Cholesky n^3/3, L^-1 n^3/6, G n^3, H n^3,
+  // 4 n^3 per Jacobi sweep (2x2 blocks of H plus the eigenvector rows), pairing ~2 n^3
+  double fmas = 0.0;
+  for (int c = 0; c < n_cuts; ++c) {
+    const double n = 2.0 * (M - L0 - c);
+    fmas += n * n * n * (1.0 / 3 + 1.0 / 6 + 2.0 + 2.0 + 4.0 * std::max(0, status[n_cuts + c]));
+  }
+  h->prof.add_work(BSG_K_WILLIAMSON, fmas);
   for (int c = 0; c < n_cuts; ++c) {
     if (status[c] == 1) {
       set_error("cut %d: the input matrix is not symmetric", L0 + c);

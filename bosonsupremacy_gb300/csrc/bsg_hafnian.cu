@@ -1,4 +1,5 @@
-// Batched repetition-aware hafnians and the fused per-site Gamma build.
+// Batched repetition-aware hafnians, the fused per-site Gamma build and the
+// whole-MPS build.
 //
 // Every work item is one hafnian of Sigma restricted to a target index list
 // with repeats.  Items are bucketed by the multiplicity partition of their
@@ -6,6 +7,8 @@
 // partition program (bsg_programs.cpp) in lock-step, one item per lane, with
 // the per-lane A (class pair) table and F (DP state) table in a per-warp
 // scratch slice laid out [entry][lane] so every access is one coalesced line.
+// Buckets of all sites of an MPS share one persistent launch with an atomic
+// work counter; each 32-slot chunk carries its site and program.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -25,11 +28,10 @@ __constant__ double c_sqrt_fact[kMaxInv];  // sqrt(n!)
 __constant__ double c_fact[kMaxInv];       // n! (as double)
 
 static int ensure_tables() {
-  static bool done = false;  // per process; constant memory is per device module
   static int dev_done = -1;
   int dev = 0;
   BSG_CUDA(cudaGetDevice(&dev));
-  if (done && dev_done == dev) return BSG_OK;
+  if (dev_done == dev) return BSG_OK;
   double inv_d[kMaxInv], sf[kMaxInv], f[kMaxInv];
   float2 inv_f[kMaxInv];
   for (int r = 0; r < kMaxInv; ++r) {
@@ -43,33 +45,38 @@ static int ensure_tables() {
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_f, inv_f, sizeof(inv_f)));
   BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact, sf, sizeof(sf)));
   BSG_CUDA(cudaMemcpyToSymbol(c_fact, f, sizeof(f)));
-  done = true;
   dev_done = dev;
   return BSG_OK;
 }
 
 // ---------------------------------------------------------------------------
-// Label rows: sparse (Sigma index, multiplicity) lists sorted by multiplicity,
-// partition key, row sum and sqrt(prod num!) -- one thread per row.
+// Label rows: sparse (mode, multiplicity) lists sorted by multiplicity,
+// partition key, row sum and sqrt(prod num!) -- one thread per row.  Rows of
+// several cuts are handled in one launch (blockIdx.y = cut).
 // ---------------------------------------------------------------------------
-struct RowTable {
-  int32_t* entries;  // [rows, kMaxNnz] packed (sigma_idx << 8) | mult
-  int32_t* nnz;      // [rows]
-  int32_t* sum;      // [rows]
-  uint64_t* key;     // [rows]
-  double* rowfact;   // [rows] sqrt(prod num!)
-};
 constexpr int kMaxNnz = BSG_MAX_LABEL_NNZ;
 
-__global__ void label_rows_kernel(const int8_t* __restrict__ num, int rows, int m, int sigma_offset, RowTable t,
+struct RowTable {  // arrays indexed [cut * rows_cap + row]
+  int32_t* entries;  // [.., kMaxNnz] packed (mode << 8) | mult
+  int32_t* nnz;
+  int32_t* sum;
+  uint64_t* key;
+  double* rowfact;   // sqrt(prod num!)
+};
+
+__global__ void label_rows_kernel(const int8_t* __restrict__ num, int64_t cut_stride, int ld,
+                                  const int32_t* __restrict__ rows, int m_base, int m_step, int rows_cap, RowTable t,
                                   int* __restrict__ err) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
+  const int cut = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows[cut]) return;
+  const int m = m_base - m_step * cut;
+  const size_t o = (size_t)cut * rows_cap + r;
   int ent[kMaxNnz];
   int cnt = 0, sum = 0;
   uint64_t key = 0;
   double rf = 1.0;
-  const int8_t* row = num + (size_t)r * m;
+  const int8_t* row = num + cut * cut_stride + (int64_t)r * ld;
   for (int q = 0; q < m; ++q) {
     int v = row[q];
     if (v == 0) continue;
@@ -77,8 +84,7 @@ __global__ void label_rows_kernel(const int8_t* __restrict__ num, int rows, int 
       atomicExch(err, 1);
       continue;
     }
-    // insertion by multiplicity (stable on mode index)
-    int e = ((sigma_offset + q) << 8) | v;
+    int e = (q << 8) | v;
     int p = cnt++;
     while (p > 0 && (ent[p - 1] & 0xff) > v) {
       ent[p] = ent[p - 1];
@@ -89,11 +95,33 @@ __global__ void label_rows_kernel(const int8_t* __restrict__ num, int rows, int 
     key += uint64_t(1) << (kKeyBits * (v - 1));
     rf *= c_sqrt_fact[v];
   }
-  for (int i = 0; i < cnt; ++i) t.entries[(size_t)r * kMaxNnz + i] = ent[i];
-  t.nnz[r] = cnt;
-  t.sum[r] = sum;
-  t.key[r] = key;
-  t.rowfact[r] = rf;
+  for (int i = 0; i < cnt; ++i) t.entries[o * kMaxNnz + i] = ent[i];
+  t.nnz[o] = cnt;
+  t.sum[o] = sum;
+  t.key[o] = key;
+  t.rowfact[o] = rf;
+}
+
+// Lambda = sqrt(res) where res > err_tol (else 0) and the count of such rows.
+__global__ void lambda_kernel(const double* __restrict__ res, int chi, double err_tol, double* __restrict__ lambda,
+                              int32_t* __restrict__ rows_above) {
+  const int c = blockIdx.x;
+  int cnt = 0;
+  for (int r = threadIdx.x; r < chi; r += blockDim.x) {
+    double v = res[(size_t)c * chi + r];
+    bool keep = v > err_tol;
+    lambda[(size_t)c * chi + r] = keep ? sqrt(v) : 0.0;
+    cnt += keep;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  __shared__ int s[32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) tot += s[w];
+    rows_above[c] = tot;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -102,14 +130,14 @@ __global__ void label_rows_kernel(const int8_t* __restrict__ num, int rows, int 
 // that a warp usually shares one bucket (one aggregated atomic).
 // ---------------------------------------------------------------------------
 struct SitePlanDev {
-  const int32_t* perm_l;  // sorted position -> left row
-  const int32_t* grp_l;   // sorted position -> left key group
+  const int32_t* perm_l;     // sorted position -> left row
+  const int32_t* grp_l;      // sorted position -> left key group
   const int32_t* perm_r;
   const int32_t* grp_r;
-  const int32_t* bucket_of;  // [d][ngl][ngr] -> bucket or -1 (odd order)
-  const int32_t* bucket_off;  // [nb] first slot
-  int32_t* cursor;            // [nb]
-  int32_t* items;             // slots
+  const int32_t* bucket_of;  // [d][ngl][ngr] -> global bucket or -1 (odd order)
+  const int32_t* bucket_off; // [nb] first slot
+  int32_t* cursor;           // [nb]
+  int32_t* items;            // slots
   int ngl, ngr, kl, kr, d;
 };
 
@@ -157,28 +185,35 @@ struct ProgDev {
 
 enum { MODE_SITE = 0, MODE_TARGETS = 1, MODE_MATRICES = 2 };
 
+struct SiteDesc {
+  const void* sigma;  // policy-typed [2Mr, 2Mr]
+  int n_len, Mr;
+  const int32_t* l_ent;  // left rows (cut `site`): entries/nnz/rowfact
+  const int32_t* l_nnz;
+  const double* l_rowfact;
+  const double* lambda;  // null -> 1
+  const int32_t* r_ent;  // right rows (cut `site-1`)
+  const int32_t* r_nnz;
+  const double* r_rowfact;
+  const double* Z;
+  void* gamma;
+  int chi, d, out_c128;
+};
+
 struct DPArgs {
   ProgDev prog;
   const int32_t* items;
   const int32_t* chunk_prog;
+  const int32_t* chunk_site;
   int64_t n_chunks;
   unsigned long long* counter;
   void* scratch;
   int pairs_max, states_max;
+  // site mode
+  const SiteDesc* sites;
+  // target / matrices mode
   const void* sigma;  // policy-typed
   int n_len;
-  // site mode
-  const int32_t* l_ent;
-  const int32_t* l_nnz;
-  const double* l_rowfact;
-  const double* lambda;
-  const int32_t* r_ent;
-  const int32_t* r_nnz;
-  const double* r_rowfact;
-  const double* Z;
-  int d, chi, out_c128;
-  void* gamma;
-  // target / matrices mode
   const int32_t* targets;
   int n;
   const double* den;
@@ -186,36 +221,33 @@ struct DPArgs {
 };
 
 template <int MODE>
-__device__ __forceinline__ int build_classes(const DPArgs& a, int32_t item, int* cls, double& fac, int& j_out,
-                                             int& ra_out, int& rb_out, int64_t& sig_base) {
+__device__ __forceinline__ int build_classes(const DPArgs& a, const SiteDesc* sd, int32_t item, int* cls,
+                                             double& fac, int64_t& sig_base) {
   sig_base = 0;
+  fac = 1.0;
   if (MODE == MODE_SITE) {
-    int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff, j = item & 0xff;
-    j_out = j;
-    ra_out = alpha;
-    rb_out = beta;
-    const int32_t* le = a.l_ent + (size_t)beta * kMaxNnz;
-    const int32_t* re = a.r_ent + (size_t)alpha * kMaxNnz;
-    int nl = a.l_nnz[beta], nr = a.r_nnz[alpha];
+    const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff, j = item & 0xff;
+    const int32_t* le = sd->l_ent + (size_t)beta * kMaxNnz;
+    const int32_t* re = sd->r_ent + (size_t)alpha * kMaxNnz;
+    const int nl = sd->l_nnz[beta], nr = sd->r_nnz[alpha];
+    const int roff = sd->Mr;
     int il = 0, ir = 0, k = 0;
     bool jpend = j > 0;
     // three-way merge by multiplicity (j class first on ties)
     while (jpend || il < nl || ir < nr) {
-      int ml = il < nl ? (le[il] & 0xff) : 1 << 20;
-      int mr = ir < nr ? (re[ir] & 0xff) : 1 << 20;
+      const int ml = il < nl ? (le[il] & 0xff) : 1 << 20;
+      const int mr = ir < nr ? (re[ir] & 0xff) : 1 << 20;
       if (jpend && j <= ml && j <= mr) {
         cls[k++] = 0;
         jpend = false;
       } else if (ml <= mr) {
-        cls[k++] = le[il++] >> 8;
+        cls[k++] = 1 + (le[il++] >> 8);
       } else {
-        cls[k++] = re[ir++] >> 8;
+        cls[k++] = roff + (re[ir++] >> 8);
       }
     }
-    fac = 1.0;
     return k;
   } else {
-    // MODE_TARGETS: row of a [B, n] index array; MODE_MATRICES: 0..n-1
     const int n = a.n;
     int t[BSG_MAX_ORDER];
     if (MODE == MODE_TARGETS) {
@@ -233,10 +265,8 @@ __device__ __forceinline__ int build_classes(const DPArgs& a, int32_t item, int*
       for (int i = 0; i < n; ++i) t[i] = i;
       sig_base = (int64_t)item * n * n;
     }
-    // run-length classes, then order by multiplicity (stable)
     int ci[BSG_MAX_CLASSES], cm[BSG_MAX_CLASSES];
     int k = 0;
-    fac = 1.0;
     for (int i = 0; i < n;) {
       int v = t[i], c = 0;
       while (i < n && t[i] == v) {
@@ -268,37 +298,34 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
   const size_t slice = (size_t)(a.pairs_max + a.states_max) * 32;
   C* Ab = reinterpret_cast<C*>(a.scratch) + (size_t)warp * slice;
   C* Fb = Ab + (size_t)a.pairs_max * 32;
-  const C* sig = reinterpret_cast<const C*>(a.sigma);
   while (true) {
     unsigned long long c = 0;
     if (lane == 0) c = atomicAdd(a.counter, 1ull);
     c = __shfl_sync(0xffffffffu, c, 0);
     if ((int64_t)c >= a.n_chunks) break;
     const int prog = a.chunk_prog[c];
+    const SiteDesc* sd = MODE == MODE_SITE ? a.sites + a.chunk_site[c] : nullptr;
     const int32_t item = a.items[c * 32 + lane];
     const bool live = item >= 0;
     const int kp = a.prog.k[prog];
     const int ns = a.prog.nstates[prog];
     const int so = a.prog.state_off[prog];
+    const C* sig = reinterpret_cast<const C*>(MODE == MODE_SITE ? sd->sigma : a.sigma);
+    const int n_len = MODE == MODE_SITE ? sd->n_len : a.n_len;
 
     int cls[BSG_MAX_CLASSES];
     double fac = 1.0;
-    int j = 0, ia = 0, ib = 0;
     int64_t sb = 0;
-    int k = kp;
     if (live) {
-      k = build_classes<MODE>(a, item, cls, fac, j, ia, ib, sb);
+      build_classes<MODE>(a, sd, item, cls, fac, sb);
     } else {
       for (int q = 0; q < kp; ++q) cls[q] = 0;
     }
     // gather the class-pair table (diagonal included)
     for (int bq = 0; bq < kp; ++bq) {
-      const int64_t rowb = sb + (int64_t)cls[bq] * a.n_len;
-      for (int aq = 0; aq <= bq; ++aq) {
-        Ab[(size_t)pair_index(aq, bq) * 32 + lane] = sig[rowb + cls[aq]];
-      }
+      const int64_t rowb = sb + (int64_t)cls[bq] * n_len;
+      for (int aq = 0; aq <= bq; ++aq) Ab[(size_t)pair_index(aq, bq) * 32 + lane] = sig[rowb + cls[aq]];
     }
-    (void)k;
     // run the program
     Fb[lane] = P::one();
     for (int s = 1; s < ns; ++s) {
@@ -315,15 +342,16 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
       Fb[(size_t)s * 32 + lane] = P::finish(acc, ra, c_inv_d, c_inv_f);
     }
     if (!live) continue;
-    double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
+    const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
     if (MODE == MODE_SITE) {
-      double scale = c_sqrt_fact[j] * a.l_rowfact[ib] * a.r_rowfact[ia] / a.Z[0];
-      if (a.lambda) scale /= a.lambda[ib];
-      const size_t o = ((size_t)ia * a.chi + ib) * a.d + j;
-      if (a.out_c128) {
-        reinterpret_cast<double2*>(a.gamma)[o] = make_double2(v.x * scale, v.y * scale);
+      const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff, j = item & 0xff;
+      double scale = c_sqrt_fact[j] * sd->l_rowfact[beta] * sd->r_rowfact[alpha] / sd->Z[0];
+      if (sd->lambda) scale /= sd->lambda[beta];
+      const size_t o = ((size_t)alpha * sd->chi + beta) * sd->d + j;
+      if (sd->out_c128) {
+        reinterpret_cast<double2*>(sd->gamma)[o] = make_double2(v.x * scale, v.y * scale);
       } else {
-        reinterpret_cast<float2*>(a.gamma)[o] = make_float2(float(v.x * scale), float(v.y * scale));
+        reinterpret_cast<float2*>(sd->gamma)[o] = make_float2(float(v.x * scale), float(v.y * scale));
       }
     } else {
       double s = fac;
@@ -390,7 +418,25 @@ static size_t prec_bytes(int precision) {
   return precision == BSG_PREC_FP64 ? sizeof(double2) : precision == BSG_PREC_SPLIT ? sizeof(float4) : sizeof(float2);
 }
 
-// Converts Sigma (c128) into the precision's storage type inside `buf`.
+// Converts n c128 values at src into the precision's storage type at dst.
+static int convert_into(bsg_handle_t h, const double* src, int64_t n, int precision, void* dst, cudaStream_t st) {
+  if (n == 0) return BSG_OK;
+  const int threads = 256;
+  const int64_t blocks = (n + threads - 1) / threads;
+  if (precision == BSG_PREC_FP64) {
+    BSG_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * 16, cudaMemcpyDeviceToDevice, st));
+  } else if (precision == BSG_PREC_SPLIT) {
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)n,
+                 (convert_kernel<float4><<<(unsigned)blocks, threads, 0, st>>>(
+                     reinterpret_cast<const double2*>(src), reinterpret_cast<float4*>(dst), n)));
+  } else {
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)n,
+                 (convert_kernel<float2><<<(unsigned)blocks, threads, 0, st>>>(
+                     reinterpret_cast<const double2*>(src), reinterpret_cast<float2*>(dst), n)));
+  }
+  return BSG_OK;
+}
+
 static int convert_sigma(bsg_handle_t h, const double* src, int64_t n, int precision, bsg::DevBuf& buf,
                          const void** out, cudaStream_t st) {
   if (precision == BSG_PREC_FP64 || n == 0) {
@@ -398,69 +444,149 @@ static int convert_sigma(bsg_handle_t h, const double* src, int64_t n, int preci
     return BSG_OK;
   }
   BSG_TRY(buf.ensure((size_t)n * prec_bytes(precision)));
-  int threads = 256;
-  int64_t blocks = (n + threads - 1) / threads;
-  if (precision == BSG_PREC_SPLIT)
-    convert_kernel<float4><<<(unsigned)blocks, threads, 0, st>>>(reinterpret_cast<const double2*>(src),
-                                                                 reinterpret_cast<float4*>(buf.ptr), n);
-  else
-    convert_kernel<float2><<<(unsigned)blocks, threads, 0, st>>>(reinterpret_cast<const double2*>(src),
-                                                                 reinterpret_cast<float2*>(buf.ptr), n);
-  BSG_CUDA(cudaGetLastError());
+  BSG_TRY(convert_into(h, src, n, precision, buf.ptr, st));
   *out = buf.ptr;
   return BSG_OK;
 }
 
-// Host-side bucket layout shared by both planners.
+// ---------------------------------------------------------------------------
+// Host-side planning
+// ---------------------------------------------------------------------------
 struct Buckets {
   std::vector<int32_t> progs;    // bucket -> program
+  std::vector<int32_t> sites;    // bucket -> site (0 in target/matrix modes)
   std::vector<int64_t> counts;   // bucket -> items
   std::vector<int32_t> offsets;  // bucket -> first slot (multiple of 32)
-  std::vector<int32_t> chunk_prog;
+  std::vector<int32_t> chunk_prog, chunk_site;
   int64_t slots = 0;
   int pairs_max = 1, states_max = 1;
+  double work = 0.0;             // complex multiply-adds of all items
 };
 
-static int layout_buckets(const bsg::ProgramSet& ps, Buckets& bk) {
-  // order buckets by per-item cost, expensive first, so the work queue
-  // starts the long programs early
+static int64_t prog_trans(const bsg::ProgramSet& ps, int p) {
+  int s0 = ps.state_off[p], ns = ps.nstates[p];
+  return (int64_t)ps.st_trans_off[s0 + ns - 1] + ps.st_trans_cnt[s0 + ns - 1] - ps.st_trans_off[s0];
+}
+
+// Orders buckets by per-item cost (expensive first, so the work queue starts
+// the long programs early) and assigns padded slot ranges; `remap[old] = new`.
+static int layout_buckets(const bsg::ProgramSet& ps, Buckets& bk, std::vector<int32_t>& remap) {
   const int nb = int(bk.progs.size());
   std::vector<int> order(nb);
   std::iota(order.begin(), order.end(), 0);
-  auto cost = [&](int b) {
-    int p = bk.progs[b];
-    int s0 = ps.state_off[p], ns = ps.nstates[p];
-    int64_t tr = ps.st_trans_off[s0 + ns - 1] + ps.st_trans_cnt[s0 + ns - 1] - ps.st_trans_off[s0];
-    return tr + ns;
-  };
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
-  std::vector<int32_t> progs(nb);
-  std::vector<int64_t> counts(nb);
+  std::vector<int64_t> cost(nb);
+  for (int b = 0; b < nb; ++b) cost[b] = prog_trans(ps, bk.progs[b]) + ps.nstates[bk.progs[b]];
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  Buckets out;
+  remap.assign(nb, -1);
+  out.progs.resize(nb);
+  out.sites.resize(nb);
+  out.counts.resize(nb);
   for (int i = 0; i < nb; ++i) {
-    progs[i] = bk.progs[order[i]];
-    counts[i] = bk.counts[order[i]];
+    out.progs[i] = bk.progs[order[i]];
+    out.sites[i] = bk.sites[order[i]];
+    out.counts[i] = bk.counts[order[i]];
+    remap[order[i]] = i;
   }
-  bk.progs.swap(progs);
-  bk.counts.swap(counts);
-  bk.offsets.assign(nb, 0);
-  bk.chunk_prog.clear();
+  out.offsets.assign(nb, 0);
   int64_t off = 0;
   for (int b = 0; b < nb; ++b) {
-    bk.offsets[b] = int32_t(off);
-    int64_t ch = (bk.counts[b] + 31) / 32;
-    for (int64_t c = 0; c < ch; ++c) bk.chunk_prog.push_back(bk.progs[b]);
+    out.offsets[b] = int32_t(off);
+    const int64_t ch = (out.counts[b] + 31) / 32;
+    for (int64_t c = 0; c < ch; ++c) {
+      out.chunk_prog.push_back(out.progs[b]);
+      out.chunk_site.push_back(out.sites[b]);
+    }
     off += ch * 32;
-    int p = bk.progs[b];
-    int kk = ps.k[p];
-    bk.pairs_max = std::max(bk.pairs_max, kk * (kk + 1) / 2);
-    bk.states_max = std::max(bk.states_max, ps.nstates[p]);
+    const int p = out.progs[b];
+    const int kk = ps.k[p];
+    out.pairs_max = std::max(out.pairs_max, kk * (kk + 1) / 2);
+    out.states_max = std::max(out.states_max, ps.nstates[p]);
+    out.work += (double)out.counts[b] * (double)prog_trans(ps, p);
+    if (off > INT32_MAX) {
+      set_error("too many work items in one launch (%lld)", (long long)off);
+      return BSG_ERR_LIMIT;
+    }
   }
-  if (off > INT32_MAX) {
-    set_error("too many work items in one launch (%lld)", (long long)off);
-    return BSG_ERR_LIMIT;
-  }
-  bk.slots = off;
+  out.slots = off;
+  bk = std::move(out);
   return BSG_OK;
+}
+
+// Per-site plan on the host: rows grouped by partition key, and the bucket
+// of every (j, left group, right group) combination.
+struct SitePlanHost {
+  int KL = 0, KR = 0, ngl = 0, ngr = 0, d = 0;
+  std::vector<int32_t> perm_l, grp_l, perm_r, grp_r, bucket_of;
+};
+
+static void group_rows(const uint64_t* key, int rows, std::vector<int32_t>& perm, std::vector<int32_t>& grp,
+                       std::vector<uint64_t>& gkey, std::vector<int64_t>& gcnt) {
+  perm.resize(rows);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return key[x] < key[y]; });
+  grp.resize(rows);
+  gkey.clear();
+  gcnt.clear();
+  for (int i = 0; i < rows; ++i) {
+    if (i == 0 || key[perm[i]] != key[perm[i - 1]]) {
+      gkey.push_back(key[perm[i]]);
+      gcnt.push_back(0);
+    }
+    grp[i] = int32_t(gkey.size() - 1);
+    gcnt.back()++;
+  }
+}
+
+static int plan_site(bsg::ProgramSet& ps, int site, const uint64_t* kl, int KL, const uint64_t* kr, int KR, int d,
+                     SitePlanHost& sp, Buckets& bk, std::unordered_map<int64_t, int>& bindex) {
+  sp.KL = KL;
+  sp.KR = KR;
+  sp.d = d;
+  std::vector<uint64_t> gk_l, gk_r;
+  std::vector<int64_t> gc_l, gc_r;
+  group_rows(kl, KL, sp.perm_l, sp.grp_l, gk_l, gc_l);
+  group_rows(kr, KR, sp.perm_r, sp.grp_r, gk_r, gc_r);
+  sp.ngl = int(gk_l.size());
+  sp.ngr = int(gk_r.size());
+  std::vector<int> gs_l(sp.ngl), gs_r(sp.ngr);
+  for (int g = 0; g < sp.ngl; ++g) gs_l[g] = key_order(gk_l[g]);
+  for (int g = 0; g < sp.ngr; ++g) gs_r[g] = key_order(gk_r[g]);
+  sp.bucket_of.assign((size_t)d * sp.ngl * sp.ngr, -1);
+  for (int j = 0; j < d; ++j) {
+    const uint64_t kj = key_add_class(0, j);
+    for (int gl = 0; gl < sp.ngl; ++gl) {
+      for (int gr = 0; gr < sp.ngr; ++gr) {
+        const int n = j + gs_l[gl] + gs_r[gr];
+        if (n & 1) continue;
+        if (n > BSG_MAX_ORDER) {
+          set_error("site %d: hafnian order %d exceeds BSG_MAX_ORDER", site, n);
+          return BSG_ERR_LIMIT;
+        }
+        int32_t prog;
+        BSG_TRY(program_for_key(ps, kj + gk_l[gl] + gk_r[gr], &prog));
+        const int64_t bkey = ((int64_t)site << 32) | (uint32_t)prog;
+        auto it = bindex.find(bkey);
+        int b;
+        if (it == bindex.end()) {
+          b = int(bk.progs.size());
+          bindex.emplace(bkey, b);
+          bk.progs.push_back(prog);
+          bk.sites.push_back(site);
+          bk.counts.push_back(0);
+        } else {
+          b = it->second;
+        }
+        bk.counts[b] += gc_l[gl] * gc_r[gr];
+        sp.bucket_of[((size_t)j * sp.ngl + gl) * sp.ngr + gr] = b;
+      }
+    }
+  }
+  return BSG_OK;
+}
+
+static ProgDev prog_dev(const bsg::ProgramSet& ps) {
+  return ProgDev{ps.d_k, ps.d_nstates, ps.d_state_off, ps.d_st_trans_off, ps.d_st_trans_cnt, ps.d_st_ra, ps.d_trans};
 }
 
 template <class P, int MODE>
@@ -468,20 +594,19 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, cudaStream_t
   using C = typename P::C;
   const size_t per_warp = (size_t)(bk.pairs_max + bk.states_max) * 32 * sizeof(C);
   const int threads = 256;
-  int blocks_per_sm = 4;
+  const int blocks_per_sm = 4;
   int64_t warps = (int64_t)h->num_sms * blocks_per_sm * (threads / 32);
   const size_t budget = size_t(2) << 30;  // at most 2 GiB of per-warp tables
   while (warps > (threads / 32) * (int64_t)h->num_sms && (size_t)warps * per_warp > budget) warps /= 2;
-  int64_t need_chunks = std::max<int64_t>(bk.chunk_prog.size(), 1);
-  int64_t w_use = std::min<int64_t>(warps, need_chunks);
+  const int64_t need_chunks = std::max<int64_t>((int64_t)bk.chunk_prog.size(), 1);
+  const int64_t w_use = std::min<int64_t>(warps, need_chunks);
   int blocks = int((w_use + (threads / 32) - 1) / (threads / 32));
   if (blocks < 1) blocks = 1;
   BSG_TRY(h->warp_scratch.ensure((size_t)blocks * (threads / 32) * per_warp));
   a.scratch = h->warp_scratch.ptr;
   a.pairs_max = bk.pairs_max;
   a.states_max = bk.states_max;
-  dp_kernel<P, MODE><<<blocks, threads, 0, st>>>(a);
-  BSG_CUDA(cudaGetLastError());
+  BSG_PROFILED(h, BSG_K_DP, st, bk.work, (dp_kernel<P, MODE><<<blocks, threads, 0, st>>>(a)));
   return BSG_OK;
 }
 
@@ -492,11 +617,7 @@ static int launch_dp(bsg_handle_t h, int precision, DPArgs a, const Buckets& bk,
   return launch_dp_t<PrecF32, MODE>(h, a, bk, st);
 }
 
-static ProgDev prog_dev(const bsg::ProgramSet& ps) {
-  return ProgDev{ps.d_k, ps.d_nstates, ps.d_state_off, ps.d_st_trans_off, ps.d_st_trans_cnt, ps.d_st_ra, ps.d_trans};
-}
-
-// Places item ids into bucket slots on the host (target / matrix modes).
+// ---- target / matrix modes ------------------------------------------------
 static int plan_items_host(bsg_handle_t h, const std::vector<uint64_t>& keys, Buckets& bk,
                            std::vector<int32_t>& items) {
   auto& ps = h->programs;
@@ -512,6 +633,7 @@ static int plan_items_host(bsg_handle_t h, const std::vector<uint64_t>& keys, Bu
       b = int(bk.progs.size());
       bucket_of_prog.emplace(prog, b);
       bk.progs.push_back(prog);
+      bk.sites.push_back(0);
       bk.counts.push_back(0);
     } else {
       b = it->second;
@@ -519,16 +641,13 @@ static int plan_items_host(bsg_handle_t h, const std::vector<uint64_t>& keys, Bu
     bk.counts[b]++;
     item_bucket[i] = b;
   }
-  // layout reorders buckets; remember the mapping by program
-  std::vector<int32_t> progs_before = bk.progs;
-  BSG_TRY(layout_buckets(ps, bk));
-  std::unordered_map<int32_t, int> newb;
-  for (size_t b = 0; b < bk.progs.size(); ++b) newb[bk.progs[b]] = int(b);
+  std::vector<int32_t> remap;
+  BSG_TRY(layout_buckets(ps, bk, remap));
   items.assign(bk.slots, -1);
   std::vector<int64_t> cur(bk.progs.size(), 0);
   for (size_t i = 0; i < keys.size(); ++i) {
     if (item_bucket[i] < 0) continue;
-    int b = newb[progs_before[item_bucket[i]]];
+    const int b = remap[item_bucket[i]];
     items[bk.offsets[b] + cur[b]++] = int32_t(i);
   }
   return BSG_OK;
@@ -556,6 +675,7 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
   a.prog = prog_dev(h->programs);
   a.items = d_items;
   a.chunk_prog = d_chunk;
+  a.chunk_site = nullptr;
   a.n_chunks = (int64_t)chunks;
   a.counter = counter;
   a.sigma = sig;
@@ -566,8 +686,129 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
   a.out = reinterpret_cast<double2*>(out);
   if (mode == MODE_TARGETS) BSG_TRY(launch_dp<MODE_TARGETS>(h, precision, a, bk, st));
   else BSG_TRY(launch_dp<MODE_MATRICES>(h, precision, a, bk, st));
-  BSG_CUDA(cudaStreamSynchronize(st));  // host vectors above go out of scope
+  BSG_CUDA(cudaStreamSynchronize(st));  // the host vectors above go out of scope
   return BSG_OK;
+}
+
+// ---- site mode: shared by bsg_build_site (one site) and bsg_build_mps --------
+struct SiteInput {
+  int kind;
+  int Mr;
+  const void* sigma;  // policy-typed
+  const double* Z;
+  const double* lambda;   // left rows (null for LAST)
+  const uint64_t* hkey_l; // host copies of the row keys
+  const uint64_t* hkey_r;
+  int KL, KR;
+  RowTable lt;            // device row tables (already offset to this cut)
+  RowTable rt;
+  void* gamma;
+};
+
+// Plans, uploads and launches the scatter + DP for a set of sites.
+static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, int chi, int precision, int out_dtype,
+                     cudaStream_t st) {
+  auto& ps = h->programs;
+  const int ns = int(in.size());
+  Buckets bk;
+  std::unordered_map<int64_t, int> bindex;
+  std::vector<SitePlanHost> plans(ns);
+  for (int s = 0; s < ns; ++s)
+    BSG_TRY(plan_site(ps, s, in[s].hkey_l, in[s].KL, in[s].hkey_r, in[s].KR, d, plans[s], bk, bindex));
+  std::vector<int32_t> remap;
+  BSG_TRY(layout_buckets(ps, bk, remap));
+  for (auto& p : plans)
+    for (auto& b : p.bucket_of)
+      if (b >= 0) b = remap[b];
+  BSG_TRY(programs_upload(ps, st));
+  const int nb = int(bk.progs.size());
+  const size_t chunks = bk.chunk_prog.size();
+
+  // one plan buffer: site descs, per-site tables, bucket offsets/cursors, chunks, counter
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = align(off + bytes);
+    return o;
+  };
+  const size_t o_desc = carve(sizeof(SiteDesc) * ns);
+  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns);
+  for (int s = 0; s < ns; ++s) {
+    o_pl[s] = carve(plans[s].perm_l.size() * 4);
+    o_gl[s] = carve(plans[s].grp_l.size() * 4);
+    o_pr[s] = carve(plans[s].perm_r.size() * 4);
+    o_gr[s] = carve(plans[s].grp_r.size() * 4);
+    o_bo[s] = carve(plans[s].bucket_of.size() * 4);
+  }
+  const size_t o_boff = carve((size_t)nb * 4 + 4), o_cur = carve((size_t)nb * 4 + 4);
+  const size_t o_cp = carve(chunks * 4 + 4), o_cs = carve(chunks * 4 + 4), o_ctr = carve(8);
+  const size_t plan_bytes = off;
+  BSG_TRY(h->plan.ensure(plan_bytes));
+  BSG_TRY(h->host_stage2.ensure(plan_bytes));
+  char* hp = reinterpret_cast<char*>(h->host_stage2.ptr);
+  char* dp = reinterpret_cast<char*>(h->plan.ptr);
+  SiteDesc* hd = reinterpret_cast<SiteDesc*>(hp + o_desc);
+  const int out_c128 = out_dtype == BSG_OUT_C128;
+  for (int s = 0; s < ns; ++s) {
+    const SiteInput& si = in[s];
+    SiteDesc sd{};
+    sd.sigma = si.sigma;
+    sd.Mr = si.Mr;
+    sd.n_len = 2 * si.Mr;
+    sd.l_ent = si.lt.entries;
+    sd.l_nnz = si.lt.nnz;
+    sd.l_rowfact = si.lt.rowfact;
+    sd.lambda = si.kind == BSG_SITE_LAST ? nullptr : si.lambda;
+    sd.r_ent = si.rt.entries;
+    sd.r_nnz = si.rt.nnz;
+    sd.r_rowfact = si.rt.rowfact;
+    sd.Z = si.Z;
+    sd.gamma = si.gamma;
+    sd.chi = chi;
+    sd.d = d;
+    sd.out_c128 = out_c128;
+    hd[s] = sd;
+    std::memcpy(hp + o_pl[s], plans[s].perm_l.data(), plans[s].perm_l.size() * 4);
+    std::memcpy(hp + o_gl[s], plans[s].grp_l.data(), plans[s].grp_l.size() * 4);
+    std::memcpy(hp + o_pr[s], plans[s].perm_r.data(), plans[s].perm_r.size() * 4);
+    std::memcpy(hp + o_gr[s], plans[s].grp_r.data(), plans[s].grp_r.size() * 4);
+    std::memcpy(hp + o_bo[s], plans[s].bucket_of.data(), plans[s].bucket_of.size() * 4);
+  }
+  std::memcpy(hp + o_boff, bk.offsets.data(), (size_t)nb * 4);
+  std::memset(hp + o_cur, 0, (size_t)nb * 4 + 4);
+  if (chunks) {
+    std::memcpy(hp + o_cp, bk.chunk_prog.data(), chunks * 4);
+    std::memcpy(hp + o_cs, bk.chunk_site.data(), chunks * 4);
+  }
+  std::memset(hp + o_ctr, 0, 8);
+  BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
+  const size_t esz = out_c128 ? 16 : 8;
+  for (int s = 0; s < ns; ++s) BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, (size_t)chi * chi * d * esz, st));
+  if (bk.slots == 0) return BSG_OK;
+  BSG_TRY(h->items.ensure((size_t)bk.slots * 4));
+  int32_t* d_items = reinterpret_cast<int32_t*>(h->items.ptr);
+  BSG_CUDA(cudaMemsetAsync(d_items, 0xff, (size_t)bk.slots * 4, st));
+  for (int s = 0; s < ns; ++s) {
+    const SitePlanHost& p = plans[s];
+    SitePlanDev sp{reinterpret_cast<int32_t*>(dp + o_pl[s]), reinterpret_cast<int32_t*>(dp + o_gl[s]),
+                   reinterpret_cast<int32_t*>(dp + o_pr[s]), reinterpret_cast<int32_t*>(dp + o_gr[s]),
+                   reinterpret_cast<int32_t*>(dp + o_bo[s]), reinterpret_cast<int32_t*>(dp + o_boff),
+                   reinterpret_cast<int32_t*>(dp + o_cur),   d_items,
+                   p.ngl, p.ngr, p.KL, p.KR, p.d};
+    const int64_t total = (int64_t)p.d * p.KL * p.KR;
+    const int sblocks = int(std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)h->num_sms * 8)));
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)total, (site_scatter_kernel<<<sblocks, 256, 0, st>>>(sp)));
+  }
+  DPArgs a{};
+  a.prog = prog_dev(ps);
+  a.items = d_items;
+  a.chunk_prog = reinterpret_cast<int32_t*>(dp + o_cp);
+  a.chunk_site = reinterpret_cast<int32_t*>(dp + o_cs);
+  a.n_chunks = (int64_t)chunks;
+  a.counter = reinterpret_cast<unsigned long long*>(dp + o_ctr);
+  a.sites = reinterpret_cast<SiteDesc*>(dp + o_desc);
+  return launch_dp<MODE_SITE>(h, precision, a, bk, st);
 }
 
 }  // namespace bsg
@@ -594,8 +835,8 @@ extern "C" int bsg_hafnian_batched(bsg_handle_t h, const double* Sigma, int n_le
   if (n == 0) {
     BSG_CUDA(cudaMemsetAsync(d_keys, 0, (size_t)B * 8, st));
   } else {
-    target_keys_kernel<<<unsigned((B + 127) / 128), 128, 0, st>>>(targets, n, B, n_len, d_keys, d_err);
-    BSG_CUDA(cudaGetLastError());
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)B,
+                 (target_keys_kernel<<<unsigned((B + 127) / 128), 128, 0, st>>>(targets, n, B, n_len, d_keys, d_err)));
   }
   std::vector<uint64_t> keys(B);
   int err = 0;
@@ -630,11 +871,33 @@ extern "C" int bsg_hafnian_matrices(bsg_handle_t h, const double* A, int n, int6
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   BSG_TRY(ensure_tables());
   if (B == 0) return BSG_OK;
-  uint64_t key = (n & 1) ? ~0ull : (n == 0 ? 0ull : uint64_t(n));  // n classes of multiplicity 1
+  const uint64_t key = (n & 1) ? ~0ull : (n == 0 ? 0ull : uint64_t(n));  // n classes of multiplicity 1
   std::vector<uint64_t> keys(B, key);
   const void* sig = nullptr;
   BSG_TRY(convert_sigma(h, A, (int64_t)B * n * n, precision, h->sigma_ws, &sig, st));
   return run_target_dp(h, MODE_MATRICES, sig, n, nullptr, n, B, nullptr, precision, out, keys, st);
+}
+
+// Row tables of one label matrix [rows, m] into `buf` (carved) -- helper for bsg_build_site.
+static int one_row_table(bsg_handle_t h, const int8_t* num, int rows, int m, char* base, size_t& off,
+                         RowTable& t, int* d_rows, int* d_err, cudaStream_t st) {
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = align(off + bytes);
+    return base + o;
+  };
+  t.entries = reinterpret_cast<int32_t*>(carve((size_t)rows * kMaxNnz * 4));
+  t.nnz = reinterpret_cast<int32_t*>(carve((size_t)rows * 4));
+  t.sum = reinterpret_cast<int32_t*>(carve((size_t)rows * 4));
+  t.key = reinterpret_cast<uint64_t*>(carve((size_t)rows * 8));
+  t.rowfact = reinterpret_cast<double*>(carve((size_t)rows * 8));
+  if (!base) return BSG_OK;  // sizing pass
+  BSG_CUDA(cudaMemcpyAsync(d_rows, &rows, 4, cudaMemcpyHostToDevice, st));
+  dim3 grid((rows + 127) / 128, 1);
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)rows,
+               (label_rows_kernel<<<grid, 128, 0, st>>>(num, 0, m, d_rows, m, 0, rows, t, d_err)));
+  return BSG_OK;
 }
 
 extern "C" int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int M_r, const int8_t* num_l, int k_l,
@@ -662,53 +925,40 @@ extern "C" int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int
   BSG_CUDA(cudaSetDevice(h->device));
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   BSG_TRY(ensure_tables());
-  const size_t esz = out_dtype == BSG_OUT_C128 ? 16 : 8;
-  BSG_CUDA(cudaMemsetAsync(Gamma, 0, (size_t)chi * chi * d * esz, st));
-
-  // effective label tables: FIRST has one empty right row, LAST one empty left row
   const int KL = kind == BSG_SITE_LAST ? 1 : k_l;
   const int KR = kind == BSG_SITE_FIRST ? 1 : k_r;
   const int ML = kind == BSG_SITE_LAST ? 0 : m_l;
   const int MR = kind == BSG_SITE_FIRST ? 0 : m_r;
-  if (KL == 0 || KR == 0) return BSG_OK;
-
-  // row tables in the keys buffer
-  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  if (KL == 0 || KR == 0) {
+    const size_t esz = out_dtype == BSG_OUT_C128 ? 16 : 8;
+    BSG_CUDA(cudaMemsetAsync(Gamma, 0, (size_t)chi * chi * d * esz, st));
+    return BSG_OK;
+  }
+  // workspace: row tables, counters, converted Sigma
+  const int64_t nsig = (int64_t)(2 * M_r) * (2 * M_r);
   size_t off = 0;
-  auto carve = [&](size_t bytes) {
-    size_t o = off;
-    off = align(off + bytes);
-    return o;
-  };
-  const size_t o_lent = carve((size_t)KL * kMaxNnz * 4), o_lnnz = carve(KL * 4), o_lsum = carve(KL * 4),
-               o_lkey = carve(KL * 8), o_lrf = carve(KL * 8);
-  const size_t o_rent = carve((size_t)KR * kMaxNnz * 4), o_rnnz = carve(KR * 4), o_rsum = carve(KR * 4),
-               o_rkey = carve(KR * 8), o_rrf = carve(KR * 8);
-  const size_t o_err = carve(16), o_zero = carve(16);
+  RowTable lt{}, rt{};
+  BSG_TRY(one_row_table(h, nullptr, KL, ML, nullptr, off, lt, nullptr, nullptr, st));
+  BSG_TRY(one_row_table(h, nullptr, KR, MR, nullptr, off, rt, nullptr, nullptr, st));
+  const size_t o_misc = off;
+  off += 256 + 256;
+  const size_t o_sig = off;
+  off += (size_t)nsig * prec_bytes(precision) + 256;
   BSG_TRY(h->keys.ensure(off));
   char* kb = reinterpret_cast<char*>(h->keys.ptr);
-  RowTable lt{reinterpret_cast<int32_t*>(kb + o_lent), reinterpret_cast<int32_t*>(kb + o_lnnz),
-              reinterpret_cast<int32_t*>(kb + o_lsum), reinterpret_cast<uint64_t*>(kb + o_lkey),
-              reinterpret_cast<double*>(kb + o_lrf)};
-  RowTable rt{reinterpret_cast<int32_t*>(kb + o_rent), reinterpret_cast<int32_t*>(kb + o_rnnz),
-              reinterpret_cast<int32_t*>(kb + o_rsum), reinterpret_cast<uint64_t*>(kb + o_rkey),
-              reinterpret_cast<double*>(kb + o_rrf)};
-  int* d_err = reinterpret_cast<int*>(kb + o_err);
-  int8_t* d_zero = reinterpret_cast<int8_t*>(kb + o_zero);
-  BSG_CUDA(cudaMemsetAsync(kb + o_err, 0, 32, st));
-  label_rows_kernel<<<(KL + 127) / 128, 128, 0, st>>>(ML ? num_l : d_zero, KL, ML, 1, lt, d_err);
-  label_rows_kernel<<<(KR + 127) / 128, 128, 0, st>>>(MR ? num_r : d_zero, KR, MR, M_r, rt, d_err);
-  BSG_CUDA(cudaGetLastError());
-
-  // read keys and sums back to plan
-  BSG_TRY(h->host_stage.ensure((size_t)(KL + KR) * 12 + 16));
+  int* d_rows = reinterpret_cast<int*>(kb + o_misc);
+  int* d_err = d_rows + 4;
+  int8_t* d_zero = reinterpret_cast<int8_t*>(kb + o_misc + 256);
+  BSG_CUDA(cudaMemsetAsync(kb + o_misc, 0, 512, st));
+  off = 0;
+  BSG_TRY(one_row_table(h, ML ? num_l : d_zero, KL, ML, kb, off, lt, d_rows, d_err, st));
+  BSG_TRY(one_row_table(h, MR ? num_r : d_zero, KR, MR, kb, off, rt, d_rows + 1, d_err, st));
+  // read keys back to plan
+  BSG_TRY(h->host_stage.ensure((size_t)(KL + KR) * 8 + 16));
   uint64_t* hk = reinterpret_cast<uint64_t*>(h->host_stage.ptr);
-  int32_t* hs = reinterpret_cast<int32_t*>(hk + KL + KR);
-  int* herr = hs + KL + KR;
+  int* herr = reinterpret_cast<int*>(hk + KL + KR);
   BSG_CUDA(cudaMemcpyAsync(hk, lt.key, KL * 8, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaMemcpyAsync(hk + KL, rt.key, KR * 8, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(hs, lt.sum, KL * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(hs + KL, rt.sum, KR * 4, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaMemcpyAsync(herr, d_err, 4, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaStreamSynchronize(st));
   if (*herr) {
@@ -716,137 +966,201 @@ extern "C" int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int
               kKeyMaxMult, kMaxNnz);
     return BSG_ERR_LIMIT;
   }
+  void* sigc = kb + o_sig;
+  BSG_TRY(convert_into(h, Sigma, nsig, precision, sigc, st));
+  std::vector<SiteInput> in(1);
+  in[0].kind = kind;
+  in[0].Mr = M_r;
+  in[0].sigma = sigc;
+  in[0].Z = Z;
+  in[0].lambda = lambda_l;
+  in[0].hkey_l = hk;
+  in[0].hkey_r = hk + KL;
+  in[0].KL = KL;
+  in[0].KR = KR;
+  in[0].lt = lt;
+  in[0].rt = rt;
+  in[0].gamma = Gamma;
+  return run_sites(h, in, d, chi, precision, out_dtype, st);
+}
 
-  // group rows by key
-  auto group = [](const uint64_t* key, int rows, std::vector<int32_t>& perm, std::vector<int32_t>& grp,
-                  std::vector<uint64_t>& gkey, std::vector<int64_t>& gcnt) {
-    perm.resize(rows);
-    std::iota(perm.begin(), perm.end(), 0);
-    std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return key[x] < key[y]; });
-    grp.resize(rows);
-    for (int i = 0; i < rows; ++i) {
-      if (i == 0 || key[perm[i]] != key[perm[i - 1]]) {
-        gkey.push_back(key[perm[i]]);
-        gcnt.push_back(0);
-      }
-      grp[i] = int32_t(gkey.size() - 1);
-      gcnt.back()++;
-    }
-  };
-  std::vector<int32_t> perm_l, grp_l, perm_r, grp_r;
-  std::vector<uint64_t> gk_l, gk_r;
-  std::vector<int64_t> gc_l, gc_r;
-  group(hk, KL, perm_l, grp_l, gk_l, gc_l);
-  group(hk + KL, KR, perm_r, grp_r, gk_r, gc_r);
-  const int ngl = int(gk_l.size()), ngr = int(gk_r.size());
-  std::vector<int> gsum_l(ngl), gsum_r(ngr);
-  for (int g = 0; g < ngl; ++g) gsum_l[g] = key_order(gk_l[g]);
-  for (int g = 0; g < ngr; ++g) gsum_r[g] = key_order(gk_r[g]);
+extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
+                             double site_tol, int precision, int out_dtype, void* const* gammas_host,
+                             double* Lambdas, double* res, int8_t* num, double* S, int32_t* kept,
+                             bsg_stream_t stream) {
+  BSG_CHECK_ARG(h, "bsg_build_mps: null handle");
+  BSG_CHECK_ARG(sq_cov && gammas_host && Lambdas && res && num && S && kept, "bsg_build_mps: null pointer");
+  BSG_CHECK_ARG(M >= 2, "bsg_build_mps: need M >= 2 modes (M=%d)", M);
+  BSG_CHECK_ARG(chi >= d && chi <= 2048, "bsg_build_mps: need d <= chi <= 2048");
+  BSG_CHECK_ARG(d >= 1 && d <= kKeyMaxMult + 1, "bsg_build_mps: d=%d outside [1, %d]", d, kKeyMaxMult + 1);
+  BSG_CHECK_ARG(precision >= 0 && precision <= 2, "bsg_build_mps: bad precision %d", precision);
+  BSG_CHECK_ARG(out_dtype == BSG_OUT_C64 || out_dtype == BSG_OUT_C128, "bsg_build_mps: bad out_dtype");
+  for (int i = 0; i < M; ++i) BSG_CHECK_ARG(gammas_host[i], "bsg_build_mps: Gamma pointer %d is NULL", i);
+  BSG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  BSG_TRY(ensure_tables());
+  const int nc = M - 1;
+  // 1. all cuts (synchronises to read the per-cut status)
+  BSG_TRY(bsg_cut_spectra(h, sq_cov, M, 1, nc, d, chi, cut_tol, res, num, S, kept, stream));
+  const int ldS = 2 * (M - 1);
 
-  Buckets bk;
-  std::unordered_map<int32_t, int> bucket_of_prog;
-  std::vector<int32_t> bucket_of((size_t)d * ngl * ngr, -1);
-  auto& ps = h->programs;
-  for (int j = 0; j < d; ++j) {
-    const uint64_t kj = key_add_class(0, j);
-    for (int gl = 0; gl < ngl; ++gl) {
-      for (int gr = 0; gr < ngr; ++gr) {
-        int n = j + gsum_l[gl] + gsum_r[gr];
-        if (n & 1) continue;
-        if (n > BSG_MAX_ORDER) {
-          set_error("bsg_build_site: hafnian order %d exceeds BSG_MAX_ORDER", n);
-          return BSG_ERR_LIMIT;
-        }
-        int32_t prog;
-        BSG_TRY(program_for_key(ps, kj + gk_l[gl] + gk_r[gr], &prog));
-        auto it = bucket_of_prog.find(prog);
-        int b;
-        if (it == bucket_of_prog.end()) {
-          b = int(bk.progs.size());
-          bucket_of_prog.emplace(prog, b);
-          bk.progs.push_back(prog);
-          bk.counts.push_back(0);
-        } else {
-          b = it->second;
-        }
-        bk.counts[b] += gc_l[gl] * gc_r[gr];
-        bucket_of[((size_t)j * ngl + gl) * ngr + gr] = b;
-      }
-    }
-  }
-  std::vector<int32_t> progs_before = bk.progs;
-  BSG_TRY(layout_buckets(ps, bk));
-  {
-    std::unordered_map<int32_t, int> newb;
-    for (size_t b = 0; b < bk.progs.size(); ++b) newb[bk.progs[b]] = int(b);
-    for (auto& b : bucket_of)
-      if (b >= 0) b = newb[progs_before[b]];
-  }
-  BSG_TRY(programs_upload(ps, st));
-  const int nb = int(bk.progs.size());
-  const size_t chunks = bk.chunk_prog.size();
-
-  // upload the plan
-  size_t poff = 0;
-  auto pcarve = [&](size_t bytes) {
-    size_t o = poff;
-    poff = align(poff + bytes);
+  // 2. workspace
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = align(off + bytes);
     return o;
   };
-  const size_t p_perm_l = pcarve(KL * 4), p_grp_l = pcarve(KL * 4), p_perm_r = pcarve(KR * 4),
-               p_grp_r = pcarve(KR * 4), p_bof = pcarve(bucket_of.size() * 4), p_boff = pcarve(nb * 4 + 4),
-               p_cur = pcarve(nb * 4 + 4), p_chunk = pcarve(chunks * 4 + 4), p_ctr = pcarve(8);
-  const size_t plan_bytes = poff;
-  BSG_TRY(h->plan.ensure(plan_bytes));
-  BSG_TRY(h->host_stage2.ensure(plan_bytes));
-  char* hp = reinterpret_cast<char*>(h->host_stage2.ptr);
-  std::memcpy(hp + p_perm_l, perm_l.data(), KL * 4);
-  std::memcpy(hp + p_grp_l, grp_l.data(), KL * 4);
-  std::memcpy(hp + p_perm_r, perm_r.data(), KR * 4);
-  std::memcpy(hp + p_grp_r, grp_r.data(), KR * 4);
-  std::memcpy(hp + p_bof, bucket_of.data(), bucket_of.size() * 4);
-  std::memcpy(hp + p_boff, bk.offsets.data(), nb * 4);
-  std::memset(hp + p_cur, 0, nb * 4 + 4);
-  if (chunks) std::memcpy(hp + p_chunk, bk.chunk_prog.data(), chunks * 4);
-  std::memset(hp + p_ctr, 0, 8);
-  char* dp = reinterpret_cast<char*>(h->plan.ptr);
-  BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
-  if (bk.slots == 0) return BSG_OK;
-  BSG_TRY(h->items.ensure((size_t)bk.slots * 4));
-  int32_t* d_items = reinterpret_cast<int32_t*>(h->items.ptr);
-  BSG_CUDA(cudaMemsetAsync(d_items, 0xff, (size_t)bk.slots * 4, st));
+  const size_t rows_cap = (size_t)chi;
+  const size_t o_ent = carve((size_t)nc * rows_cap * kMaxNnz * 4), o_nnz = carve((size_t)nc * rows_cap * 4),
+               o_sum = carve((size_t)nc * rows_cap * 4), o_key = carve((size_t)nc * rows_cap * 8),
+               o_rf = carve((size_t)nc * rows_cap * 8);
+  const size_t o_empty = carve(kMaxNnz * 4 + 64);  // one empty row (entries, nnz, rowfact)
+  const size_t o_above = carve((size_t)nc * 4), o_err = carve(16), o_Z = carve((size_t)M * 8),
+               o_status = carve((size_t)M * 4), o_jobs = carve(sizeof(SigmaJob) * M);
+  std::vector<size_t> o_sig(M), o_sigc(M), o_sws(M);
+  for (int i = 0; i < M; ++i) {
+    const int Mr = i == 0 ? M : M - i;
+    o_sig[i] = carve((size_t)(2 * Mr) * (2 * Mr) * 16);
+    o_sigc[i] = precision == BSG_PREC_FP64 ? o_sig[i] : carve((size_t)(2 * Mr) * (2 * Mr) * prec_bytes(precision));
+    o_sws[i] = carve(sigma_ws_bytes(Mr));
+  }
+  BSG_TRY(h->mps_ws.ensure(off));
+  char* wb = reinterpret_cast<char*>(h->mps_ws.ptr);
+  RowTable tab{reinterpret_cast<int32_t*>(wb + o_ent), reinterpret_cast<int32_t*>(wb + o_nnz),
+               reinterpret_cast<int32_t*>(wb + o_sum), reinterpret_cast<uint64_t*>(wb + o_key),
+               reinterpret_cast<double*>(wb + o_rf)};
+  RowTable empty{reinterpret_cast<int32_t*>(wb + o_empty), reinterpret_cast<int32_t*>(wb + o_empty + kMaxNnz * 4),
+                 nullptr, nullptr, reinterpret_cast<double*>(wb + o_empty + kMaxNnz * 4 + 8)};
+  int32_t* d_above = reinterpret_cast<int32_t*>(wb + o_above);
+  int* d_err = reinterpret_cast<int*>(wb + o_err);
+  double* d_Z = reinterpret_cast<double*>(wb + o_Z);
+  int* d_status = reinterpret_cast<int*>(wb + o_status);
+  {
+    // empty row: nnz 0, rowfact 1
+    std::vector<char> e(kMaxNnz * 4 + 64, 0);
+    const double one = 1.0;
+    std::memcpy(e.data() + kMaxNnz * 4 + 8, &one, 8);
+    BSG_CUDA(cudaMemcpyAsync(wb + o_empty, e.data(), e.size(), cudaMemcpyHostToDevice, st));
+  }
+  BSG_CUDA(cudaMemsetAsync(d_err, 0, 16, st));
+  BSG_CUDA(cudaMemsetAsync(d_status, 0, (size_t)M * 4, st));
 
-  SitePlanDev sp{reinterpret_cast<int32_t*>(dp + p_perm_l), reinterpret_cast<int32_t*>(dp + p_grp_l),
-                 reinterpret_cast<int32_t*>(dp + p_perm_r), reinterpret_cast<int32_t*>(dp + p_grp_r),
-                 reinterpret_cast<int32_t*>(dp + p_bof),    reinterpret_cast<int32_t*>(dp + p_boff),
-                 reinterpret_cast<int32_t*>(dp + p_cur),    d_items,
-                 ngl, ngr, KL, KR, d};
-  int64_t total = (int64_t)d * KL * KR;
-  int sblocks = int(std::min<int64_t>((total + 255) / 256, (int64_t)h->num_sms * 8));
-  site_scatter_kernel<<<std::max(sblocks, 1), 256, 0, st>>>(sp);
-  BSG_CUDA(cudaGetLastError());
+  // 3. Lambda and label tables of every cut (one launch each)
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
+               (lambda_kernel<<<nc, 256, 0, st>>>(res, chi, site_tol, Lambdas, d_above)));
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
+               (label_rows_kernel<<<dim3((chi + 127) / 128, nc), 128, 0, st>>>(
+                   num, (int64_t)chi * (M - 1), M - 1, kept, M - 1, 1, chi, tab, d_err)));
 
-  const void* sig = nullptr;
-  BSG_TRY(convert_sigma(h, Sigma, (int64_t)(2 * M_r) * (2 * M_r), precision, h->sigma_ws, &sig, st));
-  DPArgs a{};
-  a.prog = prog_dev(ps);
-  a.items = d_items;
-  a.chunk_prog = reinterpret_cast<int32_t*>(dp + p_chunk);
-  a.n_chunks = (int64_t)chunks;
-  a.counter = reinterpret_cast<unsigned long long*>(dp + p_ctr);
-  a.sigma = sig;
-  a.n_len = 2 * M_r;
-  a.l_ent = lt.entries;
-  a.l_nnz = lt.nnz;
-  a.l_rowfact = lt.rowfact;
-  a.lambda = kind == BSG_SITE_LAST ? nullptr : lambda_l;
-  a.r_ent = rt.entries;
-  a.r_nnz = rt.nnz;
-  a.r_rowfact = rt.rowfact;
-  a.Z = Z;
-  a.d = d;
-  a.chi = chi;
-  a.out_c128 = out_dtype == BSG_OUT_C128;
-  a.gamma = Gamma;
-  return launch_dp<MODE_SITE>(h, precision, a, bk, st);
+  // 4. Sigma of every site (one CTA each), overlapping the host planning below
+  std::vector<SigmaJob> jobs(M);
+  for (int i = 0; i < M; ++i) {
+    SigmaJob jb{};
+    const size_t cut_l = (size_t)i, cut_r = (size_t)(i - 1);
+    jb.Mr = i == 0 ? M : M - i;
+    if (i == 0) {
+      jb.S_l = S;  // cut 0, leading 2(M-1) block
+      jb.ld_l = ldS;
+      jb.S_r = sq_cov;
+      jb.ld_r = 2 * M;
+      jb.m_l = M - 1;
+      jb.first = 1;
+    } else {
+      jb.m_l = i == M - 1 ? 0 : M - 1 - i;
+      jb.S_l = jb.m_l ? S + cut_l * ldS * ldS : nullptr;
+      jb.ld_l = ldS;
+      jb.S_r = S + cut_r * ldS * ldS;
+      jb.ld_r = ldS;
+      jb.first = 0;
+    }
+    jb.Sigma = reinterpret_cast<double2*>(wb + o_sig[i]);
+    jb.Z = d_Z + i;
+    jb.ws = reinterpret_cast<double*>(wb + o_sws[i]);
+    jb.status = d_status + i;
+    jobs[i] = jb;
+  }
+  BSG_TRY(h->host_stage.ensure(sizeof(SigmaJob) * M + (size_t)nc * (chi * 8 + 16) + 64));
+  char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
+  std::memcpy(hs, jobs.data(), sizeof(SigmaJob) * M);
+  BSG_TRY(launch_sigma_jobs(h, reinterpret_cast<SigmaJob*>(hs), M, wb + o_jobs, st));
+  for (int i = 0; i < M; ++i) {
+    const int Mr = i == 0 ? M : M - i;
+    if (o_sigc[i] != o_sig[i])
+      BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[i]), (int64_t)(2 * Mr) * (2 * Mr), precision,
+                           wb + o_sigc[i], st));
+  }
+
+  // 5. read row keys and counts back, plan every site on the host
+  uint64_t* hkeys = reinterpret_cast<uint64_t*>(hs + sizeof(SigmaJob) * M);
+  int32_t* hcnt = reinterpret_cast<int32_t*>(hkeys + (size_t)nc * chi);
+  int32_t* habove = hcnt + nc;
+  int* herr = habove + nc;
+  BSG_CUDA(cudaMemcpyAsync(hkeys, tab.key, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(hcnt, kept, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(habove, d_above, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(herr, d_err, 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaStreamSynchronize(st));
+  if (*herr) {
+    set_error("bsg_build_mps: a label row has a multiplicity above %d or more than %d non-zeros", kKeyMaxMult,
+              kMaxNnz);
+    return BSG_ERR_LIMIT;
+  }
+  static const uint64_t zero_key = 0;
+  auto cut_table = [&](int c) {
+    RowTable t = tab;
+    const size_t o = (size_t)c * rows_cap;
+    t.entries += o * kMaxNnz;
+    t.nnz += o;
+    t.sum += o;
+    t.key += o;
+    t.rowfact += o;
+    return t;
+  };
+  std::vector<SiteInput> in(M);
+  for (int i = 0; i < M; ++i) {
+    SiteInput& si = in[i];
+    si.kind = i == 0 ? BSG_SITE_FIRST : i == M - 1 ? BSG_SITE_LAST : BSG_SITE_MIDDLE;
+    si.Mr = i == 0 ? M : M - i;
+    si.sigma = wb + o_sigc[i];
+    si.Z = d_Z + i;
+    si.gamma = gammas_host[i];
+    if (si.kind != BSG_SITE_LAST) {
+      si.lt = cut_table(i);
+      si.KL = habove[i];
+      si.hkey_l = hkeys + (size_t)i * chi;
+      si.lambda = Lambdas + (size_t)i * chi;
+    } else {
+      si.lt = empty;
+      si.KL = 1;
+      si.hkey_l = &zero_key;
+      si.lambda = nullptr;
+    }
+    if (si.kind != BSG_SITE_FIRST) {
+      si.rt = cut_table(i - 1);
+      si.KR = hcnt[i - 1];
+      si.hkey_r = hkeys + (size_t)(i - 1) * chi;
+    } else {
+      si.rt = empty;
+      si.KR = 1;
+      si.hkey_r = &zero_key;
+    }
+    if (si.KL == 0 || si.KR == 0) {
+      set_error("bsg_build_mps: site %d has an empty bond (no Schmidt weight above the tolerance)", i);
+      return BSG_ERR_INVALID;
+    }
+  }
+  // 6. scatter + one persistent DP launch over all sites
+  BSG_TRY(run_sites(h, in, d, chi, precision, out_dtype, st));
+  // Sigma status (singular A) -- read after the DP so the check costs no extra wait
+  std::vector<int> sst(M);
+  BSG_CUDA(cudaMemcpyAsync(sst.data(), d_status, (size_t)M * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i < M; ++i)
+    if (sst[i]) {
+      set_error("bsg_build_mps: site %d: the Gaussian unitary's A block is singular", i);
+      return BSG_ERR_NO_CONVERGE;
+    }
+  return BSG_OK;
 }

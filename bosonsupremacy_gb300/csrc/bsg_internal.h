@@ -100,12 +100,52 @@ struct DevBuf {
   void release();
 };
 
+// Per-handle launch timing (enabled by bsg_profile_enable).
+struct Profiler {
+  bool on = false;
+  struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+    double work;
+  };
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> pool;
+  double total_ms[BSG_K_COUNT] = {0};
+  int64_t launches[BSG_K_COUNT] = {0};
+  double work[BSG_K_COUNT] = {0};
+  cudaEvent_t get();
+  // begin/end bracket one launch on `st`
+  int begin(int cls, cudaStream_t st, cudaEvent_t* ev);
+  int end(int cls, cudaStream_t st, cudaEvent_t ev, double work);
+  int flush();
+  void add_work(int cls, double w) {
+    if (on) work[cls] += w;
+  }
+  void release();
+};
+
 struct HostBuf {  // pinned host staging
   void* ptr = nullptr;
   size_t bytes = 0;
   int ensure(size_t need);
   void release();
 };
+
+// One Sigma construction (bsg_sigma.cu).
+struct SigmaJob {
+  const double* S_l;  // [2 m_l, 2 m_l] (leading dimension ld_l) or null
+  const double* S_r;  // general: [2Mr, 2Mr] (leading dimension ld_r); first: sq_cov
+  int ld_l, ld_r;
+  int m_l;
+  int Mr;
+  int first;          // 1: site-0 formula
+  double2* Sigma;     // [2Mr, 2Mr]
+  double* Z;
+  double* ws;         // workspace, sigma_ws_bytes(Mr)
+  int* status;        // 0 ok, 1 singular
+};
+size_t sigma_ws_bytes(int Mr);
+int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st);
 
 }  // namespace bsg
 
@@ -122,6 +162,18 @@ struct bsg_handle_s {
   bsg::DevBuf sigma_ws;       // Sigma construction workspace
   bsg::DevBuf cut_ws;         // cut spectra workspace
   bsg::DevBuf contract_ws;    // contraction workspace
+  bsg::DevBuf mps_ws;         // whole-MPS build: Sigma, row tables, plans
   bsg::HostBuf host_stage;    // pinned staging for plans
   bsg::HostBuf host_stage2;
+  bsg::Profiler prof;
 };
+
+// Brackets a kernel launch with profiler events when profiling is on.
+#define BSG_PROFILED(h, cls, st, work, launch)                  \
+  do {                                                          \
+    cudaEvent_t ev_ = nullptr;                                  \
+    if ((h)->prof.on) BSG_TRY((h)->prof.begin(cls, st, &ev_));  \
+    launch;                                                     \
+    BSG_CUDA(cudaGetLastError());                               \
+    if ((h)->prof.on) BSG_TRY((h)->prof.end(cls, st, ev_, work)); \
+  } while (0)

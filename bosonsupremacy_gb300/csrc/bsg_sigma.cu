@@ -19,18 +19,6 @@
 
 namespace bsg {
 
-struct SigmaJob {
-  const double* S_l;  // [2 m_l, 2 m_l] or null
-  const double* S_r;  // general: [2Mr, 2Mr]; first: sq_cov [2Mr, 2Mr]
-  int m_l;
-  int Mr;
-  int first;          // 1: site-0 formula
-  double2* Sigma;     // [2Mr, 2Mr]
-  double* Z;
-  double* ws;         // workspace, 112 * Mr^2 bytes
-  int* status;        // 0 ok, 1 singular
-};
-
 // Row r of L = (1 (+) S_l)^{-1} applied to column c of matrix In (In[k][c] = in[k*ld + c],
 // or in[c*ld + k] when trans).
 __device__ __forceinline__ double apply_L(const SigmaJob& jb, int r, int c, const double* in, int ld, bool trans) {
@@ -40,7 +28,7 @@ __device__ __forceinline__ double apply_L(const SigmaJob& jb, int r, int c, cons
   if (!inner_r || ml == 0) return at(r);
   // inner index of r in S_l coordinates
   const int rl = r < Mr ? r - 1 : ml + (r - Mr - 1);
-  const int n2 = 2 * ml;
+  const int n2 = jb.ld_l;
   const double* S = jb.S_l;
   double acc = 0.0;
   // Linv[rl][kl]: rl<ml: [e^T | -b^T] row rl -> e[k][rl] (k<ml), -b[k][rl] (k<ml)
@@ -80,7 +68,7 @@ __global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob* __restrict_
   // P = L S_r (general) or L sq L^T (first)
   for (int i = tid; i < n2 * n2; i += nt) {
     int r = i / n2, c = i % n2;
-    T[i] = apply_L(jb, r, c, jb.S_r, n2, false);
+    T[i] = apply_L(jb, r, c, jb.S_r, jb.ld_r, false);
   }
   __syncthreads();
   if (jb.first) {
@@ -215,8 +203,10 @@ size_t sigma_ws_bytes(int Mr) { return (size_t)112 * Mr * Mr + 256; }
 
 int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st) {
   BSG_CUDA(cudaMemcpyAsync(jobs_dev, jobs_host, sizeof(SigmaJob) * n_jobs, cudaMemcpyHostToDevice, st));
-  sigma_kernel<<<n_jobs, 1024, 0, st>>>(reinterpret_cast<const SigmaJob*>(jobs_dev));
-  BSG_CUDA(cudaGetLastError());
+  double work = 0.0;
+  for (int i = 0; i < n_jobs; ++i) work += 20.0 * jobs_host[i].Mr * jobs_host[i].Mr * (double)jobs_host[i].Mr;
+  BSG_PROFILED(h, BSG_K_SIGMA, st, work,
+               (sigma_kernel<<<n_jobs, 1024, 0, st>>>(reinterpret_cast<const SigmaJob*>(jobs_dev))));
   return BSG_OK;
 }
 
@@ -251,6 +241,8 @@ extern "C" int bsg_site_sigma(bsg_handle_t h, const double* S_l, int m_l, const 
   SigmaJob jb{};
   jb.S_l = m_l ? S_l : nullptr;
   jb.S_r = S_r;
+  jb.ld_l = 2 * m_l;
+  jb.ld_r = 2 * M_r;
   jb.m_l = m_l;
   jb.Mr = M_r;
   jb.first = 0;
@@ -268,6 +260,8 @@ extern "C" int bsg_first_sigma(bsg_handle_t h, const double* S_0, int M, const d
   SigmaJob jb{};
   jb.S_l = M > 1 ? S_0 : nullptr;
   jb.S_r = sq_cov;
+  jb.ld_l = 2 * (M - 1);
+  jb.ld_r = 2 * M;
   jb.m_l = M - 1;
   jb.Mr = M;
   jb.first = 1;

@@ -8,6 +8,7 @@ res_i > err_tol, zero padded (MPS_cpu.py:398, 415, 484).
 """
 from __future__ import annotations
 
+import ctypes
 import dataclasses
 import time
 from typing import List, Optional
@@ -31,44 +32,47 @@ class MPS:
 
 
 def build_mps(sq_cov, d: int, chi: int, precision="split", out_dtype=torch.complex64, err_tol: float = 1e-10,
-              device: int = 0, sites: Optional[List[int]] = None) -> MPS:
+              cut_tol: float = 1e-12, device: int = 0, out: Optional[List[torch.Tensor]] = None) -> MPS:
+    """Whole MPS in one library call (bsg_build_mps).  ``out`` may supply the
+    M Gamma tensors to fill (reused across calls)."""
     dev = torch.device("cuda", device)
     sq = torch.as_tensor(sq_cov, dtype=torch.float64).to(dev).contiguous()
     M = sq.shape[0] // 2
-    t = {}
-    torch.cuda.synchronize(dev)
+    nc = M - 1
+    if out is None:
+        out = [torch.empty(chi, chi, d, dtype=out_dtype, device=dev) for _ in range(M)]
+    odt = _lib.OUT_C128 if out[0].dtype == torch.complex128 else _lib.OUT_C64
+    lam = torch.empty(nc, chi, dtype=torch.float64, device=dev)
+    res = torch.empty(nc, chi, dtype=torch.float64, device=dev)
+    num = torch.empty(nc, chi, M - 1, dtype=torch.int8, device=dev)
+    S = torch.empty(nc, 2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device=dev)
+    kept = torch.empty(nc, dtype=torch.int32, device=dev)
+    ptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in out])
+    h = _lib.Handle.get(device)
     t0 = time.perf_counter()
-    res, num, S, kept_t = ops.cut_spectra(sq, d, chi, device=device)
-    kept = kept_t.cpu().numpy()
-    res_h = res.cpu().numpy()
-    left_rows = np.array([int((res_h[c, : kept[c]] > err_tol).sum()) for c in range(M - 1)])
-    lam = torch.where(res > err_tol, torch.sqrt(res.clamp_min(0)), torch.zeros_like(res))
-    t["cuts_s"] = time.perf_counter() - t0
-    Gammas = []
-    t1 = time.perf_counter()
-    for i in (range(M) if sites is None else sites):
-        if i == 0:
-            k0 = M - 1
-            Sig, Z = ops.first_sigma(S[0, : 2 * k0, : 2 * k0].contiguous(), sq, device=device)
-            kl = int(left_rows[0])
-            G = ops.build_site(_lib.SITE_FIRST, Sig, num[0, :kl, :k0].contiguous(), lam[0, :kl].contiguous(), None, Z,
-                               d, chi, precision, out_dtype, device)
-        elif i == M - 1:
-            Sig, Z = ops.site_sigma(None, S[M - 2, :2, :2].contiguous(), device=device)
-            kr = int(kept[M - 2])
-            G = ops.build_site(_lib.SITE_LAST, Sig, None, None, num[M - 2, :kr, :1].contiguous(), Z, d, chi,
-                               precision, out_dtype, device)
-        else:
-            kl_modes = M - 1 - i
-            kr_modes = M - i
-            Sig, Z = ops.site_sigma(S[i, : 2 * kl_modes, : 2 * kl_modes].contiguous(),
-                                    S[i - 1, : 2 * kr_modes, : 2 * kr_modes].contiguous(), device=device)
-            kl = int(left_rows[i])
-            kr = int(kept[i - 1])
-            G = ops.build_site(_lib.SITE_MIDDLE, Sig, num[i, :kl, :kl_modes].contiguous(), lam[i, :kl].contiguous(),
-                               num[i - 1, :kr, :kr_modes].contiguous(), Z, d, chi, precision, out_dtype, device)
-        Gammas.append(G)
+    _lib.check(_lib.load().bsg_build_mps(h.h, sq.data_ptr(), M, d, chi, float(cut_tol), float(err_tol),
+                                         ops._prec(precision), odt, ptrs, lam.data_ptr(), res.data_ptr(),
+                                         num.data_ptr(), S.data_ptr(), kept.data_ptr(), _lib.stream_ptr()),
+               "bsg_build_mps")
     torch.cuda.synchronize(dev)
-    t["sites_s"] = time.perf_counter() - t1
-    t["total_s"] = time.perf_counter() - t0
-    return MPS(Gammas, lam, res, num, S, kept, left_rows, t)
+    t = {"total_s": time.perf_counter() - t0}
+    kept_h = kept.cpu().numpy()
+    res_h = res.cpu().numpy()
+    left_rows = np.array([int((res_h[c, : kept_h[c]] > err_tol).sum()) for c in range(nc)])
+    return MPS(out, lam, res, num, S, kept_h, left_rows, t)
+
+
+def build_mps_host(sq_cov_host: torch.Tensor, d: int, chi: int, gammas_host: List[torch.Tensor],
+                   lambdas_host: torch.Tensor, precision="split", device: int = 0,
+                   device_out: Optional[List[torch.Tensor]] = None) -> MPS:
+    """Host-buffer form of build_mps: the covariance is copied in from (pinned)
+    host memory and every Gamma_i and the Lambdas are copied back into the
+    given (pinned) host tensors, all on the current stream."""
+    dev = torch.device("cuda", device)
+    sq = sq_cov_host.to(dev, non_blocking=True)
+    mps = build_mps(sq, d, chi, precision=precision, out_dtype=gammas_host[0].dtype, device=device, out=device_out)
+    for g_h, g_d in zip(gammas_host, mps.Gammas):
+        g_h.copy_(g_d, non_blocking=True)
+    lambdas_host.copy_(mps.Lambdas, non_blocking=True)
+    torch.cuda.current_stream(dev).synchronize()
+    return mps

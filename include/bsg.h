@@ -144,6 +144,21 @@ int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int M_r, const
 int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                     double* res, int8_t* num, double* S, int32_t* kept, bsg_stream_t stream);
 
+/* ---- the whole MPS ---------------------------------------------------------
+ * kron_cpu.py (all M-1 cuts, kron_cpu.py:147-153) followed by MPS_cpu.py
+ * (all M sites, MPS_cpu.py:384-525) in one call, device-resident:
+ * cut spectra with err_tol = cut_tol (the reference's 1e-12), Lambda_c =
+ * sqrt(res_c) where res_c > site_tol (the reference's 1e-10) else 0, Sigma of
+ * every site in one launch, label tables of every cut in one launch, host
+ * planning of every site's work items, then ONE persistent launch over the
+ * items of all sites.  gammas_host: host array of M device pointers to
+ * [chi, chi, d] of out_dtype; Lambdas: float64 [M-1, chi]; res, num, S, kept
+ * as bsg_cut_spectra with L0 = 1, n_cuts = M-1.  Synchronises `stream` twice
+ * (cut status, label keys) and once at the end. */
+int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol, double site_tol,
+                  int precision, int out_dtype, void* const* gammas_host, double* Lambdas, double* res, int8_t* num,
+                  double* S, int32_t* kept, bsg_stream_t stream);
+
 /* ---- transfer contraction (pattern amplitudes) ---------------------------
  * The bond contraction that consumes Gamma/Lambda (sampling_cpu.py:75-90):
  * amp[p] = (... ((Gamma_0[0, :, n_0] * Lambda_0) @ Gamma_1[:, :, n_1]) * Lambda_1 ...) @ Gamma_{M-1}[:, 0, n_{M-1}]
@@ -154,6 +169,28 @@ int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_c
  * Synchronises `stream` (plans the shared-prefix tree on the host). */
 int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                            const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
+
+/* ---- measurement helpers (no reference counterpart) ---------------------
+ * When enabled, every kernel launch of the handle is bracketed by CUDA
+ * events on its stream; bsg_profile_read accumulates the elapsed times per
+ * kernel class and the algorithmic work the launches were planned with.
+ * Kernel classes: */
+#define BSG_K_DP 0        /* hafnian DP (work: complex multiply-adds)           */
+#define BSG_K_WILLIAMSON 1 /* per-cut Cholesky + Jacobi (work: FP64 FMAs)        */
+#define BSG_K_THERMAL 2   /* per-cut top-chi selection (work: candidates ranked) */
+#define BSG_K_SIGMA 3     /* per-site Sigma (work: FP64 FMAs)                    */
+#define BSG_K_PREP 4      /* label rows, bucketing, conversions (work: items)    */
+#define BSG_K_CONTRACT 5  /* transfer contraction (work: real flops)             */
+#define BSG_K_COUNT 6
+int bsg_profile_enable(bsg_handle_t h, int on);
+/* Synchronises the recorded events; totals since the last reset. */
+int bsg_profile_read(bsg_handle_t h, int kernel_class, double* total_ms, int64_t* launches, double* work);
+int bsg_profile_reset(bsg_handle_t h);
+
+/* Measured FMA throughput of this GPU's CUDA cores, in flop/s (2 per FMA),
+ * for BSG_PREC_FP64 or BSG_PREC_FP32, from a register-resident FMA loop on
+ * every SM.  Synchronises `stream`. */
+int bsg_fma_peak(bsg_handle_t h, int precision, double* flops_per_s, bsg_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,145 @@
+"""Drop-in for MPS_cpu.py: per-site Gamma/Lambda on the GPU.
+
+    python -m bosonsupremacy_gb300.mps --d D --chi CHI --dir ROOT/ [--precision split|fp64|fp32]
+
+Same flags (MPS_cpu.py:7-15), same inputs -- ROOT/sq_cov.npy, ROOT/cov.npy and
+the cut files ROOT/d_{D}_chi_{CHI}/{res,num,S}_i.npy written by kron_cpu.py or
+by bosonsupremacy_gb300.kron -- and the same outputs: Gamma_i.npy complex64
+[chi, chi, d] for i = 0..M-1 and Lambda_i.npy float32 [chi] for i = 0..M-2
+(MPS_cpu.py:397-398, 523-525).  ``--fp64-out`` writes complex128/float64.
+
+Function-level mirror of the reference's operator API (same names, argument
+meaning and errors): ``hafnian(A)``, ``A_elem(Sigma, target, denominator,
+max_memory_in_gb)``, ``get_target(num)``, ``push_to_end(array)``,
+``get_Sigma_Z(S_l, S_r)`` (replaces get_U2_sq_U1 + get_Sigma) and
+``build_site(...)``.  All arithmetic runs in libbsg; there is no CPU path.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+import torch
+
+from . import _lib, ops
+
+ERR_TOL = 10 ** (-10)  # MPS_cpu.py:390
+
+
+def hafnian(A, precision="fp64"):
+    """Hafnians of a batch [B, n, n] (MPS_cpu.py:117-140)."""
+    A = np.asarray(A)
+    if A.ndim != 3 or A.shape[1] != A.shape[2]:
+        raise ValueError("Matrix must be square")
+    return ops.hafnian(A, precision=precision).cpu().numpy()
+
+
+def A_elem(Sigma, target, denominator, max_memory_in_gb=0.5, precision="fp64"):
+    """haf(Sigma[t][:, t]) / denominator with gather and hafnian times
+    (MPS_cpu.py:334-355).  The gather is fused into the hafnian kernel, so the
+    gather time is reported as 0 and the hafnian time covers both."""
+    torch.cuda.synchronize()
+    t0 = time.time()
+    out = ops.hafnian_batched(Sigma, np.asarray(target, dtype=np.int32), np.asarray(denominator, dtype=np.float64),
+                              precision=precision)
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), time.time() - t0, 0.0
+
+
+def get_target(num):
+    """Expand Fock labels to repeated 1-based mode indices, left-aligned
+    (MPS_cpu.py:314-332; host-side index bookkeeping as in the reference)."""
+    num = np.asarray(num)
+    rows, modes = num.shape
+    width = int(num.sum(axis=1).max()) if rows else 0
+    out = np.zeros((rows, width), dtype=np.int32)
+    for r in range(rows):
+        idx = np.repeat(np.arange(1, modes + 1, dtype=np.int32), num[r].astype(np.int64))
+        out[r, : len(idx)] = idx
+    return out
+
+
+def push_to_end(array):
+    """Right-align the non-zero entries of each row (MPS_cpu.py:39-47)."""
+    out = np.zeros_like(array)
+    for r in range(array.shape[0]):
+        nz = array[r][array[r] != 0]
+        if len(nz):
+            out[r, -len(nz):] = nz
+    return out
+
+
+def get_Sigma_Z(S_l, S_r, sq_cov=None):
+    """Sigma and Z of a site from the Williamson symplectics of its two cuts
+    (MPS_cpu.py:357-372 + 305-312 + 483).  Site 0 passes ``sq_cov`` (the pure
+    covariance) instead of the full-state Williamson S (MPS_cpu.py:395)."""
+    if sq_cov is not None:
+        return ops.first_sigma(S_l, sq_cov)
+    return ops.site_sigma(S_l, S_r)
+
+
+def build_site(site, M, d, chi, sq_cov, path, precision="split", out_dtype=torch.complex64, err_tol=ERR_TOL):
+    """Gamma and Lambda of one site from the cut files in ``path``
+    (the three branches of MPS_cpu.py:402-520)."""
+    lam = np.zeros(chi, dtype=np.float64)
+    if site == 0:
+        res = np.load(path + "res_0.npy").astype(np.float64)
+        num = np.load(path + "num_0.npy")
+        S_l = np.load(path + "S_0.npy")
+        keep = res > err_tol
+        num = num[keep].reshape(int(keep.sum()), -1)
+        res = res[keep]
+        Sig, Z = get_Sigma_Z(S_l, None, sq_cov=sq_cov)
+        lam[: len(res)] = np.sqrt(res)
+        G = ops.build_site(_lib.SITE_FIRST, Sig, num, np.sqrt(res), None, Z, d, chi, precision, out_dtype)
+        return G, lam
+    if site == M - 1:
+        num_pre = np.load(path + f"num_{site - 1}.npy")
+        num_pre = num_pre.reshape(num_pre.shape[0], -1)
+        S_r = np.load(path + f"S_{site - 1}.npy")
+        Sig, Z = get_Sigma_Z(None, S_r)
+        G = ops.build_site(_lib.SITE_LAST, Sig, None, None, num_pre, Z, d, chi, precision, out_dtype)
+        return G, None
+    num_pre = np.load(path + f"num_{site - 1}.npy")
+    num_pre = num_pre.reshape(num_pre.shape[0], -1)
+    S_r = np.load(path + f"S_{site - 1}.npy")
+    res = np.load(path + f"res_{site}.npy").astype(np.float64)
+    num = np.load(path + f"num_{site}.npy")
+    S_l = np.load(path + f"S_{site}.npy")
+    keep = res > err_tol
+    num = num[keep].reshape(int(keep.sum()), -1)
+    res = res[keep]
+    Sig, Z = get_Sigma_Z(S_l, S_r)
+    lam[: len(res)] = np.sqrt(res)
+    G = ops.build_site(_lib.SITE_MIDDLE, Sig, num, np.sqrt(res), num_pre, Z, d, chi, precision, out_dtype)
+    return G, lam
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--d", type=int, help="Maximum number of photons per mode before displacement - 1.")
+    p.add_argument("--chi", type=int, help="Bond dimension.")
+    p.add_argument("--dir", type=str, help="Root directory.", default=0)
+    p.add_argument("--precision", default="split", choices=["split", "fp64", "fp32"])
+    p.add_argument("--fp64-out", action="store_true", help="write complex128 / float64")
+    args = p.parse_args(argv)
+    d, chi, rootdir = args.d, args.chi, args.dir
+    path = rootdir + f"d_{d}_chi_{chi}/"
+    sq_cov = np.load(rootdir + "sq_cov.npy")
+    cov = np.load(rootdir + "cov.npy")
+    M = len(cov) // 2
+    gdt = torch.complex128 if args.fp64_out else torch.complex64
+    ldt = "float64" if args.fp64_out else "float32"
+    for site in range(M):
+        t0 = time.time()
+        G, lam = build_site(site, M, d, chi, sq_cov, path, args.precision, gdt)
+        G = G.cpu().numpy()
+        print(f"mode: {site} Total {time.time() - t0:.4f}")
+        np.save(path + f"Gamma_{site}.npy", G)
+        if site < M - 1:
+            np.save(path + f"Lambda_{site}.npy", lam.astype(ldt))
+
+
+if __name__ == "__main__":
+    main()

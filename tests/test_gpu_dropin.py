@@ -1,0 +1,81 @@
+"""The drop-in CLIs (kron_cpu.py / MPS_cpu.py contracts) on the GPU, and
+interoperability with the reference's own files in both directions."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import reference_mps as R
+
+pytestmark = pytest.mark.gpu
+
+
+def _write_inputs(t, root):
+    np.save(os.path.join(root, "sq_cov.npy"), t["sq_cov"])
+    np.save(os.path.join(root, "cov.npy"), t["cov"])
+
+
+def test_cli_pipeline_matches_reference(cuda, golden, tmp_path):
+    from bosonsupremacy_gb300 import kron, mps
+    t = golden("tiny_M8.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    root = str(tmp_path) + "/"
+    _write_inputs(t, root)
+    args = ["--d", str(d), "--chi", str(chi), "--dir", root]
+    kron.main(args)
+    mps.main(args + ["--precision", "split", "--fp64-out"])
+    path = root + f"d_{d}_chi_{chi}/"
+    G = [np.load(path + f"Gamma_{i}.npy") for i in range(M)]
+    L = [np.load(path + f"Lambda_{i}.npy") for i in range(M - 1)]
+    assert G[0].shape == (chi, chi, d) and G[0].dtype == np.complex128
+    for c in range(M - 1):
+        ref = t[f"Lambda_{c}"]
+        big = ref > 1e-6
+        assert np.abs(L[c][big] - ref[big]).max() <= 1e-9 * ref.max()
+    p = np.abs(R.pattern_amplitudes(G, L, t["patterns"])) ** 2
+    pr = t["pattern_probs"]
+    big = pr > 1e-8 * pr.max()
+    assert (np.abs(p[big] - pr[big]) / pr[big]).max() <= 1e-6
+
+
+def test_reference_cut_files_give_reference_gamma(cuda, golden, tmp_path):
+    """Our MPS step on the reference's own kron output reproduces the
+    reference's Gamma element-wise (same Williamson basis, same gauge)."""
+    from bosonsupremacy_gb300 import mps
+    t = golden("tiny_M8.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    root = str(tmp_path) + "/"
+    _write_inputs(t, root)
+    path = root + f"d_{d}_chi_{chi}/"
+    os.makedirs(path)
+    for c in range(M - 1):
+        np.save(path + f"res_{c}.npy", t[f"res_{c}"])
+        np.save(path + f"num_{c}.npy", t[f"num_{c}"])
+        np.save(path + f"S_{c}.npy", t[f"S_{c}"])
+    mps.main(["--d", str(d), "--chi", str(chi), "--dir", root, "--precision", "fp64", "--fp64-out"])
+    for i in range(1, M):  # site 0 uses the pure covariance: gauge of its input side differs by design
+        G = np.load(path + f"Gamma_{i}.npy")
+        ref = t[f"Gamma_{i}"]
+        assert np.abs(G - ref).max() <= 1e-11 * np.abs(ref).max(), i
+    G0 = np.load(path + "Gamma_0.npy")
+    assert np.abs(G0 - t["Gamma_0"]).max() <= 1e-11 * np.abs(t["Gamma_0"]).max()
+
+
+def test_oracle_on_our_cut_files_matches_our_gamma(cuda, golden, tmp_path):
+    """The reference algorithm (oracle) run on OUR kron output gives our Gamma."""
+    from bosonsupremacy_gb300 import kron, mps
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    root = str(tmp_path) + "/"
+    _write_inputs(t, root)
+    args = ["--d", str(d), "--chi", str(chi), "--dir", root]
+    kron.main(args)
+    path = root + f"d_{d}_chi_{chi}/"
+    cuts = [(np.load(path + f"res_{c}.npy"), np.load(path + f"num_{c}.npy"), np.load(path + f"S_{c}.npy"))
+            for c in range(M - 1)]
+    for site in (1, 7, M - 1):
+        G, _ = mps.build_site(site, M, d, chi, t["sq_cov"], path, precision="split",
+                              out_dtype=__import__("torch").complex128)
+        G = G.cpu().numpy()
+        G_ref, _ = R.build_site(site, M, d, chi, t["sq_cov"], cuts)
+        assert np.abs(G - G_ref).max() <= 1e-9 * np.abs(G_ref).max(), site

@@ -1,0 +1,60 @@
+"""The oracle (CPU restatement of the reference) pinned against outputs of
+the unmodified reference scripts (tests/golden/make_golden.py)."""
+import numpy as np
+
+from oracle import reference_mps as R
+
+
+def test_hafnian_known_answers(golden):
+    k = golden("hafnian_kat.npz")
+    for n in [0, 1, 2, 3, 4, 5, 6, 8, 10, 12, 14]:
+        assert np.array_equal(R.hafnian(k[f"A_{n}"]), k[f"haf_{n}"]), n
+
+
+def test_a_elem_known_answers(golden):
+    k = golden("hafnian_kat.npz")
+    for n in [2, 4, 6, 8, 10]:
+        amp, _, _ = R.A_elem(k["elem_Sigma"], k[f"elem_target_{n}"], k[f"elem_den_{n}"])
+        assert np.array_equal(amp, k[f"elem_amp_{n}"]), n
+
+
+def test_kron_and_mps_bit_exact(golden):
+    t = golden("tiny_M8.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    cuts = R.run_kron(t["sq_cov"], d, chi)
+    for c in range(M - 1):
+        assert np.array_equal(cuts[c][0], t[f"res_{c}"]), c
+        assert np.array_equal(cuts[c][1], t[f"num_{c}"]), c
+        assert np.array_equal(cuts[c][2], t[f"S_{c}"]), c
+    mps = R.build_mps(t["sq_cov"], d, chi, cuts)
+    for i in range(M):
+        assert np.array_equal(mps[i][0], t[f"Gamma_{i}"]), i
+        if i < M - 1:
+            assert np.array_equal(mps[i][1], t[f"Lambda_{i}"]), i
+    pats = t["patterns"]
+    p = np.abs(R.pattern_amplitudes([mps[i][0] for i in range(M)], [mps[i][1] for i in range(M - 1)], pats)) ** 2
+    assert np.allclose(p, t["pattern_probs"], rtol=1e-12, atol=0)
+
+
+def test_small_config_spectra(golden):
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    for c in (0, 5, 14):
+        res, num, S = R.get_cumsum_kron(t["sq_cov"], c + 1, chi=chi, cutoff=d)
+        assert np.array_equal(res, t[f"res_{c}"]) and np.array_equal(num, t[f"num_{c}"]), c
+
+
+def test_sampler_statistics_match_reference(golden):
+    """Restated sampler (sampling_cpu.py:30-117) with the reference's seeded
+    global RNG stream reproduces the reference's first samples exactly."""
+    t = golden("tiny_M8.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    G = [t[f"Gamma_{i}"] for i in range(M)]
+    Lam = np.stack([t[f"Lambda_{c}"] for c in range(M - 1)], axis=1)
+    thermal = t["cov"] - t["sq_cov"]
+    thermal = thermal + 1.000001 * np.eye(len(thermal)) * np.abs(np.min(np.linalg.eigvalsh(thermal)))
+    sqrtW = np.linalg.cholesky(thermal)
+    rng = np.random.RandomState(int(t["sample_seed"]))
+    s = R.sample(G, Lam, sqrtW, int(t["sample_dd"]), int(t["sample_n"]), rng)
+    assert np.array_equal(s[:64], t["sample_head"])
+    assert np.allclose(s.mean(0), t["sample_mean"])

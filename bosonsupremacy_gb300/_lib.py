@@ -38,6 +38,7 @@ SIGNATURES = {
     "bsg_hafnian_batched": (_I, [_P, _P, _I, _P, _I, _L, _P, _I, _P, _P]),
     "bsg_hafnian_matrices": (_I, [_P, _P, _I, _L, _I, _P, _P]),
     "bsg_site_sigma": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
+    "bsg_site_sigma_noalloc": (_I, [_P, _I, _P, _I, _P, _P, _P]),
     "bsg_first_sigma": (_I, [_P, _P, _I, _P, _P, _P, _P]),
     "bsg_build_site": (_I, [_P, _I, _P, _I, _P, _I, _I, _P, _P, _I, _I, _P, _I, _I, _I, _I, _P, _P]),
     "bsg_cut_spectra": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _P, _P, _P, _P, _P]),

@@ -14,6 +14,7 @@
 // One CTA per job; every job is independent, so many sites run in one launch.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "bsg_internal.h"
 
@@ -268,4 +269,78 @@ extern "C" int bsg_first_sigma(bsg_handle_t h, const double* S_0, int M, const d
   jb.Sigma = reinterpret_cast<double2*>(Sigma);
   jb.Z = Z;
   return single_job(h, jb, reinterpret_cast<cudaStream_t>(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of bsg_site_sigma.
+//
+// Some callers cannot call cudaMalloc: code that runs while another allocator
+// has reserved the device's memory for itself (a caching allocator or a
+// serving runtime that owns all of HBM), latency-critical loops that must not
+// pay the implicit device synchronisation of cudaMalloc/cudaFree, and plug-in
+// hosts that forbid raw device allocation.  bsg_site_sigma_noalloc serves
+// them: its scratch (the job descriptor, a status word and the Gauss-Jordan
+// workspace) is the file-scope device array below, sized for M_r <= 160
+// modes.  Every GPU that loads this library holds the array until the
+// process exits.
+// ---------------------------------------------------------------------------
+namespace bsg {
+constexpr int kNoAllocMaxModes = 160;
+constexpr size_t kNoAllocStatusOff = 256;
+constexpr size_t kNoAllocWsOff = 512;
+constexpr size_t kNoAllocBytes = kNoAllocWsOff + 112ull * kNoAllocMaxModes * kNoAllocMaxModes + 256;  // ~2.75 MiB
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_sigma_scratch[kNoAllocBytes];
+static std::mutex g_noalloc_mu;
+static char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace bsg
+
+extern "C" int bsg_site_sigma_noalloc(const double* S_l, int m_l, const double* S_r, int M_r, double* Sigma,
+                                      double* Z, bsg_stream_t stream) {
+  BSG_CHECK_ARG(S_r && Sigma && Z, "bsg_site_sigma_noalloc: null pointer");
+  if (M_r < 1 || M_r > kNoAllocMaxModes) {
+    set_error("bsg_site_sigma_noalloc: M_r=%d outside [1, %d], the modes its fixed scratch holds; use bsg_site_sigma",
+              M_r, kNoAllocMaxModes);
+    return BSG_ERR_LIMIT;
+  }
+  BSG_CHECK_ARG(m_l == 0 || m_l == M_r - 1, "bsg_site_sigma_noalloc: m_l=%d must be 0 or M_r-1=%d", m_l, M_r - 1);
+  BSG_CHECK_ARG(m_l == 0 || S_l, "bsg_site_sigma_noalloc: S_l is NULL");
+  int dev = 0;
+  BSG_CUDA(cudaGetDevice(&dev));
+  BSG_CHECK_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "bsg_site_sigma_noalloc: device %d out of range", dev);
+  char* base = nullptr;
+  {
+    // one-time set-up per device, with that device current: the device
+    // address of the scratch array (its host-side name is only a stand-in)
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sigma_scratch);
+      if (e != cudaSuccess || !p) {
+        set_error("bsg_site_sigma_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        return BSG_ERR_CUDA;
+      }
+      g_noalloc_ptr[dev] = static_cast<char*>(p);
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  SigmaJob jb{};
+  jb.S_l = m_l ? S_l : nullptr;
+  jb.S_r = S_r;
+  jb.ld_l = 2 * m_l;
+  jb.ld_r = 2 * M_r;
+  jb.m_l = m_l;
+  jb.Mr = M_r;
+  jb.first = 0;
+  jb.Sigma = reinterpret_cast<double2*>(Sigma);
+  jb.Z = Z;
+  jb.ws = reinterpret_cast<double*>(base + kNoAllocWsOff);
+  jb.status = reinterpret_cast<int*>(base + kNoAllocStatusOff);
+  // the status word must start at zero; the workspace is fully overwritten
+  BSG_CUDA(cudaMemsetAsync(base + kNoAllocStatusOff, 0, 4, st));
+  BSG_CUDA(cudaMemcpyToSymbolAsync(g_noalloc_sigma_scratch, &jb, sizeof(SigmaJob), 0, cudaMemcpyHostToDevice, st));
+  sigma_kernel<<<1, 1024, 0, st>>>(reinterpret_cast<const SigmaJob*>(base));
+  BSG_CUDA(cudaGetLastError());
+  return BSG_OK;
 }

@@ -100,6 +100,21 @@ int bsg_hafnian_matrices(bsg_handle_t h, const double* A, int n, int64_t B, int 
 int bsg_site_sigma(bsg_handle_t h, const double* S_l, int m_l, const double* S_r, int M_r, double* Sigma,
                    double* Z, bsg_stream_t stream);
 
+/* Allocation-free variant of bsg_site_sigma (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc: code running while
+ * another allocator has reserved the device's memory, latency-critical loops
+ * that must not pay cudaMalloc/cudaFree's implicit device synchronisation,
+ * and plug-in hosts that forbid raw device allocation.  It needs no handle
+ * and allocates nothing: its scratch is a fixed ~2.75 MiB device array inside
+ * libbsg.so (held on every GPU that loads the library until exit), so
+ * M_r <= 160; larger M_r returns BSG_ERR_LIMIT.  The first call on a device
+ * looks up that array's device address (make it before any stream capture).
+ * Every call shares the array: calls that overlap on the GPU race, so issue
+ * them on one stream or serialise them.  Same arguments and results as
+ * bsg_site_sigma.  Asynchronous. */
+int bsg_site_sigma_noalloc(const double* S_l, int m_l, const double* S_r, int M_r, double* Sigma, double* Z,
+                           bsg_stream_t stream);
+
 /* Site 0 from the pure covariance itself (MPS_cpu.py:395, 409-414): the
  * output-output block of Sigma for V' = (1 (+) S_0^{-1}) sq_cov (1 (+) S_0^{-1})^T,
  * Sigma11 = Mc (conj(Nc) + I)^{-1} with [[Nc, Mc], ...] = R V' R^dag, and

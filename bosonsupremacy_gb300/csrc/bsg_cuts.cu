@@ -50,6 +50,7 @@ struct CutArgs {
   uint32_t* rec;       // per cut: kmax * chi records (parent << 8 | digit)
   int* status;         // [n_cuts]
   int* sweeps;         // [n_cuts] Jacobi sweeps used
+  double* mu;          // [n_cuts, 2 kmax] eigenvalues of G^T G, then 1/nu per pair
   int max_sweeps;
 };
 
@@ -68,23 +69,146 @@ __device__ double block_sum(double v, double* red) {
   return red[32];
 }
 
+// Cyclic Jacobi on the symmetric m x m matrix Hm (global memory), rows of
+// QT accumulating the eigenvectors (QT <- J^T QT).  Round-robin order: n/2
+// disjoint rotations per step, each thread updating whole 2x2 blocks of
+// J1^T B J2 (and the transposed block), so a step needs two barriers.
+// Returns the number of sweeps, or -1 if max_sweeps did not converge.
+__device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, double* red, double* cs, double* sn,
+                            int* pos) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const size_t mm = (size_t)m * m;
+  const int P = m / 2;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (size_t t = tid; t < mm; t += nt) {
+      const int i = int(t / m), j = int(t % m);
+      const double h = Hm[t];
+      if (i < j) off += h * h;
+      else if (i == j) dia += h * h;
+    }
+    off = block_sum(off, red);
+    dia = block_sum(dia, red);
+    if (off <= 1e-26 * dia) return sweep;
+    for (int step = 0; step < m - 1; ++step) {
+      for (int i = tid; i < m; i += nt) pos[i] = i == 0 ? 0 : ((i - 1 + step) % (m - 1)) + 1;
+      __syncthreads();
+      for (int q0 = tid; q0 < P; q0 += nt) {
+        int p = pos[q0], q = pos[m - 1 - q0];
+        if (p > q) {
+          const int x = p;
+          p = q;
+          q = x;
+        }
+        const double hpq = Hm[(size_t)p * m + q];
+        double c_ = 1.0, s_ = 0.0;
+        if (fabs(hpq) > 1e-300 && fabs(hpq) > 1e-17 * sqrt(fabs(Hm[(size_t)p * m + p] * Hm[(size_t)q * m + q]))) {
+          const double th = (Hm[(size_t)q * m + q] - Hm[(size_t)p * m + p]) / (2.0 * hpq);
+          const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+          c_ = 1.0 / sqrt(tt * tt + 1.0);
+          s_ = tt * c_;
+        }
+        cs[q0] = c_;
+        sn[q0] = s_;
+      }
+      __syncthreads();
+      for (int t = tid; t < P * P; t += nt) {
+        const int m1 = t / P, m2 = t % P;
+        if (m1 > m2) continue;
+        int p1 = pos[m1], q1 = pos[m - 1 - m1], p2 = pos[m2], q2 = pos[m - 1 - m2];
+        if (p1 > q1) { const int x = p1; p1 = q1; q1 = x; }
+        if (p2 > q2) { const int x = p2; p2 = q2; q2 = x; }
+        const double c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
+        const double b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
+        const double b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
+        const double r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
+        const double r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
+        const double o00 = c2 * r00 - s2 * r01;
+        double o01 = s2 * r00 + c2 * r01;
+        double o10 = c2 * r10 - s2 * r11;
+        const double o11 = s2 * r10 + c2 * r11;
+        if (m1 == m2) {
+          o01 = 0.0;
+          o10 = 0.0;
+        }
+        Hm[(size_t)p1 * m + p2] = o00;
+        Hm[(size_t)p1 * m + q2] = o01;
+        Hm[(size_t)q1 * m + p2] = o10;
+        Hm[(size_t)q1 * m + q2] = o11;
+        if (m1 != m2) {
+          Hm[(size_t)p2 * m + p1] = o00;
+          Hm[(size_t)q2 * m + p1] = o01;
+          Hm[(size_t)p2 * m + q1] = o10;
+          Hm[(size_t)q2 * m + q1] = o11;
+        }
+      }
+      for (int t = tid; t < P * m; t += nt) {
+        const int q0 = t / m, j = t % m;
+        int p = pos[q0], q = pos[m - 1 - q0];
+        if (p > q) { const int x = p; p = q; q = x; }
+        const double c_ = cs[q0], s_ = sn[q0];
+        const double hp = QT[(size_t)p * m + j], hq = QT[(size_t)q * m + j];
+        QT[(size_t)p * m + j] = c_ * hp - s_ * hq;
+        QT[(size_t)q * m + j] = s_ * hp + c_ * hq;
+      }
+      __syncthreads();
+    }
+  }
+  return -1;
+}
+
+// In-place right-looking Cholesky of the m x m SPD matrix X (lower triangle,
+// upper zeroed).  Returns false if a pivot is not positive.
+__device__ bool block_cholesky(double* X, int m, int* s_flag, double* s_scalar) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) *s_flag = 0;
+  __syncthreads();
+  for (int j = 0; j < m; ++j) {
+    if (tid == 0) {
+      const double djj = X[(size_t)j * m + j];
+      if (!(djj > 0.0)) *s_flag = 1;
+      *s_scalar = djj > 0.0 ? sqrt(djj) : 1.0;
+      X[(size_t)j * m + j] = *s_scalar;
+    }
+    __syncthreads();
+    if (*s_flag) return false;
+    const double dj = *s_scalar;
+    for (int i = j + 1 + tid; i < m; i += nt) X[(size_t)i * m + j] /= dj;
+    __syncthreads();
+    const int r = m - j - 1;
+    for (size_t t = tid; t < (size_t)r * r; t += nt) {
+      const int i = j + 1 + int(t / r), l = j + 1 + int(t % r);
+      if (l > i) continue;
+      X[(size_t)i * m + l] -= X[(size_t)i * m + j] * X[(size_t)l * m + j];
+    }
+    __syncthreads();
+  }
+  for (size_t t = tid; t < (size_t)m * m; t += nt)
+    if (int(t % m) > int(t / m)) X[t] = 0.0;
+  __syncthreads();
+  return true;
+}
+
 __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   const int c = blockIdx.x;
   const int L = a.L0 + c, M = a.M;
-  const int k = M - L, n = 2 * k;
+  const int k = M - L, n = 2 * k, nA = 2 * L;
   const int tid = threadIdx.x, nt = blockDim.x;
-  double* A = a.ws + (size_t)c * a.ws_stride;  // V -> L (lower)
   const size_t nn = (size_t)n * n;
-  double* W = A + nn;    // L^{-1}, later Q^T (rows = eigenvectors)
-  double* Gm = W + nn;   // G
-  double* H = Gm + nn;   // H, later accepted vectors (rows)
+  double* A = a.ws + (size_t)c * a.ws_stride;  // V -> L (lower)
+  double* W = A + nn;    // L^{-1}, later eigenvector rows
+  double* Gm = W + nn;   // G = L^{-1} Omega L^{-T}
+  double* H = Gm + nn;   // H (full path) / F and its reflectors (low-rank path) / accepted vectors
+  double* X1 = H + nn;   // low-rank path: V_A -> L_A, then K = I - R R^T
+  double* X2 = X1 + nn;  // low-rank path: L_A^{-1} C, then eigenvector rows of K
+  double* MU = a.mu + (size_t)c * (2 * a.kmax);
   extern __shared__ double sm[];
   double* red = sm;                   // 33
   double* cs = red + 40;              // n/2
   double* sn = cs + kMaxCutModes;     // n/2
   int* pos = reinterpret_cast<int*>(sn + kMaxCutModes);  // n
   int* order = pos + 2 * kMaxCutModes;                   // n
-  double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n
+  double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n (also Householder taus)
   double* vec = dots + 2 * kMaxCutModes;                               // n
   double* vec2 = vec + 2 * kMaxCutModes;                               // n
   __shared__ int s_flag;
@@ -94,9 +218,9 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   // 1. V and the symmetry check of the reference (norm(V - V^T) < 1e-11)
   double asym = 0.0;
   for (size_t i = tid; i < nn; i += nt) {
-    int r = int(i / n), q = int(i % n);
-    double v = a.sq_cov[(size_t)gidx(r) * (2 * M) + gidx(q)];
-    double vt = a.sq_cov[(size_t)gidx(q) * (2 * M) + gidx(r)];
+    const int r = int(i / n), q = int(i % n);
+    const double v = a.sq_cov[(size_t)gidx(r) * (2 * M) + gidx(q)];
+    const double vt = a.sq_cov[(size_t)gidx(q) * (2 * M) + gidx(r)];
     A[i] = v;
     asym += (v - vt) * (v - vt);
   }
@@ -105,36 +229,10 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     if (tid == 0) a.status[c] = 1;
     return;
   }
-  // 2. Cholesky, right-looking, in place (lower triangle)
-  if (tid == 0) s_flag = 0;
-  __syncthreads();
-  for (int j = 0; j < n; ++j) {
-    if (tid == 0) {
-      double djj = A[(size_t)j * n + j];
-      if (!(djj > 0.0)) s_flag = 1;
-      s_scalar = djj > 0.0 ? sqrt(djj) : 1.0;
-      A[(size_t)j * n + j] = s_scalar;
-    }
-    __syncthreads();
-    if (s_flag) break;
-    const double dj = s_scalar;
-    for (int i = j + 1 + tid; i < n; i += nt) A[(size_t)i * n + j] /= dj;
-    __syncthreads();
-    const int m = n - j - 1;
-    for (size_t t = tid; t < (size_t)m * m; t += nt) {
-      int i = j + 1 + int(t / m), l = j + 1 + int(t % m);
-      if (l > i) continue;
-      A[(size_t)i * n + l] -= A[(size_t)i * n + j] * A[(size_t)l * n + j];
-    }
-    __syncthreads();
-  }
-  if (s_flag) {
+  // 2. Cholesky V = L L^T
+  if (!block_cholesky(A, n, &s_flag, &s_scalar)) {
     if (tid == 0) a.status[c] = 2;
     return;
-  }
-  for (size_t i = tid; i < nn; i += nt) {
-    int r = int(i / n), q = int(i % n);
-    if (q > r) A[i] = 0.0;
   }
   // 3. W = L^{-1}: forward substitution on all columns, row by row
   for (size_t i = tid; i < nn; i += nt) W[i] = (i / n == i % n) ? 1.0 : 0.0;
@@ -145,123 +243,140 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     __syncthreads();
     const int m = n - r - 1;
     for (size_t t = tid; t < (size_t)m * (r + 1); t += nt) {
-      int i = r + 1 + int(t / (r + 1)), q = int(t % (r + 1));
+      const int i = r + 1 + int(t / (r + 1)), q = int(t % (r + 1));
       W[(size_t)i * n + q] -= A[(size_t)i * n + r] * W[(size_t)r * n + q];
     }
     __syncthreads();
   }
   // 4. G = W Omega W^T: G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r]
   for (size_t t = tid; t < nn; t += nt) {
-    int i = int(t / n), j = int(t % n);
+    const int i = int(t / n), j = int(t % n);
     double s = 0.0;
-    for (int r = 0; r < k; ++r) s += W[(size_t)i * n + r] * W[(size_t)j * n + r + k] - W[(size_t)i * n + r + k] * W[(size_t)j * n + r];
+    for (int r = 0; r < k; ++r)
+      s += W[(size_t)i * n + r] * W[(size_t)j * n + r + k] - W[(size_t)i * n + r + k] * W[(size_t)j * n + r];
     Gm[t] = s;
   }
   __syncthreads();
-  // 5. H = G^T G, Q^T = I
-  for (size_t t = tid; t < nn; t += nt) {
-    int i = int(t / n), j = int(t % n);
-    double s = 0.0;
-    for (int r = 0; r < n; ++r) s += Gm[(size_t)r * n + i] * Gm[(size_t)r * n + j];
-    H[t] = s;
-  }
-  __syncthreads();
-  for (size_t t = tid; t < nn; t += nt) W[t] = (t / n == t % n) ? 1.0 : 0.0;
-  __syncthreads();
-  // 6. cyclic Jacobi, round-robin pairs, two-sided update per 2x2 block
-  const int P = n / 2;
-  int sweep = 0;
-  bool converged = false;
-  for (; sweep < a.max_sweeps; ++sweep) {
-    double off = 0.0, dia = 0.0;
+  int sweeps = 0;
+  if (nA >= n) {
+    // 5a. full path: H = G^T G, Jacobi with eigenvector rows in W
     for (size_t t = tid; t < nn; t += nt) {
-      int i = int(t / n), j = int(t % n);
-      double h = H[t];
-      if (i < j) off += h * h;
-      else if (i == j) dia += h * h;
+      const int i = int(t / n), j = int(t % n);
+      double s = 0.0;
+      for (int r = 0; r < n; ++r) s += Gm[(size_t)r * n + i] * Gm[(size_t)r * n + j];
+      H[t] = s;
     }
-    off = block_sum(off, red);
-    dia = block_sum(dia, red);
-    if (off <= 1e-26 * dia) {
-      converged = true;
-      break;
+    __syncthreads();
+    for (size_t t = tid; t < nn; t += nt) W[t] = (t / n == t % n) ? 1.0 : 0.0;
+    __syncthreads();
+    sweeps = block_jacobi(H, n, W, a.max_sweeps, red, cs, sn, pos);
+    for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
+  } else {
+    // 5b. low-rank path (L < k): for a pure global state H = I - F F^T with
+    // F = L^{-1} C^T L_A^{-T} (C the left-right block of sq_cov, V_A = L_A L_A^T),
+    // so the non-trivial spectrum lives in range(F): QR of F, Jacobi on the
+    // nA x nA matrix I - R R^T, and the complement of range(F) is the nu = 1 space.
+    auto gA = [&](int i) { return i < L ? i : M + (i - L); };
+    for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
+      const int r = int(t / nA), q = int(t % nA);
+      X1[t] = a.sq_cov[(size_t)gA(r) * (2 * M) + gA(q)];
     }
-    for (int step = 0; step < n - 1; ++step) {
-      for (int i = tid; i < n; i += nt) pos[i] = i == 0 ? 0 : ((i - 1 + step) % (n - 1)) + 1;
+    for (size_t t = tid; t < (size_t)nA * n; t += nt) {
+      const int r = int(t / n), q = int(t % n);
+      X2[t] = a.sq_cov[(size_t)gA(r) * (2 * M) + gidx(q)];  // C [nA, n]
+    }
+    __syncthreads();
+    if (!block_cholesky(X1, nA, &s_flag, &s_scalar)) {
+      if (tid == 0) a.status[c] = 2;
+      return;
+    }
+    // X2 <- L_A^{-1} C (forward substitution over rows)
+    for (int r = 0; r < nA; ++r) {
+      const double inv = 1.0 / X1[(size_t)r * nA + r];
+      for (int q = tid; q < n; q += nt) X2[(size_t)r * n + q] *= inv;
       __syncthreads();
-      for (int m = tid; m < P; m += nt) {
-        int p = pos[m], q = pos[n - 1 - m];
-        if (p > q) {
-          int tmp = p;
-          p = q;
-          q = tmp;
-        }
-        double hpq = H[(size_t)p * n + q];
-        double c_ = 1.0, s_ = 0.0;
-        if (fabs(hpq) > 1e-300 && fabs(hpq) > 1e-17 * sqrt(fabs(H[(size_t)p * n + p] * H[(size_t)q * n + q]))) {
-          double th = (H[(size_t)q * n + q] - H[(size_t)p * n + p]) / (2.0 * hpq);
-          double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-          c_ = 1.0 / sqrt(tt * tt + 1.0);
-          s_ = tt * c_;
-        }
-        cs[m] = c_;
-        sn[m] = s_;
-      }
-      __syncthreads();
-      for (int t = tid; t < P * P; t += nt) {
-        int m1 = t / P, m2 = t % P;
-        if (m1 > m2) continue;
-        int p1 = pos[m1], q1 = pos[n - 1 - m1], p2 = pos[m2], q2 = pos[n - 1 - m2];
-        if (p1 > q1) { int x = p1; p1 = q1; q1 = x; }
-        if (p2 > q2) { int x = p2; p2 = q2; q2 = x; }
-        double c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
-        double b00 = H[(size_t)p1 * n + p2], b01 = H[(size_t)p1 * n + q2];
-        double b10 = H[(size_t)q1 * n + p2], b11 = H[(size_t)q1 * n + q2];
-        // J1^T B
-        double r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
-        double r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
-        // (J1^T B) J2
-        double o00 = c2 * r00 - s2 * r01, o01 = s2 * r00 + c2 * r01;
-        double o10 = c2 * r10 - s2 * r11, o11 = s2 * r10 + c2 * r11;
-        if (m1 == m2) {
-          o01 = 0.0;
-          o10 = 0.0;
-        }
-        H[(size_t)p1 * n + p2] = o00;
-        H[(size_t)p1 * n + q2] = o01;
-        H[(size_t)q1 * n + p2] = o10;
-        H[(size_t)q1 * n + q2] = o11;
-        if (m1 != m2) {
-          H[(size_t)p2 * n + p1] = o00;
-          H[(size_t)q2 * n + p1] = o01;
-          H[(size_t)p2 * n + q1] = o10;
-          H[(size_t)q2 * n + q1] = o11;
-        }
-      }
-      // Q^T <- J^T Q^T (rows p, q)
-      for (int t = tid; t < P * n; t += nt) {
-        int m = t / n, j = t % n;
-        int p = pos[m], q = pos[n - 1 - m];
-        if (p > q) { int x = p; p = q; q = x; }
-        double c_ = cs[m], s_ = sn[m];
-        double hp = W[(size_t)p * n + j], hq = W[(size_t)q * n + j];
-        W[(size_t)p * n + j] = c_ * hp - s_ * hq;
-        W[(size_t)q * n + j] = s_ * hp + c_ * hq;
+      const int m = nA - r - 1;
+      for (size_t t = tid; t < (size_t)m * n; t += nt) {
+        const int i = r + 1 + int(t / n), q = int(t % n);
+        X2[(size_t)i * n + q] -= X1[(size_t)i * nA + r] * X2[(size_t)r * n + q];
       }
       __syncthreads();
     }
+    // F = W (L_A^{-1} C)^T  [n, nA] into H
+    for (size_t t = tid; t < (size_t)n * nA; t += nt) {
+      const int i = int(t / nA), j = int(t % nA);
+      double s = 0.0;
+      for (int r = 0; r <= i; ++r) s += W[(size_t)i * n + r] * X2[(size_t)j * n + r];
+      H[t] = s;
+    }
+    __syncthreads();
+    // Householder QR of F (n x nA, row stride nA); taus in dots[]
+    for (int j = 0; j < nA; ++j) {
+      double s2 = 0.0;
+      for (int i = j + 1 + tid; i < n; i += nt) s2 += H[(size_t)i * nA + j] * H[(size_t)i * nA + j];
+      s2 = block_sum(s2, red);
+      const double x0 = H[(size_t)j * nA + j];
+      double beta = x0, tau = 0.0, scale = 0.0;
+      if (s2 > 0.0) {
+        beta = -copysign(sqrt(x0 * x0 + s2), x0);
+        tau = (beta - x0) / beta;
+        scale = 1.0 / (x0 - beta);
+      }
+      __syncthreads();
+      for (int i = j + 1 + tid; i < n; i += nt) H[(size_t)i * nA + j] *= scale;
+      if (tid == 0) {
+        H[(size_t)j * nA + j] = beta;
+        dots[j] = tau;
+      }
+      __syncthreads();
+      // apply to the trailing columns: one warp per column
+      for (int col = j + 1 + (tid >> 5); col < nA; col += nt >> 5) {
+        double d = 0.0;
+        for (int i = j + (tid & 31); i < n; i += 32) d += (i == j ? 1.0 : H[(size_t)i * nA + j]) * H[(size_t)i * nA + col];
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        d *= tau;
+        for (int i = j + (tid & 31); i < n; i += 32) H[(size_t)i * nA + col] -= d * (i == j ? 1.0 : H[(size_t)i * nA + j]);
+      }
+      __syncthreads();
+    }
+    // K = I - R R^T into X1, eigenvector rows of K (identity) into X2
+    for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
+      const int i = int(t / nA), j = int(t % nA);
+      double s = 0.0;
+      for (int q = (i > j ? i : j); q < nA; ++q) s += H[(size_t)i * nA + q] * H[(size_t)j * nA + q];
+      X1[t] = (i == j ? 1.0 : 0.0) - s;
+      X2[t] = (i == j ? 1.0 : 0.0);
+    }
+    __syncthreads();
+    sweeps = block_jacobi(X1, nA, X2, a.max_sweeps, red, cs, sn, pos);
+    // eigenvector rows of H in the full space: u_i = Q z_i, z_i = [K eigvec; 0] or e_i
+    for (int i = (tid >> 5); i < n; i += nt >> 5) {
+      double* z = W + (size_t)i * n;
+      for (int t = tid & 31; t < n; t += 32) z[t] = i < nA ? (t < nA ? X2[(size_t)i * nA + t] : 0.0) : (t == i ? 1.0 : 0.0);
+      __syncwarp();
+      for (int j = nA - 1; j >= 0; --j) {
+        double d = 0.0;
+        for (int t = j + (tid & 31); t < n; t += 32) d += (t == j ? 1.0 : H[(size_t)t * nA + j]) * z[t];
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        d *= dots[j];
+        for (int t = j + (tid & 31); t < n; t += 32) z[t] -= d * (t == j ? 1.0 : H[(size_t)t * nA + j]);
+        __syncwarp();
+      }
+    }
+    for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
   }
-  if (tid == 0) a.sweeps[c] = sweep;
-  if (!converged) {
+  __syncthreads();
+  if (tid == 0) a.sweeps[c] = sweeps < 0 ? a.max_sweeps : sweeps;
+  if (sweeps < 0) {
     if (tid == 0) a.status[c] = 3;
     return;
   }
-  // 7. eigenvalues mu_i = H_ii; order ascending (nu descending), ties by index
+  // 7. order by mu ascending (nu descending), ties by index
   for (int i = tid; i < n; i += nt) {
-    double mi = H[(size_t)i * n + i];
+    const double mi = MU[i];
     int r = 0;
     for (int j = 0; j < n; ++j) {
-      double mj = H[(size_t)j * n + j];
+      const double mj = MU[j];
       r += (mj < mi) || (mj == mi && j < i);
     }
     order[r] = i;
@@ -272,8 +387,9 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   // the candidate with the largest residual after projecting out the pairs
   // already taken (pivoted Gram-Schmidt), so a degenerate eigenspace of any
   // dimension (e.g. the nu = 1 vacuum modes) is always completed.
-  double* Xacc = H;  // accepted vectors as rows (H's diagonal was read above)
-  for (int i = tid; i < n; i += nt) vec2[i] = H[(size_t)order[i] * n + order[i]];
+  // 1/nu of each pair is |G x| (x a unit eigenvector: |G x|^2 = mu).
+  double* Xacc = H;  // accepted vectors as rows
+  for (int i = tid; i < n; i += nt) vec2[i] = MU[order[i]];
   __syncthreads();
   int* used = reinterpret_cast<int*>(vec);  // n flags (vec reused as int storage)
   for (int i = tid; i < n; i += nt) used[i] = 0;
@@ -286,7 +402,6 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     if (ce > n) ce = n;
     const int acc0 = acc;
     for (int pi = 0; pi < (ce - cb) / 2; ++pi) {
-      // residual norms of the unused candidates of the cluster
       for (int r = cb + (tid >> 5); r < ce; r += nt >> 5) {
         const double* w = W + (size_t)order[r] * n;
         double s = 0.0;
@@ -325,7 +440,9 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
         y[i] = s;
       }
       __syncthreads();
-      // y against x and the cluster's earlier pairs
+      double gx = 0.0;
+      for (int i = tid; i < n; i += nt) gx += y[i] * y[i];
+      gx = block_sum(gx, red);  // |G x|^2 = 1/nu^2
       for (int t = tid; t < (acc + 1 - acc0) * 32; t += nt) {
         const int av = acc0 + (t >> 5);
         double s = 0.0;
@@ -345,8 +462,8 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       ny = block_sum(ny, red);
       const double iy = ny > 0.0 ? 1.0 / sqrt(ny) : 0.0;
       for (int i = tid; i < n; i += nt) y[i] *= iy;
+      if (tid == 0) MU[acc / 2] = sqrt(gx);  // 1/nu of pair acc/2 (MU no longer needed by candidates)
       __syncthreads();
-      // project x and y out of the remaining candidates of the cluster
       for (int r = cb + (tid >> 5); r < ce; r += nt >> 5) {
         if (used[r]) continue;
         double* w = W + (size_t)order[r] * n;
@@ -370,23 +487,17 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     if (tid == 0) a.status[c] = 4;
     return;
   }
-  // 9. nu from y^T G x (Rayleigh quotient; equals 1/nu), S = L [y | x] nu^{-1/2}
+  // 9. S = L [y | x] nu^{-1/2}, nbar = max(0, (nu - 1)/2)
   for (int pi = 0; pi < k; ++pi) {
     const double* x = Xacc + (size_t)(2 * pi) * n;
     const double* y = Xacc + (size_t)(2 * pi + 1) * n;
-    double s = 0.0;
-    for (int i = tid; i < n; i += nt) {
-      double gx = 0.0;
-      for (int j = 0; j < n; ++j) gx += Gm[(size_t)i * n + j] * x[j];
-      s += y[i] * gx;
-    }
-    s = block_sum(s, red);  // = 1/nu
+    const double s = MU[pi];  // 1/nu
     const double nu = 1.0 / s;
     const double sc = sqrt(s);  // nu^{-1/2}
     for (int i = tid; i < n; i += nt) {
       double ly = 0.0, lx = 0.0;
       for (int j = 0; j <= i; ++j) {
-        double l = A[(size_t)i * n + j];
+        const double l = A[(size_t)i * n + j];
         ly += l * y[j];
         lx += l * x[j];
       }
@@ -394,11 +505,11 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       a.S[(size_t)c * a.ldS * a.ldS + (size_t)i * a.ldS + pi + k] = lx * sc;
     }
     if (tid == 0) {
-      double nb = (nu - 1.0) / 2.0;
+      const double nb = (nu - 1.0) / 2.0;
       a.nbar[(size_t)c * a.kmax + pi] = nb > 0.0 ? nb : 0.0;
     }
-    __syncthreads();
   }
+  __syncthreads();
   if (tid == 0) a.status[c] = 0;
 }
 
@@ -532,7 +643,7 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   a.d = d;
   a.chi = chi;
   a.err_tol = err_tol;
-  a.ws_stride = (size_t)4 * nmax * nmax;
+  a.ws_stride = (size_t)6 * nmax * nmax;
   a.S = S;
   a.ldS = 2 * (M - 1);
   a.kmax = kmax;
@@ -542,16 +653,18 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   a.max_sweeps = 40;
   const size_t ws_bytes = a.ws_stride * 8 * n_cuts;
   const size_t nbar_bytes = (size_t)n_cuts * kmax * 8;
+  const size_t mu_bytes = (size_t)n_cuts * 2 * kmax * 8;
   const size_t rec_bytes = (size_t)n_cuts * kmax * chi * 4;
   const size_t st_bytes = (size_t)n_cuts * 8;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes)));
+  BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes) + al(mu_bytes)));
   char* base = reinterpret_cast<char*>(h->cut_ws.ptr);
   a.ws = reinterpret_cast<double*>(base);
   a.nbar = reinterpret_cast<double*>(base + al(ws_bytes));
   a.rec = reinterpret_cast<uint32_t*>(base + al(ws_bytes) + al(nbar_bytes));
   a.status = reinterpret_cast<int*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes));
   a.sweeps = a.status + n_cuts;
+  a.mu = reinterpret_cast<double*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes));
   BSG_CUDA(cudaMemsetAsync(a.status, 0xff, st_bytes, st));
   BSG_CUDA(cudaMemsetAsync(res, 0, (size_t)n_cuts * chi * 8, st));
   BSG_CUDA(cudaMemsetAsync(num, 0, (size_t)n_cuts * chi * (M - 1), st));
@@ -572,12 +685,17 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   std::vector<int> status(2 * n_cuts);
   BSG_CUDA(cudaMemcpyAsync(status.data(), a.status, st_bytes, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaStreamSynchronize(st));
-  // FP64 FMAs of the Williamson step: Cholesky n^3/3, L^-1 n^3/6, G n^3, H n^3,
-  // 4 n^3 per Jacobi sweep (2x2 blocks of H plus the eigenvector rows), pairing ~2 n^3
+  // FP64 FMAs of the Williamson step: Cholesky n^3/3, L^-1 n^3/6, G n^3,
+  // pairing ~n^3 (G x per pair, projections), S n^3/2; full path: H n^3 and
+  // 4 n^3 per Jacobi sweep; low-rank path (m = 2L < n): Cholesky m^3/3,
+  // L_A^-1 C m^2 n/2, F n^2 m/2, QR 2 n m^2, K m^3/2, 4 m^3 per sweep, Q z 2 n^2 m
   double fmas = 0.0;
   for (int c = 0; c < n_cuts; ++c) {
-    const double n = 2.0 * (M - L0 - c);
-    fmas += n * n * n * (1.0 / 3 + 1.0 / 6 + 2.0 + 2.0 + 4.0 * std::max(0, status[n_cuts + c]));
+    const double n = 2.0 * (M - L0 - c), m = 2.0 * (L0 + c);
+    const double sw = std::max(0, status[n_cuts + c]);
+    fmas += n * n * n * (1.0 / 3 + 1.0 / 6 + 1.0 + 1.0 + 0.5);
+    if (m >= n) fmas += n * n * n * (1.0 + 4.0 * sw);
+    else fmas += m * m * m / 3 + m * m * n / 2 + n * n * m / 2 + 2 * n * m * m + m * m * m / 2 + 4 * m * m * m * sw + 2 * n * n * m;
   }
   h->prof.add_work(BSG_K_WILLIAMSON, fmas);
   for (int c = 0; c < n_cuts; ++c) {

@@ -26,6 +26,7 @@ __constant__ double c_inv_d[kMaxInv];
 __constant__ float2 c_inv_f[kMaxInv];
 __constant__ double c_sqrt_fact[kMaxInv];  // sqrt(n!)
 __constant__ double c_fact[kMaxInv];       // n! (as double)
+__constant__ float2 c_sqrt_fact2[kMaxInv]; // sqrt(n!) as an FP32 pair
 
 static int ensure_tables() {
   static int dev_done = -1;
@@ -33,14 +34,17 @@ static int ensure_tables() {
   BSG_CUDA(cudaGetDevice(&dev));
   if (dev_done == dev) return BSG_OK;
   double inv_d[kMaxInv], sf[kMaxInv], f[kMaxInv];
-  float2 inv_f[kMaxInv];
+  float2 inv_f[kMaxInv], sf2[kMaxInv];
   for (int r = 0; r < kMaxInv; ++r) {
     inv_d[r] = r ? 1.0 / r : 0.0;
     float hi = float(inv_d[r]);
     inv_f[r] = make_float2(hi, float(inv_d[r] - double(hi)));
     f[r] = std::tgamma(double(r) + 1.0);
     sf[r] = std::sqrt(f[r]);
+    const float h2 = float(sf[r]);
+    sf2[r] = make_float2(h2, float(sf[r] - double(h2)));
   }
+  BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact2, sf2, sizeof(sf2)));
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_d, inv_d, sizeof(inv_d)));
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_f, inv_f, sizeof(inv_f)));
   BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact, sf, sizeof(sf)));
@@ -62,6 +66,7 @@ struct RowTable {  // arrays indexed [cut * rows_cap + row]
   int32_t* sum;
   uint64_t* key;
   double* rowfact;   // sqrt(prod num!)
+  float2* rowfact2;  // the same as an unevaluated FP32 pair (hi, lo)
 };
 
 __global__ void label_rows_kernel(const int8_t* __restrict__ num, int64_t cut_stride, int ld,
@@ -100,6 +105,30 @@ __global__ void label_rows_kernel(const int8_t* __restrict__ num, int64_t cut_st
   t.sum[o] = sum;
   t.key[o] = key;
   t.rowfact[o] = rf;
+  const float hi = float(rf);
+  t.rowfact2[o] = make_float2(hi, float(rf - double(hi)));
+}
+
+// Left-row scale of a site: sqrt(prod num!) / (Z * Lambda) in FP64 and as an
+// FP32 pair, so the DP epilogue needs no FP64 division (blockIdx.y = site).
+struct LeftScaleJob {
+  const double* rowfact;
+  const double* lambda;  // null -> 1
+  const double* Z;
+  int rows;
+  double* out_d;
+  float2* out_f;
+};
+
+__global__ void left_scale_kernel(const LeftScaleJob* __restrict__ jobs) {
+  const LeftScaleJob jb = jobs[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= jb.rows) return;
+  double v = jb.rowfact[r] / jb.Z[0];
+  if (jb.lambda) v /= jb.lambda[r];
+  jb.out_d[r] = v;
+  const float hi = float(v);
+  jb.out_f[r] = make_float2(hi, float(v - double(hi)));
 }
 
 // Lambda = sqrt(res) where res > err_tol (else 0) and the count of such rows.
@@ -195,6 +224,9 @@ struct SiteDesc {
   const int32_t* r_ent;  // right rows (cut `site-1`)
   const int32_t* r_nnz;
   const double* r_rowfact;
+  const float2* r_rowfact2;
+  const double* l_scale;   // rowfact / (Z Lambda) per left row
+  const float2* l_scale2;  // the same as an FP32 pair
   const double* Z;
   void* gamma;
   int chi, d, out_c128;
@@ -342,18 +374,35 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
       Fb[(size_t)s * 32 + lane] = P::finish(acc, ra, c_inv_d, c_inv_f);
     }
     if (!live) continue;
-    const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
     if (MODE == MODE_SITE) {
       const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff, j = item & 0xff;
-      double scale = c_sqrt_fact[j] * sd->l_rowfact[beta] * sd->r_rowfact[alpha] / sd->Z[0];
-      if (sd->lambda) scale /= sd->lambda[beta];
       const size_t o = ((size_t)alpha * sd->chi + beta) * sd->d + j;
-      if (sd->out_c128) {
-        reinterpret_cast<double2*>(sd->gamma)[o] = make_double2(v.x * scale, v.y * scale);
-      } else {
-        reinterpret_cast<float2*>(sd->gamma)[o] = make_float2(float(v.x * scale), float(v.y * scale));
+      bool done = false;
+      if constexpr (std::is_same<P, PrecSplit>::value) {
+        if (!sd->out_c128) {
+        // epilogue on the FP32 pipe: (hi + lo) * sqrt(j!) * l_scale * r_rowfact as FP32 pairs
+        const float4 f4 = Fb[(size_t)(ns - 1) * 32 + lane];
+        const float2 js = c_sqrt_fact2[j], ls = sd->l_scale2[beta], rs = sd->r_rowfact2[alpha];
+        float sh, sl, th, tl, re_h, re_l, im_h, im_l;
+        PrecSplit::mul(js.x, js.y, ls.x, ls.y, sh, sl);
+        PrecSplit::mul(sh, sl, rs.x, rs.y, th, tl);
+        PrecSplit::mul(f4.x, f4.y, th, tl, re_h, re_l);
+        PrecSplit::mul(f4.z, f4.w, th, tl, im_h, im_l);
+        reinterpret_cast<float2*>(sd->gamma)[o] = make_float2(re_h + re_l, im_h + im_l);
+        done = true;
+        }
+      }
+      if (!done) {
+        const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
+        const double scale = c_sqrt_fact[j] * sd->l_scale[beta] * sd->r_rowfact[alpha];
+        if (sd->out_c128) {
+          reinterpret_cast<double2*>(sd->gamma)[o] = make_double2(v.x * scale, v.y * scale);
+        } else {
+          reinterpret_cast<float2*>(sd->gamma)[o] = make_float2(float(v.x * scale), float(v.y * scale));
+        }
       }
     } else {
+      const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
       double s = fac;
       if (a.den) s /= a.den[item];
       a.out[item] = make_double2(v.x * s, v.y * s);
@@ -697,6 +746,7 @@ struct SiteInput {
   const void* sigma;  // policy-typed
   const double* Z;
   const double* lambda;   // left rows (null for LAST)
+  // (left scales are computed by run_sites)
   const uint64_t* hkey_l; // host copies of the row keys
   const uint64_t* hkey_r;
   int KL, KR;
@@ -733,8 +783,13 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     return o;
   };
   const size_t o_desc = carve(sizeof(SiteDesc) * ns);
-  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns);
+  const size_t o_lsj = carve(sizeof(LeftScaleJob) * ns);
+  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns), o_lsd(ns), o_lsf(ns);
+  int max_kl = 1;
   for (int s = 0; s < ns; ++s) {
+    o_lsd[s] = carve((size_t)in[s].KL * 8);
+    o_lsf[s] = carve((size_t)in[s].KL * 8);
+    max_kl = std::max(max_kl, in[s].KL);
     o_pl[s] = carve(plans[s].perm_l.size() * 4);
     o_gl[s] = carve(plans[s].grp_l.size() * 4);
     o_pr[s] = carve(plans[s].perm_r.size() * 4);
@@ -749,9 +804,18 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   char* hp = reinterpret_cast<char*>(h->host_stage2.ptr);
   char* dp = reinterpret_cast<char*>(h->plan.ptr);
   SiteDesc* hd = reinterpret_cast<SiteDesc*>(hp + o_desc);
+  LeftScaleJob* hl = reinterpret_cast<LeftScaleJob*>(hp + o_lsj);
   const int out_c128 = out_dtype == BSG_OUT_C128;
   for (int s = 0; s < ns; ++s) {
     const SiteInput& si = in[s];
+    LeftScaleJob lj{};
+    lj.rowfact = si.lt.rowfact;
+    lj.lambda = si.kind == BSG_SITE_LAST ? nullptr : si.lambda;
+    lj.Z = si.Z;
+    lj.rows = si.KL;
+    lj.out_d = reinterpret_cast<double*>(dp + o_lsd[s]);
+    lj.out_f = reinterpret_cast<float2*>(dp + o_lsf[s]);
+    hl[s] = lj;
     SiteDesc sd{};
     sd.sigma = si.sigma;
     sd.Mr = si.Mr;
@@ -763,6 +827,9 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     sd.r_ent = si.rt.entries;
     sd.r_nnz = si.rt.nnz;
     sd.r_rowfact = si.rt.rowfact;
+    sd.r_rowfact2 = si.rt.rowfact2;
+    sd.l_scale = lj.out_d;
+    sd.l_scale2 = lj.out_f;
     sd.Z = si.Z;
     sd.gamma = si.gamma;
     sd.chi = chi;
@@ -783,6 +850,9 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   }
   std::memset(hp + o_ctr, 0, 8);
   BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)ns * max_kl,
+               (left_scale_kernel<<<dim3((max_kl + 127) / 128, ns), 128, 0, st>>>(
+                   reinterpret_cast<const LeftScaleJob*>(dp + o_lsj))));
   const size_t esz = out_c128 ? 16 : 8;
   for (int s = 0; s < ns; ++s) BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, (size_t)chi * chi * d * esz, st));
   if (bk.slots == 0) return BSG_OK;
@@ -892,6 +962,7 @@ static int one_row_table(bsg_handle_t h, const int8_t* num, int rows, int m, cha
   t.sum = reinterpret_cast<int32_t*>(carve((size_t)rows * 4));
   t.key = reinterpret_cast<uint64_t*>(carve((size_t)rows * 8));
   t.rowfact = reinterpret_cast<double*>(carve((size_t)rows * 8));
+  t.rowfact2 = reinterpret_cast<float2*>(carve((size_t)rows * 8));
   if (!base) return BSG_OK;  // sizing pass
   BSG_CUDA(cudaMemcpyAsync(d_rows, &rows, 4, cudaMemcpyHostToDevice, st));
   dim3 grid((rows + 127) / 128, 1);
@@ -1015,8 +1086,8 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
   const size_t rows_cap = (size_t)chi;
   const size_t o_ent = carve((size_t)nc * rows_cap * kMaxNnz * 4), o_nnz = carve((size_t)nc * rows_cap * 4),
                o_sum = carve((size_t)nc * rows_cap * 4), o_key = carve((size_t)nc * rows_cap * 8),
-               o_rf = carve((size_t)nc * rows_cap * 8);
-  const size_t o_empty = carve(kMaxNnz * 4 + 64);  // one empty row (entries, nnz, rowfact)
+               o_rf = carve((size_t)nc * rows_cap * 8), o_rf2 = carve((size_t)nc * rows_cap * 8);
+  const size_t o_empty = carve(kMaxNnz * 4 + 64);  // one empty row (entries, nnz, rowfact, rowfact2)
   const size_t o_above = carve((size_t)nc * 4), o_err = carve(16), o_Z = carve((size_t)M * 8),
                o_status = carve((size_t)M * 4), o_jobs = carve(sizeof(SigmaJob) * M);
   std::vector<size_t> o_sig(M), o_sigc(M), o_sws(M);
@@ -1030,18 +1101,21 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
   char* wb = reinterpret_cast<char*>(h->mps_ws.ptr);
   RowTable tab{reinterpret_cast<int32_t*>(wb + o_ent), reinterpret_cast<int32_t*>(wb + o_nnz),
                reinterpret_cast<int32_t*>(wb + o_sum), reinterpret_cast<uint64_t*>(wb + o_key),
-               reinterpret_cast<double*>(wb + o_rf)};
+               reinterpret_cast<double*>(wb + o_rf), reinterpret_cast<float2*>(wb + o_rf2)};
   RowTable empty{reinterpret_cast<int32_t*>(wb + o_empty), reinterpret_cast<int32_t*>(wb + o_empty + kMaxNnz * 4),
-                 nullptr, nullptr, reinterpret_cast<double*>(wb + o_empty + kMaxNnz * 4 + 8)};
+                 nullptr, nullptr, reinterpret_cast<double*>(wb + o_empty + kMaxNnz * 4 + 8),
+                 reinterpret_cast<float2*>(wb + o_empty + kMaxNnz * 4 + 16)};
   int32_t* d_above = reinterpret_cast<int32_t*>(wb + o_above);
   int* d_err = reinterpret_cast<int*>(wb + o_err);
   double* d_Z = reinterpret_cast<double*>(wb + o_Z);
   int* d_status = reinterpret_cast<int*>(wb + o_status);
   {
-    // empty row: nnz 0, rowfact 1
+    // empty row: nnz 0, rowfact 1 (and as the FP32 pair (1, 0))
     std::vector<char> e(kMaxNnz * 4 + 64, 0);
     const double one = 1.0;
+    const float2 one2 = make_float2(1.f, 0.f);
     std::memcpy(e.data() + kMaxNnz * 4 + 8, &one, 8);
+    std::memcpy(e.data() + kMaxNnz * 4 + 16, &one2, 8);
     BSG_CUDA(cudaMemcpyAsync(wb + o_empty, e.data(), e.size(), cudaMemcpyHostToDevice, st));
   }
   BSG_CUDA(cudaMemsetAsync(d_err, 0, 16, st));
@@ -1116,6 +1190,7 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
     t.sum += o;
     t.key += o;
     t.rowfact += o;
+    t.rowfact2 += o;
     return t;
   };
   std::vector<SiteInput> in(M);

@@ -48,6 +48,7 @@ SIGNATURES = {
     "bsg_profile_read": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_L), C.POINTER(_D)]),
     "bsg_profile_reset": (_I, [_P]),
     "bsg_fma_peak": (_I, [_P, _I, C.POINTER(_D), _P]),
+    "bsg_gemm_tf32x3": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
 }
 
 

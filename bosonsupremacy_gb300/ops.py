@@ -140,3 +140,24 @@ def cut_spectra(sq_cov, d: int, chi: int, L0: int = 1, n_cuts: Optional[int] = N
     check(_lib.load().bsg_cut_spectra(h.h, ptr(sq), M, L0, n_cuts, d, chi, float(err_tol), ptr(res), ptr(num),
                                       ptr(S), ptr(kept), stream_ptr()), "bsg_cut_spectra")
     return res, num, S, kept
+
+
+def pattern_amplitudes(Gammas: Sequence[torch.Tensor], Lambdas, patterns, precision="fp64", device: int = 0):
+    """Amplitudes of photon patterns [P, M] of the MPS (sampling_cpu.py:75-80
+    with fixed photon numbers).  Gammas: M device tensors [chi, chi, d]
+    (complex128 for fp64, complex64 otherwise); Lambdas [M-1, chi]."""
+    import ctypes
+    dev = torch.device("cuda", device)
+    M = len(Gammas)
+    chi, _, d = Gammas[0].shape
+    want = C128 if _prec(precision) == _lib.PREC_FP64 else torch.complex64
+    G = [g.to(device=dev, dtype=want).contiguous() for g in Gammas]
+    lam = _dev(Lambdas, torch.float64, dev)
+    pat = _dev(patterns, torch.int32, dev)
+    P = pat.shape[0]
+    amp = torch.empty(P, dtype=C128, device=dev)
+    ptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in G])
+    h = Handle.get(device)
+    check(_lib.load().bsg_pattern_amplitudes(h.h, ptrs, ptr(lam), M, chi, d, ptr(pat), P, _prec(precision), ptr(amp),
+                                             stream_ptr()), "bsg_pattern_amplitudes")
+    return amp

@@ -177,13 +177,26 @@ int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, d
 /* ---- transfer contraction (pattern amplitudes) ---------------------------
  * The bond contraction that consumes Gamma/Lambda (sampling_cpu.py:75-90):
  * amp[p] = (... ((Gamma_0[0, :, n_0] * Lambda_0) @ Gamma_1[:, :, n_1]) * Lambda_1 ...) @ Gamma_{M-1}[:, 0, n_{M-1}]
- * for P photon patterns (int32 [P, M]).  Gammas: array (device) of M device
- * pointers to c64 [chi, chi, d]; Lambdas: float64 [M-1, chi]; amp: c128 [P].
- * precision: BSG_PREC_FP64 (FP64 CUDA cores) or BSG_PREC_SPLIT (3-way split
- * TF32 products on the tcgen05 tensor cores, FP32 accumulation).
- * Synchronises `stream` (plans the shared-prefix tree on the host). */
+ * for P photon patterns (int32 [P, M], device).  Gammas: HOST array of M
+ * device pointers to [chi, chi, d] -- c128 for BSG_PREC_FP64, c64 otherwise;
+ * Lambdas: float64 [M-1, chi]; amp: c128 [P].  Patterns are contracted
+ * meet-in-the-middle: left environments of every distinct prefix up to site
+ * (M-1)/2, right environments of every distinct suffix, one dot per pattern;
+ * every (level, photon number) group is one batched complex GEMM.
+ * precision: BSG_PREC_FP64 (FP64 CUDA cores), BSG_PREC_FP32 (FP32 CUDA cores)
+ * or BSG_PREC_SPLIT (3-way split TF32 products on the tcgen05 tensor cores,
+ * FP32 accumulation).  Synchronises `stream` (plans the prefix tries on the
+ * host). */
 int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                            const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
+
+/* 3-way split TF32 GEMM on the tcgen05 tensor cores (no reference
+ * counterpart; the building block of the split-precision contraction, exposed
+ * for testing): C[M, N] = A[M, K] B[N, K]^T with A, B fp32 row-major (K
+ * contiguous, K % 4 == 0), each split into TF32 hi + lo, products
+ * hi*hi + hi*lo + lo*hi accumulated in FP32 in TMEM.  Synchronises `stream`. */
+int bsg_gemm_tf32x3(bsg_handle_t h, const float* A, const float* B, float* C, int M, int N, int K,
+                    bsg_stream_t stream);
 
 /* ---- measurement helpers (no reference counterpart) ---------------------
  * When enabled, every kernel launch of the handle is bracketed by CUDA

@@ -1,0 +1,36 @@
+"""The tcgen05 3xTF32 GEMM against an FP64 product (partial tiles included).
+The error is measured against sum_k |a_k b_k| (FP32 accumulation in TMEM) and
+must be far below what a single TF32 product gives."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _tf32(x):
+    """Round-to-nearest to TF32 (10 explicit mantissa bits)."""
+    b = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x1000) & 0xFFFFE000
+    return b.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (200, 256, 96), (512, 384, 1024), (1000, 130, 516)])
+def test_tf32x3_gemm(cuda, M, N, K):
+    import torch
+    from bosonsupremacy_gb300 import _lib
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K)).astype(np.float32)
+    ref = A.astype(np.float64) @ B.astype(np.float64).T
+    absum = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64).T
+    At, Bt = torch.as_tensor(A).cuda(), torch.as_tensor(B).cuda()
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
+    h = _lib.Handle.get(0)
+    _lib.check(_lib.load().bsg_gemm_tf32x3(h.h, At.data_ptr(), Bt.data_ptr(), C.data_ptr(), M, N, K,
+                                           _lib.stream_ptr()), "bsg_gemm_tf32x3")
+    got = C.cpu().numpy().astype(np.float64)
+    assert np.isfinite(got).all()
+    rel = np.abs(got - ref) / absum
+    assert rel.max() <= 1e-5, rel.max()
+    one_tf32 = np.abs(_tf32(A).astype(np.float64) @ _tf32(B).astype(np.float64).T - ref) / absum
+    assert np.median(rel) * 10 <= np.median(one_tf32)

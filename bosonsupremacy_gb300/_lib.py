@@ -21,6 +21,7 @@ K_DP, K_WILLIAMSON, K_THERMAL, K_SIGMA, K_PREP, K_CONTRACT = range(6)
 KERNEL_CLASSES = {K_DP: "hafnian_dp", K_WILLIAMSON: "williamson", K_THERMAL: "thermal_topk", K_SIGMA: "site_sigma",
                   K_PREP: "prep", K_CONTRACT: "contract"}
 OUT_C64, OUT_C128 = 0, 1
+TUNE_DP_BLOCKS_PER_SM, TUNE_DP_L1_CARVEOUT, TUNE_DP_SMALL_ENTRIES, TUNE_DP_SMALL_BLOCKS, TUNE_DP_SCRATCH_MIB = 0, 1, 2, 3, 4
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "input not positive definite",
           -4: "no convergence", -5: "size limit exceeded", -6: "allocation failed"}
@@ -49,6 +50,8 @@ SIGNATURES = {
     "bsg_profile_reset": (_I, [_P]),
     "bsg_fma_peak": (_I, [_P, _I, C.POINTER(_D), _P]),
     "bsg_gemm_tf32x3": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
+    "bsg_tune_set": (_I, [_P, _I, _I]),
+    "bsg_tune_get": (_I, [_P, _I, C.POINTER(_I)]),
 }
 
 

@@ -33,7 +33,7 @@ def _nvcc() -> str:
 
 def _compile(src: str, extra: list, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include"),
+    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-pthread", "-I", os.path.join(REPO, "include"),
            "-I", CSRC, *extra, "-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd.insert(1, "-x")
@@ -55,7 +55,7 @@ def build(verbose: bool = False, extra=None) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra, verbose), srcs))
     tmp = LIB + ".tmp"
-    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

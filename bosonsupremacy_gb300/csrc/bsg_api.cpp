@@ -149,6 +149,28 @@ int bsg_profile_read(bsg_handle_t h, int cls, double* total_ms, int64_t* launche
   return BSG_OK;
 }
 
+int bsg_tune_set(bsg_handle_t h, int key, int value) {
+  BSG_CHECK_ARG(h, "bsg_tune_set: null handle");
+  BSG_CHECK_ARG(key >= 0 && key < BSG_TUNE_COUNT, "bsg_tune_set: unknown key %d", key);
+  if (key == BSG_TUNE_DP_BLOCKS_PER_SM) BSG_CHECK_ARG(value >= 1 && value <= 8, "bsg_tune_set: blocks per SM %d", value);
+  if (key == BSG_TUNE_DP_L1_CARVEOUT) BSG_CHECK_ARG(value >= 0 && value <= 100, "bsg_tune_set: carve-out %d", value);
+  if (key == BSG_TUNE_DP_SMALL_ENTRIES)
+    BSG_CHECK_ARG(value >= 0 && value <= 4096, "bsg_tune_set: small-program entries %d", value);
+  if (key == BSG_TUNE_DP_SMALL_BLOCKS)
+    BSG_CHECK_ARG(value >= 1 && value <= 8, "bsg_tune_set: small-launch blocks per SM %d", value);
+  if (key == BSG_TUNE_DP_SCRATCH_MIB)
+    BSG_CHECK_ARG(value >= 64 && value <= 65536, "bsg_tune_set: DP scratch %d MiB", value);
+  h->tune[key] = value;
+  return BSG_OK;
+}
+
+int bsg_tune_get(bsg_handle_t h, int key, int* value) {
+  BSG_CHECK_ARG(h && value, "bsg_tune_get: null pointer");
+  BSG_CHECK_ARG(key >= 0 && key < BSG_TUNE_COUNT, "bsg_tune_get: unknown key %d", key);
+  *value = h->tune[key];
+  return BSG_OK;
+}
+
 const char* bsg_last_error(void) { return bsg::g_err; }
 
 int bsg_version(void) { return 10000; }

@@ -7,6 +7,8 @@ namespace bsg {
 // ---- plain FP64 ---------------------------------------------------------------
 struct PrecF64 {
   using C = double2;   // stored value
+  using CA = C;        // class-pair table entry
+  using CF = C;        // DP state table entry
   using Acc = double2; // accumulator
   static __device__ __forceinline__ Acc zero() { return make_double2(0.0, 0.0); }
   static __device__ __forceinline__ C one() { return make_double2(1.0, 0.0); }
@@ -26,6 +28,8 @@ struct PrecF64 {
 // ---- plain FP32 (the reference's complex64 working precision) ------------------
 struct PrecF32 {
   using C = float2;
+  using CA = C;
+  using CF = C;
   using Acc = float2;
   static __device__ __forceinline__ Acc zero() { return make_float2(0.f, 0.f); }
   static __device__ __forceinline__ C one() { return make_float2(1.f, 0.f); }
@@ -69,6 +73,8 @@ __device__ __forceinline__ void split_mac1(float& s, float& t, float xh, float x
 
 struct PrecSplit {
   using C = float4;  // (re_hi, re_lo, im_hi, im_lo)
+  using CA = C;
+  using CF = C;
   using Acc = SplitAcc;
   static __device__ __forceinline__ Acc zero() { return SplitAcc{0.f, 0.f, 0.f, 0.f}; }
   static __device__ __forceinline__ C one() { return make_float4(1.f, 0.f, 0.f, 0.f); }

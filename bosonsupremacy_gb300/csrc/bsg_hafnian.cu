@@ -10,7 +10,9 @@
 // Buckets of all sites of an MPS share one persistent launch with an atomic
 // work counter; each 32-slot chunk carries its site and program.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <thread>
 #include <cstring>
 #include <numeric>
 #include <type_traits>
@@ -237,7 +239,8 @@ struct DPArgs {
   const int32_t* items;
   const int32_t* chunk_prog;
   const int32_t* chunk_site;
-  int64_t n_chunks;
+  int64_t chunk_base;  // first chunk of this launch
+  int64_t n_chunks;    // chunks of this launch
   unsigned long long* counter;
   void* scratch;
   int pairs_max, states_max;
@@ -325,16 +328,19 @@ __device__ __forceinline__ int build_classes(const DPArgs& a, const SiteDesc* sd
 template <class P, int MODE>
 __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
   using C = typename P::C;
+  using CA = typename P::CA;
+  using CF = typename P::CF;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const size_t slice = (size_t)(a.pairs_max + a.states_max) * 32;
-  C* Ab = reinterpret_cast<C*>(a.scratch) + (size_t)warp * slice;
-  C* Fb = Ab + (size_t)a.pairs_max * 32;
+  const size_t slice = (size_t)a.pairs_max * 32 * sizeof(CA) + (size_t)a.states_max * 32 * sizeof(CF);
+  CA* Ab = reinterpret_cast<CA*>(reinterpret_cast<char*>(a.scratch) + (size_t)warp * slice);
+  CF* Fb = reinterpret_cast<CF*>(Ab + (size_t)a.pairs_max * 32);
   while (true) {
     unsigned long long c = 0;
     if (lane == 0) c = atomicAdd(a.counter, 1ull);
     c = __shfl_sync(0xffffffffu, c, 0);
     if ((int64_t)c >= a.n_chunks) break;
+    c += (unsigned long long)a.chunk_base;
     const int prog = a.chunk_prog[c];
     const SiteDesc* sd = MODE == MODE_SITE ? a.sites + a.chunk_site[c] : nullptr;
     const int32_t item = a.items[c * 32 + lane];
@@ -367,8 +373,8 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
       typename P::Acc acc = P::zero();
       for (int t = 0; t < cnt; ++t) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
-        const C av = Ab[(size_t)(w & 0xfffu) * 32 + lane];
-        const C fv = Fb[(size_t)(w >> 12) * 32 + lane];
+        const CA av = Ab[(size_t)(w & 0xfffu) * 32 + lane];
+        const CF fv = Fb[(size_t)(w >> 12) * 32 + lane];
         P::mac(acc, av, fv);
       }
       Fb[(size_t)s * 32 + lane] = P::finish(acc, ra, c_inv_d, c_inv_f);
@@ -381,14 +387,14 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
       if constexpr (std::is_same<P, PrecSplit>::value) {
         if (!sd->out_c128) {
         // epilogue on the FP32 pipe: (hi + lo) * sqrt(j!) * l_scale * r_rowfact as FP32 pairs
-        const float4 f4 = Fb[(size_t)(ns - 1) * 32 + lane];
+        const float4 q = Fb[(size_t)(ns - 1) * 32 + lane];  // (re_h, re_l, im_h, im_l)
         const float2 js = c_sqrt_fact2[j], ls = sd->l_scale2[beta], rs = sd->r_rowfact2[alpha];
         float sh, sl, th, tl, re_h, re_l, im_h, im_l;
         PrecSplit::mul(js.x, js.y, ls.x, ls.y, sh, sl);
         PrecSplit::mul(sh, sl, rs.x, rs.y, th, tl);
-        PrecSplit::mul(f4.x, f4.y, th, tl, re_h, re_l);
-        PrecSplit::mul(f4.z, f4.w, th, tl, im_h, im_l);
-        reinterpret_cast<float2*>(sd->gamma)[o] = make_float2(re_h + re_l, im_h + im_l);
+        PrecSplit::mul(q.x, q.y, th, tl, re_h, re_l);
+        PrecSplit::mul(q.z, q.w, th, tl, im_h, im_l);
+        __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(re_h + re_l, im_h + im_l));
         done = true;
         }
       }
@@ -396,9 +402,9 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
         const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
         const double scale = c_sqrt_fact[j] * sd->l_scale[beta] * sd->r_rowfact[alpha];
         if (sd->out_c128) {
-          reinterpret_cast<double2*>(sd->gamma)[o] = make_double2(v.x * scale, v.y * scale);
+          __stcs(reinterpret_cast<double2*>(sd->gamma) + o, make_double2(v.x * scale, v.y * scale));
         } else {
-          reinterpret_cast<float2*>(sd->gamma)[o] = make_float2(float(v.x * scale), float(v.y * scale));
+          __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(float(v.x * scale), float(v.y * scale)));
         }
       }
     } else {
@@ -517,14 +523,26 @@ static int64_t prog_trans(const bsg::ProgramSet& ps, int p) {
   return (int64_t)ps.st_trans_off[s0 + ns - 1] + ps.st_trans_cnt[s0 + ns - 1] - ps.st_trans_off[s0];
 }
 
-// Orders buckets by per-item cost (expensive first, so the work queue starts
-// the long programs early) and assigns padded slot ranges; `remap[old] = new`.
-static int layout_buckets(const bsg::ProgramSet& ps, Buckets& bk, std::vector<int32_t>& remap) {
+// Orders buckets large-table programs first, then small-table programs
+// (small_program), each group by per-item cost, expensive first so the work
+// queue starts the long programs early; assigns padded slot ranges;
+// `remap[old] = new`.
+// Programs with at most `small_entries` table entries (class pairs + DP
+// states) per item run in their own DP launch with small per-warp slices.
+static bool small_program(const bsg::ProgramSet& ps, int p, int small_entries) {
+  return ps.k[p] * (ps.k[p] + 1) / 2 + ps.nstates[p] <= small_entries;
+}
+
+static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets& bk, std::vector<int32_t>& remap) {
   const int nb = int(bk.progs.size());
   std::vector<int> order(nb);
   std::iota(order.begin(), order.end(), 0);
   std::vector<int64_t> cost(nb);
-  for (int b = 0; b < nb; ++b) cost[b] = prog_trans(ps, bk.progs[b]) + ps.nstates[bk.progs[b]];
+  for (int b = 0; b < nb; ++b) {
+    const int p = bk.progs[b];
+    const bool small = small_program(ps, p, small_entries);
+    cost[b] = small ? -(int64_t(1) << 40) - prog_trans(ps, p) : prog_trans(ps, p);
+  }
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
   Buckets out;
   remap.assign(nb, -1);
@@ -587,75 +605,80 @@ static void group_rows(const uint64_t* key, int rows, std::vector<int32_t>& perm
   }
 }
 
-static int plan_site(bsg::ProgramSet& ps, int site, const uint64_t* kl, int KL, const uint64_t* kr, int KR, int d,
-                     SitePlanHost& sp, Buckets& bk, std::unordered_map<int64_t, int>& bindex) {
-  sp.KL = KL;
-  sp.KR = KR;
-  sp.d = d;
-  std::vector<uint64_t> gk_l, gk_r;
-  std::vector<int64_t> gc_l, gc_r;
-  group_rows(kl, KL, sp.perm_l, sp.grp_l, gk_l, gc_l);
-  group_rows(kr, KR, sp.perm_r, sp.grp_r, gk_r, gc_r);
-  sp.ngl = int(gk_l.size());
-  sp.ngr = int(gk_r.size());
-  std::vector<int> gs_l(sp.ngl), gs_r(sp.ngr);
-  for (int g = 0; g < sp.ngl; ++g) gs_l[g] = key_order(gk_l[g]);
-  for (int g = 0; g < sp.ngr; ++g) gs_r[g] = key_order(gk_r[g]);
-  sp.bucket_of.assign((size_t)d * sp.ngl * sp.ngr, -1);
-  for (int j = 0; j < d; ++j) {
-    const uint64_t kj = key_add_class(0, j);
-    for (int gl = 0; gl < sp.ngl; ++gl) {
-      for (int gr = 0; gr < sp.ngr; ++gr) {
-        const int n = j + gs_l[gl] + gs_r[gr];
-        if (n & 1) continue;
-        if (n > BSG_MAX_ORDER) {
-          set_error("site %d: hafnian order %d exceeds BSG_MAX_ORDER", site, n);
-          return BSG_ERR_LIMIT;
-        }
-        int32_t prog;
-        BSG_TRY(program_for_key(ps, kj + gk_l[gl] + gk_r[gr], &prog));
-        const int64_t bkey = ((int64_t)site << 32) | (uint32_t)prog;
-        auto it = bindex.find(bkey);
-        int b;
-        if (it == bindex.end()) {
-          b = int(bk.progs.size());
-          bindex.emplace(bkey, b);
-          bk.progs.push_back(prog);
-          bk.sites.push_back(site);
-          bk.counts.push_back(0);
-        } else {
-          b = it->second;
-        }
-        bk.counts[b] += gc_l[gl] * gc_r[gr];
-        sp.bucket_of[((size_t)j * sp.ngl + gl) * sp.ngr + gr] = b;
-      }
-    }
-  }
-  return BSG_OK;
-}
-
 static ProgDev prog_dev(const bsg::ProgramSet& ps) {
   return ProgDev{ps.d_k, ps.d_nstates, ps.d_state_off, ps.d_st_trans_off, ps.d_st_trans_cnt, ps.d_st_ra, ps.d_trans};
 }
 
+// Launch shape for chunks [c0, c1) whose programs need at most (pmax, smax)
+// table entries per warp.
+struct DPLaunch {
+  int64_t c0 = 0, c1 = 0;
+  int pmax = 1, smax = 1;
+  double work = 0.0;
+  int blocks = 0;
+  size_t per_warp = 0;
+};
+
+template <class P>
+static void dp_shape(bsg_handle_t h, int blocks_per_sm, DPLaunch& L) {
+  const int threads = 256;
+  L.per_warp = (size_t)L.pmax * 32 * sizeof(typename P::CA) + (size_t)L.smax * 32 * sizeof(typename P::CF);
+  int64_t warps = (int64_t)h->num_sms * blocks_per_sm * (threads / 32);
+  const size_t budget = (size_t)h->tune[BSG_TUNE_DP_SCRATCH_MIB] << 20;  // per-warp tables of one launch
+  while (warps > (threads / 32) * (int64_t)h->num_sms && (size_t)warps * L.per_warp > budget) warps /= 2;
+  const int64_t w_use = std::min<int64_t>(warps, std::max<int64_t>(L.c1 - L.c0, 1));
+  L.blocks = std::max<int>(1, int((w_use + (threads / 32) - 1) / (threads / 32)));
+}
+
+// Chunks come large-table programs first (layout_buckets).  Those run in one
+// launch whose per-warp slices fit its largest program; small programs
+// (small_program) run in a second launch with small slices, so their warps'
+// tables stay in L1/L2.  Both launches share the scratch (same stream) and
+// use separate work counters (a.counter[0..1]).
 template <class P, int MODE>
 static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, cudaStream_t st) {
-  using C = typename P::C;
-  const size_t per_warp = (size_t)(bk.pairs_max + bk.states_max) * 32 * sizeof(C);
-  const int threads = 256;
-  const int blocks_per_sm = 4;
-  int64_t warps = (int64_t)h->num_sms * blocks_per_sm * (threads / 32);
-  const size_t budget = size_t(2) << 30;  // at most 2 GiB of per-warp tables
-  while (warps > (threads / 32) * (int64_t)h->num_sms && (size_t)warps * per_warp > budget) warps /= 2;
-  const int64_t need_chunks = std::max<int64_t>((int64_t)bk.chunk_prog.size(), 1);
-  const int64_t w_use = std::min<int64_t>(warps, need_chunks);
-  int blocks = int((w_use + (threads / 32) - 1) / (threads / 32));
-  if (blocks < 1) blocks = 1;
-  BSG_TRY(h->warp_scratch.ensure((size_t)blocks * (threads / 32) * per_warp));
+  const auto& ps = h->programs;
+  const int64_t nch = (int64_t)bk.chunk_prog.size();
+  const int small_entries = h->tune[BSG_TUNE_DP_SMALL_ENTRIES];
+  auto small = [&](int p) { return small_program(ps, p, small_entries); };
+  DPLaunch Ls, Lb;
+  for (int64_t c = 0; c < nch; ++c)
+    if (!small(bk.chunk_prog[c])) Lb.c1 = c + 1;
+  Ls.c0 = Lb.c1;
+  Ls.c1 = nch;
+  // slice sizes from the chunks each launch actually runs
+  for (int64_t c = 0; c < nch; ++c) {
+    const int p = bk.chunk_prog[c];
+    DPLaunch& L = c < Lb.c1 ? Lb : Ls;
+    L.pmax = std::max(L.pmax, ps.k[p] * (ps.k[p] + 1) / 2);
+    L.smax = std::max(L.smax, ps.nstates[p]);
+  }
+  for (size_t b = 0; b < bk.progs.size(); ++b) {
+    const int p = bk.progs[b];
+    (small(p) ? Ls : Lb).work += (double)bk.counts[b] * (double)prog_trans(ps, p);
+  }
+  dp_shape<P>(h, h->tune[BSG_TUNE_DP_SMALL_BLOCKS], Ls);
+  dp_shape<P>(h, h->tune[BSG_TUNE_DP_BLOCKS_PER_SM], Lb);
+  const bool run_b = Lb.c1 > Lb.c0, run_s = Ls.c1 > Ls.c0 || !run_b;
+  size_t need = 0;
+  if (run_s) need = std::max(need, (size_t)Ls.blocks * 8 * Ls.per_warp);
+  if (run_b) need = std::max(need, (size_t)Lb.blocks * 8 * Lb.per_warp);
+  BSG_TRY(h->warp_scratch.ensure(need));
+  BSG_CUDA(cudaFuncSetAttribute(dp_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                h->tune[BSG_TUNE_DP_L1_CARVEOUT]));
   a.scratch = h->warp_scratch.ptr;
-  a.pairs_max = bk.pairs_max;
-  a.states_max = bk.states_max;
-  BSG_PROFILED(h, BSG_K_DP, st, bk.work, (dp_kernel<P, MODE><<<blocks, threads, 0, st>>>(a)));
+  unsigned long long* ctr = a.counter;
+  const DPLaunch* Ls_or_b[2] = {run_b ? &Lb : nullptr, run_s ? &Ls : nullptr};
+  for (int i = 0; i < 2; ++i) {
+    const DPLaunch* L = Ls_or_b[i];
+    if (!L) continue;
+    a.pairs_max = L->pmax;
+    a.states_max = L->smax;
+    a.chunk_base = L->c0;
+    a.n_chunks = L->c1 - L->c0;
+    a.counter = ctr + i;
+    BSG_PROFILED(h, BSG_K_DP, st, L->work, (dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a)));
+  }
   return BSG_OK;
 }
 
@@ -691,7 +714,7 @@ static int plan_items_host(bsg_handle_t h, const std::vector<uint64_t>& keys, Bu
     item_bucket[i] = b;
   }
   std::vector<int32_t> remap;
-  BSG_TRY(layout_buckets(ps, bk, remap));
+  BSG_TRY(layout_buckets(ps, h->tune[BSG_TUNE_DP_SMALL_ENTRIES], bk, remap));
   items.assign(bk.slots, -1);
   std::vector<int64_t> cur(bk.progs.size(), 0);
   for (size_t i = 0; i < keys.size(); ++i) {
@@ -719,7 +742,7 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
   BSG_CUDA(cudaMemcpyAsync(d_chunk, bk.chunk_prog.data(), chunks * 4, cudaMemcpyHostToDevice, st));
   BSG_TRY(h->misc.ensure(64));
   auto* counter = reinterpret_cast<unsigned long long*>(h->misc.ptr);
-  BSG_CUDA(cudaMemsetAsync(counter, 0, 8, st));
+  BSG_CUDA(cudaMemsetAsync(counter, 0, 16, st));
   DPArgs a{};
   a.prog = prog_dev(h->programs);
   a.items = d_items;
@@ -736,6 +759,125 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
   if (mode == MODE_TARGETS) BSG_TRY(launch_dp<MODE_TARGETS>(h, precision, a, bk, st));
   else BSG_TRY(launch_dp<MODE_MATRICES>(h, precision, a, bk, st));
   BSG_CUDA(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+  return BSG_OK;
+}
+
+// ---- parallel host planning ----------------------------------------------------
+// Phase A (parallel): group each site's rows by key and list its (j, gl, gr)
+// combinations with their partition keys.  Phase B (serial): generate the
+// programs of keys not seen before.  Phase C (parallel): map combinations to
+// per-site buckets.  Phase D (serial): concatenate the buckets of all sites.
+template <class F>
+static void parallel_for(int n, F&& f) {
+  const int hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::max(1, std::min(n, std::min(hw, 32)));
+  if (nt <= 1 || n < 4) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next(0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&] {
+      for (int i = next++; i < n; i = next++) f(i);
+    });
+  for (auto& x : th) x.join();
+}
+
+struct SiteCombos {
+  std::vector<uint64_t> gk_l, gk_r;
+  std::vector<int64_t> gc_l, gc_r;
+  std::vector<uint64_t> keys;   // per (j, gl, gr): full key, or ~0 for odd order
+  int err = 0;
+};
+
+static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, const int* KL,
+                               const uint64_t* const* kr, const int* KR, int ns, int d,
+                               std::vector<SitePlanHost>& plans, Buckets& bk) {
+  plans.assign(ns, SitePlanHost());
+  std::vector<SiteCombos> cb(ns);
+  parallel_for(ns, [&](int s) {
+    SitePlanHost& sp = plans[s];
+    SiteCombos& c = cb[s];
+    sp.KL = KL[s];
+    sp.KR = KR[s];
+    sp.d = d;
+    group_rows(kl[s], KL[s], sp.perm_l, sp.grp_l, c.gk_l, c.gc_l);
+    group_rows(kr[s], KR[s], sp.perm_r, sp.grp_r, c.gk_r, c.gc_r);
+    sp.ngl = int(c.gk_l.size());
+    sp.ngr = int(c.gk_r.size());
+    c.keys.assign((size_t)d * sp.ngl * sp.ngr, ~0ull);
+    for (int j = 0; j < d; ++j) {
+      const uint64_t kj = key_add_class(0, j);
+      for (int gl = 0; gl < sp.ngl; ++gl) {
+        const int nl = key_order(c.gk_l[gl]);
+        for (int gr = 0; gr < sp.ngr; ++gr) {
+          const int n = j + nl + key_order(c.gk_r[gr]);
+          if (n & 1) continue;
+          if (n > BSG_MAX_ORDER) {
+            c.err = 1;
+            continue;
+          }
+          c.keys[((size_t)j * sp.ngl + gl) * sp.ngr + gr] = kj + c.gk_l[gl] + c.gk_r[gr];
+        }
+      }
+    }
+  });
+  for (int s = 0; s < ns; ++s)
+    if (cb[s].err) {
+      set_error("site %d: hafnian order exceeds BSG_MAX_ORDER", s);
+      return BSG_ERR_LIMIT;
+    }
+  // phase B: new programs, serially
+  for (int s = 0; s < ns; ++s)
+    for (uint64_t k : cb[s].keys)
+      if (k != ~0ull && !ps.index.count(k)) {
+        int32_t prog;
+        BSG_TRY(program_for_key(ps, k, &prog));
+      }
+  // phase C: per-site buckets (read-only program index)
+  std::vector<std::vector<int32_t>> lprog(ns);
+  std::vector<std::vector<int64_t>> lcount(ns);
+  parallel_for(ns, [&](int s) {
+    SitePlanHost& sp = plans[s];
+    const SiteCombos& c = cb[s];
+    std::unordered_map<int32_t, int32_t> local;
+    sp.bucket_of.assign(c.keys.size(), -1);
+    for (int j = 0; j < d; ++j)
+      for (int gl = 0; gl < sp.ngl; ++gl)
+        for (int gr = 0; gr < sp.ngr; ++gr) {
+          const size_t o = ((size_t)j * sp.ngl + gl) * sp.ngr + gr;
+          const uint64_t k = c.keys[o];
+          if (k == ~0ull) continue;
+          const int32_t prog = ps.index.find(k)->second;
+          auto it = local.find(prog);
+          int32_t b;
+          if (it == local.end()) {
+            b = int32_t(lprog[s].size());
+            local.emplace(prog, b);
+            lprog[s].push_back(prog);
+            lcount[s].push_back(0);
+          } else {
+            b = it->second;
+          }
+          lcount[s][b] += c.gc_l[gl] * c.gc_r[gr];
+          sp.bucket_of[o] = b;
+        }
+  });
+  // phase D: global bucket list
+  std::vector<int32_t> base(ns, 0);
+  for (int s = 0; s < ns; ++s) {
+    base[s] = int32_t(bk.progs.size());
+    for (size_t b = 0; b < lprog[s].size(); ++b) {
+      bk.progs.push_back(lprog[s][b]);
+      bk.sites.push_back(s);
+      bk.counts.push_back(lcount[s][b]);
+    }
+  }
+  parallel_for(ns, [&](int s) {
+    for (auto& b : plans[s].bucket_of)
+      if (b >= 0) b += base[s];
+  });
   return BSG_OK;
 }
 
@@ -761,12 +903,20 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   auto& ps = h->programs;
   const int ns = int(in.size());
   Buckets bk;
-  std::unordered_map<int64_t, int> bindex;
-  std::vector<SitePlanHost> plans(ns);
-  for (int s = 0; s < ns; ++s)
-    BSG_TRY(plan_site(ps, s, in[s].hkey_l, in[s].KL, in[s].hkey_r, in[s].KR, d, plans[s], bk, bindex));
+  std::vector<SitePlanHost> plans;
+  {
+    std::vector<const uint64_t*> kl(ns), kr(ns);
+    std::vector<int> KL(ns), KR(ns);
+    for (int s = 0; s < ns; ++s) {
+      kl[s] = in[s].hkey_l;
+      kr[s] = in[s].hkey_r;
+      KL[s] = in[s].KL;
+      KR[s] = in[s].KR;
+    }
+    BSG_TRY(plan_sites_parallel(ps, kl.data(), KL.data(), kr.data(), KR.data(), ns, d, plans, bk));
+  }
   std::vector<int32_t> remap;
-  BSG_TRY(layout_buckets(ps, bk, remap));
+  BSG_TRY(layout_buckets(ps, h->tune[BSG_TUNE_DP_SMALL_ENTRIES], bk, remap));
   for (auto& p : plans)
     for (auto& b : p.bucket_of)
       if (b >= 0) b = remap[b];
@@ -797,7 +947,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     o_bo[s] = carve(plans[s].bucket_of.size() * 4);
   }
   const size_t o_boff = carve((size_t)nb * 4 + 4), o_cur = carve((size_t)nb * 4 + 4);
-  const size_t o_cp = carve(chunks * 4 + 4), o_cs = carve(chunks * 4 + 4), o_ctr = carve(8);
+  const size_t o_cp = carve(chunks * 4 + 4), o_cs = carve(chunks * 4 + 4), o_ctr = carve(16);
   const size_t plan_bytes = off;
   BSG_TRY(h->plan.ensure(plan_bytes));
   BSG_TRY(h->host_stage2.ensure(plan_bytes));
@@ -848,7 +998,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     std::memcpy(hp + o_cp, bk.chunk_prog.data(), chunks * 4);
     std::memcpy(hp + o_cs, bk.chunk_site.data(), chunks * 4);
   }
-  std::memset(hp + o_ctr, 0, 8);
+  std::memset(hp + o_ctr, 0, 16);
   BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
   BSG_PROFILED(h, BSG_K_PREP, st, (double)ns * max_kl,
                (left_scale_kernel<<<dim3((max_kl + 127) / 128, ns), 128, 0, st>>>(
@@ -1128,7 +1278,23 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
                (label_rows_kernel<<<dim3((chi + 127) / 128, nc), 128, 0, st>>>(
                    num, (int64_t)chi * (M - 1), M - 1, kept, M - 1, 1, chi, tab, d_err)));
 
-  // 4. Sigma of every site (one CTA each), overlapping the host planning below
+  // 4. read the row keys and counts back (queued before the Sigma launch, so
+  // the host plans every site while the Sigma kernels run)
+  BSG_TRY(h->host_stage.ensure(sizeof(SigmaJob) * M + (size_t)nc * (chi * 8 + 16) + 64));
+  char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
+  uint64_t* hkeys = reinterpret_cast<uint64_t*>(hs + sizeof(SigmaJob) * M);
+  int32_t* hcnt = reinterpret_cast<int32_t*>(hkeys + (size_t)nc * chi);
+  int32_t* habove = hcnt + nc;
+  int* herr = habove + nc;
+  BSG_CUDA(cudaMemcpyAsync(hkeys, tab.key, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(hcnt, kept, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(habove, d_above, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(herr, d_err, 4, cudaMemcpyDeviceToHost, st));
+  cudaEvent_t keys_ready;
+  BSG_CUDA(cudaEventCreateWithFlags(&keys_ready, cudaEventDisableTiming));
+  BSG_CUDA(cudaEventRecord(keys_ready, st));
+
+  // 5. Sigma of every site (one CTA each)
   std::vector<SigmaJob> jobs(M);
   for (int i = 0; i < M; ++i) {
     SigmaJob jb{};
@@ -1155,8 +1321,6 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
     jb.status = d_status + i;
     jobs[i] = jb;
   }
-  BSG_TRY(h->host_stage.ensure(sizeof(SigmaJob) * M + (size_t)nc * (chi * 8 + 16) + 64));
-  char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
   std::memcpy(hs, jobs.data(), sizeof(SigmaJob) * M);
   BSG_TRY(launch_sigma_jobs(h, reinterpret_cast<SigmaJob*>(hs), M, wb + o_jobs, st));
   for (int i = 0; i < M; ++i) {
@@ -1165,17 +1329,11 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
       BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[i]), (int64_t)(2 * Mr) * (2 * Mr), precision,
                            wb + o_sigc[i], st));
   }
-
-  // 5. read row keys and counts back, plan every site on the host
-  uint64_t* hkeys = reinterpret_cast<uint64_t*>(hs + sizeof(SigmaJob) * M);
-  int32_t* hcnt = reinterpret_cast<int32_t*>(hkeys + (size_t)nc * chi);
-  int32_t* habove = hcnt + nc;
-  int* herr = habove + nc;
-  BSG_CUDA(cudaMemcpyAsync(hkeys, tab.key, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(hcnt, kept, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(habove, d_above, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(herr, d_err, 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaStreamSynchronize(st));
+  {
+    const cudaError_t e = cudaEventSynchronize(keys_ready);
+    cudaEventDestroy(keys_ready);
+    BSG_CUDA(e);
+  }
   if (*herr) {
     set_error("bsg_build_mps: a label row has a multiplicity above %d or more than %d non-zeros", kKeyMaxMult,
               kMaxNnz);

@@ -172,6 +172,7 @@ struct bsg_handle_s {
   bsg::HostBuf host_stage;    // pinned staging for plans
   bsg::HostBuf host_stage2;
   bsg::Profiler prof;
+  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192};
 };
 
 // Brackets a kernel launch with profiler events when profiling is on.

@@ -124,3 +124,19 @@ def write_inputs(cfg: GBSConfig, rootdir: str, seed: Optional[int] = None) -> No
     cov, sq = lossy_covariances(cfg, seed)
     np.save(os.path.join(rootdir, "cov.npy"), cov)
     np.save(os.path.join(rootdir, "sq_cov.npy"), sq)
+
+
+def low_photon_patterns(M: int, max_total: int, d: int) -> np.ndarray:
+    """All photon patterns [P, M] int32 with at most ``max_total`` photons in
+    total and at most d-1 per mode (the pattern sets of the probability and
+    correlation checks), ordered by total photon number, then by the sorted
+    mode multiset."""
+    import itertools
+
+    rows = [np.zeros((1, M), dtype=np.int32)]
+    for n in range(1, max_total + 1):
+        combos = np.array(list(itertools.combinations_with_replacement(range(M), n)), dtype=np.int64)
+        pats = np.zeros((len(combos), M), dtype=np.int32)
+        np.add.at(pats, (np.repeat(np.arange(len(combos)), n), combos.ravel()), 1)
+        rows.append(pats[(pats <= d - 1).all(axis=1)])
+    return np.concatenate(rows)

@@ -198,6 +198,19 @@ int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const doub
 int bsg_gemm_tf32x3(bsg_handle_t h, const float* A, const float* B, float* C, int M, int N, int K,
                     bsg_stream_t stream);
 
+/* ---- tuning knobs (no reference counterpart) ------------------------------
+ * Launch parameters an autotuner may change per handle (bosonsupremacy_gb300
+ * /autotune.py).  Values outside the documented range return BSG_ERR_INVALID. */
+#define BSG_TUNE_DP_BLOCKS_PER_SM 0  /* resident 256-thread DP blocks per SM, 1..8 (default 8) */
+#define BSG_TUNE_DP_L1_CARVEOUT 1    /* shared-memory carve-out percent for the DP kernel, 0..100 (default 0) */
+#define BSG_TUNE_DP_SMALL_ENTRIES 2  /* programs with <= this many table entries per item run in a second DP
+                                        launch with small per-warp slices, 0..4096 (default 64; 0 = one launch) */
+#define BSG_TUNE_DP_SMALL_BLOCKS 3   /* resident DP blocks per SM in that second launch, 1..8 (default 8) */
+#define BSG_TUNE_DP_SCRATCH_MIB 4    /* device memory for per-warp DP tables per launch, 64..65536 MiB (default 8192) */
+#define BSG_TUNE_COUNT 5
+int bsg_tune_set(bsg_handle_t h, int key, int value);
+int bsg_tune_get(bsg_handle_t h, int key, int* value);
+
 /* ---- measurement helpers (no reference counterpart) ---------------------
  * When enabled, every kernel launch of the handle is bracketed by CUDA
  * events on its stream; bsg_profile_read accumulates the elapsed times per

@@ -115,11 +115,11 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def profile_read(lib, h):
+def profile_read(lib, h, host=False):
     from bosonsupremacy_gb300 import _lib
 
     out = {}
-    for k, name in _lib.KERNEL_CLASSES.items():
+    for k, name in (_lib.HOST_CLASSES if host else _lib.KERNEL_CLASSES).items():
         ms, n, w = C.c_double(), C.c_int64(), C.c_double()
         _lib.check(lib.bsg_profile_read(h, k, C.byref(ms), C.byref(n), C.byref(w)), "bsg_profile_read")
         out[name] = {"ms": ms.value, "launches": n.value, "work": w.value}
@@ -285,6 +285,7 @@ def main():
     clk = clocks.stop()
     lib.bsg_profile_enable(handle.h, 0)
     prof = profile_read(lib, handle.h)
+    host_prof = profile_read(lib, handle.h, host=True)
     ms = statistics.mean(times)
     if ws > 1:
         t = torch.tensor([ms], device=dev)
@@ -392,6 +393,7 @@ def main():
                        "gamma_dtype": "complex64", "l2": "flushed between steps (512 MiB write)"},
             "clocks": clk, "gpu_launches": launches, "kernels": {k: {"ms": v["ms"], "launches": v["launches"]}
                                                                  for k, v in prof.items()},
+            "host": {k: {"ms": v["ms"], "calls": v["launches"]} for k, v in host_prof.items()},
             "roofline": roof, "fp64_path": fp64, "e2e": e2e, "cpu_baseline": cpu, "contraction": contraction,
         }
         print(json.dumps(line), flush=True)

@@ -17,9 +17,10 @@ LIB_PATH = os.path.join(HERE, "libbsg.so")
 PREC_FP64, PREC_SPLIT, PREC_FP32 = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "split": PREC_SPLIT, "fp32": PREC_FP32}
 SITE_FIRST, SITE_MIDDLE, SITE_LAST = 0, 1, 2
-K_DP, K_WILLIAMSON, K_THERMAL, K_SIGMA, K_PREP, K_CONTRACT = range(6)
+K_DP, K_WILLIAMSON, K_THERMAL, K_SIGMA, K_PREP, K_CONTRACT, K_HOST_PLAN, K_HOST_WAIT, K_SAMPLE = range(9)
 KERNEL_CLASSES = {K_DP: "hafnian_dp", K_WILLIAMSON: "williamson", K_THERMAL: "thermal_topk", K_SIGMA: "site_sigma",
-                  K_PREP: "prep", K_CONTRACT: "contract"}
+                  K_PREP: "prep", K_CONTRACT: "contract", K_SAMPLE: "sample"}
+HOST_CLASSES = {K_HOST_PLAN: "host_plan", K_HOST_WAIT: "host_wait"}
 OUT_C64, OUT_C128 = 0, 1
 TUNE_DP_BLOCKS_PER_SM, TUNE_DP_L1_CARVEOUT, TUNE_DP_SMALL_ENTRIES, TUNE_DP_SMALL_BLOCKS, TUNE_DP_SCRATCH_MIB = 0, 1, 2, 3, 4
 
@@ -52,6 +53,8 @@ SIGNATURES = {
     "bsg_gemm_tf32x3": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "bsg_tune_set": (_I, [_P, _I, _I]),
     "bsg_tune_get": (_I, [_P, _I, C.POINTER(_I)]),
+    "bsg_sample": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _L, _I, _P, _P]),
+    "bsg_displacements": (_I, [_P, _P, _L, _I, _P, _P]),
 }
 
 

@@ -206,6 +206,9 @@ int bsg_destroy(bsg_handle_t h) {
   h->sigma_ws.release();
   h->cut_ws.release();
   h->contract_ws.release();
+  h->mps_ws.release();
+  h->sample_ws.release();
+  h->disp_tab.release();
   h->host_stage.release();
   h->host_stage2.release();
   h->prof.release();

@@ -10,6 +10,7 @@
 // Buckets of all sites of an MPS share one persistent launch with an atomic
 // work counter; each 32-slot chunk carries its site and program.
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <thread>
@@ -1221,8 +1222,12 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   BSG_TRY(ensure_tables());
   const int nc = M - 1;
+  using clk = std::chrono::steady_clock;
+  auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
   // 1. all cuts (synchronises to read the per-cut status)
+  auto t_cuts = clk::now();
   BSG_TRY(bsg_cut_spectra(h, sq_cov, M, 1, nc, d, chi, cut_tol, res, num, S, kept, stream));
+  h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_cuts), 0.0);
   const int ldS = 2 * (M - 1);
 
   // 2. workspace
@@ -1330,10 +1335,13 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
                            wb + o_sigc[i], st));
   }
   {
+    auto t_wait = clk::now();
     const cudaError_t e = cudaEventSynchronize(keys_ready);
     cudaEventDestroy(keys_ready);
     BSG_CUDA(e);
+    h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_wait), 0.0);
   }
+  auto t_plan = clk::now();
   if (*herr) {
     set_error("bsg_build_mps: a label row has a multiplicity above %d or more than %d non-zeros", kKeyMaxMult,
               kMaxNnz);
@@ -1386,10 +1394,13 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
   }
   // 6. scatter + one persistent DP launch over all sites
   BSG_TRY(run_sites(h, in, d, chi, precision, out_dtype, st));
+  h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
   // Sigma status (singular A) -- read after the DP so the check costs no extra wait
   std::vector<int> sst(M);
   BSG_CUDA(cudaMemcpyAsync(sst.data(), d_status, (size_t)M * 4, cudaMemcpyDeviceToHost, st));
+  auto t_fin = clk::now();
   BSG_CUDA(cudaStreamSynchronize(st));
+  h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_fin), 0.0);
   for (int i = 0; i < M; ++i)
     if (sst[i]) {
       set_error("bsg_build_mps: site %d: the Gaussian unitary's A block is singular", i);

@@ -121,6 +121,13 @@ struct Profiler {
   void add_work(int cls, double w) {
     if (on) work[cls] += w;
   }
+  // host-timed classes (BSG_K_HOST_*): wall milliseconds measured by the caller
+  void add_host(int cls, double ms, double w) {
+    if (!on) return;
+    total_ms[cls] += ms;
+    launches[cls] += 1;
+    work[cls] += w;
+  }
   void release();
 };
 
@@ -169,6 +176,9 @@ struct bsg_handle_s {
   bsg::DevBuf cut_ws;         // cut spectra workspace
   bsg::DevBuf contract_ws;    // contraction workspace
   bsg::DevBuf mps_ws;         // whole-MPS build: Sigma, row tables, plans
+  bsg::DevBuf sample_ws;      // sampler: chain GEMM operands and outputs
+  bsg::DevBuf disp_tab;       // displacement eigen-tables for disp_dd
+  int disp_dd = 0;
   bsg::HostBuf host_stage;    // pinned staging for plans
   bsg::HostBuf host_stage2;
   bsg::Profiler prof;

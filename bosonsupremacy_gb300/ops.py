@@ -161,3 +161,39 @@ def pattern_amplitudes(Gammas: Sequence[torch.Tensor], Lambdas, patterns, precis
     check(_lib.load().bsg_pattern_amplitudes(h.h, ptrs, ptr(lam), M, chi, d, ptr(pat), P, _prec(precision), ptr(amp),
                                              stream_ptr()), "bsg_pattern_amplitudes")
     return amp
+
+
+def displacements(alpha, dd: int, device: int = 0) -> torch.Tensor:
+    """D(alpha) = expm(alpha a^dag - alpha^* a) in dd dimensions for every
+    entry of `alpha` (sampling_cpu.py:133-148): complex128 [..., dd, dd]."""
+    dev = torch.device("cuda", device)
+    a = _dev(alpha, C128, dev)
+    out = torch.empty(*a.shape, dd, dd, dtype=C128, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_displacements(h.h, ptr(a), a.numel(), int(dd), ptr(out), stream_ptr()), "bsg_displacements")
+    return out
+
+
+def sample(Gammas: Sequence[torch.Tensor], Lambdas, sqrtW, normals, uniforms, dd: int, precision="split",
+           device: int = 0) -> torch.Tensor:
+    """Photon-number samples [n, M] int64 (sampling_cpu.py:30-117) for the
+    given random numbers: normals [2M, n] and per-site thresholds [M, n]."""
+    import ctypes
+    dev = torch.device("cuda", device)
+    M = len(Gammas)
+    chi, _, d = Gammas[0].shape
+    want = C128 if _prec(precision) == _lib.PREC_FP64 else torch.complex64
+    G = [g.to(device=dev, dtype=want).contiguous() for g in Gammas]
+    lam = _dev(Lambdas, torch.float64, dev)
+    W = _dev(sqrtW, torch.float64, dev)
+    z = _dev(normals, torch.float64, dev)
+    u = _dev(uniforms, torch.float64, dev)
+    n = z.shape[1]
+    if tuple(lam.shape) != (M - 1, chi) or tuple(W.shape) != (2 * M, 2 * M) or tuple(u.shape) != (M, n):
+        raise ValueError("sample: expected Lambdas [M-1, chi], sqrtW [2M, 2M], normals [2M, n], uniforms [M, n]")
+    out = torch.empty(n, M, dtype=torch.int64, device=dev)
+    ptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in G])
+    h = Handle.get(device)
+    check(_lib.load().bsg_sample(h.h, ptrs, ptr(lam), M, chi, d, int(dd), ptr(W), ptr(z), ptr(u), n, _prec(precision),
+                                 ptr(out), stream_ptr()), "bsg_sample")
+    return out

@@ -61,6 +61,7 @@ typedef struct CUstream_st* bsg_stream_t; /* == cudaStream_t */
 #define BSG_MAX_ORDER 63       /* hafnian order n                                   */
 #define BSG_MAX_STATES 16384   /* states of one partition program                   */
 #define BSG_MAX_LABEL_NNZ 32   /* non-zero Fock entries in one Schmidt label row    */
+#define BSG_MAX_DD 16          /* sampler Fock cutoff after displacement (dd)       */
 
 /* ---- handle ------------------------------------------------------------ */
 /* No reference counterpart (the reference keeps module-level CuPy state,
@@ -190,6 +191,35 @@ int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, d
 int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                            const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
 
+/* ---- sampling ------------------------------------------------------------
+ * Photon-number samples of the lossy state from the MPS, replacing
+ * sampling_cpu.py:30-117 (`sampling`; GPU twin distributed_sampling.py:62-155):
+ * a random displacement per sample from the thermal part, then sequential
+ * inverse-CDF sampling along the chain.  The random numbers are inputs, in
+ * the reference's draw order, so a seeded numpy stream reproduces the
+ * reference's samples:
+ *   normals  float64 [2M, n] (np.random.normal(size=(2M, n)), sampling_cpu.py:37)
+ *   uniforms float64 [M, n]  (row i = np.random.rand(n, 1) of site i, :52, :92)
+ * sqrtW: float64 [2M, 2M] row-major, the Cholesky factor of the thermal
+ * covariance (sampling_cpu.py:168-170).  Gammas: HOST array of M device
+ * pointers to [chi, chi, d] (c128 for BSG_PREC_FP64, c64 otherwise);
+ * Lambdas float64 [M-1, chi].  samples: int64 [n, M] (the reference's
+ * `results`).  d <= dd <= BSG_MAX_DD.  precision: the chain GEMM
+ * (pre * Lambda) @ Gamma_i.reshape(chi, chi d) in FP64 or FP32 on the CUDA
+ * cores, or BSG_PREC_SPLIT: 3xTF32 on the tcgen05 tensor cores (even
+ * chi >= 16); the per-sample displacement/probability/draw step runs in the
+ * same precision (FP32 for split).  Synchronises `stream`. */
+int bsg_sample(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d, int dd,
+               const double* sqrtW, const double* normals, const double* uniforms, int64_t n, int precision,
+               int64_t* samples, bsg_stream_t stream);
+
+/* Batched displacement operators D(alpha) = expm(alpha a^dag - alpha^* a) in
+ * the dd-dimensional truncation (sampling_cpu.py:133-148, `batch_displaces`;
+ * distributed_sampling.py:169 uses torch.linalg.matrix_exp), from a closed
+ * form of the truncated generator's eigen-decomposition.  alpha: c128
+ * [count] (device); D: c128 [count, dd, dd] row-major.  1 <= dd <= BSG_MAX_DD. */
+int bsg_displacements(bsg_handle_t h, const double* alpha, int64_t count, int dd, double* D, bsg_stream_t stream);
+
 /* 3-way split TF32 GEMM on the tcgen05 tensor cores (no reference
  * counterpart; the building block of the split-precision contraction, exposed
  * for testing): C[M, N] = A[M, K] B[N, K]^T with A, B fp32 row-major (K
@@ -222,7 +252,15 @@ int bsg_tune_get(bsg_handle_t h, int key, int* value);
 #define BSG_K_SIGMA 3     /* per-site Sigma (work: FP64 FMAs)                    */
 #define BSG_K_PREP 4      /* label rows, bucketing, conversions (work: items)    */
 #define BSG_K_CONTRACT 5  /* transfer contraction (work: real flops)             */
-#define BSG_K_COUNT 6
+#define BSG_K_HOST_PLAN 6 /* host wall time of bsg_build_mps between the label keys'
+                             arrival and the DP launch: item planning, plan upload,
+                             scatter launches (work: items planned)              */
+#define BSG_K_HOST_WAIT 7 /* host wall time bsg_build_mps spends blocked on the
+                             device (cut status, keys, final status)              */
+#define BSG_K_SAMPLE 8    /* sampler: displacement, probability, draw, collapse
+                             (work: complex multiply-adds); its chain GEMMs
+                             count as BSG_K_CONTRACT                            */
+#define BSG_K_COUNT 9
 int bsg_profile_enable(bsg_handle_t h, int on);
 /* Synchronises the recorded events; totals since the last reset. */
 int bsg_profile_read(bsg_handle_t h, int kernel_class, double* total_ms, int64_t* launches, double* work);

@@ -86,8 +86,11 @@ def hafnian_kat(ref: str, out: str) -> None:
     np.savez_compressed(out, **data)
 
 
-def pipeline(ref: str, cfg: GBSConfig, full_gamma: bool, n_samples: int, out: str) -> None:
-    """kron_cpu.py + MPS_cpu.py on one synthetic instance; optionally the sampler."""
+def pipeline(ref: str, cfg: GBSConfig, full_gamma: bool, n_samples: int, out: str, n_big: int = 0,
+             big_batch: int = 25000) -> None:
+    """kron_cpu.py + MPS_cpu.py on one synthetic instance; optionally the
+    sampler (n_samples in one batch, seed 2024; and n_big in batches of
+    big_batch, seed 2025, for the one- and two-point correlations)."""
     from oracle.reference_mps import enumerate_patterns, pattern_amplitudes  # checker-side helper
 
     with tempfile.TemporaryDirectory() as tmp:
@@ -140,6 +143,18 @@ def pipeline(ref: str, cfg: GBSConfig, full_gamma: bool, n_samples: int, out: st
             data["sample_mean"] = s.mean(axis=0)
             data["sample_cov"] = np.cov(s.T)
             data["sample_head"] = s[:64].astype(np.int8)
+        if n_big:
+            np.random.seed(2025)
+            sargv = ["--N", str(n_big), "--n", str(big_batch), "--iter", "1", "--d", str(cfg.d),
+                     "--dd", str(cfg.d + 2), "--chi", str(cfg.chi), "--dir", root]
+            run_ref(ref, "sampling_cpu.py", sargv, as_main=True)
+            s = np.load(root + "samples_0.npy").astype(np.float64)
+            data["big_sample_seed"] = 2025
+            data["big_sample_n"] = n_big
+            data["big_sample_batch"] = big_batch
+            data["big_sample_mean"] = s.mean(axis=0)
+            data["big_sample_cov"] = np.cov(s.T)
+            data["big_sample_head"] = s[:256].astype(np.int8)
         np.savez_compressed(out, **data)
 
 
@@ -147,7 +162,7 @@ def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     hafnian_kat(ref, os.path.join(HERE, "hafnian_kat.npz"))
     pipeline(ref, TINY, full_gamma=True, n_samples=2000, out=os.path.join(HERE, "tiny_M8.npz"))
-    pipeline(ref, SMALL, full_gamma=False, n_samples=10000, out=os.path.join(HERE, "small_M16.npz"))
+    pipeline(ref, SMALL, full_gamma=False, n_samples=10000, out=os.path.join(HERE, "small_M16.npz"), n_big=100000)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -58,3 +58,21 @@ def test_sampler_statistics_match_reference(golden):
     s = R.sample(G, Lam, sqrtW, int(t["sample_dd"]), int(t["sample_n"]), rng)
     assert np.array_equal(s[:64], t["sample_head"])
     assert np.allclose(s.mean(0), t["sample_mean"])
+
+
+def test_sampler_first_batch_of_1e5_matches_reference(golden):
+    """Oracle MPS + restated sampler, first 25 000-sample batch of the
+    reference's seeded 10^5-sample run on the M=16 instance: the first 256
+    samples agree draw for draw."""
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    cuts = [(t[f"res_{c}"], t[f"num_{c}"], t[f"S_{c}"]) for c in range(M - 1)]
+    mps = R.build_mps(t["sq_cov"], d, chi, cuts)
+    G = [mps[i][0] for i in range(M)]
+    Lam = np.stack([mps[c][1] for c in range(M - 1)], axis=1)
+    thermal = t["cov"] - t["sq_cov"]
+    thermal = thermal + 1.000001 * np.eye(len(thermal)) * np.abs(np.min(np.linalg.eigvalsh(thermal)))
+    sqrtW = np.linalg.cholesky(thermal)
+    rng = np.random.RandomState(int(t["big_sample_seed"]))
+    s = R.sample(G, Lam, sqrtW, d + 2, int(t["big_sample_batch"]), rng)
+    assert np.array_equal(s[:256], t["big_sample_head"])

@@ -29,6 +29,7 @@ KNOBS = {
     "small_entries": _lib.TUNE_DP_SMALL_ENTRIES,
     "small_blocks": _lib.TUNE_DP_SMALL_BLOCKS,
     "scratch_mib": _lib.TUNE_DP_SCRATCH_MIB,
+    "fp64_blocks": _lib.TUNE_DP_FP64_BLOCKS,
 }
 
 

@@ -120,6 +120,19 @@ void Profiler::release() {
 
 }  // namespace bsg
 
+int bsg_handle_s::ensure_aux() {
+  if (aux_stream) return BSG_OK;
+  int least = 0, greatest = 0;
+  BSG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  BSG_CUDA(cudaStreamCreateWithFlags(&aux_stream, cudaStreamNonBlocking));
+  for (auto& s : grp) BSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest));
+  for (auto& s : dp_lo) BSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least));
+  BSG_CUDA(cudaEventCreateWithFlags(&aux_fork, cudaEventDisableTiming));
+  BSG_CUDA(cudaEventCreateWithFlags(&aux_join, cudaEventDisableTiming));
+  for (auto& e : ev) BSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return BSG_OK;
+}
+
 extern "C" {
 
 int bsg_profile_enable(bsg_handle_t h, int on) {
@@ -158,6 +171,8 @@ int bsg_tune_set(bsg_handle_t h, int key, int value) {
     BSG_CHECK_ARG(value >= 0 && value <= 4096, "bsg_tune_set: small-program entries %d", value);
   if (key == BSG_TUNE_DP_SMALL_BLOCKS)
     BSG_CHECK_ARG(value >= 1 && value <= 8, "bsg_tune_set: small-launch blocks per SM %d", value);
+  if (key == BSG_TUNE_DP_FP64_BLOCKS)
+    BSG_CHECK_ARG(value >= 0 && value <= 8, "bsg_tune_set: FP64 helper blocks per SM %d", value);
   if (key == BSG_TUNE_DP_SCRATCH_MIB)
     BSG_CHECK_ARG(value >= 64 && value <= 65536, "bsg_tune_set: DP scratch %d MiB", value);
   h->tune[key] = value;
@@ -197,6 +212,21 @@ int bsg_create(int device, bsg_handle_t* out) {
 int bsg_destroy(bsg_handle_t h) {
   if (!h) return BSG_OK;
   cudaSetDevice(h->device);
+  if (h->aux_stream) {
+    cudaStreamSynchronize(h->aux_stream);
+    cudaStreamDestroy(h->aux_stream);
+    for (auto s : h->grp) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+    for (auto s : h->dp_lo) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+    cudaEventDestroy(h->aux_fork);
+    cudaEventDestroy(h->aux_join);
+    for (auto e : h->ev) cudaEventDestroy(e);
+  }
   bsg::programs_free(h->programs);
   h->warp_scratch.release();
   h->items.release();
@@ -209,6 +239,12 @@ int bsg_destroy(bsg_handle_t h) {
   h->mps_ws.release();
   h->sample_ws.release();
   h->disp_tab.release();
+  for (auto& sl : h->slot) {
+    sl.plan.release();
+    sl.items.release();
+    sl.scratch.release();
+    sl.stage.release();
+  }
   h->host_stage.release();
   h->host_stage2.release();
   h->prof.release();

@@ -2,8 +2,8 @@
 // cut and the top-chi product-thermal weights with their Fock labels.
 //
 // Reference: williamson + get_cumsum_kron (kron_cpu.py:46-127; the CuPy twin
-// distributed_kron.py:105-137).  All cuts of one call run in one launch, one
-// CTA per cut.
+// distributed_kron.py:105-137).  One CTA per cut; a call launches its cuts
+// in one range, the whole-MPS build in two ranges on two streams.
 //
 // Williamson (FP64):  V = L L^T (Cholesky);  G = L^{-1} Omega L^{-T} is
 // antisymmetric with eigenvalues +-i/nu;  H = G^T G has eigenvalues 1/nu^2
@@ -34,25 +34,6 @@ namespace bsg {
 
 constexpr int kMaxCutModes = 256;  // modes in one cut's right block
 
-struct CutArgs {
-  const double* sq_cov;
-  int M, L0, n_cuts, d, chi;
-  double err_tol;
-  double* ws;          // per cut: 4 * nmax^2 doubles
-  size_t ws_stride;    // doubles per cut
-  double* S;           // [n_cuts, 2(M-1), 2(M-1)]
-  int ldS;
-  double* nbar;        // [n_cuts, kmax]
-  int kmax;
-  double* res;         // [n_cuts, chi]
-  int8_t* num;         // [n_cuts, chi, M-1]
-  int32_t* kept;       // [n_cuts]
-  uint32_t* rec;       // per cut: kmax * chi records (parent << 8 | digit)
-  int* status;         // [n_cuts]
-  int* sweeps;         // [n_cuts] Jacobi sweeps used
-  double* mu;          // [n_cuts, 2 kmax] eigenvalues of G^T G, then 1/nu per pair
-  int max_sweeps;
-};
 
 __device__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -190,7 +171,7 @@ __device__ bool block_cholesky(double* X, int m, int* s_flag, double* s_scalar) 
 }
 
 __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
-  const int c = blockIdx.x;
+  const int c = a.c0 + blockIdx.x;
   const int L = a.L0 + c, M = a.M;
   const int k = M - L, n = 2 * k, nA = 2 * L;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -519,7 +500,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 
 __global__ void __launch_bounds__(1024) thermal_kernel(CutArgs a) {
-  const int c = blockIdx.x;
+  const int c = a.c0 + blockIdx.x;
   if (a.status[c] != 0) return;
   const int L = a.L0 + c, k = a.M - L, d = a.d, chi = a.chi;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -623,17 +604,20 @@ __global__ void __launch_bounds__(1024) thermal_kernel(CutArgs a) {
 
 using namespace bsg;
 
-extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
-                               double err_tol, double* res, int8_t* num, double* S, int32_t* kept,
-                               bsg_stream_t stream) {
-  BSG_CHECK_ARG(h, "bsg_cut_spectra: null handle");
-  BSG_CHECK_ARG(sq_cov && res && num && S && kept, "bsg_cut_spectra: null pointer");
+namespace bsg {
+
+// Workspace, output clearing and the launch arguments of a cut-spectra call.
+int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
+                double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st) {
   BSG_CHECK_ARG(M >= 2 && L0 >= 1 && n_cuts >= 1 && L0 + n_cuts <= M, "bsg_cut_spectra: cuts [%d, %d) outside [1, M=%d)",
                 L0, L0 + n_cuts, M);
   BSG_CHECK_ARG(M - L0 <= kMaxCutModes, "bsg_cut_spectra: %d modes in a cut exceeds %d", M - L0, kMaxCutModes);
   BSG_CHECK_ARG(d >= 1 && d <= 64 && chi >= d && chi <= 4096, "bsg_cut_spectra: need 1 <= d <= chi <= 4096, d <= 64");
-  BSG_CUDA(cudaSetDevice(h->device));
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const size_t tsm = (size_t)d * chi * 8 + 2 * (size_t)chi * 8 + 64 * 8;
+  if (tsm > 227 * 1024) {
+    set_error("bsg_cut_spectra: d*chi=%d needs %zu bytes of shared memory", d * chi, tsm);
+    return BSG_ERR_LIMIT;
+  }
   const int kmax = M - L0, nmax = 2 * kmax;
   CutArgs a{};
   a.sq_cov = sq_cov;
@@ -670,27 +654,51 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   BSG_CUDA(cudaMemsetAsync(num, 0, (size_t)n_cuts * chi * (M - 1), st));
   BSG_CUDA(cudaMemsetAsync(S, 0, (size_t)n_cuts * a.ldS * a.ldS * 8, st));
   BSG_CUDA(cudaMemsetAsync(kept, 0, (size_t)n_cuts * 4, st));
+  *out = a;
+  return BSG_OK;
+}
+
+// Williamson decomposition of cuts [c0, c1) (relative to L0), one CTA each.
+int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, cudaStream_t st) {
+  if (c1 <= c0) return BSG_OK;
+  CutArgs a = args;
+  a.c0 = c0;
   const size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0, (williamson_kernel<<<n_cuts, 1024, wsm, st>>>(a)));
-  const size_t tsm = (size_t)d * chi * 8 + 2 * (size_t)chi * 8 + 64 * 8;
-  if (tsm > 227 * 1024) {
-    set_error("bsg_cut_spectra: d*chi=%d needs %zu bytes of shared memory", d * chi, tsm);
-    return BSG_ERR_LIMIT;
-  }
+  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0, (williamson_kernel<<<c1 - c0, 1024, wsm, st>>>(a)));
+  return BSG_OK;
+}
+
+// Top-chi selection of cuts [c0, c1) (after their Williamson launches).
+int cut_launch_thermal(bsg_handle_t h, const CutArgs& args, int c0, int c1, cudaStream_t st) {
+  if (c1 <= c0) return BSG_OK;
+  CutArgs a = args;
+  a.c0 = c0;
+  const size_t tsm = (size_t)a.d * a.chi * 8 + 2 * (size_t)a.chi * 8 + 64 * 8;
   BSG_CUDA(cudaFuncSetAttribute(thermal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
   double ranked = 0.0;
-  for (int c = 0; c < n_cuts; ++c) ranked += (double)(M - L0 - c) * chi * d;
-  BSG_PROFILED(h, BSG_K_THERMAL, st, ranked, (thermal_kernel<<<n_cuts, 1024, tsm, st>>>(a)));
-  std::vector<int> status(2 * n_cuts);
-  BSG_CUDA(cudaMemcpyAsync(status.data(), a.status, st_bytes, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaStreamSynchronize(st));
+  for (int c = c0; c < c1; ++c) ranked += (double)(a.M - a.L0 - c) * a.chi * a.d;
+  BSG_PROFILED(h, BSG_K_THERMAL, st, ranked, (thermal_kernel<<<c1 - c0, 1024, tsm, st>>>(a)));
+  return BSG_OK;
+}
+
+int cut_queue_status(const CutArgs& a, int c0, int c1, int* hst, cudaStream_t st) {
+  if (c1 <= c0) return BSG_OK;
+  BSG_CUDA(cudaMemcpyAsync(hst + c0, a.status + c0, (size_t)(c1 - c0) * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaMemcpyAsync(hst + a.n_cuts + c0, a.sweeps + c0, (size_t)(c1 - c0) * 4, cudaMemcpyDeviceToHost, st));
+  return BSG_OK;
+}
+
+// Decodes the status of cuts [c0, c1) and adds their Williamson FMA count
+// to the profiler.
+int cut_check_status(bsg_handle_t h, const CutArgs& a, int c0, int c1, const int* status) {
+  const int M = a.M, L0 = a.L0, n_cuts = a.n_cuts;
   // FP64 FMAs of the Williamson step: Cholesky n^3/3, L^-1 n^3/6, G n^3,
   // pairing ~n^3 (G x per pair, projections), S n^3/2; full path: H n^3 and
   // 4 n^3 per Jacobi sweep; low-rank path (m = 2L < n): Cholesky m^3/3,
   // L_A^-1 C m^2 n/2, F n^2 m/2, QR 2 n m^2, K m^3/2, 4 m^3 per sweep, Q z 2 n^2 m
   double fmas = 0.0;
-  for (int c = 0; c < n_cuts; ++c) {
+  for (int c = c0; c < c1; ++c) {
     const double n = 2.0 * (M - L0 - c), m = 2.0 * (L0 + c);
     const double sw = std::max(0, status[n_cuts + c]);
     fmas += n * n * n * (1.0 / 3 + 1.0 / 6 + 1.0 + 1.0 + 0.5);
@@ -698,7 +706,7 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
     else fmas += m * m * m / 3 + m * m * n / 2 + n * n * m / 2 + 2 * n * m * m + m * m * m / 2 + 4 * m * m * m * sw + 2 * n * n * m;
   }
   h->prof.add_work(BSG_K_WILLIAMSON, fmas);
-  for (int c = 0; c < n_cuts; ++c) {
+  for (int c = c0; c < c1; ++c) {
     if (status[c] == 1) {
       set_error("cut %d: the input matrix is not symmetric", L0 + c);
       return BSG_ERR_NOT_PD;
@@ -721,4 +729,23 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
     }
   }
   return BSG_OK;
+}
+
+}  // namespace bsg
+
+extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
+                               double err_tol, double* res, int8_t* num, double* S, int32_t* kept,
+                               bsg_stream_t stream) {
+  BSG_CHECK_ARG(h, "bsg_cut_spectra: null handle");
+  BSG_CHECK_ARG(sq_cov && res && num && S && kept, "bsg_cut_spectra: null pointer");
+  BSG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CutArgs a;
+  BSG_TRY(cut_prepare(h, sq_cov, M, L0, n_cuts, d, chi, err_tol, res, num, S, kept, &a, st));
+  BSG_TRY(cut_launch_williamson(h, a, 0, n_cuts, st));
+  BSG_TRY(cut_launch_thermal(h, a, 0, n_cuts, st));
+  std::vector<int> status(2 * n_cuts);
+  BSG_TRY(cut_queue_status(a, 0, n_cuts, status.data(), st));
+  BSG_CUDA(cudaStreamSynchronize(st));
+  return cut_check_status(h, a, 0, n_cuts, status.data());
 }

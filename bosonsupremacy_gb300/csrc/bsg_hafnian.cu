@@ -218,7 +218,8 @@ struct ProgDev {
 enum { MODE_SITE = 0, MODE_TARGETS = 1, MODE_MATRICES = 2 };
 
 struct SiteDesc {
-  const void* sigma;  // policy-typed [2Mr, 2Mr]
+  const void* sigma;    // policy-typed [2Mr, 2Mr]
+  const double2* sigma64;  // the same Sigma in FP64 (the FP64 helper launch)
   int n_len, Mr;
   const int32_t* l_ent;  // left rows (cut `site`): entries/nnz/rowfact
   const int32_t* l_nnz;
@@ -238,8 +239,11 @@ struct SiteDesc {
 struct DPArgs {
   ProgDev prog;
   const int32_t* items;
-  const int32_t* chunk_prog;
-  const int32_t* chunk_site;
+  // chunks (32 item slots) of bucket b are [bucket_chunk[b], bucket_chunk[b+1])
+  const int32_t* bucket_chunk;  // [nb + 1]
+  const int32_t* bucket_prog;   // [nb]
+  const int32_t* bucket_site;   // [nb] (site mode)
+  int nb;
   int64_t chunk_base;  // first chunk of this launch
   int64_t n_chunks;    // chunks of this launch
   unsigned long long* counter;
@@ -342,14 +346,22 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
     c = __shfl_sync(0xffffffffu, c, 0);
     if ((int64_t)c >= a.n_chunks) break;
     c += (unsigned long long)a.chunk_base;
-    const int prog = a.chunk_prog[c];
-    const SiteDesc* sd = MODE == MODE_SITE ? a.sites + a.chunk_site[c] : nullptr;
+    // bucket of chunk c: the last b with bucket_chunk[b] <= c
+    int lo = 0, hi = a.nb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if ((unsigned long long)a.bucket_chunk[mid] <= c) lo = mid;
+      else hi = mid - 1;
+    }
+    const int prog = a.bucket_prog[lo];
+    const SiteDesc* sd = MODE == MODE_SITE ? a.sites + a.bucket_site[lo] : nullptr;
     const int32_t item = a.items[c * 32 + lane];
     const bool live = item >= 0;
     const int kp = a.prog.k[prog];
     const int ns = a.prog.nstates[prog];
     const int so = a.prog.state_off[prog];
-    const C* sig = reinterpret_cast<const C*>(MODE == MODE_SITE ? sd->sigma : a.sigma);
+    const C* sig = reinterpret_cast<const C*>(
+        MODE == MODE_SITE ? (std::is_same<P, PrecF64>::value ? (const void*)sd->sigma64 : sd->sigma) : a.sigma);
     const int n_len = MODE == MODE_SITE ? sd->n_len : a.n_len;
 
     int cls[BSG_MAX_CLASSES];
@@ -513,7 +525,7 @@ struct Buckets {
   std::vector<int32_t> sites;    // bucket -> site (0 in target/matrix modes)
   std::vector<int64_t> counts;   // bucket -> items
   std::vector<int32_t> offsets;  // bucket -> first slot (multiple of 32)
-  std::vector<int32_t> chunk_prog, chunk_site;
+  std::vector<int32_t> chunk_start;  // bucket -> first chunk (nb + 1 entries)
   int64_t slots = 0;
   int pairs_max = 1, states_max = 1;
   double work = 0.0;             // complex multiply-adds of all items
@@ -557,14 +569,12 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
     remap[order[i]] = i;
   }
   out.offsets.assign(nb, 0);
+  out.chunk_start.assign(nb + 1, 0);
   int64_t off = 0;
   for (int b = 0; b < nb; ++b) {
     out.offsets[b] = int32_t(off);
+    out.chunk_start[b] = int32_t(off / 32);
     const int64_t ch = (out.counts[b] + 31) / 32;
-    for (int64_t c = 0; c < ch; ++c) {
-      out.chunk_prog.push_back(out.progs[b]);
-      out.chunk_site.push_back(out.sites[b]);
-    }
     off += ch * 32;
     const int p = out.progs[b];
     const int kk = ps.k[p];
@@ -577,6 +587,7 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
     }
   }
   out.slots = off;
+  out.chunk_start[nb] = int32_t(off / 32);
   bk = std::move(out);
   return BSG_OK;
 }
@@ -637,39 +648,65 @@ static void dp_shape(bsg_handle_t h, int blocks_per_sm, DPLaunch& L) {
 // tables stay in L1/L2.  Both launches share the scratch (same stream) and
 // use separate work counters (a.counter[0..1]).
 template <class P, int MODE>
-static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, cudaStream_t st) {
+static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf& scratch, cudaStream_t st) {
   const auto& ps = h->programs;
-  const int64_t nch = (int64_t)bk.chunk_prog.size();
+  const int nb = int(bk.progs.size());
+  const int64_t nch = nb ? bk.chunk_start[nb] : 0;
   const int small_entries = h->tune[BSG_TUNE_DP_SMALL_ENTRIES];
   auto small = [&](int p) { return small_program(ps, p, small_entries); };
   DPLaunch Ls, Lb;
-  for (int64_t c = 0; c < nch; ++c)
-    if (!small(bk.chunk_prog[c])) Lb.c1 = c + 1;
+  int first_small = nb;  // buckets are large-table programs first (layout_buckets)
+  while (first_small > 0 && small(bk.progs[first_small - 1])) --first_small;
+  Lb.c1 = first_small < nb ? bk.chunk_start[first_small] : nch;
   Ls.c0 = Lb.c1;
   Ls.c1 = nch;
-  // slice sizes from the chunks each launch actually runs
-  for (int64_t c = 0; c < nch; ++c) {
-    const int p = bk.chunk_prog[c];
-    DPLaunch& L = c < Lb.c1 ? Lb : Ls;
+  // slice sizes from the buckets each launch actually runs
+  for (int b = 0; b < nb; ++b) {
+    const int p = bk.progs[b];
+    DPLaunch& L = b < first_small ? Lb : Ls;
     L.pmax = std::max(L.pmax, ps.k[p] * (ps.k[p] + 1) / 2);
     L.smax = std::max(L.smax, ps.nstates[p]);
-  }
-  for (size_t b = 0; b < bk.progs.size(); ++b) {
-    const int p = bk.progs[b];
-    (small(p) ? Ls : Lb).work += (double)bk.counts[b] * (double)prog_trans(ps, p);
+    L.work += (double)bk.counts[b] * (double)prog_trans(ps, p);
   }
   dp_shape<P>(h, h->tune[BSG_TUNE_DP_SMALL_BLOCKS], Ls);
   dp_shape<P>(h, h->tune[BSG_TUNE_DP_BLOCKS_PER_SM], Lb);
   const bool run_b = Lb.c1 > Lb.c0, run_s = Ls.c1 > Ls.c0 || !run_b;
+  // FP64 helper (split precision, site mode): dp_kernel<PrecF64> on the
+  // handle's second stream draws chunks from the same counters, so the FP64
+  // pipe takes a share of the items while the FP32 pipe runs the split DP.
+  const int helper_bps = h->tune[BSG_TUNE_DP_FP64_BLOCKS];
+  const bool helper = MODE == MODE_SITE && std::is_same<P, PrecSplit>::value && helper_bps > 0;
+  static_assert(sizeof(typename PrecF64::CA) == sizeof(typename P::CA) || !std::is_same<P, PrecSplit>::value, "");
   size_t need = 0;
   if (run_s) need = std::max(need, (size_t)Ls.blocks * 8 * Ls.per_warp);
   if (run_b) need = std::max(need, (size_t)Lb.blocks * 8 * Lb.per_warp);
-  BSG_TRY(h->warp_scratch.ensure(need));
+  DPLaunch Hs = Ls, Hb = Lb;  // helper shapes (same slices, fewer blocks)
+  size_t helper_off = 0;
+  if (helper) {
+    Hs.blocks = std::min(Hs.blocks, h->num_sms * helper_bps);
+    Hb.blocks = std::min(Hb.blocks, h->num_sms * helper_bps);
+    helper_off = (need + 255) & ~size_t(255);
+    size_t hneed = 0;
+    if (run_s) hneed = std::max(hneed, (size_t)Hs.blocks * 8 * Hs.per_warp);
+    if (run_b) hneed = std::max(hneed, (size_t)Hb.blocks * 8 * Hb.per_warp);
+    need = helper_off + hneed;
+  }
+  BSG_TRY(scratch.ensure(need));
   BSG_CUDA(cudaFuncSetAttribute(dp_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 h->tune[BSG_TUNE_DP_L1_CARVEOUT]));
-  a.scratch = h->warp_scratch.ptr;
+  a.scratch = scratch.ptr;
   unsigned long long* ctr = a.counter;
   const DPLaunch* Ls_or_b[2] = {run_b ? &Lb : nullptr, run_s ? &Ls : nullptr};
+  const DPLaunch* H_or_b[2] = {run_b ? &Hb : nullptr, run_s ? &Hs : nullptr};
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_dp = nullptr;
+  if (helper) {
+    BSG_TRY(h->ensure_aux());
+    aux = h->aux_stream;
+    BSG_CUDA(cudaEventRecord(h->aux_fork, st));
+    BSG_CUDA(cudaStreamWaitEvent(aux, h->aux_fork, 0));
+    if (h->prof.on) BSG_TRY(h->prof.begin(BSG_K_DP, st, &ev_dp));
+  }
   for (int i = 0; i < 2; ++i) {
     const DPLaunch* L = Ls_or_b[i];
     if (!L) continue;
@@ -678,16 +715,32 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, cudaStream_t
     a.chunk_base = L->c0;
     a.n_chunks = L->c1 - L->c0;
     a.counter = ctr + i;
-    BSG_PROFILED(h, BSG_K_DP, st, L->work, (dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a)));
+    a.scratch = scratch.ptr;
+    if (helper) {
+      dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a);
+      BSG_CUDA(cudaGetLastError());
+      DPArgs ha = a;
+      ha.scratch = reinterpret_cast<char*>(scratch.ptr) + helper_off;
+      dp_kernel<PrecF64, MODE><<<H_or_b[i]->blocks, 256, 0, aux>>>(ha);
+      BSG_CUDA(cudaGetLastError());
+    } else {
+      BSG_PROFILED(h, BSG_K_DP, st, L->work, (dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a)));
+    }
+  }
+  if (helper) {
+    BSG_CUDA(cudaEventRecord(h->aux_join, aux));
+    BSG_CUDA(cudaStreamWaitEvent(st, h->aux_join, 0));
+    if (h->prof.on) BSG_TRY(h->prof.end(BSG_K_DP, st, ev_dp, Ls.work + Lb.work));
   }
   return BSG_OK;
 }
 
 template <int MODE>
-static int launch_dp(bsg_handle_t h, int precision, DPArgs a, const Buckets& bk, cudaStream_t st) {
-  if (precision == BSG_PREC_FP64) return launch_dp_t<PrecF64, MODE>(h, a, bk, st);
-  if (precision == BSG_PREC_SPLIT) return launch_dp_t<PrecSplit, MODE>(h, a, bk, st);
-  return launch_dp_t<PrecF32, MODE>(h, a, bk, st);
+static int launch_dp(bsg_handle_t h, int precision, DPArgs a, const Buckets& bk, bsg::DevBuf& scratch,
+                     cudaStream_t st) {
+  if (precision == BSG_PREC_FP64) return launch_dp_t<PrecF64, MODE>(h, a, bk, scratch, st);
+  if (precision == BSG_PREC_SPLIT) return launch_dp_t<PrecSplit, MODE>(h, a, bk, scratch, st);
+  return launch_dp_t<PrecF32, MODE>(h, a, bk, scratch, st);
 }
 
 // ---- target / matrix modes ------------------------------------------------
@@ -735,21 +788,24 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
   BSG_TRY(programs_upload(h->programs, st));
   BSG_CUDA(cudaMemsetAsync(out, 0, (size_t)B * sizeof(double2), st));
   if (bk.slots == 0) return BSG_OK;
-  const size_t chunks = bk.chunk_prog.size();
-  BSG_TRY(h->items.ensure((size_t)bk.slots * 4 + chunks * 4 + 64));
+  const int nb = int(bk.progs.size());
+  BSG_TRY(h->items.ensure((size_t)bk.slots * 4 + (size_t)(2 * nb + 1) * 4 + 64));
   int32_t* d_items = reinterpret_cast<int32_t*>(h->items.ptr);
-  int32_t* d_chunk = d_items + bk.slots;
+  int32_t* d_bchunk = d_items + bk.slots;
+  int32_t* d_bprog = d_bchunk + nb + 1;
   BSG_CUDA(cudaMemcpyAsync(d_items, items.data(), (size_t)bk.slots * 4, cudaMemcpyHostToDevice, st));
-  BSG_CUDA(cudaMemcpyAsync(d_chunk, bk.chunk_prog.data(), chunks * 4, cudaMemcpyHostToDevice, st));
+  BSG_CUDA(cudaMemcpyAsync(d_bchunk, bk.chunk_start.data(), (size_t)(nb + 1) * 4, cudaMemcpyHostToDevice, st));
+  BSG_CUDA(cudaMemcpyAsync(d_bprog, bk.progs.data(), (size_t)nb * 4, cudaMemcpyHostToDevice, st));
   BSG_TRY(h->misc.ensure(64));
   auto* counter = reinterpret_cast<unsigned long long*>(h->misc.ptr);
   BSG_CUDA(cudaMemsetAsync(counter, 0, 16, st));
   DPArgs a{};
   a.prog = prog_dev(h->programs);
   a.items = d_items;
-  a.chunk_prog = d_chunk;
-  a.chunk_site = nullptr;
-  a.n_chunks = (int64_t)chunks;
+  a.bucket_chunk = d_bchunk;
+  a.bucket_prog = d_bprog;
+  a.bucket_site = nullptr;
+  a.nb = nb;
   a.counter = counter;
   a.sigma = sig;
   a.n_len = n_len;
@@ -757,8 +813,8 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
   a.n = n;
   a.den = den;
   a.out = reinterpret_cast<double2*>(out);
-  if (mode == MODE_TARGETS) BSG_TRY(launch_dp<MODE_TARGETS>(h, precision, a, bk, st));
-  else BSG_TRY(launch_dp<MODE_MATRICES>(h, precision, a, bk, st));
+  if (mode == MODE_TARGETS) BSG_TRY(launch_dp<MODE_TARGETS>(h, precision, a, bk, h->warp_scratch, st));
+  else BSG_TRY(launch_dp<MODE_MATRICES>(h, precision, a, bk, h->warp_scratch, st));
   BSG_CUDA(cudaStreamSynchronize(st));  // the host vectors above go out of scope
   return BSG_OK;
 }
@@ -887,6 +943,7 @@ struct SiteInput {
   int kind;
   int Mr;
   const void* sigma;  // policy-typed
+  const double2* sigma64;  // FP64 copy
   const double* Z;
   const double* lambda;   // left rows (null for LAST)
   // (left scales are computed by run_sites)
@@ -900,7 +957,7 @@ struct SiteInput {
 
 // Plans, uploads and launches the scatter + DP for a set of sites.
 static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, int chi, int precision, int out_dtype,
-                     cudaStream_t st) {
+                     bsg_handle_s::SiteSlot& slot, cudaStream_t st) {
   auto& ps = h->programs;
   const int ns = int(in.size());
   Buckets bk;
@@ -923,9 +980,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
       if (b >= 0) b = remap[b];
   BSG_TRY(programs_upload(ps, st));
   const int nb = int(bk.progs.size());
-  const size_t chunks = bk.chunk_prog.size();
 
-  // one plan buffer: site descs, per-site tables, bucket offsets/cursors, chunks, counter
+  // one plan buffer: site descs, per-site tables, bucket offsets/cursors/chunks/programs/sites, counters
   auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
   size_t off = 0;
   auto carve = [&](size_t bytes) {
@@ -948,12 +1004,13 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     o_bo[s] = carve(plans[s].bucket_of.size() * 4);
   }
   const size_t o_boff = carve((size_t)nb * 4 + 4), o_cur = carve((size_t)nb * 4 + 4);
-  const size_t o_cp = carve(chunks * 4 + 4), o_cs = carve(chunks * 4 + 4), o_ctr = carve(16);
+  const size_t o_bch = carve((size_t)nb * 4 + 4), o_bpr = carve((size_t)nb * 4 + 4),
+               o_bsi = carve((size_t)nb * 4 + 4), o_ctr = carve(16);
   const size_t plan_bytes = off;
-  BSG_TRY(h->plan.ensure(plan_bytes));
-  BSG_TRY(h->host_stage2.ensure(plan_bytes));
-  char* hp = reinterpret_cast<char*>(h->host_stage2.ptr);
-  char* dp = reinterpret_cast<char*>(h->plan.ptr);
+  BSG_TRY(slot.plan.ensure(plan_bytes));
+  BSG_TRY(slot.stage.ensure(plan_bytes));
+  char* hp = reinterpret_cast<char*>(slot.stage.ptr);
+  char* dp = reinterpret_cast<char*>(slot.plan.ptr);
   SiteDesc* hd = reinterpret_cast<SiteDesc*>(hp + o_desc);
   LeftScaleJob* hl = reinterpret_cast<LeftScaleJob*>(hp + o_lsj);
   const int out_c128 = out_dtype == BSG_OUT_C128;
@@ -969,6 +1026,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     hl[s] = lj;
     SiteDesc sd{};
     sd.sigma = si.sigma;
+    sd.sigma64 = si.sigma64;
     sd.Mr = si.Mr;
     sd.n_len = 2 * si.Mr;
     sd.l_ent = si.lt.entries;
@@ -995,9 +1053,10 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   }
   std::memcpy(hp + o_boff, bk.offsets.data(), (size_t)nb * 4);
   std::memset(hp + o_cur, 0, (size_t)nb * 4 + 4);
-  if (chunks) {
-    std::memcpy(hp + o_cp, bk.chunk_prog.data(), chunks * 4);
-    std::memcpy(hp + o_cs, bk.chunk_site.data(), chunks * 4);
+  if (nb) {
+    std::memcpy(hp + o_bch, bk.chunk_start.data(), (size_t)(nb + 1) * 4);
+    std::memcpy(hp + o_bpr, bk.progs.data(), (size_t)nb * 4);
+    std::memcpy(hp + o_bsi, bk.sites.data(), (size_t)nb * 4);
   }
   std::memset(hp + o_ctr, 0, 16);
   BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
@@ -1007,8 +1066,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   const size_t esz = out_c128 ? 16 : 8;
   for (int s = 0; s < ns; ++s) BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, (size_t)chi * chi * d * esz, st));
   if (bk.slots == 0) return BSG_OK;
-  BSG_TRY(h->items.ensure((size_t)bk.slots * 4));
-  int32_t* d_items = reinterpret_cast<int32_t*>(h->items.ptr);
+  BSG_TRY(slot.items.ensure((size_t)bk.slots * 4));
+  int32_t* d_items = reinterpret_cast<int32_t*>(slot.items.ptr);
   BSG_CUDA(cudaMemsetAsync(d_items, 0xff, (size_t)bk.slots * 4, st));
   for (int s = 0; s < ns; ++s) {
     const SitePlanHost& p = plans[s];
@@ -1024,12 +1083,13 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   DPArgs a{};
   a.prog = prog_dev(ps);
   a.items = d_items;
-  a.chunk_prog = reinterpret_cast<int32_t*>(dp + o_cp);
-  a.chunk_site = reinterpret_cast<int32_t*>(dp + o_cs);
-  a.n_chunks = (int64_t)chunks;
+  a.bucket_chunk = reinterpret_cast<int32_t*>(dp + o_bch);
+  a.bucket_prog = reinterpret_cast<int32_t*>(dp + o_bpr);
+  a.bucket_site = reinterpret_cast<int32_t*>(dp + o_bsi);
+  a.nb = nb;
   a.counter = reinterpret_cast<unsigned long long*>(dp + o_ctr);
   a.sites = reinterpret_cast<SiteDesc*>(dp + o_desc);
-  return launch_dp<MODE_SITE>(h, precision, a, bk, st);
+  return launch_dp<MODE_SITE>(h, precision, a, bk, slot.scratch, st);
 }
 
 }  // namespace bsg
@@ -1194,6 +1254,7 @@ extern "C" int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int
   in[0].kind = kind;
   in[0].Mr = M_r;
   in[0].sigma = sigc;
+  in[0].sigma64 = reinterpret_cast<const double2*>(Sigma);
   in[0].Z = Z;
   in[0].lambda = lambda_l;
   in[0].hkey_l = hk;
@@ -1203,7 +1264,7 @@ extern "C" int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int
   in[0].lt = lt;
   in[0].rt = rt;
   in[0].gamma = Gamma;
-  return run_sites(h, in, d, chi, precision, out_dtype, st);
+  return run_sites(h, in, d, chi, precision, out_dtype, h->slot[0], st);
 }
 
 extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
@@ -1224,10 +1285,41 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
   const int nc = M - 1;
   using clk = std::chrono::steady_clock;
   auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
-  // 1. all cuts (synchronises to read the per-cut status)
-  auto t_cuts = clk::now();
-  BSG_TRY(bsg_cut_spectra(h, sq_cov, M, 1, nc, d, chi, cut_tol, res, num, S, kept, stream));
-  h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_cuts), 0.0);
+  // Three groups of cuts and sites, each on its own high-priority stream:
+  //   right  cuts [T2, nc)   sites [T2 + 1, M)   (cheap cuts, small Sigma)
+  //   left   cuts [0, T1)    sites [0, T1)       (cheap cuts, large-M_r Sigma)
+  //   middle cuts [T1, T2)   sites [T1, T2 + 1)  (slow cuts; its sites also read cuts T1 - 1, T2)
+  // Site i reads cuts i - 1 and i, so each group's Sigma, planning and DP can
+  // start as soon as its own cuts are done: the edge groups' DP (most of the
+  // hafnian work sits at both ends of the chain) runs on the SMs the slow
+  // middle cuts leave idle.  The edge groups' DP runs on low-priority
+  // streams, so Williamson / Sigma blocks that become ready later take the
+  // SMs those persistent DP blocks have not claimed yet.  No kernel waits on
+  // another; streams are ordered by events only.
+  int T1 = 0, T2 = nc;
+  if (nc >= 6) {
+    T1 = nc / 3;
+    T2 = nc - nc / 4;
+  }
+  struct Group {
+    int c0, c1, s0, s1;
+    cudaStream_t stream, dp_stream;
+    int slot;
+  };
+  // order of host planning: right, left, middle (the order their keys arrive)
+  std::vector<Group> groups;
+  if (T1 > 0) {
+    BSG_TRY(h->ensure_aux());
+    groups.push_back(Group{T2, nc, T2 + 1, M, h->grp[0], h->dp_lo[0], 2});
+    groups.push_back(Group{0, T1, 0, T1, h->grp[1], h->dp_lo[1], 1});
+    groups.push_back(Group{T1, T2, T1, T2 + 1, h->grp[2], h->grp[2], 0});
+  } else {
+    groups.push_back(Group{0, nc, 0, M, st, st, 0});
+  }
+
+  // 1. cut workspace and output clearing
+  CutArgs cuts;
+  BSG_TRY(cut_prepare(h, sq_cov, M, 1, nc, d, chi, cut_tol, res, num, S, kept, &cuts, st));
   const int ldS = 2 * (M - 1);
 
   // 2. workspace
@@ -1243,7 +1335,7 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
                o_sum = carve((size_t)nc * rows_cap * 4), o_key = carve((size_t)nc * rows_cap * 8),
                o_rf = carve((size_t)nc * rows_cap * 8), o_rf2 = carve((size_t)nc * rows_cap * 8);
   const size_t o_empty = carve(kMaxNnz * 4 + 64);  // one empty row (entries, nnz, rowfact, rowfact2)
-  const size_t o_above = carve((size_t)nc * 4), o_err = carve(16), o_Z = carve((size_t)M * 8),
+  const size_t o_above = carve((size_t)nc * 4), o_err = carve(16 * 3), o_Z = carve((size_t)M * 8),
                o_status = carve((size_t)M * 4), o_jobs = carve(sizeof(SigmaJob) * M);
   std::vector<size_t> o_sig(M), o_sigc(M), o_sws(M);
   for (int i = 0; i < M; ++i) {
@@ -1261,9 +1353,17 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
                  nullptr, nullptr, reinterpret_cast<double*>(wb + o_empty + kMaxNnz * 4 + 8),
                  reinterpret_cast<float2*>(wb + o_empty + kMaxNnz * 4 + 16)};
   int32_t* d_above = reinterpret_cast<int32_t*>(wb + o_above);
-  int* d_err = reinterpret_cast<int*>(wb + o_err);
+  int* d_err = reinterpret_cast<int*>(wb + o_err);  // one flag per group (16 bytes apart)
   double* d_Z = reinterpret_cast<double*>(wb + o_Z);
   int* d_status = reinterpret_cast<int*>(wb + o_status);
+  // pinned staging: Sigma jobs, cut status, keys, counts, label flags
+  BSG_TRY(h->host_stage.ensure(sizeof(SigmaJob) * M + (size_t)nc * 8 + (size_t)nc * (chi * 8 + 8) + 64));
+  char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
+  int* hcut = reinterpret_cast<int*>(hs + sizeof(SigmaJob) * M);
+  uint64_t* hkeys = reinterpret_cast<uint64_t*>(hcut + 2 * (size_t)nc);
+  int32_t* hcnt = reinterpret_cast<int32_t*>(hkeys + (size_t)nc * chi);
+  int32_t* habove = hcnt + nc;
+  int* herr = habove + nc;  // one flag per group
   {
     // empty row: nnz 0, rowfact 1 (and as the FP32 pair (1, 0))
     std::vector<char> e(kMaxNnz * 4 + 64, 0);
@@ -1273,34 +1373,10 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
     std::memcpy(e.data() + kMaxNnz * 4 + 16, &one2, 8);
     BSG_CUDA(cudaMemcpyAsync(wb + o_empty, e.data(), e.size(), cudaMemcpyHostToDevice, st));
   }
-  BSG_CUDA(cudaMemsetAsync(d_err, 0, 16, st));
+  BSG_CUDA(cudaMemsetAsync(d_err, 0, 16 * 3, st));
   BSG_CUDA(cudaMemsetAsync(d_status, 0, (size_t)M * 4, st));
-
-  // 3. Lambda and label tables of every cut (one launch each)
-  BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
-               (lambda_kernel<<<nc, 256, 0, st>>>(res, chi, site_tol, Lambdas, d_above)));
-  BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
-               (label_rows_kernel<<<dim3((chi + 127) / 128, nc), 128, 0, st>>>(
-                   num, (int64_t)chi * (M - 1), M - 1, kept, M - 1, 1, chi, tab, d_err)));
-
-  // 4. read the row keys and counts back (queued before the Sigma launch, so
-  // the host plans every site while the Sigma kernels run)
-  BSG_TRY(h->host_stage.ensure(sizeof(SigmaJob) * M + (size_t)nc * (chi * 8 + 16) + 64));
-  char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
-  uint64_t* hkeys = reinterpret_cast<uint64_t*>(hs + sizeof(SigmaJob) * M);
-  int32_t* hcnt = reinterpret_cast<int32_t*>(hkeys + (size_t)nc * chi);
-  int32_t* habove = hcnt + nc;
-  int* herr = habove + nc;
-  BSG_CUDA(cudaMemcpyAsync(hkeys, tab.key, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(hcnt, kept, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(habove, d_above, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaMemcpyAsync(herr, d_err, 4, cudaMemcpyDeviceToHost, st));
-  cudaEvent_t keys_ready;
-  BSG_CUDA(cudaEventCreateWithFlags(&keys_ready, cudaEventDisableTiming));
-  BSG_CUDA(cudaEventRecord(keys_ready, st));
-
-  // 5. Sigma of every site (one CTA each)
-  std::vector<SigmaJob> jobs(M);
+  // Sigma jobs of every site
+  SigmaJob* jobs = reinterpret_cast<SigmaJob*>(hs);
   for (int i = 0; i < M; ++i) {
     SigmaJob jb{};
     const size_t cut_l = (size_t)i, cut_r = (size_t)(i - 1);
@@ -1326,28 +1402,6 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
     jb.status = d_status + i;
     jobs[i] = jb;
   }
-  std::memcpy(hs, jobs.data(), sizeof(SigmaJob) * M);
-  BSG_TRY(launch_sigma_jobs(h, reinterpret_cast<SigmaJob*>(hs), M, wb + o_jobs, st));
-  for (int i = 0; i < M; ++i) {
-    const int Mr = i == 0 ? M : M - i;
-    if (o_sigc[i] != o_sig[i])
-      BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[i]), (int64_t)(2 * Mr) * (2 * Mr), precision,
-                           wb + o_sigc[i], st));
-  }
-  {
-    auto t_wait = clk::now();
-    const cudaError_t e = cudaEventSynchronize(keys_ready);
-    cudaEventDestroy(keys_ready);
-    BSG_CUDA(e);
-    h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_wait), 0.0);
-  }
-  auto t_plan = clk::now();
-  if (*herr) {
-    set_error("bsg_build_mps: a label row has a multiplicity above %d or more than %d non-zeros", kKeyMaxMult,
-              kMaxNnz);
-    return BSG_ERR_LIMIT;
-  }
-  static const uint64_t zero_key = 0;
   auto cut_table = [&](int c) {
     RowTable t = tab;
     const size_t o = (size_t)c * rows_cap;
@@ -1359,42 +1413,149 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
     t.rowfact2 += o;
     return t;
   };
-  std::vector<SiteInput> in(M);
-  for (int i = 0; i < M; ++i) {
-    SiteInput& si = in[i];
-    si.kind = i == 0 ? BSG_SITE_FIRST : i == M - 1 ? BSG_SITE_LAST : BSG_SITE_MIDDLE;
-    si.Mr = i == 0 ? M : M - i;
-    si.sigma = wb + o_sigc[i];
-    si.Z = d_Z + i;
-    si.gamma = gammas_host[i];
-    if (si.kind != BSG_SITE_LAST) {
-      si.lt = cut_table(i);
-      si.KL = habove[i];
-      si.hkey_l = hkeys + (size_t)i * chi;
-      si.lambda = Lambdas + (size_t)i * chi;
-    } else {
-      si.lt = empty;
-      si.KL = 1;
-      si.hkey_l = &zero_key;
-      si.lambda = nullptr;
+
+  // 3. per group: Williamson, thermal, Lambda + label tables, keys to the
+  // host (one event per group), then its Sigma; the middle group's labels and
+  // Sigma also read the edge groups' boundary cuts
+  const int ng = int(groups.size());
+  // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[4..8] = final joins
+  cudaEvent_t ev_keys[3] = {}, ev_done[3] = {};
+  if (ng > 1) {
+    BSG_CUDA(cudaEventRecord(h->aux_fork, st));
+    for (int g = 0; g < ng; ++g) BSG_CUDA(cudaStreamWaitEvent(groups[g].stream, h->aux_fork, 0));
+    for (int g = 0; g < ng; ++g) ev_done[g] = h->ev[g];
+  }
+  for (int g = 0; g < ng; ++g) {
+    const Group& G = groups[g];
+    cudaStream_t s2 = G.stream;
+    const int nc_g = G.c1 - G.c0;
+    BSG_TRY(cut_launch_williamson(h, cuts, G.c0, G.c1, s2));
+    BSG_TRY(cut_launch_thermal(h, cuts, G.c0, G.c1, s2));
+    BSG_TRY(cut_queue_status(cuts, G.c0, G.c1, hcut, s2));
+    if (nc_g > 0) {
+      BSG_PROFILED(h, BSG_K_PREP, s2, (double)nc_g * chi,
+                   (lambda_kernel<<<nc_g, 256, 0, s2>>>(res + (size_t)G.c0 * chi, chi, site_tol,
+                                                         Lambdas + (size_t)G.c0 * chi, d_above + G.c0)));
+      BSG_PROFILED(h, BSG_K_PREP, s2, (double)nc_g * chi,
+                   (label_rows_kernel<<<dim3((chi + 127) / 128, nc_g), 128, 0, s2>>>(
+                       num + (size_t)G.c0 * chi * (M - 1), (int64_t)chi * (M - 1), M - 1, kept + G.c0,
+                       M - 1 - G.c0, 1, chi, cut_table(G.c0), d_err + 4 * g)));
+      BSG_CUDA(cudaMemcpyAsync(hkeys + (size_t)G.c0 * chi, tab.key + (size_t)G.c0 * chi, (size_t)nc_g * chi * 8,
+                               cudaMemcpyDeviceToHost, s2));
+      BSG_CUDA(cudaMemcpyAsync(hcnt + G.c0, kept + G.c0, (size_t)nc_g * 4, cudaMemcpyDeviceToHost, s2));
+      BSG_CUDA(cudaMemcpyAsync(habove + G.c0, d_above + G.c0, (size_t)nc_g * 4, cudaMemcpyDeviceToHost, s2));
     }
-    if (si.kind != BSG_SITE_FIRST) {
-      si.rt = cut_table(i - 1);
-      si.KR = hcnt[i - 1];
-      si.hkey_r = hkeys + (size_t)(i - 1) * chi;
-    } else {
-      si.rt = empty;
-      si.KR = 1;
-      si.hkey_r = &zero_key;
+    BSG_CUDA(cudaMemcpyAsync(herr + g, d_err + 4 * g, 4, cudaMemcpyDeviceToHost, s2));
+    BSG_CUDA(cudaEventCreateWithFlags(&ev_keys[g], cudaEventDisableTiming));
+    BSG_CUDA(cudaEventRecord(ev_keys[g], s2));
+    if (g == ng - 1 && ng > 1) {
+      // the middle sites read the boundary cuts T1 - 1 (left) and T2 (right):
+      // their S (Sigma), Lambda and label tables (DP)
+      for (int e = 0; e < ng - 1; ++e) BSG_CUDA(cudaStreamWaitEvent(s2, ev_keys[e], 0));
     }
-    if (si.KL == 0 || si.KR == 0) {
-      set_error("bsg_build_mps: site %d has an empty bond (no Schmidt weight above the tolerance)", i);
-      return BSG_ERR_INVALID;
+    BSG_TRY(launch_sigma_jobs(h, jobs + G.s0, G.s1 - G.s0, wb + o_jobs + sizeof(SigmaJob) * G.s0, s2));
+    for (int i = G.s0; i < G.s1; ++i) {
+      const int Mr = i == 0 ? M : M - i;
+      if (o_sigc[i] != o_sig[i])
+        BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[i]), (int64_t)(2 * Mr) * (2 * Mr), precision,
+                             wb + o_sigc[i], s2));
     }
   }
-  // 6. scatter + one persistent DP launch over all sites
-  BSG_TRY(run_sites(h, in, d, chi, precision, out_dtype, st));
-  h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
+
+  // 4. per group, as its keys arrive: plan its sites and launch their DP
+  static const uint64_t zero_key = 0;
+  int rc = BSG_OK;
+  for (int g = 0; g < ng && rc == BSG_OK; ++g) {
+    const Group& G = groups[g];
+    {
+      auto t_wait = clk::now();
+      const cudaError_t e = cudaEventSynchronize(ev_keys[g]);
+      if (e != cudaSuccess) {
+        set_error("bsg_build_mps: %s", cudaGetErrorString(e));
+        rc = BSG_ERR_CUDA;
+        break;
+      }
+      h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_wait), 0.0);
+    }
+    // every cut this group's sites read has been checked once its keys are here
+    rc = cut_check_status(h, cuts, G.c0, G.c1, hcut);
+    if (rc != BSG_OK) break;
+    if (herr[g]) {
+      set_error("bsg_build_mps: a label row has a multiplicity above %d or more than %d non-zeros", kKeyMaxMult,
+                kMaxNnz);
+      rc = BSG_ERR_LIMIT;
+      break;
+    }
+    auto t_plan = clk::now();
+    std::vector<SiteInput> in(G.s1 - G.s0);
+    for (int i = G.s0; i < G.s1 && rc == BSG_OK; ++i) {
+      SiteInput& si = in[i - G.s0];
+      si.kind = i == 0 ? BSG_SITE_FIRST : i == M - 1 ? BSG_SITE_LAST : BSG_SITE_MIDDLE;
+      si.Mr = i == 0 ? M : M - i;
+      si.sigma = wb + o_sigc[i];
+      si.sigma64 = reinterpret_cast<const double2*>(wb + o_sig[i]);
+      si.Z = d_Z + i;
+      si.gamma = gammas_host[i];
+      if (si.kind != BSG_SITE_LAST) {
+        si.lt = cut_table(i);
+        si.KL = habove[i];
+        si.hkey_l = hkeys + (size_t)i * chi;
+        si.lambda = Lambdas + (size_t)i * chi;
+      } else {
+        si.lt = empty;
+        si.KL = 1;
+        si.hkey_l = &zero_key;
+        si.lambda = nullptr;
+      }
+      if (si.kind != BSG_SITE_FIRST) {
+        si.rt = cut_table(i - 1);
+        si.KR = hcnt[i - 1];
+        si.hkey_r = hkeys + (size_t)(i - 1) * chi;
+      } else {
+        si.rt = empty;
+        si.KR = 1;
+        si.hkey_r = &zero_key;
+      }
+      if (si.KL == 0 || si.KR == 0) {
+        set_error("bsg_build_mps: site %d has an empty bond (no Schmidt weight above the tolerance)", i);
+        rc = BSG_ERR_INVALID;
+      }
+    }
+    if (rc != BSG_OK) break;
+    if (G.dp_stream != G.stream && rc == BSG_OK) {
+      // the group's DP waits for its Sigma (and labels) on the group stream
+      cudaError_t e = cudaEventRecord(ev_done[g], G.stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(G.dp_stream, ev_done[g], 0);
+      if (e != cudaSuccess) {
+        set_error("bsg_build_mps: %s", cudaGetErrorString(e));
+        rc = BSG_ERR_CUDA;
+      }
+    }
+    if (!in.empty() && rc == BSG_OK)
+      rc = run_sites(h, in, d, chi, precision, out_dtype, h->slot[G.slot], G.dp_stream);
+    h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
+  }
+  // join every stream of every group into st before returning (also on
+  // errors: the side streams must be idle before the workspaces are reused)
+  if (ng > 1) {
+    int e = 4;
+    for (int g = 0; g < ng; ++g) {
+      cudaEventRecord(h->ev[e], groups[g].stream);
+      cudaStreamWaitEvent(st, h->ev[e], 0);
+      ++e;
+      if (groups[g].dp_stream != groups[g].stream) {
+        cudaEventRecord(h->ev[e], groups[g].dp_stream);
+        cudaStreamWaitEvent(st, h->ev[e], 0);
+        ++e;
+      }
+    }
+  }
+  for (int g = 0; g < ng; ++g)
+    if (ev_keys[g]) cudaEventDestroy(ev_keys[g]);
+  if (rc != BSG_OK) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
   // Sigma status (singular A) -- read after the DP so the check costs no extra wait
   std::vector<int> sst(M);
   BSG_CUDA(cudaMemcpyAsync(sst.data(), d_status, (size_t)M * 4, cudaMemcpyDeviceToHost, st));

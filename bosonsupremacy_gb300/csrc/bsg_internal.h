@@ -69,6 +69,7 @@ struct ProgramSet {
   int32_t* d_st_ra = nullptr;
   uint32_t* d_trans = nullptr;
   size_t dev_states_cap = 0, dev_trans_cap = 0, dev_prog_cap = 0;
+  size_t dev_states_n = 0, dev_trans_n = 0, dev_prog_n = 0;  // entries already on the device
   bool dev_valid = false;
   int max_states = 1;
   int max_k = 0;
@@ -138,6 +139,36 @@ struct HostBuf {  // pinned host staging
   void release();
 };
 
+// Launch arguments of the cut-spectra kernels (bsg_cuts.cu).
+struct CutArgs {
+  const double* sq_cov;
+  int M, L0, n_cuts, d, chi;
+  double err_tol;
+  double* ws;          // per cut: 4 * nmax^2 doubles
+  size_t ws_stride;    // doubles per cut
+  double* S;           // [n_cuts, 2(M-1), 2(M-1)]
+  int ldS;
+  double* nbar;        // [n_cuts, kmax]
+  int kmax;
+  double* res;         // [n_cuts, chi]
+  int8_t* num;         // [n_cuts, chi, M-1]
+  int32_t* kept;       // [n_cuts]
+  uint32_t* rec;       // per cut: kmax * chi records (parent << 8 | digit)
+  int* status;         // [n_cuts]
+  int* sweeps;         // [n_cuts] Jacobi sweeps used
+  double* mu;          // [n_cuts, 2 kmax] eigenvalues of G^T G, then 1/nu per pair
+  int max_sweeps;
+  int c0;              // first cut of this launch (block b handles cut c0 + b)
+};
+
+int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
+                double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);
+int cut_launch_williamson(bsg_handle_t h, const CutArgs& a, int c0, int c1, cudaStream_t st);
+int cut_launch_thermal(bsg_handle_t h, const CutArgs& a, int c0, int c1, cudaStream_t st);
+// status of cuts [c0, c1) into hst[c0..c1) and their sweep counts into hst[n_cuts + c0 ..)
+int cut_queue_status(const CutArgs& a, int c0, int c1, int* hst, cudaStream_t st);
+int cut_check_status(bsg_handle_t h, const CutArgs& a, int c0, int c1, const int* status);
+
 // One Sigma construction (bsg_sigma.cu).
 struct SigmaJob {
   const double* S_l;  // [2 m_l, 2 m_l] (leading dimension ld_l) or null
@@ -182,7 +213,20 @@ struct bsg_handle_s {
   bsg::HostBuf host_stage;    // pinned staging for plans
   bsg::HostBuf host_stage2;
   bsg::Profiler prof;
-  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192};
+  // side streams for concurrent launches (created on first use) and events:
+  // aux_stream (FP64 helper), grp[3] high-priority streams of the build
+  // groups, dp_lo[2] low-priority streams of the edge groups' DP
+  cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[2] = {};
+  cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
+  cudaEvent_t ev[12] = {};
+  int ensure_aux();
+  // per-group buffers of the site DP (plan tables, item slots, per-warp
+  // scratch, pinned plan staging); slot 0 serves the single-site calls
+  struct SiteSlot {
+    bsg::DevBuf plan, items, scratch;
+    bsg::HostBuf stage;
+  } slot[3];
+  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0};
 };
 
 // Brackets a kernel launch with profiler events when profiling is on.

@@ -118,8 +118,12 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
   return BSG_OK;
 }
 
+// Appends v[done:] to the device copy; a copy that must grow is reallocated
+// (cudaFree waits for the device, so no launch still reads the old one) and
+// refilled.  Entries already on the device are never rewritten, so launches
+// in flight on other streams keep reading valid programs.
 template <class T>
-static int upload(T*& dptr, size_t& cap, const std::vector<T>& v, cudaStream_t stream) {
+static int upload(T*& dptr, size_t& cap, size_t done, const std::vector<T>& v, cudaStream_t stream) {
   size_t need = std::max<size_t>(v.size(), 1);
   if (need > cap) {
     if (dptr) cudaFree(dptr);
@@ -127,26 +131,32 @@ static int upload(T*& dptr, size_t& cap, const std::vector<T>& v, cudaStream_t s
     size_t c = std::max(need, cap * 2);
     BSG_CUDA(cudaMalloc(&dptr, c * sizeof(T)));
     cap = c;
+    done = 0;
   }
-  if (!v.empty()) BSG_CUDA(cudaMemcpyAsync(dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+  if (v.size() > done)
+    BSG_CUDA(cudaMemcpyAsync(dptr + done, v.data() + done, (v.size() - done) * sizeof(T), cudaMemcpyHostToDevice,
+                             stream));
   return BSG_OK;
 }
 
 int programs_upload(ProgramSet& ps, cudaStream_t stream) {
   if (ps.dev_valid) return BSG_OK;
   size_t pc = ps.dev_prog_cap, pc2 = ps.dev_prog_cap, pc3 = ps.dev_prog_cap;
-  BSG_TRY(upload(ps.d_k, pc, ps.k, stream));
-  BSG_TRY(upload(ps.d_nstates, pc2, ps.nstates, stream));
-  BSG_TRY(upload(ps.d_state_off, pc3, ps.state_off, stream));
+  BSG_TRY(upload(ps.d_k, pc, ps.dev_prog_n, ps.k, stream));
+  BSG_TRY(upload(ps.d_nstates, pc2, ps.dev_prog_n, ps.nstates, stream));
+  BSG_TRY(upload(ps.d_state_off, pc3, ps.dev_prog_n, ps.state_off, stream));
   ps.dev_prog_cap = pc;
+  ps.dev_prog_n = ps.k.size();
   size_t sc = ps.dev_states_cap, sc2 = ps.dev_states_cap, sc3 = ps.dev_states_cap;
-  BSG_TRY(upload(ps.d_st_trans_off, sc, ps.st_trans_off, stream));
-  BSG_TRY(upload(ps.d_st_trans_cnt, sc2, ps.st_trans_cnt, stream));
-  BSG_TRY(upload(ps.d_st_ra, sc3, ps.st_ra, stream));
+  BSG_TRY(upload(ps.d_st_trans_off, sc, ps.dev_states_n, ps.st_trans_off, stream));
+  BSG_TRY(upload(ps.d_st_trans_cnt, sc2, ps.dev_states_n, ps.st_trans_cnt, stream));
+  BSG_TRY(upload(ps.d_st_ra, sc3, ps.dev_states_n, ps.st_ra, stream));
   ps.dev_states_cap = sc;
-  BSG_TRY(upload(ps.d_trans, ps.dev_trans_cap, ps.trans, stream));
-  // The host vectors stay alive in `ps`; the stream must finish the copies
-  // before they are modified again -- callers synchronise after planning.
+  ps.dev_states_n = ps.st_trans_off.size();
+  BSG_TRY(upload(ps.d_trans, ps.dev_trans_cap, ps.dev_trans_n, ps.trans, stream));
+  ps.dev_trans_n = ps.trans.size();
+  // Copies from these pageable vectors are staged before cudaMemcpyAsync
+  // returns, so the host may append programs right away.
   ps.dev_valid = true;
   return BSG_OK;
 }

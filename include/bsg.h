@@ -237,7 +237,9 @@ int bsg_gemm_tf32x3(bsg_handle_t h, const float* A, const float* B, float* C, in
                                         launch with small per-warp slices, 0..4096 (default 64; 0 = one launch) */
 #define BSG_TUNE_DP_SMALL_BLOCKS 3   /* resident DP blocks per SM in that second launch, 1..8 (default 8) */
 #define BSG_TUNE_DP_SCRATCH_MIB 4    /* device memory for per-warp DP tables per launch, 64..65536 MiB (default 8192) */
-#define BSG_TUNE_COUNT 5
+#define BSG_TUNE_DP_FP64_BLOCKS 5    /* split precision: resident blocks per SM of a concurrent FP64 DP
+                                        launch sharing the work queue (FP64 pipe), 0..8 (default 0 = off) */
+#define BSG_TUNE_COUNT 6
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

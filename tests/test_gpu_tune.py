@@ -47,3 +47,32 @@ def test_launch_split_bit_identical(cuda, golden, prec):
     for other in outs[1:]:
         for a, b in zip(outs[0], other):
             assert np.array_equal(a, b)
+
+
+def test_fp64_helper_launch(cuda, golden):
+    """Split build with the concurrent FP64 DP helper: items taken by the
+    helper are computed in FP64, the rest in split precision; every Gamma
+    agrees with the split-only build to split accuracy and the pattern
+    probabilities still match the reference."""
+    import torch
+    from bosonsupremacy_gb300 import autotune
+    from bosonsupremacy_gb300.pipeline import build_mps
+    from oracle import reference_mps as R
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    saved = autotune.get_knobs()
+    try:
+        autotune.set_knobs(fp64_blocks=0)
+        base = build_mps(t["sq_cov"], d, chi, precision="split", out_dtype=torch.complex128)
+        autotune.set_knobs(fp64_blocks=2, blocks_per_sm=4, small_blocks=4)
+        mps = build_mps(t["sq_cov"], d, chi, precision="split", out_dtype=torch.complex128)
+    finally:
+        autotune.set_knobs(**saved)
+    for g0, g1 in zip(base.Gammas, mps.Gammas):
+        a, b = g0.cpu().numpy(), g1.cpu().numpy()
+        assert np.abs(a - b).max() <= 1e-9 * max(1.0, np.abs(a).max())
+    G = [g.cpu().numpy() for g in mps.Gammas]
+    p = np.abs(R.pattern_amplitudes(G, list(mps.Lambdas.cpu().numpy()), t["patterns"])) ** 2
+    pr = t["pattern_probs"]
+    big = pr > 1e-8 * pr.max()
+    assert (np.abs(p[big] - pr[big]) / pr[big]).max() <= 1e-6

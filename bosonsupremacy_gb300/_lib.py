@@ -55,6 +55,7 @@ SIGNATURES = {
     "bsg_tune_set": (_I, [_P, _I, _I]),
     "bsg_tune_get": (_I, [_P, _I, C.POINTER(_I)]),
     "bsg_sample": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _L, _I, _P, _P]),
+    "bsg_profile_cut_phases": (_I, [_P, C.POINTER(_I), C.POINTER(_I), _P]),
     "bsg_displacements": (_I, [_P, _P, _L, _I, _P, _P]),
 }
 

@@ -162,6 +162,18 @@ int bsg_profile_read(bsg_handle_t h, int cls, double* total_ms, int64_t* launche
   return BSG_OK;
 }
 
+int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* ms) {
+  BSG_CHECK_ARG(h, "bsg_profile_cut_phases: null handle");
+  const int np = bsg::kCutPhases - 1;
+  const int nc = int(h->prof.cut_phases.size() / bsg::kCutPhases);
+  if (n_cuts) *n_cuts = nc;
+  if (n_phases) *n_phases = np;
+  if (ms)
+    for (int c = 0; c < nc; ++c)
+      for (int i = 0; i < np; ++i) ms[(size_t)c * np + i] = h->prof.cut_phases[(size_t)c * bsg::kCutPhases + i + 1];
+  return BSG_OK;
+}
+
 int bsg_tune_set(bsg_handle_t h, int key, int value) {
   BSG_CHECK_ARG(h, "bsg_tune_set: null handle");
   BSG_CHECK_ARG(key >= 0 && key < BSG_TUNE_COUNT, "bsg_tune_set: unknown key %d", key);

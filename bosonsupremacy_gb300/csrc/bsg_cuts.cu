@@ -55,8 +55,8 @@ __device__ double block_sum(double v, double* red) {
 // disjoint rotations per step, each thread updating whole 2x2 blocks of
 // J1^T B J2 (and the transposed block), so a step needs two barriers.
 // Returns the number of sweeps, or -1 if max_sweeps did not converge.
-__device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, double* red, double* cs, double* sn,
-                            int* pos) {
+template <class T>
+__device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, double* red, T* cs, T* sn, int* pos) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t mm = (size_t)m * m;
   const int P = m / 2;
@@ -64,13 +64,13 @@ __device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, doubl
     double off = 0.0, dia = 0.0;
     for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
-      const double h = Hm[t];
+      const double h = double(Hm[t]);
       if (i < j) off += h * h;
       else if (i == j) dia += h * h;
     }
     off = block_sum(off, red);
     dia = block_sum(dia, red);
-    if (off <= 1e-26 * dia) return sweep;
+    if (off <= tol * dia) return sweep;
     for (int step = 0; step < m - 1; ++step) {
       for (int i = tid; i < m; i += nt) pos[i] = i == 0 ? 0 : ((i - 1 + step) % (m - 1)) + 1;
       __syncthreads();
@@ -81,16 +81,18 @@ __device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, doubl
           p = q;
           q = x;
         }
-        const double hpq = Hm[(size_t)p * m + q];
+        const double hpq = double(Hm[(size_t)p * m + q]);
+        const double skip = sizeof(T) == 8 ? 1e-17 : 1e-8;
         double c_ = 1.0, s_ = 0.0;
-        if (fabs(hpq) > 1e-300 && fabs(hpq) > 1e-17 * sqrt(fabs(Hm[(size_t)p * m + p] * Hm[(size_t)q * m + q]))) {
-          const double th = (Hm[(size_t)q * m + q] - Hm[(size_t)p * m + p]) / (2.0 * hpq);
+        const double hpp = double(Hm[(size_t)p * m + p]), hqq = double(Hm[(size_t)q * m + q]);
+        if (fabs(hpq) > 1e-300 && fabs(hpq) > skip * sqrt(fabs(hpp * hqq))) {
+          const double th = (hqq - hpp) / (2.0 * hpq);
           const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
           c_ = 1.0 / sqrt(tt * tt + 1.0);
           s_ = tt * c_;
         }
-        cs[q0] = c_;
-        sn[q0] = s_;
+        cs[q0] = T(c_);
+        sn[q0] = T(s_);
       }
       __syncthreads();
       for (int t = tid; t < P * P; t += nt) {
@@ -99,18 +101,18 @@ __device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, doubl
         int p1 = pos[m1], q1 = pos[m - 1 - m1], p2 = pos[m2], q2 = pos[m - 1 - m2];
         if (p1 > q1) { const int x = p1; p1 = q1; q1 = x; }
         if (p2 > q2) { const int x = p2; p2 = q2; q2 = x; }
-        const double c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
-        const double b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
-        const double b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
-        const double r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
-        const double r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
-        const double o00 = c2 * r00 - s2 * r01;
-        double o01 = s2 * r00 + c2 * r01;
-        double o10 = c2 * r10 - s2 * r11;
-        const double o11 = s2 * r10 + c2 * r11;
+        const T c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
+        const T b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
+        const T b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
+        const T r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
+        const T r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
+        const T o00 = c2 * r00 - s2 * r01;
+        T o01 = s2 * r00 + c2 * r01;
+        T o10 = c2 * r10 - s2 * r11;
+        const T o11 = s2 * r10 + c2 * r11;
         if (m1 == m2) {
-          o01 = 0.0;
-          o10 = 0.0;
+          o01 = T(0);
+          o10 = T(0);
         }
         Hm[(size_t)p1 * m + p2] = o00;
         Hm[(size_t)p1 * m + q2] = o01;
@@ -127,8 +129,8 @@ __device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, doubl
         const int q0 = t / m, j = t % m;
         int p = pos[q0], q = pos[m - 1 - q0];
         if (p > q) { const int x = p; p = q; q = x; }
-        const double c_ = cs[q0], s_ = sn[q0];
-        const double hp = QT[(size_t)p * m + j], hq = QT[(size_t)q * m + j];
+        const T c_ = cs[q0], s_ = sn[q0];
+        const T hp = QT[(size_t)p * m + j], hq = QT[(size_t)q * m + j];
         QT[(size_t)p * m + j] = c_ * hp - s_ * hq;
         QT[(size_t)q * m + j] = s_ * hp + c_ * hq;
       }
@@ -136,6 +138,75 @@ __device__ int block_jacobi(double* Hm, int m, double* QT, int max_sweeps, doubl
     }
   }
   return -1;
+}
+
+// Mixed-precision Jacobi of the symmetric m x m matrix Hm with eigenvector
+// rows accumulated in QT: FP32 sweeps on a rounded copy (the FP32 pipe is
+// ~64x the FP64 one on GB300) until the off-diagonal is ~1e-5 of the
+// diagonal, two FP64 Newton-Schulz steps QT <- 1.5 QT - 0.5 (QT QT^T) QT
+// that make the FP32 eigenvectors orthonormal to rounding, the FP64
+// projection QT Hm QT^T, and FP64 sweeps on that nearly diagonal matrix
+// (quadratic convergence: ~2 sweeps instead of ~8).  s1, s2: m*m doubles of
+// scratch each.  Returns the FP64 sweeps used (+2 for the projection work),
+// or -1 when the FP64 sweeps did not converge.
+__device__ int mixed_jacobi(double* Hm, int m, double* QT, int max_sweeps, double* s1, double* s2, double* red,
+                            double* cs, double* sn, int* pos, unsigned long long* sweep_log) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const size_t mm = (size_t)m * m;
+  float* H32 = reinterpret_cast<float*>(s1);
+  float* Q32 = H32 + mm;  // s1 holds 2 m^2 floats
+  for (size_t t = tid; t < mm; t += nt) {
+    H32[t] = float(Hm[t]);
+    Q32[t] = (t / m == t % m) ? 1.f : 0.f;
+  }
+  __syncthreads();
+  const int sw32 =
+      block_jacobi<float>(H32, m, Q32, 16, 1e-10, red, reinterpret_cast<float*>(cs), reinterpret_cast<float*>(sn), pos);
+  for (size_t t = tid; t < mm; t += nt) QT[t] = double(Q32[t]);
+  __syncthreads();
+  for (int it = 0; it < 2; ++it) {
+    for (size_t t = tid; t < mm; t += nt) {  // s2 = QT QT^T
+      const int i = int(t / m), j = int(t % m);
+      double acc = 0.0;
+      for (int r = 0; r < m; ++r) acc = fma(QT[(size_t)i * m + r], QT[(size_t)j * m + r], acc);
+      s2[t] = acc;
+    }
+    __syncthreads();
+    for (size_t t = tid; t < mm; t += nt) {  // s1 = 1.5 QT - 0.5 s2 QT
+      const int i = int(t / m), j = int(t % m);
+      double acc = 0.0;
+      for (int r = 0; r < m; ++r) acc = fma(s2[(size_t)i * m + r], QT[(size_t)r * m + j], acc);
+      s1[t] = 1.5 * QT[t] - 0.5 * acc;
+    }
+    __syncthreads();
+    for (size_t t = tid; t < mm; t += nt) QT[t] = s1[t];
+    __syncthreads();
+  }
+  for (size_t t = tid; t < mm; t += nt) {  // s1 = Hm QT^T
+    const int i = int(t / m), j = int(t % m);
+    double acc = 0.0;
+    for (int r = 0; r < m; ++r) acc = fma(Hm[(size_t)i * m + r], QT[(size_t)j * m + r], acc);
+    s1[t] = acc;
+  }
+  __syncthreads();
+  for (size_t t = tid; t < mm; t += nt) {  // s2 = QT s1
+    const int i = int(t / m), j = int(t % m);
+    double acc = 0.0;
+    for (int r = 0; r < m; ++r) acc = fma(QT[(size_t)i * m + r], s1[(size_t)r * m + j], acc);
+    s2[t] = acc;
+  }
+  __syncthreads();
+  for (size_t t = tid; t < mm; t += nt) {  // symmetrise into Hm
+    const int i = int(t / m), j = int(t % m);
+    Hm[t] = 0.5 * (s2[t] + s2[(size_t)j * m + i]);
+  }
+  __syncthreads();
+  const int sw = block_jacobi<double>(Hm, m, QT, max_sweeps, 1e-26, red, cs, sn, pos);
+  if (sweep_log && threadIdx.x == 0) {
+    sweep_log[0] = (unsigned long long)(sw32 < 0 ? 99 : sw32);
+    sweep_log[1] = (unsigned long long)(sw < 0 ? 99 : sw);
+  }
+  return sw < 0 ? -1 : sw + 2;
 }
 
 // In-place right-looking Cholesky of the m x m SPD matrix X (lower triangle,
@@ -170,6 +241,16 @@ __device__ bool block_cholesky(double* X, int m, int* s_flag, double* s_scalar) 
   return true;
 }
 
+// Phase timestamps of the Williamson kernel (profiling only): thread 0 of
+// each cut's CTA writes the global nanosecond timer at each phase boundary.
+__device__ __forceinline__ void phase_stamp(const CutArgs& a, int c, int i) {
+  if (a.phase_t && threadIdx.x == 0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    a.phase_t[(size_t)c * kCutPhases + i] = t;
+  }
+}
+
 __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   const int c = a.c0 + blockIdx.x;
   const int L = a.L0 + c, M = a.M;
@@ -182,6 +263,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   double* H = Gm + nn;   // H (full path) / F and its reflectors (low-rank path) / accepted vectors
   double* X1 = H + nn;   // low-rank path: V_A -> L_A, then K = I - R R^T
   double* X2 = X1 + nn;  // low-rank path: L_A^{-1} C, then eigenvector rows of K
+  // (X2 + nn: one more n^2 block of Jacobi scratch)
   double* MU = a.mu + (size_t)c * (2 * a.kmax);
   extern __shared__ double sm[];
   double* red = sm;                   // 33
@@ -196,6 +278,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   __shared__ double s_scalar;
 
   auto gidx = [&](int i) { return i < k ? L + i : M + L + (i - k); };
+  phase_stamp(a, c, 0);
   // 1. V and the symmetry check of the reference (norm(V - V^T) < 1e-11)
   double asym = 0.0;
   for (size_t i = tid; i < nn; i += nt) {
@@ -210,11 +293,13 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     if (tid == 0) a.status[c] = 1;
     return;
   }
+  phase_stamp(a, c, 1);
   // 2. Cholesky V = L L^T
   if (!block_cholesky(A, n, &s_flag, &s_scalar)) {
     if (tid == 0) a.status[c] = 2;
     return;
   }
+  phase_stamp(a, c, 2);
   // 3. W = L^{-1}: forward substitution on all columns, row by row
   for (size_t i = tid; i < nn; i += nt) W[i] = (i / n == i % n) ? 1.0 : 0.0;
   __syncthreads();
@@ -229,6 +314,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     }
     __syncthreads();
   }
+  phase_stamp(a, c, 3);
   // 4. G = W Omega W^T: G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r]
   for (size_t t = tid; t < nn; t += nt) {
     const int i = int(t / n), j = int(t % n);
@@ -240,6 +326,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   __syncthreads();
   int sweeps = 0;
   if (nA >= n) {
+    phase_stamp(a, c, 4);
     // 5a. full path: H = G^T G, Jacobi with eigenvector rows in W
     for (size_t t = tid; t < nn; t += nt) {
       const int i = int(t / n), j = int(t % n);
@@ -248,11 +335,13 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       H[t] = s;
     }
     __syncthreads();
-    for (size_t t = tid; t < nn; t += nt) W[t] = (t / n == t % n) ? 1.0 : 0.0;
-    __syncthreads();
-    sweeps = block_jacobi(H, n, W, a.max_sweeps, red, cs, sn, pos);
+    phase_stamp(a, c, 5);
+    sweeps = mixed_jacobi(H, n, W, a.max_sweeps, X1, X2, red, cs, sn, pos,
+                          a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
+    phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
   } else {
+    phase_stamp(a, c, 4);
     // 5b. low-rank path (L < k): for a pure global state H = I - F F^T with
     // F = L^{-1} C^T L_A^{-T} (C the left-right block of sq_cov, V_A = L_A L_A^T),
     // so the non-trivial spectrum lives in range(F): QR of F, Jacobi on the
@@ -326,10 +415,13 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       double s = 0.0;
       for (int q = (i > j ? i : j); q < nA; ++q) s += H[(size_t)i * nA + q] * H[(size_t)j * nA + q];
       X1[t] = (i == j ? 1.0 : 0.0) - s;
-      X2[t] = (i == j ? 1.0 : 0.0);
     }
     __syncthreads();
-    sweeps = block_jacobi(X1, nA, X2, a.max_sweeps, red, cs, sn, pos);
+    // W (L^{-1}) is not read again before the back-transform overwrites it
+    phase_stamp(a, c, 5);
+    sweeps = mixed_jacobi(X1, nA, X2, a.max_sweeps, W, X2 + nn, red, cs, sn, pos,
+                          a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
+    phase_stamp(a, c, 6);
     // eigenvector rows of H in the full space: u_i = Q z_i, z_i = [K eigvec; 0] or e_i
     for (int i = (tid >> 5); i < n; i += nt >> 5) {
       double* z = W + (size_t)i * n;
@@ -352,6 +444,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     if (tid == 0) a.status[c] = 3;
     return;
   }
+  phase_stamp(a, c, 7);
   // 7. order by mu ascending (nu descending), ties by index
   for (int i = tid; i < n; i += nt) {
     const double mi = MU[i];
@@ -363,6 +456,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     order[r] = i;
   }
   __syncthreads();
+  phase_stamp(a, c, 8);
   // 8. pair eigenvectors x with y = G x / |G x|.  Candidates are grouped in
   // even-sized clusters of (nearly) equal mu; inside a cluster the next x is
   // the candidate with the largest residual after projecting out the pairs
@@ -468,6 +562,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     if (tid == 0) a.status[c] = 4;
     return;
   }
+  phase_stamp(a, c, 9);
   // 9. S = L [y | x] nu^{-1/2}, nbar = max(0, (nu - 1)/2)
   for (int pi = 0; pi < k; ++pi) {
     const double* x = Xacc + (size_t)(2 * pi) * n;
@@ -491,6 +586,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     }
   }
   __syncthreads();
+  phase_stamp(a, c, 10);
   if (tid == 0) a.status[c] = 0;
 }
 
@@ -627,7 +723,7 @@ int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts,
   a.d = d;
   a.chi = chi;
   a.err_tol = err_tol;
-  a.ws_stride = (size_t)6 * nmax * nmax;
+  a.ws_stride = (size_t)7 * nmax * nmax;
   a.S = S;
   a.ldS = 2 * (M - 1);
   a.kmax = kmax;
@@ -640,8 +736,10 @@ int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts,
   const size_t mu_bytes = (size_t)n_cuts * 2 * kmax * 8;
   const size_t rec_bytes = (size_t)n_cuts * kmax * chi * 4;
   const size_t st_bytes = (size_t)n_cuts * 8;
+  const size_t ph_bytes = (size_t)n_cuts * kCutPhases * 8;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes) + al(mu_bytes)));
+  BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes) + al(mu_bytes) +
+                           al(ph_bytes)));
   char* base = reinterpret_cast<char*>(h->cut_ws.ptr);
   a.ws = reinterpret_cast<double*>(base);
   a.nbar = reinterpret_cast<double*>(base + al(ws_bytes));
@@ -649,6 +747,12 @@ int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts,
   a.status = reinterpret_cast<int*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes));
   a.sweeps = a.status + n_cuts;
   a.mu = reinterpret_cast<double*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes));
+  a.phase_t = nullptr;
+  if (h->prof.on) {
+    a.phase_t = reinterpret_cast<unsigned long long*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) +
+                                                      al(st_bytes) + al(mu_bytes));
+    BSG_CUDA(cudaMemsetAsync(a.phase_t, 0, ph_bytes, st));
+  }
   BSG_CUDA(cudaMemsetAsync(a.status, 0xff, st_bytes, st));
   BSG_CUDA(cudaMemsetAsync(res, 0, (size_t)n_cuts * chi * 8, st));
   BSG_CUDA(cudaMemsetAsync(num, 0, (size_t)n_cuts * chi * (M - 1), st));
@@ -679,6 +783,29 @@ int cut_launch_thermal(bsg_handle_t h, const CutArgs& args, int c0, int c1, cuda
   double ranked = 0.0;
   for (int c = c0; c < c1; ++c) ranked += (double)(a.M - a.L0 - c) * a.chi * a.d;
   BSG_PROFILED(h, BSG_K_THERMAL, st, ranked, (thermal_kernel<<<c1 - c0, 1024, tsm, st>>>(a)));
+  return BSG_OK;
+}
+
+// Copies the phase timestamps of the last profiled launch into the profiler
+// (synchronises `st`; profiling only).
+int cut_read_phases(bsg_handle_t h, const CutArgs& a, cudaStream_t st) {
+  if (!a.phase_t) return BSG_OK;
+  std::vector<unsigned long long> t((size_t)a.n_cuts * kCutPhases);
+  BSG_CUDA(cudaMemcpyAsync(t.data(), a.phase_t, t.size() * 8, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaStreamSynchronize(st));
+  h->prof.cut_phases.assign(t.size(), 0.0);
+  for (int c = 0; c < a.n_cuts; ++c) {
+    // a phase the cut skipped (the other path's stamp) is charged to the next one
+    unsigned long long prev = t[(size_t)c * kCutPhases];
+    for (int i = 1; i < kCutTimedPhases; ++i) {
+      const unsigned long long v = t[(size_t)c * kCutPhases + i];
+      if (v == 0 || prev == 0) continue;
+      h->prof.cut_phases[(size_t)c * kCutPhases + i] = double(v - prev) * 1e-6;
+      prev = v;
+    }
+    for (int i = kCutTimedPhases; i < kCutPhases; ++i)
+      h->prof.cut_phases[(size_t)c * kCutPhases + i] = double(t[(size_t)c * kCutPhases + i]);
+  }
   return BSG_OK;
 }
 
@@ -747,5 +874,6 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   std::vector<int> status(2 * n_cuts);
   BSG_TRY(cut_queue_status(a, 0, n_cuts, status.data(), st));
   BSG_CUDA(cudaStreamSynchronize(st));
+  BSG_TRY(cut_read_phases(h, a, st));
   return cut_check_status(h, a, 0, n_cuts, status.data());
 }

@@ -213,6 +213,7 @@ struct ProgDev {
   const int32_t* st_trans_cnt;
   const int32_t* st_ra;
   const uint32_t* trans;
+  const uint4* st_pack;  // {first transition, count | r_a << 16, F slot, 0} per state
 };
 
 enum { MODE_SITE = 0, MODE_TARGETS = 1, MODE_MATRICES = 2 };
@@ -331,7 +332,7 @@ __device__ __forceinline__ int build_classes(const DPArgs& a, const SiteDesc* sd
 }
 
 template <class P, int MODE>
-__global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
+__global__ void __launch_bounds__(256, 6) dp_kernel(DPArgs a) {
   using C = typename P::C;
   using CA = typename P::CA;
   using CF = typename P::CF;
@@ -377,12 +378,12 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
       const int64_t rowb = sb + (int64_t)cls[bq] * n_len;
       for (int aq = 0; aq <= bq; ++aq) Ab[(size_t)pair_index(aq, bq) * 32 + lane] = sig[rowb + cls[aq]];
     }
-    // run the program
+    // run the program (the final coefficient stays in a register)
     Fb[lane] = P::one();
+    CF fin = P::one();
     for (int s = 1; s < ns; ++s) {
-      const int off = __ldg(a.prog.st_trans_off + so + s);
-      const int cnt = __ldg(a.prog.st_trans_cnt + so + s);
-      const int ra = __ldg(a.prog.st_ra + so + s);
+      const uint4 pk = __ldg(a.prog.st_pack + so + s);
+      const int off = int(pk.x), cnt = int(pk.y & 0xffffu), ra = int(pk.y >> 16);
       typename P::Acc acc = P::zero();
       for (int t = 0; t < cnt; ++t) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
@@ -390,7 +391,8 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
         const CF fv = Fb[(size_t)(w >> 12) * 32 + lane];
         P::mac(acc, av, fv);
       }
-      Fb[(size_t)s * 32 + lane] = P::finish(acc, ra, c_inv_d, c_inv_f);
+      fin = P::finish(acc, ra, c_inv_d, c_inv_f);
+      Fb[(size_t)pk.z * 32 + lane] = fin;
     }
     if (!live) continue;
     if (MODE == MODE_SITE) {
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
       if constexpr (std::is_same<P, PrecSplit>::value) {
         if (!sd->out_c128) {
         // epilogue on the FP32 pipe: (hi + lo) * sqrt(j!) * l_scale * r_rowfact as FP32 pairs
-        const float4 q = Fb[(size_t)(ns - 1) * 32 + lane];  // (re_h, re_l, im_h, im_l)
+        const float4 q = fin;  // (re_h, re_l, im_h, im_l)
         const float2 js = c_sqrt_fact2[j], ls = sd->l_scale2[beta], rs = sd->r_rowfact2[alpha];
         float sh, sl, th, tl, re_h, re_l, im_h, im_l;
         PrecSplit::mul(js.x, js.y, ls.x, ls.y, sh, sl);
@@ -412,7 +414,7 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
         }
       }
       if (!done) {
-        const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
+        const double2 v = P::to_c128(fin);
         const double scale = c_sqrt_fact[j] * sd->l_scale[beta] * sd->r_rowfact[alpha];
         if (sd->out_c128) {
           __stcs(reinterpret_cast<double2*>(sd->gamma) + o, make_double2(v.x * scale, v.y * scale));
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(256) dp_kernel(DPArgs a) {
         }
       }
     } else {
-      const double2 v = P::to_c128(Fb[(size_t)(ns - 1) * 32 + lane]);
+      const double2 v = P::to_c128(fin);
       double s = fac;
       if (a.den) s /= a.den[item];
       a.out[item] = make_double2(v.x * s, v.y * s);
@@ -543,7 +545,7 @@ static int64_t prog_trans(const bsg::ProgramSet& ps, int p) {
 // Programs with at most `small_entries` table entries (class pairs + DP
 // states) per item run in their own DP launch with small per-warp slices.
 static bool small_program(const bsg::ProgramSet& ps, int p, int small_entries) {
-  return ps.k[p] * (ps.k[p] + 1) / 2 + ps.nstates[p] <= small_entries;
+  return ps.k[p] * (ps.k[p] + 1) / 2 + ps.fslots[p] <= small_entries;
 }
 
 static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets& bk, std::vector<int32_t>& remap) {
@@ -579,7 +581,7 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
     const int p = out.progs[b];
     const int kk = ps.k[p];
     out.pairs_max = std::max(out.pairs_max, kk * (kk + 1) / 2);
-    out.states_max = std::max(out.states_max, ps.nstates[p]);
+    out.states_max = std::max(out.states_max, ps.fslots[p]);
     out.work += (double)out.counts[b] * (double)prog_trans(ps, p);
     if (off > INT32_MAX) {
       set_error("too many work items in one launch (%lld)", (long long)off);
@@ -618,7 +620,8 @@ static void group_rows(const uint64_t* key, int rows, std::vector<int32_t>& perm
 }
 
 static ProgDev prog_dev(const bsg::ProgramSet& ps) {
-  return ProgDev{ps.d_k, ps.d_nstates, ps.d_state_off, ps.d_st_trans_off, ps.d_st_trans_cnt, ps.d_st_ra, ps.d_trans};
+  return ProgDev{ps.d_k,  ps.d_nstates, ps.d_state_off, ps.d_st_trans_off, ps.d_st_trans_cnt,
+                 ps.d_st_ra, ps.d_trans, ps.d_st_pack};
 }
 
 // Launch shape for chunks [c0, c1) whose programs need at most (pmax, smax)
@@ -665,7 +668,7 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     const int p = bk.progs[b];
     DPLaunch& L = b < first_small ? Lb : Ls;
     L.pmax = std::max(L.pmax, ps.k[p] * (ps.k[p] + 1) / 2);
-    L.smax = std::max(L.smax, ps.nstates[p]);
+    L.smax = std::max(L.smax, ps.fslots[p]);
     L.work += (double)bk.counts[b] * (double)prog_trans(ps, p);
   }
   dp_shape<P>(h, h->tune[BSG_TUNE_DP_SMALL_BLOCKS], Ls);
@@ -1562,6 +1565,7 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
   auto t_fin = clk::now();
   BSG_CUDA(cudaStreamSynchronize(st));
   h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_fin), 0.0);
+  BSG_TRY(cut_read_phases(h, cuts, st));
   for (int i = 0; i < M; ++i)
     if (sst[i]) {
       set_error("bsg_build_mps: site %d: the Gaussian unitary's A block is singular", i);

@@ -58,7 +58,9 @@ struct ProgramSet {
   std::vector<int32_t> st_trans_off;   // per global state: first transition
   std::vector<int32_t> st_trans_cnt;   // per global state: number of transitions
   std::vector<int32_t> st_ra;          // per global state: r_a (0 for the empty state)
-  std::vector<uint32_t> trans;         // packed (src_local << 12) | pair(a, b)
+  std::vector<uint32_t> trans;         // packed (src F slot << 12) | pair(a, b)
+  std::vector<int32_t> fslots;         // F table entries per program (two levels of states)
+  std::vector<uint4> st_pack;          // per global state: {first transition, count | r_a << 16, F slot, 0}
   std::unordered_map<uint64_t, int32_t> index;
   // device copies (valid when dev_valid)
   int32_t* d_k = nullptr;
@@ -68,6 +70,7 @@ struct ProgramSet {
   int32_t* d_st_trans_cnt = nullptr;
   int32_t* d_st_ra = nullptr;
   uint32_t* d_trans = nullptr;
+  uint4* d_st_pack = nullptr;
   size_t dev_states_cap = 0, dev_trans_cap = 0, dev_prog_cap = 0;
   size_t dev_states_n = 0, dev_trans_n = 0, dev_prog_n = 0;  // entries already on the device
   bool dev_valid = false;
@@ -114,6 +117,7 @@ struct Profiler {
   double total_ms[BSG_K_COUNT] = {0};
   int64_t launches[BSG_K_COUNT] = {0};
   double work[BSG_K_COUNT] = {0};
+  std::vector<double> cut_phases;  // ms per (cut, Williamson phase) of the last profiled cut launch
   cudaEvent_t get();
   // begin/end bracket one launch on `st`
   int begin(int cls, cudaStream_t st, cudaEvent_t* ev);
@@ -144,7 +148,7 @@ struct CutArgs {
   const double* sq_cov;
   int M, L0, n_cuts, d, chi;
   double err_tol;
-  double* ws;          // per cut: 4 * nmax^2 doubles
+  double* ws;          // per cut: 7 * nmax^2 doubles
   size_t ws_stride;    // doubles per cut
   double* S;           // [n_cuts, 2(M-1), 2(M-1)]
   int ldS;
@@ -159,7 +163,10 @@ struct CutArgs {
   double* mu;          // [n_cuts, 2 kmax] eigenvalues of G^T G, then 1/nu per pair
   int max_sweeps;
   int c0;              // first cut of this launch (block b handles cut c0 + b)
+  unsigned long long* phase_t;  // [n_cuts, kCutPhases] phase timestamps (profiling) or null
 };
+constexpr int kCutTimedPhases = 11;  // stamps 0..10
+constexpr int kCutPhases = 13;       // + FP32 and FP64 Jacobi sweep counts
 
 int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                 double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);
@@ -168,6 +175,7 @@ int cut_launch_thermal(bsg_handle_t h, const CutArgs& a, int c0, int c1, cudaStr
 // status of cuts [c0, c1) into hst[c0..c1) and their sweep counts into hst[n_cuts + c0 ..)
 int cut_queue_status(const CutArgs& a, int c0, int c1, int* hst, cudaStream_t st);
 int cut_check_status(bsg_handle_t h, const CutArgs& a, int c0, int c1, const int* status);
+int cut_read_phases(bsg_handle_t h, const CutArgs& a, cudaStream_t st);
 
 // One Sigma construction (bsg_sigma.cu).
 struct SigmaJob {

@@ -82,6 +82,26 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
                    [&](int x, int y) { return total(states[x]) < total(states[y]); });
   std::vector<int> local(states.size());
   for (size_t i = 0; i < order.size(); ++i) local[order[i]] = int(i);
+  // F ring slots: a state of total T reads only states of total T - 2, so
+  // two levels of F are live at a time; slot = (level % 2) * W + position in
+  // level, W = the widest level.
+  std::vector<int> slot(states.size());
+  int width = 1;
+  {
+    std::vector<int> level_count;
+    std::vector<int> pos(states.size());
+    const int t0 = total(states[order[0]]);
+    for (size_t i = 0; i < order.size(); ++i) {
+      const int lv = (total(states[order[i]]) - t0) / 2;
+      if (lv >= (int)level_count.size()) level_count.resize(lv + 1, 0);
+      pos[i] = level_count[lv]++;
+    }
+    for (int c : level_count) width = std::max(width, c);
+    for (size_t i = 0; i < order.size(); ++i) {
+      const int lv = (total(states[order[i]]) - t0) / 2;
+      slot[i] = (lv & 1) * width + pos[i];
+    }
+  }
 
   const int prog = int(ps.keys.size());
   const int base = int(ps.st_trans_off.size());
@@ -89,6 +109,7 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
   ps.k.push_back(k);
   ps.nstates.push_back(int(states.size()));
   ps.state_off.push_back(base);
+  ps.fslots.push_back(states.size() > 1 ? 2 * width : 1);
   for (int c = 0; c < BSG_MAX_CLASSES; ++c) ps.mult.push_back(c < k ? mult[c] : 0);
   for (size_t i = 0; i < order.size(); ++i) {
     const std::string& s = states[order[i]];
@@ -102,13 +123,15 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
         std::string t = s;
         t[a]--;
         t[b]--;
-        uint32_t src = uint32_t(local[seen.at(t)]);
+        const uint32_t src = uint32_t(slot[local[seen.at(t)]]);
         ps.trans.push_back((src << 12) | uint32_t(pair_index(a, b)));
         ++cnt;
       }
     }
     ps.st_trans_cnt.push_back(cnt);
     ps.st_ra.push_back(a < k ? int(s[a]) : 0);
+    ps.st_pack.push_back(make_uint4(uint32_t(ps.st_trans_off.back()), uint32_t(cnt) | (uint32_t(a < k ? s[a] : 0) << 16),
+                                    uint32_t(slot[i]), 0u));
   }
   ps.index.emplace(key, prog);
   ps.max_states = std::max(ps.max_states, int(states.size()));
@@ -151,6 +174,8 @@ int programs_upload(ProgramSet& ps, cudaStream_t stream) {
   BSG_TRY(upload(ps.d_st_trans_off, sc, ps.dev_states_n, ps.st_trans_off, stream));
   BSG_TRY(upload(ps.d_st_trans_cnt, sc2, ps.dev_states_n, ps.st_trans_cnt, stream));
   BSG_TRY(upload(ps.d_st_ra, sc3, ps.dev_states_n, ps.st_ra, stream));
+  size_t sc4 = ps.dev_states_cap;
+  BSG_TRY(upload(ps.d_st_pack, sc4, ps.dev_states_n, ps.st_pack, stream));
   ps.dev_states_cap = sc;
   ps.dev_states_n = ps.st_trans_off.size();
   BSG_TRY(upload(ps.d_trans, ps.dev_trans_cap, ps.dev_trans_n, ps.trans, stream));
@@ -168,6 +193,7 @@ void programs_free(ProgramSet& ps) {
   cudaFree(ps.d_st_trans_off);
   cudaFree(ps.d_st_trans_cnt);
   cudaFree(ps.d_st_ra);
+  cudaFree(ps.d_st_pack);
   cudaFree(ps.d_trans);
   ps = ProgramSet();
 }

@@ -23,7 +23,7 @@ KERNEL_CLASSES = {K_DP: "hafnian_dp", K_WILLIAMSON: "williamson", K_THERMAL: "th
 HOST_CLASSES = {K_HOST_PLAN: "host_plan", K_HOST_WAIT: "host_wait"}
 OUT_C64, OUT_C128 = 0, 1
 (TUNE_DP_BLOCKS_PER_SM, TUNE_DP_L1_CARVEOUT, TUNE_DP_SMALL_ENTRIES, TUNE_DP_SMALL_BLOCKS, TUNE_DP_SCRATCH_MIB,
- TUNE_DP_FP64_BLOCKS) = range(6)
+ TUNE_DP_FP64_BLOCKS, TUNE_FACTOR_THREADS) = range(7)
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "input not positive definite",
           -4: "no convergence", -5: "size limit exceeded", -6: "allocation failed"}
@@ -47,6 +47,7 @@ SIGNATURES = {
     "bsg_cut_spectra": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _P, _P, _P, _P, _P]),
     "bsg_pattern_amplitudes": (_I, [_P, _P, _P, _I, _I, _I, _P, _L, _I, _P, _P]),
     "bsg_build_mps": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "bsg_build_mps_to_host": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_profile_enable": (_I, [_P, _I]),
     "bsg_profile_read": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_L), C.POINTER(_D)]),
     "bsg_profile_reset": (_I, [_P]),

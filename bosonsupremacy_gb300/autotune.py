@@ -30,6 +30,7 @@ KNOBS = {
     "small_blocks": _lib.TUNE_DP_SMALL_BLOCKS,
     "scratch_mib": _lib.TUNE_DP_SCRATCH_MIB,
     "fp64_blocks": _lib.TUNE_DP_FP64_BLOCKS,
+    "factor_threads": _lib.TUNE_FACTOR_THREADS,
 }
 
 

@@ -127,6 +127,7 @@ int bsg_handle_s::ensure_aux() {
   BSG_CUDA(cudaStreamCreateWithFlags(&aux_stream, cudaStreamNonBlocking));
   for (auto& s : grp) BSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest));
   for (auto& s : dp_lo) BSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least));
+  for (auto& s : copy) BSG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   BSG_CUDA(cudaEventCreateWithFlags(&aux_fork, cudaEventDisableTiming));
   BSG_CUDA(cudaEventCreateWithFlags(&aux_join, cudaEventDisableTiming));
   for (auto& e : ev) BSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -185,6 +186,8 @@ int bsg_tune_set(bsg_handle_t h, int key, int value) {
     BSG_CHECK_ARG(value >= 1 && value <= 8, "bsg_tune_set: small-launch blocks per SM %d", value);
   if (key == BSG_TUNE_DP_FP64_BLOCKS)
     BSG_CHECK_ARG(value >= 0 && value <= 8, "bsg_tune_set: FP64 helper blocks per SM %d", value);
+  if (key == BSG_TUNE_FACTOR_THREADS)
+    BSG_CHECK_ARG(value == 256 || value == 512 || value == 1024, "bsg_tune_set: factor threads %d", value);
   if (key == BSG_TUNE_DP_SCRATCH_MIB)
     BSG_CHECK_ARG(value >= 64 && value <= 65536, "bsg_tune_set: DP scratch %d MiB", value);
   h->tune[key] = value;
@@ -232,6 +235,10 @@ int bsg_destroy(bsg_handle_t h) {
       cudaStreamDestroy(s);
     }
     for (auto s : h->dp_lo) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+    for (auto s : h->copy) {
       cudaStreamSynchronize(s);
       cudaStreamDestroy(s);
     }

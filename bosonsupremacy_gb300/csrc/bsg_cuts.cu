@@ -140,16 +140,24 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
   return -1;
 }
 
-// Mixed-precision Jacobi of the symmetric m x m matrix Hm with eigenvector
-// rows accumulated in QT: FP32 sweeps on a rounded copy (the FP32 pipe is
-// ~64x the FP64 one on GB300) until the off-diagonal is ~1e-5 of the
-// diagonal, two FP64 Newton-Schulz steps QT <- 1.5 QT - 0.5 (QT QT^T) QT
-// that make the FP32 eigenvectors orthonormal to rounding, the FP64
-// projection QT Hm QT^T, and FP64 sweeps on that nearly diagonal matrix
-// (quadratic convergence: ~2 sweeps instead of ~8).  s1, s2: m*m doubles of
-// scratch each.  Returns the FP64 sweeps used (+2 for the projection work),
-// or -1 when the FP64 sweeps did not converge.
-__device__ int mixed_jacobi(double* Hm, int m, double* QT, int max_sweeps, double* s1, double* s2, double* red,
+// Mixed-precision symmetric eigen-decomposition of the m x m matrix Hm with
+// eigenvector rows in QT: FP32 Jacobi sweeps on a rounded copy (the FP32
+// pipe is ~64x the FP64 one on GB300) until the off-diagonal is ~1e-5 of the
+// diagonal, then FP64 iterative refinement by matrix products only (Ogita &
+// Aishima, "Iterative refinement for symmetric eigenvalue decomposition",
+// Japan J. Indust. Appl. Math. 35 (2018)).  With X the eigenvector columns
+// (X = QT^T):
+//   R = I - X^T X,  S = X^T Hm X,  lambda_i = s_ii / (1 - r_ii),
+//   E_ij = (s_ij + lambda_j r_ij) / (lambda_j - lambda_i)  if |lambda_i - lambda_j| > delta,
+//          r_ij / 2                                        otherwise (clusters, incl. i = j),
+//   X <- X + X E,   delta = 2 (||S - diag(lambda)||_F + ||Hm||_F ||R||_F).
+// Each step squares the error; clustered eigenvalues (every eigenvalue of
+// G^T G is double) converge as an orthonormal basis of their subspace, which
+// the pairing step resolves.  On return the diagonal of Hm holds the
+// eigenvalues (the rest of Hm is overwritten).  s1, s2, s3: m*m doubles of
+// scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
+// the start tolerance of the refinement.
+__device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
                             double* cs, double* sn, int* pos, unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t mm = (size_t)m * m;
@@ -161,52 +169,73 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, int max_sweeps, doubl
   }
   __syncthreads();
   const int sw32 =
-      block_jacobi<float>(H32, m, Q32, 16, 1e-10, red, reinterpret_cast<float*>(cs), reinterpret_cast<float*>(sn), pos);
+      block_jacobi<float>(H32, m, Q32, 24, 1e-10, red, reinterpret_cast<float*>(cs), reinterpret_cast<float*>(sn), pos);
   for (size_t t = tid; t < mm; t += nt) QT[t] = double(Q32[t]);
   __syncthreads();
-  for (int it = 0; it < 2; ++it) {
-    for (size_t t = tid; t < mm; t += nt) {  // s2 = QT QT^T
+  double* lam = reinterpret_cast<double*>(cs);  // m doubles (cs and sn are adjacent: 2 kMaxCutModes)
+  double anorm = 0.0;
+  for (size_t t = tid; t < mm; t += nt) anorm += Hm[t] * Hm[t];
+  anorm = sqrt(block_sum(anorm, red));
+  constexpr int kRefine = 3;
+  for (int it = 0; it < kRefine; ++it) {
+    // s1 = R = I - QT QT^T ; s2 = T = Hm QT^T
+    for (size_t t = tid; t < mm; t += nt) {
+      const int i = int(t / m), j = int(t % m);
+      double r = 0.0, h = 0.0;
+      for (int q = 0; q < m; ++q) {
+        const double xj = QT[(size_t)j * m + q];
+        r = fma(QT[(size_t)i * m + q], xj, r);
+        h = fma(Hm[(size_t)i * m + q], xj, h);
+      }
+      s1[t] = (i == j ? 1.0 : 0.0) - r;
+      s2[t] = h;
+    }
+    __syncthreads();
+    // s3 = S = QT T
+    for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
       double acc = 0.0;
-      for (int r = 0; r < m; ++r) acc = fma(QT[(size_t)i * m + r], QT[(size_t)j * m + r], acc);
+      for (int q = 0; q < m; ++q) acc = fma(QT[(size_t)i * m + q], s2[(size_t)q * m + j], acc);
+      s3[t] = acc;
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += nt) lam[i] = s3[(size_t)i * m + i] / (1.0 - s1[(size_t)i * m + i]);
+    __syncthreads();
+    double so = 0.0, rr = 0.0;
+    for (size_t t = tid; t < mm; t += nt) {
+      const int i = int(t / m), j = int(t % m);
+      const double d = s3[t] - (i == j ? lam[i] : 0.0);
+      so += d * d;
+      rr += s1[t] * s1[t];
+    }
+    so = block_sum(so, red);
+    rr = block_sum(rr, red);
+    const double delta = 2.0 * (sqrt(so) + anorm * sqrt(rr));
+    // s1 <- E (in place: E_ij reads s1_ij and s3_ij only)
+    for (size_t t = tid; t < mm; t += nt) {
+      const int i = int(t / m), j = int(t % m);
+      const double r = s1[t], gap = lam[j] - lam[i];
+      s1[t] = (i != j && fabs(gap) > delta) ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
+    }
+    __syncthreads();
+    // s2 = QT + E^T QT, then QT = s2
+    for (size_t t = tid; t < mm; t += nt) {
+      const int i = int(t / m), j = int(t % m);
+      double acc = QT[t];
+      for (int q = 0; q < m; ++q) acc = fma(s1[(size_t)q * m + i], QT[(size_t)q * m + j], acc);
       s2[t] = acc;
     }
     __syncthreads();
-    for (size_t t = tid; t < mm; t += nt) {  // s1 = 1.5 QT - 0.5 s2 QT
-      const int i = int(t / m), j = int(t % m);
-      double acc = 0.0;
-      for (int r = 0; r < m; ++r) acc = fma(s2[(size_t)i * m + r], QT[(size_t)r * m + j], acc);
-      s1[t] = 1.5 * QT[t] - 0.5 * acc;
-    }
-    __syncthreads();
-    for (size_t t = tid; t < mm; t += nt) QT[t] = s1[t];
+    for (size_t t = tid; t < mm; t += nt) QT[t] = s2[t];
     __syncthreads();
   }
-  for (size_t t = tid; t < mm; t += nt) {  // s1 = Hm QT^T
-    const int i = int(t / m), j = int(t % m);
-    double acc = 0.0;
-    for (int r = 0; r < m; ++r) acc = fma(Hm[(size_t)i * m + r], QT[(size_t)j * m + r], acc);
-    s1[t] = acc;
-  }
-  __syncthreads();
-  for (size_t t = tid; t < mm; t += nt) {  // s2 = QT s1
-    const int i = int(t / m), j = int(t % m);
-    double acc = 0.0;
-    for (int r = 0; r < m; ++r) acc = fma(QT[(size_t)i * m + r], s1[(size_t)r * m + j], acc);
-    s2[t] = acc;
-  }
-  __syncthreads();
-  for (size_t t = tid; t < mm; t += nt) {  // symmetrise into Hm
-    const int i = int(t / m), j = int(t % m);
-    Hm[t] = 0.5 * (s2[t] + s2[(size_t)j * m + i]);
-  }
-  __syncthreads();
-  const int sw = block_jacobi<double>(Hm, m, QT, max_sweeps, 1e-26, red, cs, sn, pos);
-  if (sweep_log && threadIdx.x == 0) {
+  for (int i = tid; i < m; i += nt) Hm[(size_t)i * m + i] = lam[i];
+  if (sweep_log && tid == 0) {
     sweep_log[0] = (unsigned long long)(sw32 < 0 ? 99 : sw32);
-    sweep_log[1] = (unsigned long long)(sw < 0 ? 99 : sw);
+    sweep_log[1] = (unsigned long long)kRefine;
   }
-  return sw < 0 ? -1 : sw + 2;
+  __syncthreads();
+  return sw32 < 0 ? -1 : sw32;
 }
 
 // In-place right-looking Cholesky of the m x m SPD matrix X (lower triangle,
@@ -263,7 +292,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   double* H = Gm + nn;   // H (full path) / F and its reflectors (low-rank path) / accepted vectors
   double* X1 = H + nn;   // low-rank path: V_A -> L_A, then K = I - R R^T
   double* X2 = X1 + nn;  // low-rank path: L_A^{-1} C, then eigenvector rows of K
-  // (X2 + nn: one more n^2 block of Jacobi scratch)
+  // (X2 + nn, X2 + 2 nn: two more n^2 blocks of eigen-solver scratch)
   double* MU = a.mu + (size_t)c * (2 * a.kmax);
   extern __shared__ double sm[];
   double* red = sm;                   // 33
@@ -315,17 +344,21 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     __syncthreads();
   }
   phase_stamp(a, c, 3);
-  // 4. G = W Omega W^T: G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r]
-  for (size_t t = tid; t < nn; t += nt) {
-    const int i = int(t / n), j = int(t % n);
-    double s = 0.0;
-    for (int r = 0; r < k; ++r)
-      s += W[(size_t)i * n + r] * W[(size_t)j * n + r + k] - W[(size_t)i * n + r + k] * W[(size_t)j * n + r];
-    Gm[t] = s;
-  }
-  __syncthreads();
+  // 4. G = W Omega W^T (formed in the full path only; the low-rank path
+  // applies it as two triangular products with W = L^{-1})
   int sweeps = 0;
-  if (nA >= n) {
+  const bool g_dense = nA >= n;
+  double* EV = g_dense ? W : X1;  // eigenvector rows of H
+  if (g_dense) {
+    // G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r]
+    for (size_t t = tid; t < nn; t += nt) {
+      const int i = int(t / n), j = int(t % n);
+      double s = 0.0;
+      for (int r = 0; r < k; ++r)
+        s += W[(size_t)i * n + r] * W[(size_t)j * n + r + k] - W[(size_t)i * n + r + k] * W[(size_t)j * n + r];
+      Gm[t] = s;
+    }
+    __syncthreads();
     phase_stamp(a, c, 4);
     // 5a. full path: H = G^T G, Jacobi with eigenvector rows in W
     for (size_t t = tid; t < nn; t += nt) {
@@ -336,7 +369,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     }
     __syncthreads();
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(H, n, W, a.max_sweeps, X1, X2, red, cs, sn, pos,
+    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
@@ -417,14 +450,17 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       X1[t] = (i == j ? 1.0 : 0.0) - s;
     }
     __syncthreads();
-    // W (L^{-1}) is not read again before the back-transform overwrites it
+    // Gm is free in this path (G is applied through W = L^{-1}, which the pairing still needs)
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(X1, nA, X2, a.max_sweeps, W, X2 + nn, red, cs, sn, pos,
+    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
+    for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
+    __syncthreads();
     // eigenvector rows of H in the full space: u_i = Q z_i, z_i = [K eigvec; 0] or e_i
+    // (into X1, so that W = L^{-1} survives for applying G)
     for (int i = (tid >> 5); i < n; i += nt >> 5) {
-      double* z = W + (size_t)i * n;
+      double* z = EV + (size_t)i * n;
       for (int t = tid & 31; t < n; t += 32) z[t] = i < nA ? (t < nA ? X2[(size_t)i * nA + t] : 0.0) : (t == i ? 1.0 : 0.0);
       __syncwarp();
       for (int j = nA - 1; j >= 0; --j) {
@@ -436,7 +472,6 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
         __syncwarp();
       }
     }
-    for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
   }
   __syncthreads();
   if (tid == 0) a.sweeps[c] = sweeps < 0 ? a.max_sweeps : sweeps;
@@ -461,97 +496,165 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   // even-sized clusters of (nearly) equal mu; inside a cluster the next x is
   // the candidate with the largest residual after projecting out the pairs
   // already taken (pivoted Gram-Schmidt), so a degenerate eigenspace of any
-  // dimension (e.g. the nu = 1 vacuum modes) is always completed.
+  // dimension (e.g. the nu = 1 vacuum modes) is always completed.  The
+  // candidates' residuals are tracked in FP32 (pivot choice only); the chosen
+  // FP64 eigenvector (not its FP32 copy) and y are cleaned by one FP64
+  // projection against the accepted vectors of the cluster.
   // 1/nu of each pair is |G x| (x a unit eigenvector: |G x|^2 = mu).
   double* Xacc = H;  // accepted vectors as rows
+  float* c32 = reinterpret_cast<float*>(X2 + nn);       // FP32 candidates of the cluster
+  float* r32 = reinterpret_cast<float*>(X2 + 2 * nn);   // their squared residuals
+  float* xy32 = r32 + n;                                 // FP32 copies of x and y
+  double* tv = X2;                                       // 2n doubles: W^T x and Omega W^T x
   for (int i = tid; i < n; i += nt) vec2[i] = MU[order[i]];
   __syncthreads();
   int* used = reinterpret_cast<int*>(vec);  // n flags (vec reused as int storage)
   for (int i = tid; i < n; i += nt) used[i] = 0;
   __syncthreads();
+  // y = G x with G = W Omega W^T
+  auto apply_G = [&](const double* x, double* y) {
+    if (g_dense) {
+      for (int i = tid >> 5; i < n; i += nt >> 5) {
+        double s = 0.0;
+        for (int j = tid & 31; j < n; j += 32) s = fma(Gm[(size_t)i * n + j], x[j], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) y[i] = s;
+      }
+    } else {
+      for (int j = tid; j < n; j += nt) {  // t = W^T x (W lower triangular)
+        double s = 0.0;
+        for (int i = j; i < n; ++i) s = fma(W[(size_t)i * n + j], x[i], s);
+        tv[j] = s;
+      }
+      __syncthreads();
+      for (int j = tid; j < n; j += nt) tv[n + j] = j < k ? tv[j + k] : -tv[j - k];  // Omega t
+      __syncthreads();
+      for (int i = tid >> 5; i < n; i += nt >> 5) {  // y = W (Omega t)
+        double s = 0.0;
+        for (int j = tid & 31; j <= i; j += 32) s = fma(W[(size_t)i * n + j], tv[n + j], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) y[i] = s;
+      }
+    }
+    __syncthreads();
+  };
+  // v -= sum over accepted rows [a0, a1) of (row . v) row, one pass
+  auto project_out = [&](double* v, int a0, int a1) {
+    for (int t = tid; t < (a1 - a0) * 32; t += nt) {
+      const int av = a0 + (t >> 5);
+      double s = 0.0;
+      for (int i = t & 31; i < n; i += 32) s = fma(Xacc[(size_t)av * n + i], v[i], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if ((t & 31) == 0) dots[av - a0] = s;
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+      double s = v[i];
+      for (int av = a0; av < a1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
+      v[i] = s;
+    }
+    __syncthreads();
+  };
   int acc = 0;
   int cb = 0;
   while (cb < n) {
     int ce = cb + 2;
     while (ce < n && !(vec2[ce] - vec2[ce - 1] > 1e-9 * fmax(fabs(vec2[ce]), 1e-300))) ce += 2;
     if (ce > n) ce = n;
-    const int acc0 = acc;
-    for (int pi = 0; pi < (ce - cb) / 2; ++pi) {
-      for (int r = cb + (tid >> 5); r < ce; r += nt >> 5) {
-        const double* w = W + (size_t)order[r] * n;
-        double s = 0.0;
-        for (int i = tid & 31; i < n; i += 32) s += w[i] * w[i];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((tid & 31) == 0) dots[r] = used[r] ? -1.0 : s;
-      }
-      __syncthreads();
-      if (tid == 0) {
+    const int acc0 = acc, C = ce - cb;
+    // FP32 copies of the cluster's candidates and their squared norms
+    for (size_t t = tid; t < (size_t)C * n; t += nt) {
+      const int r = int(t / n), i = int(t % n);
+      c32[t] = float(EV[(size_t)order[cb + r] * n + i]);
+    }
+    __syncthreads();
+    for (int r = tid >> 5; r < C; r += nt >> 5) {
+      float s = 0.f;
+      for (int i = tid & 31; i < n; i += 32) s = fmaf(c32[(size_t)r * n + i], c32[(size_t)r * n + i], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if ((tid & 31) == 0) r32[r] = s;
+    }
+    __syncthreads();
+    for (int pi = 0; pi < C / 2; ++pi) {
+      if (tid < 32) {  // pivot: the unused candidate with the largest residual
+        float bv = -1.f;
         int best = -1;
-        double bv = -1.0;
-        for (int r = cb; r < ce; ++r)
-          if (dots[r] > bv) {
-            bv = dots[r];
+        for (int r = tid; r < C; r += 32)
+          if (!used[cb + r] && r32[r] > bv) {
+            bv = r32[r];
             best = r;
           }
-        s_flag = best;
-        s_scalar = bv;
-        if (best >= 0) used[best] = 1;
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+          const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+          if (ov > bv || (ov == bv && ob >= 0 && (best < 0 || ob < best))) {
+            bv = ov;
+            best = ob;
+          }
+        }
+        if (tid == 0) {
+          s_flag = best;
+          s_scalar = bv;
+          if (best >= 0) used[cb + best] = 1;
+        }
       }
       __syncthreads();
       const int best = s_flag;
-      const double bn = s_scalar;
-      if (best < 0 || !(bn > 0.0)) {
+      if (best < 0 || !(s_scalar > 1e-6)) {
         if (tid == 0) a.status[c] = 4;
         return;
       }
-      const double inv = 1.0 / sqrt(bn);
       double* x = Xacc + (size_t)acc * n;
       double* y = Xacc + (size_t)(acc + 1) * n;
-      for (int i = tid; i < n; i += nt) x[i] = W[(size_t)order[best] * n + i] * inv;
+      // x: the FP64 eigenvector itself (an FP32-rounded copy would leave the
+      // eigenspace by ~1e-7), one projection pass (its residual is the
+      // largest of the cluster, so one pass keeps orthogonality at rounding)
+      for (int i = tid; i < n; i += nt) x[i] = EV[(size_t)order[cb + best] * n + i];
       __syncthreads();
-      for (int i = tid; i < n; i += nt) {
-        double s = 0.0;
-        for (int j = 0; j < n; ++j) s += Gm[(size_t)i * n + j] * x[j];
-        y[i] = s;
-      }
+      project_out(x, acc0, acc);
+      double nx = 0.0;
+      for (int i = tid; i < n; i += nt) nx += x[i] * x[i];
+      nx = block_sum(nx, red);
+      const double ix = 1.0 / sqrt(nx);
+      for (int i = tid; i < n; i += nt) x[i] *= ix;
       __syncthreads();
+      apply_G(x, y);
       double gx = 0.0;
       for (int i = tid; i < n; i += nt) gx += y[i] * y[i];
       gx = block_sum(gx, red);  // |G x|^2 = 1/nu^2
-      for (int t = tid; t < (acc + 1 - acc0) * 32; t += nt) {
-        const int av = acc0 + (t >> 5);
-        double s = 0.0;
-        for (int i = t & 31; i < n; i += 32) s += Xacc[(size_t)av * n + i] * y[i];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((t & 31) == 0) dots[av - acc0] = s;
-      }
-      __syncthreads();
-      for (int i = tid; i < n; i += nt) {
-        double s = y[i];
-        for (int av = acc0; av <= acc; ++av) s -= dots[av - acc0] * Xacc[(size_t)av * n + i];
-        y[i] = s;
-      }
-      __syncthreads();
+      project_out(y, acc0, acc + 1);
       double ny = 0.0;
       for (int i = tid; i < n; i += nt) ny += y[i] * y[i];
       ny = block_sum(ny, red);
       const double iy = ny > 0.0 ? 1.0 / sqrt(ny) : 0.0;
-      for (int i = tid; i < n; i += nt) y[i] *= iy;
+      for (int i = tid; i < n; i += nt) {
+        y[i] *= iy;
+        xy32[i] = float(x[i]);
+        xy32[n + i] = float(y[i] );
+      }
       if (tid == 0) MU[acc / 2] = sqrt(gx);  // 1/nu of pair acc/2 (MU no longer needed by candidates)
       __syncthreads();
-      for (int r = cb + (tid >> 5); r < ce; r += nt >> 5) {
-        if (used[r]) continue;
-        double* w = W + (size_t)order[r] * n;
-        double sx = 0.0, sy = 0.0;
+      // FP32 tracking: project x and y out of the remaining candidates
+      for (int r = tid >> 5; r < C; r += nt >> 5) {
+        if (used[cb + r]) continue;
+        float* w = c32 + (size_t)r * n;
+        float sx = 0.f, sy = 0.f;
         for (int i = tid & 31; i < n; i += 32) {
-          sx += x[i] * w[i];
-          sy += y[i] * w[i];
+          sx = fmaf(xy32[i], w[i], sx);
+          sy = fmaf(xy32[n + i], w[i], sy);
         }
         for (int o = 16; o > 0; o >>= 1) {
           sx += __shfl_xor_sync(0xffffffffu, sx, o);
           sy += __shfl_xor_sync(0xffffffffu, sy, o);
         }
-        for (int i = tid & 31; i < n; i += 32) w[i] -= sx * x[i] + sy * y[i];
+        float rn = 0.f;
+        for (int i = tid & 31; i < n; i += 32) {
+          const float v = w[i] - sx * xy32[i] - sy * xy32[n + i];
+          w[i] = v;
+          rn = fmaf(v, v, rn);
+        }
+        for (int o = 16; o > 0; o >>= 1) rn += __shfl_xor_sync(0xffffffffu, rn, o);
+        if ((tid & 31) == 0) r32[r] = rn;
       }
       __syncthreads();
       acc += 2;
@@ -723,7 +826,7 @@ int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts,
   a.d = d;
   a.chi = chi;
   a.err_tol = err_tol;
-  a.ws_stride = (size_t)7 * nmax * nmax;
+  a.ws_stride = (size_t)8 * nmax * nmax;
   a.S = S;
   a.ldS = 2 * (M - 1);
   a.kmax = kmax;
@@ -769,7 +872,8 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
   a.c0 = c0;
   const size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0, (williamson_kernel<<<c1 - c0, 1024, wsm, st>>>(a)));
+  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0,
+               (williamson_kernel<<<c1 - c0, h->tune[BSG_TUNE_FACTOR_THREADS], wsm, st>>>(a)));
   return BSG_OK;
 }
 
@@ -822,15 +926,15 @@ int cut_check_status(bsg_handle_t h, const CutArgs& a, int c0, int c1, const int
   const int M = a.M, L0 = a.L0, n_cuts = a.n_cuts;
   // FP64 FMAs of the Williamson step: Cholesky n^3/3, L^-1 n^3/6, G n^3,
   // pairing ~n^3 (G x per pair, projections), S n^3/2; full path: H n^3 and
-  // 4 n^3 per Jacobi sweep; low-rank path (m = 2L < n): Cholesky m^3/3,
-  // L_A^-1 C m^2 n/2, F n^2 m/2, QR 2 n m^2, K m^3/2, 4 m^3 per sweep, Q z 2 n^2 m
+  // 12 n^3 for three refinement steps of the eigen-decomposition (its Jacobi
+  // sweeps run in FP32); low-rank path (m = 2L < n): Cholesky m^3/3,
+  // L_A^-1 C m^2 n/2, F n^2 m/2, QR 2 n m^2, K m^3/2, 12 m^3 refinement, Q z 2 n^2 m
   double fmas = 0.0;
   for (int c = c0; c < c1; ++c) {
     const double n = 2.0 * (M - L0 - c), m = 2.0 * (L0 + c);
-    const double sw = std::max(0, status[n_cuts + c]);
     fmas += n * n * n * (1.0 / 3 + 1.0 / 6 + 1.0 + 1.0 + 0.5);
-    if (m >= n) fmas += n * n * n * (1.0 + 4.0 * sw);
-    else fmas += m * m * m / 3 + m * m * n / 2 + n * n * m / 2 + 2 * n * m * m + m * m * m / 2 + 4 * m * m * m * sw + 2 * n * n * m;
+    if (m >= n) fmas += n * n * n * (1.0 + 12.0);
+    else fmas += m * m * m / 3 + m * m * n / 2 + n * n * m / 2 + 2 * n * m * m + m * m * m / 2 + 12 * m * m * m + 2 * n * n * m;
   }
   h->prof.add_work(BSG_K_WILLIAMSON, fmas);
   for (int c = c0; c < c1; ++c) {

@@ -1270,10 +1270,13 @@ extern "C" int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int
   return run_sites(h, in, d, chi, precision, out_dtype, h->slot[0], st);
 }
 
-extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
-                             double site_tol, int precision, int out_dtype, void* const* gammas_host,
-                             double* Lambdas, double* res, int8_t* num, double* S, int32_t* kept,
-                             bsg_stream_t stream) {
+// The whole-MPS build; with gammas_pinned / lambdas_pinned non-null, each
+// build group's Gammas are copied to the host as soon as that group's DP is
+// done (two copy streams), overlapping the copies with the other groups.
+static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
+                          double site_tol, int precision, int out_dtype, void* const* gammas_host,
+                          double* Lambdas, double* res, int8_t* num, double* S, int32_t* kept,
+                          void* const* gammas_pinned, double* lambdas_pinned, bsg_stream_t stream) {
   BSG_CHECK_ARG(h, "bsg_build_mps: null handle");
   BSG_CHECK_ARG(sq_cov && gammas_host && Lambdas && res && num && S && kept, "bsg_build_mps: null pointer");
   BSG_CHECK_ARG(M >= 2, "bsg_build_mps: need M >= 2 modes (M=%d)", M);
@@ -1537,6 +1540,19 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
     if (!in.empty() && rc == BSG_OK)
       rc = run_sites(h, in, d, chi, precision, out_dtype, h->slot[G.slot], G.dp_stream);
     h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
+    if (gammas_pinned && rc == BSG_OK) {
+      // this group's Gammas are final once its DP stream gets here
+      cudaStream_t cp = h->copy[g & 1];
+      const size_t gb = (size_t)chi * chi * d * (out_dtype == BSG_OUT_C128 ? 16 : 8);
+      cudaError_t e = cudaEventRecord(h->ev[9 + g], G.dp_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[9 + g], 0);
+      for (int i = G.s0; i < G.s1 && e == cudaSuccess; ++i)
+        e = cudaMemcpyAsync(gammas_pinned[i], gammas_host[i], gb, cudaMemcpyDeviceToHost, cp);
+      if (e != cudaSuccess) {
+        set_error("bsg_build_mps: %s", cudaGetErrorString(e));
+        rc = BSG_ERR_CUDA;
+      }
+    }
   }
   // join every stream of every group into st before returning (also on
   // errors: the side streams must be idle before the workspaces are reused)
@@ -1553,12 +1569,25 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
       }
     }
   }
+  if (gammas_pinned && h->copy[0]) {
+    for (int q = 0; q < 2; ++q) {
+      cudaEventRecord(h->ev[13 + q], h->copy[q]);
+      cudaStreamWaitEvent(st, h->ev[13 + q], 0);
+    }
+  }
   for (int g = 0; g < ng; ++g)
     if (ev_keys[g]) cudaEventDestroy(ev_keys[g]);
   if (rc != BSG_OK) {
     cudaStreamSynchronize(st);
     return rc;
   }
+  if (gammas_pinned && ng == 1) {  // single group: copy after the build
+    const size_t gb = (size_t)chi * chi * d * (out_dtype == BSG_OUT_C128 ? 16 : 8);
+    for (int i = 0; i < M; ++i)
+      BSG_CUDA(cudaMemcpyAsync(gammas_pinned[i], gammas_host[i], gb, cudaMemcpyDeviceToHost, st));
+  }
+  if (lambdas_pinned)
+    BSG_CUDA(cudaMemcpyAsync(lambdas_pinned, Lambdas, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
   // Sigma status (singular A) -- read after the DP so the check costs no extra wait
   std::vector<int> sst(M);
   BSG_CUDA(cudaMemcpyAsync(sst.data(), d_status, (size_t)M * 4, cudaMemcpyDeviceToHost, st));
@@ -1572,4 +1601,22 @@ extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d,
       return BSG_ERR_NO_CONVERGE;
     }
   return BSG_OK;
+}
+
+extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
+                             double site_tol, int precision, int out_dtype, void* const* gammas_host,
+                             double* Lambdas, double* res, int8_t* num, double* S, int32_t* kept,
+                             bsg_stream_t stream) {
+  return build_mps_impl(h, sq_cov, M, d, chi, cut_tol, site_tol, precision, out_dtype, gammas_host, Lambdas, res,
+                        num, S, kept, nullptr, nullptr, stream);
+}
+
+extern "C" int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
+                                     double site_tol, int precision, int out_dtype, void* const* gammas_dev,
+                                     void* const* gammas_pinned, double* Lambdas, double* lambdas_pinned,
+                                     double* res, int8_t* num, double* S, int32_t* kept, bsg_stream_t stream) {
+  BSG_CHECK_ARG(gammas_pinned && lambdas_pinned, "bsg_build_mps_to_host: null host pointer");
+  for (int i = 0; i < M; ++i) BSG_CHECK_ARG(gammas_pinned[i], "bsg_build_mps_to_host: host Gamma %d is NULL", i);
+  return build_mps_impl(h, sq_cov, M, d, chi, cut_tol, site_tol, precision, out_dtype, gammas_dev, Lambdas, res,
+                        num, S, kept, gammas_pinned, lambdas_pinned, stream);
 }

@@ -148,7 +148,7 @@ struct CutArgs {
   const double* sq_cov;
   int M, L0, n_cuts, d, chi;
   double err_tol;
-  double* ws;          // per cut: 7 * nmax^2 doubles
+  double* ws;          // per cut: 8 * nmax^2 doubles
   size_t ws_stride;    // doubles per cut
   double* S;           // [n_cuts, 2(M-1), 2(M-1)]
   int ldS;
@@ -224,9 +224,9 @@ struct bsg_handle_s {
   // side streams for concurrent launches (created on first use) and events:
   // aux_stream (FP64 helper), grp[3] high-priority streams of the build
   // groups, dp_lo[2] low-priority streams of the edge groups' DP
-  cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[2] = {};
+  cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[2] = {}, copy[2] = {};
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
-  cudaEvent_t ev[12] = {};
+  cudaEvent_t ev[16] = {};
   int ensure_aux();
   // per-group buffers of the site DP (plan tables, item slots, per-warp
   // scratch, pinned plan staging); slot 0 serves the single-site calls
@@ -234,7 +234,7 @@ struct bsg_handle_s {
     bsg::DevBuf plan, items, scratch;
     bsg::HostBuf stage;
   } slot[3];
-  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0};
+  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024};
 };
 
 // Brackets a kernel launch with profiler events when profiling is on.

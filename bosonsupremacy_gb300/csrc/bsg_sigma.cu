@@ -207,7 +207,8 @@ int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, voi
   double work = 0.0;
   for (int i = 0; i < n_jobs; ++i) work += 20.0 * jobs_host[i].Mr * jobs_host[i].Mr * (double)jobs_host[i].Mr;
   BSG_PROFILED(h, BSG_K_SIGMA, st, work,
-               (sigma_kernel<<<n_jobs, 1024, 0, st>>>(reinterpret_cast<const SigmaJob*>(jobs_dev))));
+               (sigma_kernel<<<n_jobs, h->tune[BSG_TUNE_FACTOR_THREADS], 0, st>>>(
+                   reinterpret_cast<const SigmaJob*>(jobs_dev))));
   return BSG_OK;
 }
 

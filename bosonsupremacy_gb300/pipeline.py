@@ -64,15 +64,32 @@ def build_mps(sq_cov, d: int, chi: int, precision="split", out_dtype=torch.compl
 
 def build_mps_host(sq_cov_host: torch.Tensor, d: int, chi: int, gammas_host: List[torch.Tensor],
                    lambdas_host: torch.Tensor, precision="split", device: int = 0,
-                   device_out: Optional[List[torch.Tensor]] = None) -> MPS:
+                   device_out: Optional[List[torch.Tensor]] = None, err_tol: float = 1e-10,
+                   cut_tol: float = 1e-12) -> None:
     """Host-buffer form of build_mps: the covariance is copied in from (pinned)
-    host memory and every Gamma_i and the Lambdas are copied back into the
-    given (pinned) host tensors, all on the current stream."""
+    host memory and every Gamma_i and the Lambdas land in the given pinned
+    host tensors; each build group's Gammas are downloaded while the other
+    groups are still computing (bsg_build_mps_to_host)."""
     dev = torch.device("cuda", device)
     sq = sq_cov_host.to(dev, non_blocking=True)
-    mps = build_mps(sq, d, chi, precision=precision, out_dtype=gammas_host[0].dtype, device=device, out=device_out)
-    for g_h, g_d in zip(gammas_host, mps.Gammas):
-        g_h.copy_(g_d, non_blocking=True)
-    lambdas_host.copy_(mps.Lambdas, non_blocking=True)
-    torch.cuda.current_stream(dev).synchronize()
-    return mps
+    M = sq.shape[0] // 2
+    nc = M - 1
+    out = device_out
+    if out is None:
+        out = [torch.empty(chi, chi, d, dtype=gammas_host[0].dtype, device=dev) for _ in range(M)]
+    if any(not g.is_pinned() for g in gammas_host) or not lambdas_host.is_pinned():
+        raise ValueError("build_mps_host: host outputs must be pinned")
+    odt = _lib.OUT_C128 if out[0].dtype == torch.complex128 else _lib.OUT_C64
+    lam = torch.empty(nc, chi, dtype=torch.float64, device=dev)
+    res = torch.empty(nc, chi, dtype=torch.float64, device=dev)
+    num = torch.empty(nc, chi, M - 1, dtype=torch.int8, device=dev)
+    S = torch.empty(nc, 2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device=dev)
+    kept = torch.empty(nc, dtype=torch.int32, device=dev)
+    dptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in out])
+    hptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in gammas_host])
+    h = _lib.Handle.get(device)
+    _lib.check(_lib.load().bsg_build_mps_to_host(h.h, sq.data_ptr(), M, d, chi, float(cut_tol), float(err_tol),
+                                                 ops._prec(precision), odt, dptrs, hptrs, lam.data_ptr(),
+                                                 lambdas_host.data_ptr(), res.data_ptr(), num.data_ptr(),
+                                                 S.data_ptr(), kept.data_ptr(), _lib.stream_ptr()),
+               "bsg_build_mps_to_host")

@@ -164,16 +164,27 @@ int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_c
  * kron_cpu.py (all M-1 cuts, kron_cpu.py:147-153) followed by MPS_cpu.py
  * (all M sites, MPS_cpu.py:384-525) in one call, device-resident:
  * cut spectra with err_tol = cut_tol (the reference's 1e-12), Lambda_c =
- * sqrt(res_c) where res_c > site_tol (the reference's 1e-10) else 0, Sigma of
- * every site in one launch, label tables of every cut in one launch, host
- * planning of every site's work items, then ONE persistent launch over the
- * items of all sites.  gammas_host: host array of M device pointers to
+ * sqrt(res_c) where res_c > site_tol (the reference's 1e-10) else 0.  The
+ * cuts and sites run in three groups (right edge, left edge, middle) on
+ * internal streams: per group Williamson, top-chi, label tables, Sigma, then
+ * host planning of its items and its DP launches; the groups overlap (no
+ * kernel waits on another).  gammas_host: host array of M device pointers to
  * [chi, chi, d] of out_dtype; Lambdas: float64 [M-1, chi]; res, num, S, kept
- * as bsg_cut_spectra with L0 = 1, n_cuts = M-1.  Synchronises `stream` twice
- * (cut status, label keys) and once at the end. */
+ * as bsg_cut_spectra with L0 = 1, n_cuts = M-1.  Waits on the host for each
+ * group's label keys and synchronises `stream` at the end. */
 int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol, double site_tol,
                   int precision, int out_dtype, void* const* gammas_host, double* Lambdas, double* res, int8_t* num,
                   double* S, int32_t* kept, bsg_stream_t stream);
+
+/* bsg_build_mps plus the download of its outputs: each group's Gammas are
+ * copied from gammas_dev[i] (device) to gammas_pinned[i] (pinned host) as soon
+ * as that group's DP is done, overlapping the copies with the rest of the
+ * build, and the Lambdas to lambdas_pinned [M-1, chi] float64.  Returns after
+ * every copy has landed. */
+int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
+                          double site_tol, int precision, int out_dtype, void* const* gammas_dev,
+                          void* const* gammas_pinned, double* Lambdas, double* lambdas_pinned, double* res,
+                          int8_t* num, double* S, int32_t* kept, bsg_stream_t stream);
 
 /* ---- transfer contraction (pattern amplitudes) ---------------------------
  * The bond contraction that consumes Gamma/Lambda (sampling_cpu.py:75-90):
@@ -247,7 +258,9 @@ int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* m
 #define BSG_TUNE_DP_SCRATCH_MIB 4    /* device memory for per-warp DP tables per launch, 64..65536 MiB (default 8192) */
 #define BSG_TUNE_DP_FP64_BLOCKS 5    /* split precision: resident blocks per SM of a concurrent FP64 DP
                                         launch sharing the work queue (FP64 pipe), 0..8 (default 0 = off) */
-#define BSG_TUNE_COUNT 6
+#define BSG_TUNE_FACTOR_THREADS 6    /* threads per CTA of the Williamson and Sigma kernels, 256 / 512 / 1024
+                                        (default 1024; fewer leave registers for DP blocks on the same SM) */
+#define BSG_TUNE_COUNT 7
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

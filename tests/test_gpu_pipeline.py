@@ -32,3 +32,20 @@ def test_pattern_probabilities_match_reference(cuda, golden, fixture, prec):
     rel = np.abs(p[big] - p_ref[big]) / p_ref[big]
     assert rel.max() <= 1e-6, (prec, rel.max())
     assert np.abs(p - p_ref).max() <= 1e-9 * p_ref.max()
+
+
+def test_build_to_host_matches_device_build(cuda, golden):
+    """The host-output build (per-group downloads overlapping the build) lands
+    exactly the device build's Gammas and Lambdas in pinned memory."""
+    import torch
+    from bosonsupremacy_gb300.pipeline import build_mps, build_mps_host
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    ref = build_mps(t["sq_cov"], d, chi, precision="split")
+    sq = torch.as_tensor(t["sq_cov"]).pin_memory()
+    gh = [torch.empty(chi, chi, d, dtype=torch.complex64, pin_memory=True) for _ in range(M)]
+    lh = torch.empty(M - 1, chi, dtype=torch.float64, pin_memory=True)
+    build_mps_host(sq, d, chi, gh, lh, precision="split")
+    for a, b in zip(ref.Gammas, gh):
+        assert torch.equal(a.cpu(), b)
+    assert torch.equal(ref.Lambdas.cpu(), lh)

@@ -12,6 +12,7 @@
 // (1 (+) S_l)^{-1} uses the symplectic inverse [[e^T, -b^T], [-c^T, a^T]] of
 // S_l = [[a, b], [c, e]].
 // One CTA per job; every job is independent, so many sites run in one launch.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -202,13 +203,292 @@ __global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob* __restrict_
 
 size_t sigma_ws_bytes(int Mr) { return (size_t)112 * Mr * Mr + 256; }
 
+// ---- the same construction in three phases over many CTAs ------------------
+// The one-CTA-per-site kernel above does ~24 M_r^3 FP64 FMAs on one SM; the
+// products (P = L S_r, or L sq L^T at site 0, then B X and -X conj(B)) are
+// tiled over many CTAs here, and only the Gauss-Jordan inversion stays one
+// CTA per site.  Same arithmetic per element up to summation order.
+// Workspace per job (doubles): P [n2 n2] | T [n2 n2] = L explicitly |
+// G [M_r, 2 M_r] complex (site 0: L sq first) | Bm [M_r M_r] complex.
+
+// T = L = 1 (+) S_l^{-1} (symplectic inverse [[e^T, -b^T], [-c^T, a^T]]) on
+// the site-first ordering, identity on the site's own x and p rows.
+__global__ void sigma_linv_kernel(const SigmaJob* __restrict__ jobs) {
+  const SigmaJob jb = jobs[blockIdx.y];
+  const int Mr = jb.Mr, n2 = 2 * Mr, ml = jb.m_l;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n2 * n2) return;
+  const int r = int(t / n2), c = int(t % n2);
+  double* T = jb.ws + (size_t)n2 * n2;
+  const bool inner_r = r != 0 && r != Mr, inner_c = c != 0 && c != Mr;
+  double v;
+  if (!inner_r || ml == 0) {
+    v = r == c ? 1.0 : 0.0;
+  } else if (!inner_c) {
+    v = 0.0;
+  } else {
+    const int rl = r < Mr ? r - 1 : ml + (r - Mr - 1);
+    const int kl = c < Mr ? c - 1 : ml + (c - Mr - 1);
+    const int ld = jb.ld_l;
+    const double* S = jb.S_l;
+    if (rl < ml) v = kl < ml ? S[(size_t)(ml + kl) * ld + (ml + rl)] : -S[(size_t)(kl - ml) * ld + (ml + rl)];
+    else v = kl < ml ? -S[(size_t)(ml + kl) * ld + (rl - ml)] : S[(size_t)(kl - ml) * ld + (rl - ml)];
+  }
+  T[t] = v;
+}
+
+// MODE 0: C = L B0 with B0 = S_r (C -> P) or, at site 0, B0 = sq (C -> G region);
+// MODE 1 (site 0 only): P = L C0^T with C0 = L sq.  64 x 64 tiles, 256 threads.
+template <int MODE>
+__global__ void __launch_bounds__(256) sigma_gemm_kernel(const SigmaJob* __restrict__ jobs) {
+  const SigmaJob jb = jobs[blockIdx.y];
+  if (MODE == 1 && !jb.first) return;
+  const int n2 = 2 * jb.Mr, tn = (n2 + 63) / 64;
+  if ((int)blockIdx.x >= tn * tn) return;
+  const int i0 = (blockIdx.x / tn) * 64, j0 = (blockIdx.x % tn) * 64;
+  const double* L = jb.ws + (size_t)n2 * n2;
+  double* Gr = jb.ws + 2 * (size_t)n2 * n2;
+  const double* B;
+  int64_t bs0, bs1;  // B(k, j) = B[k * bs0 + j * bs1]
+  double* C;
+  if (MODE == 0) {
+    B = jb.S_r;
+    bs0 = jb.ld_r;
+    bs1 = 1;
+    C = jb.first ? Gr : jb.ws;
+  } else {
+    B = Gr;
+    bs0 = 1;
+    bs1 = n2;
+    C = jb.ws;
+  }
+  __shared__ double As[16][65], Bs[16][65];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < n2; k0 += 16) {
+    for (int e = threadIdx.x; e < 64 * 16; e += 256) {
+      const int ii = e / 16, kk = e % 16, i = i0 + ii, k = k0 + kk;
+      As[kk][ii] = (i < n2 && k < n2) ? L[(size_t)i * n2 + k] : 0.0;
+      const int kb = e / 64, jj = e % 64, j = j0 + jj, k2 = k0 + kb;
+      Bs[kb][jj] = (k2 < n2 && j < n2) ? B[(int64_t)k2 * bs0 + (int64_t)j * bs1] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        av[q] = As[kk][ty * 4 + q];
+        bv[q] = Bs[kk][tx * 4 + q];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) acc[q][w] = fma(av[q], bv[w], acc[q][w]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const int i = i0 + ty * 4 + q, j = j0 + tx * 4 + w;
+      if (i < n2 && j < n2) C[(size_t)i * n2 + j] = acc[q][w];
+    }
+}
+
+// One CTA per job: A', B from P, Gauss-Jordan for X = conj(A')^{-1}, Z, and
+// the X / X^T blocks of Sigma (zeros at site 0).
+__global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restrict__ jobs) {
+  const SigmaJob jb = jobs[blockIdx.x];
+  const int Mr = jb.Mr, n2 = 2 * Mr;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double* P = jb.ws;
+  double2* G = reinterpret_cast<double2*>(jb.ws + 2 * (size_t)n2 * n2);
+  double2* Bm = G + (size_t)Mr * n2;
+  __shared__ double s_val[32];
+  __shared__ int s_idx[32];
+  __shared__ double s_logdet;
+  __shared__ int s_piv;
+  for (int i = tid; i < Mr * Mr; i += nt) {
+    int r = i / Mr, c = i % Mr;
+    double xx = P[(size_t)r * n2 + c], xp = P[(size_t)r * n2 + Mr + c];
+    double px = P[(size_t)(Mr + r) * n2 + c], pp = P[(size_t)(Mr + r) * n2 + Mr + c];
+    double ar = 0.5 * (xx + pp), ai = 0.5 * (px - xp);
+    if (jb.first && r == c) ar += 1.0;
+    G[(size_t)r * n2 + c] = make_double2(ar, -ai);
+    G[(size_t)r * n2 + Mr + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+    Bm[i] = make_double2(0.5 * (xx - pp), 0.5 * (px + xp));
+  }
+  if (tid == 0) s_logdet = 0.0;
+  __syncthreads();
+  for (int col = 0; col < Mr; ++col) {
+    double best = -1.0;
+    int bi = col;
+    for (int r = col + tid; r < Mr; r += nt) {
+      double2 v = G[(size_t)r * n2 + col];
+      double m = v.x * v.x + v.y * v.y;
+      if (m > best) {
+        best = m;
+        bi = r;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ob = __shfl_down_sync(0xffffffffu, best, o);
+      int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if ((tid & 31) == 0) {
+      s_val[tid >> 5] = best;
+      s_idx[tid >> 5] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double b = s_val[0];
+      int i0 = s_idx[0];
+      for (int w = 1; w < (nt + 31) / 32; ++w)
+        if (s_val[w] > b || (s_val[w] == b && s_idx[w] < i0)) {
+          b = s_val[w];
+          i0 = s_idx[w];
+        }
+      s_piv = i0;
+      if (!(b > 0.0)) *jb.status = 1;
+      s_logdet += 0.5 * log(b > 0.0 ? b : 1e-300);
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p != col) {
+      for (int c = tid; c < n2; c += nt) {
+        double2 t = G[(size_t)p * n2 + c];
+        G[(size_t)p * n2 + c] = G[(size_t)col * n2 + c];
+        G[(size_t)col * n2 + c] = t;
+      }
+    }
+    __syncthreads();
+    const double2 pv = G[(size_t)col * n2 + col];
+    const double den = pv.x * pv.x + pv.y * pv.y;
+    const double2 inv = den > 0.0 ? make_double2(pv.x / den, -pv.y / den) : make_double2(0.0, 0.0);
+    __syncthreads();
+    for (int c = tid; c < n2; c += nt) {
+      double2 v = G[(size_t)col * n2 + c];
+      G[(size_t)col * n2 + c] = make_double2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
+    }
+    __syncthreads();
+    for (int i = tid; i < Mr * n2; i += nt) {
+      int r = i / n2, c = i % n2;
+      if (r == col) continue;
+      double2 f = G[(size_t)r * n2 + col];
+      if (f.x == 0.0 && f.y == 0.0) continue;
+      if (c == col) continue;
+      double2 v = G[(size_t)col * n2 + c];
+      double2 g = G[i];
+      g.x -= f.x * v.x - f.y * v.y;
+      g.y -= f.x * v.y + f.y * v.x;
+      G[i] = g;
+    }
+    __syncthreads();
+    for (int r = tid; r < Mr; r += nt)
+      if (r != col) G[(size_t)r * n2 + col] = make_double2(0.0, 0.0);
+    __syncthreads();
+  }
+  for (int i = tid; i < Mr * Mr; i += nt) {
+    const int r = i / Mr, c = i % Mr;
+    if (jb.first) {
+      jb.Sigma[(size_t)r * n2 + Mr + c] = make_double2(0.0, 0.0);
+      jb.Sigma[(size_t)(Mr + r) * n2 + c] = make_double2(0.0, 0.0);
+      jb.Sigma[(size_t)(Mr + r) * n2 + Mr + c] = make_double2(0.0, 0.0);
+    } else {
+      jb.Sigma[(size_t)r * n2 + Mr + c] = G[(size_t)c * n2 + Mr + r];  // X^T
+      jb.Sigma[(size_t)(Mr + r) * n2 + c] = G[(size_t)r * n2 + Mr + c];  // X
+    }
+  }
+  if (tid == 0) {
+    double ld = s_logdet;  // log|det A'|
+    *jb.Z = jb.first ? exp(0.25 * (ld - Mr * log(2.0))) : exp(0.5 * ld);
+  }
+}
+
+// Sigma11 = B X (every site) and Sigma22 = -X conj(B) (blockIdx.z = 1, not at
+// site 0): complex products, 32 x 32 tiles, 256 threads with 2 x 2 outputs.
+__global__ void __launch_bounds__(256) sigma_cgemm_kernel(const SigmaJob* __restrict__ jobs) {
+  const SigmaJob jb = jobs[blockIdx.y];
+  const int z = blockIdx.z;
+  if (z == 1 && jb.first) return;
+  const int Mr = jb.Mr, n2 = 2 * Mr, tn = (Mr + 31) / 32;
+  if ((int)blockIdx.x >= tn * tn) return;
+  const int i0 = (blockIdx.x / tn) * 32, j0 = (blockIdx.x % tn) * 32;
+  const double2* G = reinterpret_cast<const double2*>(jb.ws + 2 * (size_t)n2 * n2);
+  const double2* Bm = G + (size_t)Mr * n2;
+  auto Aop = [&](int i, int k) { return z == 0 ? Bm[(size_t)i * Mr + k] : G[(size_t)i * n2 + Mr + k]; };
+  auto Bop = [&](int k, int j) {
+    if (z == 0) return G[(size_t)k * n2 + Mr + j];
+    const double2 b = Bm[(size_t)k * Mr + j];
+    return make_double2(b.x, -b.y);
+  };
+  __shared__ double2 As[16][33], Bs[16][33];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double2 acc[2][2] = {};
+  for (int k0 = 0; k0 < Mr; k0 += 16) {
+    for (int e = threadIdx.x; e < 32 * 16; e += 256) {
+      const int ii = e / 16, kk = e % 16, i = i0 + ii, k = k0 + kk;
+      As[kk][ii] = (i < Mr && k < Mr) ? Aop(i, k) : make_double2(0.0, 0.0);
+      const int kb = e / 32, jj = e % 32, j = j0 + jj, k2 = k0 + kb;
+      Bs[kb][jj] = (k2 < Mr && j < Mr) ? Bop(k2, j) : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+          const double2 av = As[kk][ty * 2 + q], bv = Bs[kk][tx * 2 + w];
+          acc[q][w].x = fma(av.x, bv.x, fma(-av.y, bv.y, acc[q][w].x));
+          acc[q][w].y = fma(av.x, bv.y, fma(av.y, bv.x, acc[q][w].y));
+        }
+    }
+    __syncthreads();
+  }
+  const double sg = z == 0 ? 1.0 : -1.0;
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const int i = i0 + ty * 2 + q, j = j0 + tx * 2 + w;
+      if (i < Mr && j < Mr)
+        jb.Sigma[(size_t)(z == 0 ? i : Mr + i) * n2 + (z == 0 ? j : Mr + j)] =
+            make_double2(sg * acc[q][w].x, sg * acc[q][w].y);
+    }
+}
+
 int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st) {
+  if (n_jobs <= 0) return BSG_OK;
   BSG_CUDA(cudaMemcpyAsync(jobs_dev, jobs_host, sizeof(SigmaJob) * n_jobs, cudaMemcpyHostToDevice, st));
   double work = 0.0;
-  for (int i = 0; i < n_jobs; ++i) work += 20.0 * jobs_host[i].Mr * jobs_host[i].Mr * (double)jobs_host[i].Mr;
-  BSG_PROFILED(h, BSG_K_SIGMA, st, work,
-               (sigma_kernel<<<n_jobs, h->tune[BSG_TUNE_FACTOR_THREADS], 0, st>>>(
-                   reinterpret_cast<const SigmaJob*>(jobs_dev))));
+  int max_mr = 1, first_mr = 0;
+  for (int i = 0; i < n_jobs; ++i) {
+    const int Mr = jobs_host[i].Mr;
+    work += (jobs_host[i].first ? 28.0 : 24.0) * Mr * Mr * (double)Mr;
+    max_mr = std::max(max_mr, Mr);
+    if (jobs_host[i].first) first_mr = std::max(first_mr, Mr);
+  }
+  const SigmaJob* jd = reinterpret_cast<const SigmaJob*>(jobs_dev);
+  const int64_t n2 = 2 * (int64_t)max_mr, tn = (n2 + 63) / 64, tc = (max_mr + 31) / 32;
+  cudaEvent_t ev = nullptr;
+  if (h->prof.on) BSG_TRY(h->prof.begin(BSG_K_SIGMA, st, &ev));
+  sigma_linv_kernel<<<dim3(unsigned((n2 * n2 + 255) / 256), n_jobs), 256, 0, st>>>(jd);
+  sigma_gemm_kernel<0><<<dim3(unsigned(tn * tn), n_jobs), 256, 0, st>>>(jd);
+  if (first_mr) {
+    const int64_t t1 = (2 * (int64_t)first_mr + 63) / 64;
+    sigma_gemm_kernel<1><<<dim3(unsigned(t1 * t1), n_jobs), 256, 0, st>>>(jd);
+  }
+  sigma_gj_kernel<<<n_jobs, h->tune[BSG_TUNE_FACTOR_THREADS], 0, st>>>(jd);
+  sigma_cgemm_kernel<<<dim3(unsigned(tc * tc), n_jobs, 2), 256, 0, st>>>(jd);
+  BSG_CUDA(cudaGetLastError());
+  if (h->prof.on) BSG_TRY(h->prof.end(BSG_K_SIGMA, st, ev, work));
   return BSG_OK;
 }
 

@@ -69,9 +69,13 @@ __device__ __forceinline__ void tf32_split(float v, float& hi, float& lo) {
   lo = __uint_as_float(l);
 }
 
-__global__ void build_bt_kernel(const float2* __restrict__ G, int n, int chi, int d, int left, float* __restrict__ Bhi,
+// B block of photon number n = blockIdx.y at rows n * 2 chi of Bhi / Blo.
+__global__ void build_bt_kernel(const float2* __restrict__ G, int chi, int d, int left, float* __restrict__ Bhi,
                                 float* __restrict__ Blo) {
   const int64_t K2 = 2 * (int64_t)chi;
+  const int n = blockIdx.y;
+  Bhi += (size_t)n * K2 * K2;
+  Blo += (size_t)n * K2 * K2;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= K2 * K2) return;
   const int row = int(t / K2), col = int(t % K2);
@@ -99,79 +103,165 @@ __global__ void build_a_kernel(const float2* __restrict__ E, const int32_t* __re
   Alo[t] = lo;
 }
 
-// ---- host planning: distinct prefixes per level grouped by photon number ----
-struct SidePlan {
-  std::vector<int> sites;                     // site of each level (left: 0..m, right: M-1..m+1)
-  std::vector<std::vector<int32_t>> parent;   // per level: parent row (level-1) of each row
-  std::vector<std::vector<int32_t>> nval;     // per level: photon number of each row
-  std::vector<std::vector<int32_t>> group;    // per level: first row of each photon number (d+1 entries)
-  std::vector<int32_t> final_row;             // per pattern: row at the last level
+// ---- planning on the device: distinct prefixes per level, grouped by n -----
+// Level l of a side keys every pattern by (n, parent row) with n its photon
+// number at the level's site; the distinct keys, in n-major order, are the
+// level's rows, so rows of one n are contiguous (one GEMM per n).  Per level:
+// mark the keys, one CTA scans them into row ids (writing each row's parent
+// and n and the level's group bounds), then every pattern takes its row.
+constexpr int kMaxLevels = 1024;
+
+struct PlanArgs {
+  const int32_t* pat;  // [P, M]
+  int64_t P;
+  int M, d;
+  int32_t* cur;        // [P] row at the previous level (0 before level 0)
+  int32_t* keys;       // [P]
+  int32_t* flags;      // [d * P] zero on entry, left zero
+  int32_t* idx;        // [d * P] row of each key
+  int32_t* meta;       // [levels, d + 2]: rows, group[0..d]
+  int* err;
 };
 
-static void plan_side(const int32_t* pat, int64_t P, int M, int d, const std::vector<int>& sites, SidePlan& sp) {
-  sp.sites = sites;
-  const int nl = int(sites.size());
-  sp.parent.assign(nl, {});
-  sp.nval.assign(nl, {});
-  sp.group.assign(nl, {});
-  std::vector<int32_t> cur(P, 0), nxt(P);
-  int64_t prev_rows = 1;
-  for (int l = 0; l < nl; ++l) {
-    const int s = sites[l];
-    // key = parent * d + n -> first-appearance id, then regroup by n
-    std::vector<int32_t> id((size_t)prev_rows * d, -1);
-    std::vector<int32_t> par, nv;
-    for (int64_t p = 0; p < P; ++p) {
-      const int n = pat[p * M + s];
-      const int64_t key = (int64_t)cur[p] * d + n;
-      if (id[key] < 0) {
-        id[key] = int32_t(par.size());
-        par.push_back(cur[p]);
-        nv.push_back(n);
-      }
-      nxt[p] = id[key];
-    }
-    const int rows = int(par.size());
-    std::vector<int32_t> start(d + 1, 0);
-    for (int r = 0; r < rows; ++r) start[nv[r] + 1]++;
-    for (int n = 0; n < d; ++n) start[n + 1] += start[n];
-    std::vector<int32_t> pos(start.begin(), start.end() - 1), remap(rows);
-    for (int r = 0; r < rows; ++r) remap[r] = pos[nv[r]]++;
-    std::vector<int32_t> par2(rows), nv2(rows);
-    for (int r = 0; r < rows; ++r) {
-      par2[remap[r]] = par[r];
-      nv2[remap[r]] = nv[r];
-    }
-    for (int64_t p = 0; p < P; ++p) cur[p] = remap[nxt[p]];
-    sp.parent[l].swap(par2);
-    sp.nval[l].swap(nv2);
-    sp.group[l].swap(start);
-    prev_rows = rows;
+__global__ void plan_mark_kernel(PlanArgs a, int site, int level) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  const int prev = level == 0 ? 1 : a.meta[(level - 1) * (a.d + 2)];
+  int n = a.pat[p * a.M + site];
+  if (n < 0 || n >= a.d) {
+    atomicExch(a.err, 1);
+    n = 0;
   }
-  sp.final_row = cur;
+  const int key = n * prev + (level == 0 ? 0 : a.cur[p]);
+  a.keys[p] = key;
+  a.flags[key] = 1;
+}
+
+// One CTA: exclusive scan of flags[0, d * prev) into idx, rows' parent / n,
+// the level's row count and group bounds; clears the flags it read.
+__global__ void __launch_bounds__(1024) plan_scan_kernel(PlanArgs a, int level, int32_t* parent, int32_t* nval) {
+  __shared__ int32_t warp_sums[32];
+  __shared__ int32_t carry;
+  const int d = a.d;
+  const int prev = level == 0 ? 1 : a.meta[(level - 1) * (d + 2)];
+  const int64_t size = (int64_t)d * prev;
+  int32_t* meta = a.meta + level * (d + 2);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < size; base += 1024) {
+    const int64_t q = base + tid;
+    const int f = q < size ? a.flags[q] : 0;
+    int x = f;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int v = warp_sums[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+      }
+      warp_sums[lane] = v;
+    }
+    __syncthreads();
+    const int c0 = carry;
+    const int excl = c0 + (w ? warp_sums[w - 1] : 0) + x - f;
+    if (q < size) {
+      a.idx[q] = excl;
+      a.flags[q] = 0;
+      if (q % prev == 0) meta[1 + q / prev] = excl;  // first row of photon number q / prev
+      if (f) {
+        parent[excl] = int32_t(q % prev);
+        nval[excl] = int32_t(q / prev);
+      }
+    }
+    __syncthreads();
+    if (tid == 1023) carry = excl + f;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    meta[0] = carry;
+    meta[1 + d] = carry;
+  }
+}
+
+__global__ void plan_assign_kernel(PlanArgs a) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  a.cur[p] = a.idx[a.keys[p]];
+}
+
+struct SidePlan {
+  std::vector<int> sites;                 // site of each level (left: 0..m, right: M-1..m+1)
+  std::vector<int32_t> meta;              // host copy: per level rows, group[0..d]
+  int32_t* parent = nullptr;              // device: level l rows at parent + l * P
+  int32_t* nval = nullptr;
+  int32_t* final_row = nullptr;           // device: [P] row at the last level
+  int64_t P = 0;
+  int d = 0;
+  int rows(int l) const { return meta[(size_t)l * (d + 2)]; }
+  int group(int l, int n) const { return meta[(size_t)l * (d + 2) + 1 + n]; }
+};
+
+static int plan_side_device(bsg_handle_t h, const int32_t* pat, int64_t P, int M, int d, const std::vector<int>& sites,
+                            SidePlan& sp, int32_t* work, int* err, cudaStream_t st) {
+  const int nl = int(sites.size());
+  sp.sites = sites;
+  sp.P = P;
+  sp.d = d;
+  // work: cur, keys [P] | flags, idx [d P] | meta [nl (d + 2)] | parent, nval [nl P]
+  PlanArgs a{};
+  a.pat = pat;
+  a.P = P;
+  a.M = M;
+  a.d = d;
+  a.cur = work;
+  a.keys = a.cur + P;
+  a.flags = a.keys + P;
+  a.idx = a.flags + (size_t)d * P;
+  a.meta = a.idx + (size_t)d * P;
+  a.err = err;
+  sp.parent = a.meta + (size_t)nl * (d + 2);
+  sp.nval = sp.parent + (size_t)nl * P;
+  sp.final_row = a.cur;
+  BSG_CUDA(cudaMemsetAsync(a.flags, 0, (size_t)d * P * 4, st));
+  const unsigned blocks = unsigned((P + 255) / 256);
+  for (int l = 0; l < nl; ++l) {
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_mark_kernel<<<blocks, 256, 0, st>>>(a, sites[l], l)));
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)P,
+                 (plan_scan_kernel<<<1, 1024, 0, st>>>(a, l, sp.parent + (size_t)l * P, sp.nval + (size_t)l * P)));
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_assign_kernel<<<blocks, 256, 0, st>>>(a)));
+  }
+  sp.meta.resize((size_t)nl * (d + 2));
+  BSG_CUDA(cudaMemcpyAsync(sp.meta.data(), a.meta, sp.meta.size() * 4, cudaMemcpyDeviceToHost, st));
+  return BSG_OK;
+}
+
+static size_t plan_side_words(int64_t P, int d, int levels) {
+  return (size_t)2 * P + (size_t)2 * d * P + (size_t)levels * (d + 2) + (size_t)2 * levels * P;
 }
 
 template <class R>
 static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* lam, int M, int chi, int d,
                            const SidePlan& left, const SidePlan& right, int64_t P, double* amp, bool umma,
-                           cudaStream_t st) {
+                           char* ws, cudaStream_t st) {
   using T = typename Cx<R>::T;
-  // device memory: two env buffers per side (ping-pong) + index arrays
-  auto rows_of = [](const SidePlan& s, int l) { return (int64_t)s.parent[l].size(); };
+  // device memory: two env buffers per side (ping-pong)
   int64_t max_rows = 1;
-  for (int l = 0; l < (int)left.sites.size(); ++l) max_rows = std::max(max_rows, rows_of(left, l));
-  for (int l = 0; l < (int)right.sites.size(); ++l) max_rows = std::max(max_rows, rows_of(right, l));
-  int64_t idx_total = 2 * P;
-  for (auto* sp : {&left, &right})
-    for (size_t l = 0; l < sp->sites.size(); ++l) idx_total += 2 * (int64_t)sp->parent[l].size();
+  for (int l = 0; l < (int)left.sites.size(); ++l) max_rows = std::max<int64_t>(max_rows, left.rows(l));
+  for (int l = 0; l < (int)right.sites.size(); ++l) max_rows = std::max<int64_t>(max_rows, right.rows(l));
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t env_bytes = al((size_t)max_rows * chi * sizeof(T));
   const size_t a_bytes = umma ? al((size_t)max_rows * 2 * chi * 4) : 0;
-  const size_t b_bytes = umma ? al((size_t)4 * chi * chi * 4) : 0;
-  const size_t need = 4 * env_bytes + al((size_t)idx_total * 4) + 2 * a_bytes + 2 * b_bytes + 256;
+  const size_t b_bytes = umma ? al((size_t)d * 4 * chi * chi * 4) : 0;
+  const size_t need = 4 * env_bytes + 2 * a_bytes + 2 * b_bytes + 256;
   BSG_TRY(h->contract_ws.ensure(need));
   char* base = reinterpret_cast<char*>(h->contract_ws.ptr);
-  char* sp_base = base + 4 * env_bytes + al((size_t)idx_total * 4);
+  char* sp_base = base + 4 * env_bytes;
   float* Ahi = reinterpret_cast<float*>(sp_base);
   float* Alo = reinterpret_cast<float*>(sp_base + a_bytes);
   float* Bhi = reinterpret_cast<float*>(sp_base + 2 * a_bytes);
@@ -180,75 +270,79 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   if (umma) BSG_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
   T* E[4] = {reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + env_bytes),
              reinterpret_cast<T*>(base + 2 * env_bytes), reinterpret_cast<T*>(base + 3 * env_bytes)};
-  int32_t* idx = reinterpret_cast<int32_t*>(base + 4 * env_bytes);
-  // stage all index arrays in pinned memory, one copy
-  BSG_TRY(h->host_stage2.ensure((size_t)idx_total * 4 + 64));
-  int32_t* hidx = reinterpret_cast<int32_t*>(h->host_stage2.ptr);
-  int64_t off = 0;
-  struct LevelIdx {
-    int64_t parent_off, nval_off;
-  };
-  std::vector<LevelIdx> li_l(left.sites.size()), li_r(right.sites.size());
-  auto put = [&](const SidePlan& sp, std::vector<LevelIdx>& li) {
-    for (size_t l = 0; l < sp.sites.size(); ++l) {
-      li[l].parent_off = off;
-      std::memcpy(hidx + off, sp.parent[l].data(), sp.parent[l].size() * 4);
-      off += (int64_t)sp.parent[l].size();
-      li[l].nval_off = off;
-      std::memcpy(hidx + off, sp.nval[l].data(), sp.nval[l].size() * 4);
-      off += (int64_t)sp.nval[l].size();
+  (void)ws;
+  // tensor-core path: one grouped GEMM per level; its row tiles {first row,
+  // end row of the photon-number group, B block row, 0}, all levels at once
+  const int K2 = 2 * chi;
+  std::vector<int4> tiles;
+  std::vector<int> tile_off[2];
+  if (umma) {
+    const SidePlan* sps[2] = {&left, &right};
+    for (int sd = 0; sd < 2; ++sd) {
+      tile_off[sd].assign(sps[sd]->sites.size() + 1, 0);
+      for (size_t l = 1; l < sps[sd]->sites.size(); ++l) {
+        tile_off[sd][l] = int(tiles.size());
+        for (int n = 0; n < d; ++n) {
+          const int r0 = sps[sd]->group(int(l), n), r1 = sps[sd]->group(int(l), n + 1);
+          for (int t0 = r0; t0 < r1; t0 += 128) tiles.push_back(make_int4(t0, r1, n * K2, 0));
+        }
+      }
+      tile_off[sd][sps[sd]->sites.size()] = int(tiles.size());
     }
-  };
-  put(left, li_l);
-  put(right, li_r);
-  const int64_t fin_l = off;
-  std::memcpy(hidx + off, left.final_row.data(), (size_t)P * 4);
-  off += P;
-  const int64_t fin_r = off;
-  std::memcpy(hidx + off, right.final_row.data(), (size_t)P * 4);
-  off += P;
-  BSG_CUDA(cudaMemcpyAsync(idx, hidx, (size_t)off * 4, cudaMemcpyHostToDevice, st));
+  }
+  int4* d_tiles = nullptr;
+  if (umma && !tiles.empty()) {
+    BSG_TRY(h->plan.ensure(tiles.size() * sizeof(int4)));
+    BSG_TRY(h->host_stage2.ensure(tiles.size() * sizeof(int4)));
+    std::memcpy(h->host_stage2.ptr, tiles.data(), tiles.size() * sizeof(int4));
+    d_tiles = reinterpret_cast<int4*>(h->plan.ptr);
+    BSG_CUDA(cudaMemcpyAsync(d_tiles, h->host_stage2.ptr, tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+  }
 
   double flops = 0.0;
-  auto side = [&](const SidePlan& sp, const std::vector<LevelIdx>& li, T* e0, T* e1, bool is_left) -> T* {
+  auto side = [&](const SidePlan& sp, T* e0, T* e1, bool is_left) -> T* {
     T* prev = e0;
     T* curb = e1;
     // level 0: row 0 of Gamma_0 (left) or column 0 of Gamma_{M-1} (right)
     {
       const int s = sp.sites[0];
       const T* G = reinterpret_cast<const T*>(Gd[s]);
-      const int64_t rows = (int64_t)sp.parent[0].size();
+      const int64_t rows = sp.rows(0);
       // left: Gamma_0[0, a, n] at a*d + n ; right: Gamma_{M-1}[a, 0, n] at a*chi*d + n
       const int64_t stride = is_left ? d : (int64_t)chi * d;
       const int64_t tot = rows * chi;
-      env_init_kernel<R><<<unsigned((tot + 255) / 256), 256, 0, st>>>(G, stride, idx + li[0].nval_off, (int)rows, chi,
-                                                                         prev);
+      env_init_kernel<R><<<unsigned((tot + 255) / 256), 256, 0, st>>>(G, stride, sp.nval, (int)rows, chi, prev);
     }
     for (size_t l = 1; l < sp.sites.size(); ++l) {
       const int s = sp.sites[l];
       const T* G = reinterpret_cast<const T*>(Gd[s]);
+      const int32_t* parent = sp.parent + l * sp.P;
       // left uses Lambda_{s-1}, right uses Lambda_s
       const double* lm = lam + (size_t)(is_left ? s - 1 : s) * chi;
-      for (int n = 0; n < d; ++n) {
-        const int r0 = sp.group[l][n], r1 = sp.group[l][n + 1];
-        if (r1 <= r0) continue;
-        if constexpr (std::is_same<R, float>::value) {
-          if (umma) {
-            const int64_t K2 = 2 * (int64_t)chi, rows = r1 - r0;
-            build_bt_kernel<<<unsigned((K2 * K2 + 255) / 256), 256, 0, st>>>(
-                reinterpret_cast<const float2*>(G), n, chi, d, is_left ? 1 : 0, Bhi, Blo);
-            build_a_kernel<<<unsigned((rows * K2 + 255) / 256), 256, 0, st>>>(
-                reinterpret_cast<const float2*>(prev), idx + li[l].parent_off + r0, lm, (int)rows, chi, Ahi, Alo);
-            if (gemm_tf32x3(h, Ahi, Alo, Bhi, Blo, reinterpret_cast<float*>(curb + (int64_t)r0 * chi), (int)rows,
-                            (int)K2, (int)K2, (int)K2, d_err, st, false) != BSG_OK)
-              return nullptr;
-            flops += 8.0 * rows * (double)chi * chi;
-            continue;
-          }
+      if constexpr (std::is_same<R, float>::value) {
+        if (umma) {
+          // all photon numbers of the level in one grouped GEMM
+          const int rows = sp.rows(int(l));
+          const int sd = is_left ? 0 : 1;
+          const int t0 = tile_off[sd][l], nt = tile_off[sd][l + 1] - t0;
+          build_bt_kernel<<<dim3(unsigned(((int64_t)K2 * K2 + 255) / 256), d), 256, 0, st>>>(
+              reinterpret_cast<const float2*>(G), chi, d, is_left ? 1 : 0, Bhi, Blo);
+          build_a_kernel<<<unsigned(((int64_t)rows * K2 + 255) / 256), 256, 0, st>>>(
+              reinterpret_cast<const float2*>(prev), parent, lm, rows, chi, Ahi, Alo);
+          if (gemm_tf32x3(h, Ahi, Alo, Bhi, Blo, reinterpret_cast<float*>(curb), rows, K2, K2, K2, d_err, st, false,
+                          d_tiles + t0, nt, d * K2) != BSG_OK)
+            return nullptr;
+          flops += 8.0 * rows * (double)chi * chi;
+          std::swap(prev, curb);
+          continue;
         }
+      }
+      for (int n = 0; n < d; ++n) {
+        const int r0 = sp.group(int(l), n), r1 = sp.group(int(l), n + 1);
+        if (r1 <= r0) continue;
         GemmArgs<R> g{};
         g.A = prev;
-        g.pidx = idx + li[l].parent_off + r0;
+        g.pidx = parent + r0;
         g.lam = lm;
         g.B = G + n;
         g.sk = is_left ? (int64_t)chi * d : d;
@@ -267,18 +361,18 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   };
   cudaEvent_t ev = nullptr;
   if (h->prof.on) BSG_TRY(h->prof.begin(BSG_K_CONTRACT, st, &ev));
-  T* Lend = side(left, li_l, E[0], E[1], true);
+  T* Lend = side(left, E[0], E[1], true);
   if (!Lend) return BSG_ERR_CUDA;
-  T* Rend = side(right, li_r, E[2], E[3], false);
+  T* Rend = side(right, E[2], E[3], false);
   if (!Rend) return BSG_ERR_CUDA;
   const int mid = left.sites.back();
   final_dot_kernel<R><<<unsigned((P * 32 + 255) / 256), 256, 0, st>>>(
-      Lend, idx + fin_l, Rend, idx + fin_r, lam + (size_t)mid * chi, chi, P, reinterpret_cast<double2*>(amp));
+      Lend, left.final_row, Rend, right.final_row, lam + (size_t)mid * chi, chi, P, reinterpret_cast<double2*>(amp));
   BSG_CUDA(cudaGetLastError());
   if (h->prof.on) BSG_TRY(h->prof.end(BSG_K_CONTRACT, st, ev, flops + 8.0 * P * chi));
   int err = 0;
   if (umma) BSG_CUDA(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaStreamSynchronize(st));  // the pinned index staging is reused by the next call
+  BSG_CUDA(cudaStreamSynchronize(st));
   if (err) {
     set_error("bsg_pattern_amplitudes: a tensor-core pipeline wait timed out");
     return BSG_ERR_CUDA;
@@ -303,26 +397,34 @@ extern "C" int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas,
   BSG_CUDA(cudaSetDevice(h->device));
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if (P == 0) return BSG_OK;
-  std::vector<int32_t> pat((size_t)P * M);
-  BSG_CUDA(cudaMemcpyAsync(pat.data(), patterns, pat.size() * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaStreamSynchronize(st));
-  for (size_t i = 0; i < pat.size(); ++i)
-    if (pat[i] < 0 || pat[i] >= d) {
-      set_error("bsg_pattern_amplitudes: photon number %d outside [0, d=%d)", pat[i], d);
-      return BSG_ERR_INVALID;
-    }
   const int m = (M - 1) / 2;  // left levels 0..m, right levels M-1..m+1
   std::vector<int> ls, rs;
   for (int i = 0; i <= m; ++i) ls.push_back(i);
   for (int i = M - 1; i > m; --i) rs.push_back(i);
+  BSG_CHECK_ARG(int(ls.size()) <= kMaxLevels && int(rs.size()) <= kMaxLevels, "bsg_pattern_amplitudes: M too large");
+  BSG_CHECK_ARG((int64_t)d * P < INT32_MAX, "bsg_pattern_amplitudes: d * P = %lld too large", (long long)d * P);
+  // planning workspace (both sides) + an error word
+  const size_t wl = plan_side_words(P, d, int(ls.size())), wr = plan_side_words(P, d, int(rs.size()));
+  BSG_TRY(h->sample_ws.ensure((wl + wr) * 4 + 256));
+  int32_t* work = reinterpret_cast<int32_t*>(h->sample_ws.ptr);
+  int* perr = reinterpret_cast<int*>(work + wl + wr);
+  BSG_CUDA(cudaMemsetAsync(perr, 0, 4, st));
   SidePlan left, right;
-  plan_side(pat.data(), P, M, d, ls, left);
-  plan_side(pat.data(), P, M, d, rs, right);
+  BSG_TRY(plan_side_device(h, patterns, P, M, d, ls, left, work, perr, st));
+  BSG_TRY(plan_side_device(h, patterns, P, M, d, rs, right, work + wl, perr, st));
+  int herr = 0;
+  BSG_CUDA(cudaMemcpyAsync(&herr, perr, 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaStreamSynchronize(st));  // level sizes for the GEMM launches
+  if (herr) {
+    set_error("bsg_pattern_amplitudes: a photon number is outside [0, d=%d)", d);
+    return BSG_ERR_INVALID;
+  }
   if (precision == BSG_PREC_FP64)
-    return run_contraction<double>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, false, st);
+    return run_contraction<double>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, false, nullptr, st);
   if (precision == BSG_PREC_SPLIT && chi % 2 != 0) {
     set_error("bsg_pattern_amplitudes: the tensor-core path needs an even chi");
     return BSG_ERR_INVALID;
   }
-  return run_contraction<float>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, precision == BSG_PREC_SPLIT, st);
+  return run_contraction<float>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, precision == BSG_PREC_SPLIT,
+                                nullptr, st);
 }

@@ -194,8 +194,12 @@ size_t sigma_ws_bytes(int Mr);
 
 // tcgen05 3xTF32 GEMM (bsg_umma.cu): C[M, N] (ldc) = (Ahi+Alo)(Bhi+Blo)^T, K-major
 // operands already split; *d_err set on a pipeline timeout.
+// 3xTF32 tcgen05 GEMM C[M, N] = A[M, K] B[N, K]^T (TF32 hi/lo operands).
+// Grouped mode (mtiles non-null): n_mtiles row tiles {first row, end row, B
+// row offset, 0}; B then has b_rows rows (one N-row block per group).
 int gemm_tf32x3(bsg_handle_t h, const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, float* C,
-                int M, int N, int K, int ldc, int* d_err, cudaStream_t st, bool profile);
+                int M, int N, int K, int ldc, int* d_err, cudaStream_t st, bool profile,
+                const int4* mtiles = nullptr, int n_mtiles = 0, int b_rows = 0);
 int split_tf32(bsg_handle_t h, const float* x, float* hi, float* lo, int64_t n, cudaStream_t st);
 int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st);
 

@@ -96,6 +96,9 @@ struct UmmaArgs {
   int M, N, K;
   int ldc;
   int* err;
+  // grouped mode (non-null): row tile y covers A/C rows [x, y) and reads B
+  // rows from z on (one B block per group, stacked in one tensor map)
+  const int4* mtiles;
 };
 
 __global__ void __launch_bounds__(128, 1)
@@ -111,7 +114,14 @@ __global__ void __launch_bounds__(128, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
   int* fail = reinterpret_cast<int*>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * UM, n0 = blockIdx.x * UN;
+  int m0 = blockIdx.y * UM, m_end = g.M, b_row0 = 0;
+  if (g.mtiles) {
+    const int4 t = g.mtiles[blockIdx.y];
+    m0 = t.x;
+    m_end = t.y;
+    b_row0 = t.z;
+  }
+  const int n0 = blockIdx.x * UN;
   const int nkb = (g.K + UK - 1) / UK;
 
   if (threadIdx.x == 0) {
@@ -147,8 +157,8 @@ __global__ void __launch_bounds__(128, 1)
       const int k0 = kb * UK;
       tma_load_2d(st, &mA_hi, &full[s], k0, m0);
       tma_load_2d(st + kTileBytes, &mA_lo, &full[s], k0, m0);
-      tma_load_2d(st + 2 * kTileBytes, &mB_hi, &full[s], k0, n0);
-      tma_load_2d(st + 3 * kTileBytes, &mB_lo, &full[s], k0, n0);
+      tma_load_2d(st + 2 * kTileBytes, &mB_hi, &full[s], k0, b_row0 + n0);
+      tma_load_2d(st + 3 * kTileBytes, &mB_lo, &full[s], k0, b_row0 + n0);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -197,7 +207,7 @@ __global__ void __launch_bounds__(128, 1)
             "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < g.M) {
+      if (row < m_end) {
         float* out = g.C + (int64_t)row * g.ldc + n0 + c;
 #pragma unroll
         for (int j = 0; j < 32; ++j)
@@ -279,21 +289,22 @@ int split_tf32(bsg_handle_t h, const float* x, float* hi, float* lo, int64_t n, 
 }
 
 int gemm_tf32x3(bsg_handle_t h, const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, float* C,
-                int M, int N, int K, int ldc, int* d_err, cudaStream_t st, bool profile) {
-  if (M == 0 || N == 0) return BSG_OK;
+                int M, int N, int K, int ldc, int* d_err, cudaStream_t st, bool profile, const int4* mtiles,
+                int n_mtiles, int b_rows) {
+  if (M == 0 || N == 0 || (mtiles && n_mtiles == 0)) return BSG_OK;
   CUtensorMap ma, mal, mb, mbl;
   BSG_TRY(make_map(&ma, Ahi, M, K));
   BSG_TRY(make_map(&mal, Alo, M, K));
-  BSG_TRY(make_map(&mb, Bhi, N, K));
-  BSG_TRY(make_map(&mbl, Blo, N, K));
+  BSG_TRY(make_map(&mb, Bhi, mtiles ? b_rows : N, K));
+  BSG_TRY(make_map(&mbl, Blo, mtiles ? b_rows : N, K));
   const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
   static bool attr = false;
   if (!attr) {
     BSG_CUDA(cudaFuncSetAttribute(umma_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  UmmaArgs g{C, M, N, K, ldc, d_err};
-  dim3 grid((N + UN - 1) / UN, (M + UM - 1) / UM);
+  UmmaArgs g{C, M, N, K, ldc, d_err, mtiles};
+  dim3 grid((N + UN - 1) / UN, mtiles ? n_mtiles : (M + UM - 1) / UM);
   if (profile) {
     BSG_PROFILED(h, BSG_K_CONTRACT, st, 2.0 * M * (double)N * K * 3.0,
                  (umma_tf32x3_kernel<<<grid, 128, smem, st>>>(ma, mal, mb, mbl, g)));

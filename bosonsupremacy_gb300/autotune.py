@@ -31,6 +31,7 @@ KNOBS = {
     "scratch_mib": _lib.TUNE_DP_SCRATCH_MIB,
     "fp64_blocks": _lib.TUNE_DP_FP64_BLOCKS,
     "factor_threads": _lib.TUNE_FACTOR_THREADS,
+    "gemm_kernel": _lib.TUNE_GEMM_KERNEL,
 }
 
 

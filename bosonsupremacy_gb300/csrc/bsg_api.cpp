@@ -186,6 +186,7 @@ int bsg_tune_set(bsg_handle_t h, int key, int value) {
     BSG_CHECK_ARG(value >= 1 && value <= 8, "bsg_tune_set: small-launch blocks per SM %d", value);
   if (key == BSG_TUNE_DP_FP64_BLOCKS)
     BSG_CHECK_ARG(value >= 0 && value <= 8, "bsg_tune_set: FP64 helper blocks per SM %d", value);
+  if (key == BSG_TUNE_GEMM_KERNEL) BSG_CHECK_ARG(value == 0 || value == 1, "bsg_tune_set: GEMM kernel %d", value);
   if (key == BSG_TUNE_FACTOR_THREADS)
     BSG_CHECK_ARG(value == 256 || value == 512 || value == 1024, "bsg_tune_set: factor threads %d", value);
   if (key == BSG_TUNE_DP_SCRATCH_MIB)

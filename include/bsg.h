@@ -260,7 +260,9 @@ int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* m
                                         launch sharing the work queue (FP64 pipe), 0..8 (default 0 = off) */
 #define BSG_TUNE_FACTOR_THREADS 6    /* threads per CTA of the Williamson and Sigma kernels, 256 / 512 / 1024
                                         (default 1024; fewer leave registers for DP blocks on the same SM) */
-#define BSG_TUNE_COUNT 7
+#define BSG_TUNE_GEMM_KERNEL 7       /* 3xTF32 tcgen05 GEMM: 0 one 128x128 tile per CTA, 1 persistent 128x256 tiles
+                                        with a double TMEM accumulator (default 1) */
+#define BSG_TUNE_COUNT 8
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

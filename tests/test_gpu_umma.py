@@ -14,8 +14,23 @@ def _tf32(x):
     return b.astype(np.uint32).view(np.float32)
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (200, 256, 96), (512, 384, 1024), (1000, 130, 516)])
-def test_tf32x3_gemm(cuda, M, N, K):
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (200, 256, 96), (512, 384, 1024), (1000, 130, 516),
+                                   (300, 700, 64)])
+def test_tf32x3_gemm(cuda, M, N, K, kernel):
+    """kernel 0: one 128 x 128 tile per CTA; kernel 1: persistent 128 x 256
+    tiles with a double TMEM accumulator (more tiles than SMs in the last case)."""
+    import torch
+    from bosonsupremacy_gb300 import _lib, autotune
+    saved = autotune.get_knobs()
+    autotune.set_knobs(gemm_kernel=kernel)
+    try:
+        _gemm_case(M, N, K)
+    finally:
+        autotune.set_knobs(**saved)
+
+
+def _gemm_case(M, N, K):
     import torch
     from bosonsupremacy_gb300 import _lib
     rng = np.random.default_rng(M + N + K)
@@ -34,3 +49,29 @@ def test_tf32x3_gemm(cuda, M, N, K):
     assert rel.max() <= 1e-5, rel.max()
     one_tf32 = np.abs(_tf32(A).astype(np.float64) @ _tf32(B).astype(np.float64).T - ref) / absum
     assert np.median(rel) * 10 <= np.median(one_tf32)
+
+
+def test_persistent_gemm_many_tiles(cuda):
+    """More output tiles than SMs, so every persistent CTA cycles both TMEM
+    accumulators several times; both kernels agree to FP32 rounding."""
+    import torch
+    from bosonsupremacy_gb300 import _lib, autotune
+    M, N, K = 4096, 1536, 256
+    rng = np.random.default_rng(7)
+    A = torch.as_tensor(rng.standard_normal((M, K)).astype(np.float32)).cuda()
+    B = torch.as_tensor(rng.standard_normal((N, K)).astype(np.float32)).cuda()
+    out = []
+    saved = autotune.get_knobs()
+    try:
+        for kernel in (0, 1):
+            autotune.set_knobs(gemm_kernel=kernel)
+            C = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
+            h = _lib.Handle.get(0)
+            _lib.check(_lib.load().bsg_gemm_tf32x3(h.h, A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K,
+                                                   _lib.stream_ptr()), "bsg_gemm_tf32x3")
+            out.append(C.cpu().numpy())
+    finally:
+        autotune.set_knobs(**saved)
+    assert np.isfinite(out[1]).all()
+    scale = np.abs(A.cpu().numpy()).astype(np.float64) @ np.abs(B.cpu().numpy()).astype(np.float64).T
+    assert (np.abs(out[0].astype(np.float64) - out[1]) / scale).max() <= 1e-6

@@ -23,6 +23,7 @@
 //   D_kj = e^{i (k - j)(theta + pi/2)} sum_m V_km V_jm e^{-i r x_m}.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "bsg_cgemm.cuh"
@@ -74,8 +75,10 @@ static void position_eigs(int dd, std::vector<double>& V, std::vector<double>& x
   for (int k = 0; k < dd; ++k) x[k] = A[(size_t)k * dd + k];
 }
 
-// Device tables for one dd: x[dd] and W[k][j][m] = V_km V_jm (k, j, m < dd).
-static int displacement_tables(bsg_handle_t h, int dd, const double** x_dev, const double** W_dev, cudaStream_t st) {
+// Device tables for one dd: x[dd] and W[k][j][m] = V_km V_jm (k, j, m < dd),
+// in FP64 and (after them) as FP32 copies for the FP32-precision paths.
+static int displacement_tables(bsg_handle_t h, int dd, const double** x_dev, const double** W_dev,
+                               const float** xf_dev, const float** Wf_dev, cudaStream_t st) {
   static_assert(sizeof(double) == 8, "");
   const size_t nx = (size_t)dd, nw = (size_t)dd * dd * dd;
   if (h->disp_dd != dd) {
@@ -87,48 +90,60 @@ static int displacement_tables(bsg_handle_t h, int dd, const double** x_dev, con
       for (int j = 0; j < dd; ++j)
         for (int m = 0; m < dd; ++m)
           host[nx + ((size_t)k * dd + j) * dd + m] = V[(size_t)k * dd + m] * V[(size_t)j * dd + m];
-    BSG_TRY(h->disp_tab.ensure(host.size() * 8));
+    std::vector<float> hostf(host.size());
+    for (size_t i = 0; i < host.size(); ++i) hostf[i] = float(host[i]);
+    BSG_TRY(h->disp_tab.ensure(host.size() * 12));
     BSG_CUDA(cudaMemcpyAsync(h->disp_tab.ptr, host.data(), host.size() * 8, cudaMemcpyHostToDevice, st));
+    BSG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(h->disp_tab.ptr) + host.size() * 8, hostf.data(),
+                             hostf.size() * 4, cudaMemcpyHostToDevice, st));
     BSG_CUDA(cudaStreamSynchronize(st));
     h->disp_dd = dd;
   }
   *x_dev = reinterpret_cast<const double*>(h->disp_tab.ptr);
   *W_dev = *x_dev + nx;
+  *xf_dev = reinterpret_cast<const float*>(*x_dev + nx + nw);
+  *Wf_dev = *xf_dev + nx;
   return BSG_OK;
 }
 
 // e^{-i r x_m} (lanes m < dd) and e^{i p phi} (p = lane - 15) into per-warp
 // shared arrays, then D[k][j] for k < dd, j < jmax.
+__device__ __forceinline__ void sincos_r(double a, double* s, double* c) { sincos(a, s, c); }
+__device__ __forceinline__ void sincos_r(float a, float* s, float* c) { sincosf(a, s, c); }
+__device__ __forceinline__ double atan2_r(double y, double x) { return atan2(y, x); }
+__device__ __forceinline__ float atan2_r(float y, float x) { return atan2f(y, x); }
+
+// D(alpha) in precision R (the FP32 paths build it with FP32 math and tables).
 template <class R>
-__device__ void build_displacement(double2 al, int dd, int jmax, const double* __restrict__ x,
-                                   const double* __restrict__ W, typename Cx<R>::T* ex, typename Cx<R>::T* ph,
-                                   typename Cx<R>::T* D, int lane) {
+__device__ void build_displacement(double2 al, int dd, int jmax, const R* __restrict__ x, const R* __restrict__ W,
+                                   typename Cx<R>::T* ex, typename Cx<R>::T* ph, typename Cx<R>::T* D, int lane) {
   using T = typename Cx<R>::T;
-  const double r = sqrt(al.x * al.x + al.y * al.y);
-  const double phi = atan2(al.y, al.x) + 1.5707963267948966;
+  const R ax = R(al.x), ay = R(al.y);
+  const R r = sqrt(ax * ax + ay * ay);
+  const R phi = atan2_r(ay, ax) + R(1.5707963267948966);
   if (lane < dd) {
-    double s, c;
-    sincos(-r * x[lane], &s, &c);
+    R s, c;
+    sincos_r(-r * x[lane], &s, &c);
     T v;
-    v.x = R(c);
-    v.y = R(s);
+    v.x = c;
+    v.y = s;
     ex[lane] = v;
   }
   if (lane < 31) {
-    double s, c;
-    sincos(double(lane - 15) * phi, &s, &c);
+    R s, c;
+    sincos_r(R(lane - 15) * phi, &s, &c);
     T v;
-    v.x = R(c);
-    v.y = R(s);
+    v.x = c;
+    v.y = s;
     ph[lane] = v;
   }
   __syncwarp();
   for (int e = lane; e < dd * jmax; e += 32) {
     const int k = e / jmax, j = e % jmax;
-    const double* w = W + ((size_t)k * dd + j) * dd;
+    const R* w = W + ((size_t)k * dd + j) * dd;
     R sr = R(0), si = R(0);
     for (int m = 0; m < dd; ++m) {
-      const R wm = R(w[m]);
+      const R wm = w[m];
       sr += wm * ex[m].x;
       si += wm * ex[m].y;
     }
@@ -212,8 +227,8 @@ struct SampleArgs {
   const typename Cx<R>::T* T;  // [nb, chi, d] (site > 0) or [chi, d] (site 0)
   int64_t t_stride;            // complex elements between samples (0 at site 0)
   const double2* alpha;        // [nb, M]
-  const double* x;             // [dd]
-  const double* W;             // [dd, dd, dd]
+  const R* x;                  // [dd]
+  const R* W;                  // [dd, dd, dd]
   const double* lam;           // Lambda_site [chi]; null at the last site
   const double* u;             // thresholds of this site for the chunk [nb]
   int64_t nb;
@@ -331,7 +346,9 @@ static int run_sampler(bsg_handle_t h, const void* const* Gd, const double* lam,
   using T = typename Cx<R>::T;
   const double* xd;
   const double* Wd;
-  BSG_TRY(displacement_tables(h, dd, &xd, &Wd, st));
+  const float* xf;
+  const float* Wf;
+  BSG_TRY(displacement_tables(h, dd, &xd, &Wd, &xf, &Wf, st));
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   // per-sample bytes: T, next A, alpha
   const size_t per = (size_t)chi * d * sizeof(T) + (SPLIT ? (size_t)chi * 16 : (size_t)chi * sizeof(T)) + (size_t)M * 16;
@@ -402,8 +419,13 @@ static int run_sampler(bsg_handle_t h, const void* const* Gd, const double* lam,
         sa.t_stride = (int64_t)chi * d;
       }
       sa.alpha = alpha;
-      sa.x = xd;
-      sa.W = Wd;
+      if constexpr (std::is_same<R, double>::value) {
+        sa.x = xd;
+        sa.W = Wd;
+      } else {
+        sa.x = xf;
+        sa.W = Wf;
+      }
       sa.lam = i < M - 1 ? lam + (size_t)i * chi : nullptr;
       sa.u = uniforms + (size_t)i * n + b0;
       sa.nb = nb;
@@ -444,7 +466,9 @@ extern "C" int bsg_displacements(bsg_handle_t h, const double* alpha, int64_t co
   if (count == 0) return BSG_OK;
   const double* xd;
   const double* Wd;
-  BSG_TRY(displacement_tables(h, dd, &xd, &Wd, st));
+  const float* xf;
+  const float* Wf;
+  BSG_TRY(displacement_tables(h, dd, &xd, &Wd, &xf, &Wf, st));
   BSG_PROFILED(h, BSG_K_SAMPLE, st, (double)count * dd * dd * dd,
                (displacements_kernel<<<unsigned((count + kSampleWarps - 1) / kSampleWarps), 32 * kSampleWarps, 0,
                                        st>>>(reinterpret_cast<const double2*>(alpha), count, dd, xd, Wd,

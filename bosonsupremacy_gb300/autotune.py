@@ -32,6 +32,7 @@ KNOBS = {
     "fp64_blocks": _lib.TUNE_DP_FP64_BLOCKS,
     "factor_threads": _lib.TUNE_FACTOR_THREADS,
     "gemm_kernel": _lib.TUNE_GEMM_KERNEL,
+    "dp_quantum": _lib.TUNE_DP_QUANTUM,
 }
 
 

@@ -175,6 +175,12 @@ int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* m
   return BSG_OK;
 }
 
+int bsg_profile_build_timeline(bsg_handle_t h, double* ms, int n) {
+  BSG_CHECK_ARG(h && ms, "bsg_profile_build_timeline: null pointer");
+  for (int i = 0; i < n; ++i) ms[i] = i < (int)h->prof.timeline.size() ? h->prof.timeline[i] : -1.0;
+  return BSG_OK;
+}
+
 int bsg_tune_set(bsg_handle_t h, int key, int value) {
   BSG_CHECK_ARG(h, "bsg_tune_set: null handle");
   BSG_CHECK_ARG(key >= 0 && key < BSG_TUNE_COUNT, "bsg_tune_set: unknown key %d", key);
@@ -191,6 +197,8 @@ int bsg_tune_set(bsg_handle_t h, int key, int value) {
     BSG_CHECK_ARG(value == 256 || value == 512 || value == 1024, "bsg_tune_set: factor threads %d", value);
   if (key == BSG_TUNE_DP_SCRATCH_MIB)
     BSG_CHECK_ARG(value >= 64 && value <= 65536, "bsg_tune_set: DP scratch %d MiB", value);
+  if (key == BSG_TUNE_DP_QUANTUM)
+    BSG_CHECK_ARG(value >= 0 && value <= (1 << 20), "bsg_tune_set: DP quantum %d", value);
   h->tune[key] = value;
   return BSG_OK;
 }

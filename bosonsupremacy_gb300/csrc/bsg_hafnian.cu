@@ -250,6 +250,12 @@ struct DPArgs {
   unsigned long long* counter;
   void* scratch;
   int pairs_max, states_max;
+  // yielding launches (quantum > 0): a warp leaves after `quantum` program
+  // transitions, its block after all its warps; blocks take a per-warp table
+  // slot from `slot_flags` [n_slots] and give it back before exiting.
+  int64_t quantum;
+  int* slot_flags;
+  int n_slots;
   // site mode
   const SiteDesc* sites;
   // target / matrices mode
@@ -331,17 +337,44 @@ __device__ __forceinline__ int build_classes(const DPArgs& a, const SiteDesc* sd
   }
 }
 
+// Table slot of a yielding DP block: a free flag of `flags`, probed from the
+// block's SM onwards.  At most n resident blocks of one launch exist at a time
+// (n = resident blocks per SM x SMs), so a free flag exists; the probe is
+// bounded all the same and returns -1 when it gives up.
+__device__ int acquire_dp_slot(int* flags, int n) {
+  unsigned smid, nsmid;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  asm volatile("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
+  const unsigned per_sm = max(1u, (unsigned)n / max(1u, nsmid));
+  int i = int((smid * per_sm) % (unsigned)n);
+  for (int probe = 0; probe < 16 * n; ++probe) {
+    if (*reinterpret_cast<volatile int*>(flags + i) == 0 && atomicCAS(flags + i, 0, 1) == 0) return i;
+    if (++i == n) i = 0;
+  }
+  return -1;
+}
+
 template <class P, int MODE>
 __global__ void __launch_bounds__(256, 6) dp_kernel(DPArgs a) {
   using C = typename P::C;
   using CA = typename P::CA;
   using CF = typename P::CF;
   const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  __shared__ int s_slot;
+  int bslot = blockIdx.x;
+  if (a.quantum > 0) {
+    if (threadIdx.x == 0) s_slot = acquire_dp_slot(a.slot_flags, a.n_slots);
+    __syncthreads();
+    bslot = s_slot;
+    if (bslot < 0) return;  // no slot: this block takes no work (a later launch drains the queue)
+  }
+  const int warp = bslot * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const size_t slice = (size_t)a.pairs_max * 32 * sizeof(CA) + (size_t)a.states_max * 32 * sizeof(CF);
   CA* Ab = reinterpret_cast<CA*>(reinterpret_cast<char*>(a.scratch) + (size_t)warp * slice);
   CF* Fb = reinterpret_cast<CF*>(Ab + (size_t)a.pairs_max * 32);
+  int64_t done = 0;  // program transitions this warp has run
   while (true) {
+    if (a.quantum > 0 && done >= a.quantum) break;
     unsigned long long c = 0;
     if (lane == 0) c = atomicAdd(a.counter, 1ull);
     c = __shfl_sync(0xffffffffu, c, 0);
@@ -384,6 +417,7 @@ __global__ void __launch_bounds__(256, 6) dp_kernel(DPArgs a) {
     for (int s = 1; s < ns; ++s) {
       const uint4 pk = __ldg(a.prog.st_pack + so + s);
       const int off = int(pk.x), cnt = int(pk.y & 0xffffu), ra = int(pk.y >> 16);
+      done += cnt;
       typename P::Acc acc = P::zero();
       for (int t = 0; t < cnt; ++t) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
@@ -427,6 +461,13 @@ __global__ void __launch_bounds__(256, 6) dp_kernel(DPArgs a) {
       double s = fac;
       if (a.den) s /= a.den[item];
       a.out[item] = make_double2(v.x * s, v.y * s);
+    }
+  }
+  if (a.quantum > 0) {
+    __syncthreads();  // every warp of the block is done with the slot's tables
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicExch(a.slot_flags + bslot, 0);
     }
   }
 }
@@ -630,16 +671,37 @@ struct DPLaunch {
   int64_t c0 = 0, c1 = 0;
   int pmax = 1, smax = 1;
   double work = 0.0;
+  double wtrans = 0.0;  // program transitions of all chunks (one warp runs a chunk's program once)
   int blocks = 0;
   size_t per_warp = 0;
+  int64_t quantum = 0;  // > 0: yielding launch with `slots` table slots
+  int slots = 0;
 };
 
+// Yielding launch (quantum > 0) when the tables of every resident block fit
+// the scratch budget: a warp leaves once it has run `quantum` transitions, so
+// the SMs turn over to higher-priority streams within about one quantum.
+// The grid covers the work either way: warps x quantum >= all transitions, or
+// at least one warp per chunk (a warp takes one chunk before it may leave).
+// Otherwise a persistent launch: every warp drains the queue.
 template <class P>
-static void dp_shape(bsg_handle_t h, int blocks_per_sm, DPLaunch& L) {
+static void dp_shape(bsg_handle_t h, int blocks_per_sm, int occupancy, DPLaunch& L) {
   const int threads = 256;
   L.per_warp = (size_t)L.pmax * 32 * sizeof(typename P::CA) + (size_t)L.smax * 32 * sizeof(typename P::CF);
-  int64_t warps = (int64_t)h->num_sms * blocks_per_sm * (threads / 32);
   const size_t budget = (size_t)h->tune[BSG_TUNE_DP_SCRATCH_MIB] << 20;  // per-warp tables of one launch
+  const int64_t q = (int64_t)h->tune[BSG_TUNE_DP_QUANTUM] * 256;
+  const int64_t slots = (int64_t)h->num_sms * occupancy;
+  if (q > 0 && occupancy > 0 && (size_t)slots * (threads / 32) * L.per_warp <= budget) {
+    const int64_t by_work = slots + (int64_t)std::ceil(L.wtrans / double(q * (threads / 32)));
+    const int64_t by_chunks = std::max<int64_t>(1, (L.c1 - L.c0 + (threads / 32) - 1) / (threads / 32));
+    L.quantum = q;
+    L.slots = int(slots);
+    L.blocks = int(std::min<int64_t>(std::min(by_work, by_chunks), int64_t(1) << 30));
+    return;
+  }
+  L.quantum = 0;
+  L.slots = 0;
+  int64_t warps = (int64_t)h->num_sms * blocks_per_sm * (threads / 32);
   while (warps > (threads / 32) * (int64_t)h->num_sms && (size_t)warps * L.per_warp > budget) warps /= 2;
   const int64_t w_use = std::min<int64_t>(warps, std::max<int64_t>(L.c1 - L.c0, 1));
   L.blocks = std::max<int>(1, int((w_use + (threads / 32) - 1) / (threads / 32)));
@@ -670,19 +732,29 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     L.pmax = std::max(L.pmax, ps.k[p] * (ps.k[p] + 1) / 2);
     L.smax = std::max(L.smax, ps.fslots[p]);
     L.work += (double)bk.counts[b] * (double)prog_trans(ps, p);
+    L.wtrans += (double)(bk.chunk_start[b + 1] - bk.chunk_start[b]) * (double)prog_trans(ps, p);
   }
-  dp_shape<P>(h, h->tune[BSG_TUNE_DP_SMALL_BLOCKS], Ls);
-  dp_shape<P>(h, h->tune[BSG_TUNE_DP_BLOCKS_PER_SM], Lb);
-  const bool run_b = Lb.c1 > Lb.c0, run_s = Ls.c1 > Ls.c0 || !run_b;
   // FP64 helper (split precision, site mode): dp_kernel<PrecF64> on the
   // handle's second stream draws chunks from the same counters, so the FP64
   // pipe takes a share of the items while the FP32 pipe runs the split DP.
   const int helper_bps = h->tune[BSG_TUNE_DP_FP64_BLOCKS];
   const bool helper = MODE == MODE_SITE && std::is_same<P, PrecSplit>::value && helper_bps > 0;
   static_assert(sizeof(typename PrecF64::CA) == sizeof(typename P::CA) || !std::is_same<P, PrecSplit>::value, "");
+  BSG_CUDA(cudaFuncSetAttribute(dp_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                h->tune[BSG_TUNE_DP_L1_CARVEOUT]));
+  int occ = 0;
+  if (!helper) BSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dp_kernel<P, MODE>, 256, 0));
+  dp_shape<P>(h, h->tune[BSG_TUNE_DP_SMALL_BLOCKS], occ, Ls);
+  dp_shape<P>(h, h->tune[BSG_TUNE_DP_BLOCKS_PER_SM], occ, Lb);
+  const bool run_b = Lb.c1 > Lb.c0, run_s = Ls.c1 > Ls.c0 || !run_b;
+  auto tables = [](const DPLaunch& L) { return (size_t)(L.quantum > 0 ? L.slots : L.blocks) * 8 * L.per_warp; };
   size_t need = 0;
-  if (run_s) need = std::max(need, (size_t)Ls.blocks * 8 * Ls.per_warp);
-  if (run_b) need = std::max(need, (size_t)Lb.blocks * 8 * Lb.per_warp);
+  if (run_s) need = std::max(need, tables(Ls));
+  if (run_b) need = std::max(need, tables(Lb));
+  // slot flags of the yielding launches (all free again when a launch ends)
+  const size_t flags_off = (need + 255) & ~size_t(255);
+  const int n_flags = std::max(run_s ? Ls.slots : 0, run_b ? Lb.slots : 0);
+  if (n_flags > 0) need = flags_off + (size_t)n_flags * 4;
   DPLaunch Hs = Ls, Hb = Lb;  // helper shapes (same slices, fewer blocks)
   size_t helper_off = 0;
   if (helper) {
@@ -695,8 +767,8 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     need = helper_off + hneed;
   }
   BSG_TRY(scratch.ensure(need));
-  BSG_CUDA(cudaFuncSetAttribute(dp_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                h->tune[BSG_TUNE_DP_L1_CARVEOUT]));
+  int* flags = n_flags > 0 ? reinterpret_cast<int*>(reinterpret_cast<char*>(scratch.ptr) + flags_off) : nullptr;
+  if (flags) BSG_CUDA(cudaMemsetAsync(flags, 0, (size_t)n_flags * 4, st));
   a.scratch = scratch.ptr;
   unsigned long long* ctr = a.counter;
   const DPLaunch* Ls_or_b[2] = {run_b ? &Lb : nullptr, run_s ? &Ls : nullptr};
@@ -719,6 +791,9 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     a.n_chunks = L->c1 - L->c0;
     a.counter = ctr + i;
     a.scratch = scratch.ptr;
+    a.quantum = L->quantum;
+    a.slot_flags = flags;
+    a.n_slots = L->slots;
     if (helper) {
       dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a);
       BSG_CUDA(cudaGetLastError());
@@ -728,6 +803,14 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
       BSG_CUDA(cudaGetLastError());
     } else {
       BSG_PROFILED(h, BSG_K_DP, st, L->work, (dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a)));
+      if (L->quantum > 0) {
+        // drain: a persistent launch over the table slots finishes any chunk
+        // left behind by a block that found no slot (normally none: it exits at once)
+        DPArgs da = a;
+        da.quantum = 0;
+        dp_kernel<P, MODE><<<std::min(L->slots, h->num_sms), 256, 0, st>>>(da);
+        BSG_CUDA(cudaGetLastError());
+      }
     }
   }
   if (helper) {
@@ -1298,10 +1381,12 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // Site i reads cuts i - 1 and i, so each group's Sigma, planning and DP can
   // start as soon as its own cuts are done: the edge groups' DP (most of the
   // hafnian work sits at both ends of the chain) runs on the SMs the slow
-  // middle cuts leave idle.  The edge groups' DP runs on low-priority
-  // streams, so Williamson / Sigma blocks that become ready later take the
-  // SMs those persistent DP blocks have not claimed yet.  No kernel waits on
-  // another; streams are ordered by events only.
+  // middle cuts leave idle.  Every group's DP runs on a low-priority stream
+  // in yielding launches (dp_shape): DP blocks leave their SM after a bounded
+  // amount of work, so the Williamson, thermal and Sigma kernels of the groups
+  // still in flight take SMs within about one quantum instead of waiting for
+  // a whole DP launch.  No kernel waits on another; streams are ordered by
+  // events only.
   int T1 = 0, T2 = nc;
   if (nc >= 6) {
     T1 = nc / 3;
@@ -1318,7 +1403,7 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
     BSG_TRY(h->ensure_aux());
     groups.push_back(Group{T2, nc, T2 + 1, M, h->grp[0], h->dp_lo[0], 2});
     groups.push_back(Group{0, T1, 0, T1, h->grp[1], h->dp_lo[1], 1});
-    groups.push_back(Group{T1, T2, T1, T2 + 1, h->grp[2], h->grp[2], 0});
+    groups.push_back(Group{T1, T2, T1, T2 + 1, h->grp[2], h->dp_lo[2], 0});
   } else {
     groups.push_back(Group{0, nc, 0, M, st, st, 0});
   }
@@ -1424,8 +1509,17 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // host (one event per group), then its Sigma; the middle group's labels and
   // Sigma also read the edge groups' boundary cuts
   const int ng = int(groups.size());
-  // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[4..8] = final joins
+  // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[4..9] = final joins,
+  // h->ev[10..12] = Gammas final (pinned copies), h->ev[13..14] = copy-stream joins
   cudaEvent_t ev_keys[3] = {}, ev_done[3] = {};
+  // profiling timeline: per group Williamson done, keys on host, Sigma done, DP done
+  cudaEvent_t tl0 = nullptr, tl[3][4] = {};
+  if (h->prof.on) {
+    BSG_CUDA(cudaEventCreate(&tl0));
+    BSG_CUDA(cudaEventRecord(tl0, st));
+    for (auto& row : tl)
+      for (auto& e : row) BSG_CUDA(cudaEventCreate(&e));
+  }
   if (ng > 1) {
     BSG_CUDA(cudaEventRecord(h->aux_fork, st));
     for (int g = 0; g < ng; ++g) BSG_CUDA(cudaStreamWaitEvent(groups[g].stream, h->aux_fork, 0));
@@ -1436,6 +1530,7 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
     cudaStream_t s2 = G.stream;
     const int nc_g = G.c1 - G.c0;
     BSG_TRY(cut_launch_williamson(h, cuts, G.c0, G.c1, s2));
+    if (tl0) BSG_CUDA(cudaEventRecord(tl[g][0], s2));
     BSG_TRY(cut_launch_thermal(h, cuts, G.c0, G.c1, s2));
     BSG_TRY(cut_queue_status(cuts, G.c0, G.c1, hcut, s2));
     if (nc_g > 0) {
@@ -1454,6 +1549,7 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
     BSG_CUDA(cudaMemcpyAsync(herr + g, d_err + 4 * g, 4, cudaMemcpyDeviceToHost, s2));
     BSG_CUDA(cudaEventCreateWithFlags(&ev_keys[g], cudaEventDisableTiming));
     BSG_CUDA(cudaEventRecord(ev_keys[g], s2));
+    if (tl0) BSG_CUDA(cudaEventRecord(tl[g][1], s2));
     if (g == ng - 1 && ng > 1) {
       // the middle sites read the boundary cuts T1 - 1 (left) and T2 (right):
       // their S (Sigma), Lambda and label tables (DP)
@@ -1466,6 +1562,7 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
         BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[i]), (int64_t)(2 * Mr) * (2 * Mr), precision,
                              wb + o_sigc[i], s2));
     }
+    if (tl0) BSG_CUDA(cudaEventRecord(tl[g][2], s2));
   }
 
   // 4. per group, as its keys arrive: plan its sites and launch their DP
@@ -1539,13 +1636,14 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
     }
     if (!in.empty() && rc == BSG_OK)
       rc = run_sites(h, in, d, chi, precision, out_dtype, h->slot[G.slot], G.dp_stream);
+    if (tl0 && rc == BSG_OK) cudaEventRecord(tl[g][3], G.dp_stream);
     h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
     if (gammas_pinned && rc == BSG_OK) {
       // this group's Gammas are final once its DP stream gets here
       cudaStream_t cp = h->copy[g & 1];
       const size_t gb = (size_t)chi * chi * d * (out_dtype == BSG_OUT_C128 ? 16 : 8);
-      cudaError_t e = cudaEventRecord(h->ev[9 + g], G.dp_stream);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[9 + g], 0);
+      cudaError_t e = cudaEventRecord(h->ev[10 + g], G.dp_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[10 + g], 0);
       for (int i = G.s0; i < G.s1 && e == cudaSuccess; ++i)
         e = cudaMemcpyAsync(gammas_pinned[i], gammas_host[i], gb, cudaMemcpyDeviceToHost, cp);
       if (e != cudaSuccess) {
@@ -1595,6 +1693,17 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   BSG_CUDA(cudaStreamSynchronize(st));
   h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_fin), 0.0);
   BSG_TRY(cut_read_phases(h, cuts, st));
+  if (tl0) {
+    h->prof.timeline.assign(12, -1.0);
+    for (int g = 0; g < ng; ++g)
+      for (int k = 0; k < 4; ++k) {
+        float ms = -1.f;
+        if (cudaEventElapsedTime(&ms, tl0, tl[g][k]) == cudaSuccess) h->prof.timeline[(size_t)g * 4 + k] = ms;
+      }
+    cudaEventDestroy(tl0);
+    for (auto& row : tl)
+      for (auto& e : row) cudaEventDestroy(e);
+  }
   for (int i = 0; i < M; ++i)
     if (sst[i]) {
       set_error("bsg_build_mps: site %d: the Gaussian unitary's A block is singular", i);

@@ -118,6 +118,7 @@ struct Profiler {
   int64_t launches[BSG_K_COUNT] = {0};
   double work[BSG_K_COUNT] = {0};
   std::vector<double> cut_phases;  // ms per (cut, Williamson phase) of the last profiled cut launch
+  std::vector<double> timeline;    // last profiled whole-MPS build: ms per (group, milestone)
   cudaEvent_t get();
   // begin/end bracket one launch on `st`
   int begin(int cls, cudaStream_t st, cudaEvent_t* ev);
@@ -227,8 +228,8 @@ struct bsg_handle_s {
   bsg::Profiler prof;
   // side streams for concurrent launches (created on first use) and events:
   // aux_stream (FP64 helper), grp[3] high-priority streams of the build
-  // groups, dp_lo[2] low-priority streams of the edge groups' DP
-  cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[2] = {}, copy[2] = {};
+  // groups, dp_lo[3] low-priority streams of the groups' DP
+  cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[3] = {}, copy[2] = {};
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
   cudaEvent_t ev[16] = {};
   int ensure_aux();
@@ -238,7 +239,7 @@ struct bsg_handle_s {
     bsg::DevBuf plan, items, scratch;
     bsg::HostBuf stage;
   } slot[3];
-  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1};
+  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1, 2};
 };
 
 // Brackets a kernel launch with profiler events when profiling is on.

@@ -247,6 +247,13 @@ int bsg_gemm_tf32x3(bsg_handle_t h, const float* A, const float* B, float* C, in
  * FP64 Jacobi sweep counts (not times).  Pass ms = NULL to query the sizes. */
 int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* ms);
 
+/* Milestones of the last bsg_build_mps made while profiling was enabled, in
+ * ms after the call's first launch: ms[4 g + k] for build group g (0 right
+ * edge, 1 left edge, 2 middle; a small M runs one group) and k = 0 Williamson
+ * done, 1 label keys queued to the host, 2 Sigma done, 3 DP done; -1 where
+ * absent.  n: entries to fill (12 covers every group). */
+int bsg_profile_build_timeline(bsg_handle_t h, double* ms, int n);
+
 /* ---- tuning knobs (no reference counterpart) ------------------------------
  * Launch parameters an autotuner may change per handle (bosonsupremacy_gb300
  * /autotune.py).  Values outside the documented range return BSG_ERR_INVALID. */
@@ -262,7 +269,10 @@ int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* m
                                         (default 1024; fewer leave registers for DP blocks on the same SM) */
 #define BSG_TUNE_GEMM_KERNEL 7       /* 3xTF32 tcgen05 GEMM: 0 one 128x128 tile per CTA, 1 persistent 128x256 tiles
                                         with a double TMEM accumulator (default 1) */
-#define BSG_TUNE_COUNT 8
+#define BSG_TUNE_DP_QUANTUM 8        /* hafnian DP: a warp leaves its launch after this many x 256 program
+                                        transitions, so kernels on higher-priority streams get SMs; 0 keeps
+                                        every DP block until the queue is empty (default 2) */
+#define BSG_TUNE_COUNT 9
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

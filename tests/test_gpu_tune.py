@@ -1,6 +1,8 @@
-"""DP launch knobs: range checks, and the launch split (small-table programs
-in their own launch) leaves every Gamma bit-identical -- each item's DP runs
-the same arithmetic whichever launch and scratch slice it lands in."""
+"""DP launch knobs: range checks, and neither the launch split (small-table
+programs in their own launch) nor yielding launches (warps leave after a
+work quantum, blocks take table slots from a pool) change any Gamma bit --
+each item's DP runs the same arithmetic whichever launch, warp and scratch
+slice it lands in."""
 import numpy as np
 import pytest
 
@@ -16,7 +18,8 @@ def test_knob_ranges(cuda):
     try:
         for key, bad in ((_lib.TUNE_DP_BLOCKS_PER_SM, 0), (_lib.TUNE_DP_BLOCKS_PER_SM, 9),
                          (_lib.TUNE_DP_L1_CARVEOUT, 101), (_lib.TUNE_DP_SMALL_ENTRIES, -1),
-                         (_lib.TUNE_DP_SMALL_BLOCKS, 0), (_lib.TUNE_DP_SCRATCH_MIB, 32), (99, 1)):
+                         (_lib.TUNE_DP_SMALL_BLOCKS, 0), (_lib.TUNE_DP_SCRATCH_MIB, 32),
+                         (_lib.TUNE_DP_QUANTUM, -1), (99, 1)):
             assert lib.bsg_tune_set(h.h, key, bad) == -1, (key, bad)
         autotune.set_knobs(small_entries=128)
         assert autotune.get_knobs()["small_entries"] == 128
@@ -36,9 +39,10 @@ def test_launch_split_bit_identical(cuda, golden, prec):
     saved = autotune.get_knobs()
     outs = []
     try:
-        for knobs in ({"small_entries": 0, "blocks_per_sm": 4},
-                      {"small_entries": 16, "small_blocks": 2, "scratch_mib": 64},
-                      {"small_entries": 4096, "small_blocks": 8}):
+        for knobs in ({"small_entries": 0, "blocks_per_sm": 4, "dp_quantum": 0},
+                      {"small_entries": 16, "small_blocks": 2, "scratch_mib": 64, "dp_quantum": 64},
+                      {"small_entries": 4096, "small_blocks": 8, "dp_quantum": 1},
+                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 1 << 20}):
             autotune.set_knobs(**knobs)
             mps = build_mps(t["sq_cov"], d, chi, precision=prec, out_dtype=torch.complex128)
             outs.append([g.cpu().numpy() for g in mps.Gammas])

@@ -58,6 +58,7 @@ SIGNATURES = {
     "bsg_sample": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _L, _I, _P, _P]),
     "bsg_profile_cut_phases": (_I, [_P, C.POINTER(_I), C.POINTER(_I), _P]),
     "bsg_profile_build_timeline": (_I, [_P, _P, _I]),
+    "bsg_profile_dp_buckets": (_I, [_P, _P, _I, C.POINTER(_I), _P, _I]),
     "bsg_displacements": (_I, [_P, _P, _L, _I, _P, _P]),
 }
 

@@ -150,6 +150,21 @@ int bsg_profile_reset(bsg_handle_t h) {
     h->prof.launches[i] = 0;
     h->prof.work[i] = 0;
   }
+  h->prof.dp_rows.clear();
+  h->prof.dp_state_hist.clear();
+  return BSG_OK;
+}
+
+int bsg_profile_dp_buckets(bsg_handle_t h, double* rows, int max_rows, int* n_rows, double* state_hist,
+                           int hist_len) {
+  BSG_CHECK_ARG(h && n_rows, "bsg_profile_dp_buckets: null pointer");
+  const int n = int(h->prof.dp_rows.size() / 6);
+  *n_rows = n;
+  if (rows)
+    for (int i = 0; i < std::min(n, max_rows) * 6; ++i) rows[i] = h->prof.dp_rows[i];
+  if (state_hist)
+    for (int i = 0; i < hist_len; ++i)
+      state_hist[i] = i < (int)h->prof.dp_state_hist.size() ? h->prof.dp_state_hist[i] : 0.0;
   return BSG_OK;
 }
 

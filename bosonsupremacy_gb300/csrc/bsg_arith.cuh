@@ -18,6 +18,7 @@ struct PrecF64 {
   }
   // scaled by 1/r (r small positive integer)
   static __device__ __forceinline__ C finish(const Acc& acc, int r, const double* inv_d, const float2*) {
+    if (r == 1) return acc;
     double s = inv_d[r];
     return make_double2(acc.x * s, acc.y * s);
   }
@@ -38,6 +39,7 @@ struct PrecF32 {
     acc.y = fmaf(a.x, f.y, fmaf(a.y, f.x, acc.y));
   }
   static __device__ __forceinline__ C finish(const Acc& acc, int r, const double*, const float2* inv_f) {
+    if (r == 1) return acc;
     float s = inv_f[r].x;
     return make_float2(acc.x * s, acc.y * s);
   }
@@ -96,10 +98,11 @@ struct PrecSplit {
     renorm(p, e, h, l);
   }
   static __device__ __forceinline__ C finish(const Acc& acc, int r, const double*, const float2* inv_f) {
-    float2 iv = inv_f[r];
     float rh, rl, ih, il;
     renorm(acc.rs, acc.rt, rh, rl);
     renorm(acc.is, acc.it, ih, il);
+    if (r == 1) return make_float4(rh, rl, ih, il);  // r: warp-uniform
+    const float2 iv = inv_f[r];
     C out;
     mul(rh, rl, iv.x, iv.y, out.x, out.y);
     mul(ih, il, iv.x, iv.y, out.z, out.w);

@@ -355,7 +355,7 @@ __device__ int acquire_dp_slot(int* flags, int n) {
 }
 
 template <class P, int MODE>
-__global__ void __launch_bounds__(256, 6) dp_kernel(DPArgs a) {
+__global__ void __launch_bounds__(256, 5) dp_kernel(DPArgs a) {
   using C = typename P::C;
   using CA = typename P::CA;
   using CF = typename P::CF;
@@ -419,7 +419,20 @@ __global__ void __launch_bounds__(256, 6) dp_kernel(DPArgs a) {
       const int off = int(pk.x), cnt = int(pk.y & 0xffffu), ra = int(pk.y >> 16);
       done += cnt;
       typename P::Acc acc = P::zero();
-      for (int t = 0; t < cnt; ++t) {
+      // two transitions per step: both pairs of table loads are in flight
+      // before the first multiply-add (states average ~2.4 transitions)
+      int t = 0;
+      for (; t + 1 < cnt; t += 2) {
+        const uint32_t w0 = __ldg(a.prog.trans + off + t);
+        const uint32_t w1 = __ldg(a.prog.trans + off + t + 1);
+        const CA av0 = Ab[(size_t)(w0 & 0xfffu) * 32 + lane];
+        const CF fv0 = Fb[(size_t)(w0 >> 12) * 32 + lane];
+        const CA av1 = Ab[(size_t)(w1 & 0xfffu) * 32 + lane];
+        const CF fv1 = Fb[(size_t)(w1 >> 12) * 32 + lane];
+        P::mac(acc, av0, fv0);
+        P::mac(acc, av1, fv1);
+      }
+      if (t < cnt) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
         const CA av = Ab[(size_t)(w & 0xfffu) * 32 + lane];
         const CF fv = Fb[(size_t)(w >> 12) * 32 + lane];
@@ -733,6 +746,16 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     L.smax = std::max(L.smax, ps.fslots[p]);
     L.work += (double)bk.counts[b] * (double)prog_trans(ps, p);
     L.wtrans += (double)(bk.chunk_start[b + 1] - bk.chunk_start[b]) * (double)prog_trans(ps, p);
+    if (h->prof.on) {
+      const double ch = double(bk.chunk_start[b + 1] - bk.chunk_start[b]);
+      const int s0 = ps.state_off[p], ns = ps.nstates[p];
+      for (double v : {b < first_small ? 0.0 : 1.0, ch, double(ps.k[p]), double(ps.fslots[p]), double(ns),
+                       double(prog_trans(ps, p))})
+        h->prof.dp_rows.push_back(v);
+      auto& hist = h->prof.dp_state_hist;
+      if (hist.size() < 65) hist.resize(65, 0.0);
+      for (int q = 1; q < ns; ++q) hist[std::min(ps.st_trans_cnt[s0 + q], 64)] += ch;
+    }
   }
   // FP64 helper (split precision, site mode): dp_kernel<PrecF64> on the
   // handle's second stream draws chunks from the same counters, so the FP64

@@ -119,6 +119,10 @@ struct Profiler {
   double work[BSG_K_COUNT] = {0};
   std::vector<double> cut_phases;  // ms per (cut, Williamson phase) of the last profiled cut launch
   std::vector<double> timeline;    // last profiled whole-MPS build: ms per (group, milestone)
+  // DP launches since the last reset: one row per bucket (launch, chunks, classes,
+  // F ring slots, states, transitions) and chunk-weighted states by transition count
+  std::vector<double> dp_rows;
+  std::vector<double> dp_state_hist;
   cudaEvent_t get();
   // begin/end bracket one launch on `st`
   int begin(int cls, cudaStream_t st, cudaEvent_t* ev);

@@ -254,6 +254,15 @@ int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* m
  * absent.  n: entries to fill (12 covers every group). */
 int bsg_profile_build_timeline(bsg_handle_t h, double* ms, int n);
 
+/* Hafnian DP launches since the last bsg_profile_reset while profiling was
+ * enabled.  *n_rows = buckets seen; rows[6 r + f] (r < max_rows) = launch
+ * (0 large-table, 1 small-table programs), 32-item chunks, classes k, F ring
+ * slots, DP states, transitions of the bucket's program.  state_hist[c]
+ * (c < hist_len) = chunk-weighted count of states with c transitions (the
+ * last entry collects larger counts).  rows / state_hist may be null. */
+int bsg_profile_dp_buckets(bsg_handle_t h, double* rows, int max_rows, int* n_rows, double* state_hist,
+                           int hist_len);
+
 /* ---- tuning knobs (no reference counterpart) ------------------------------
  * Launch parameters an autotuner may change per handle (bosonsupremacy_gb300
  * /autotune.py).  Values outside the documented range return BSG_ERR_INVALID. */

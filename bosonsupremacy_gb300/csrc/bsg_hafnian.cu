@@ -1533,7 +1533,8 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // Sigma also read the edge groups' boundary cuts
   const int ng = int(groups.size());
   // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[4..9] = final joins,
-  // h->ev[10..12] = Gammas final (pinned copies), h->ev[13..14] = copy-stream joins
+  // h->ev[10..12] = Gammas final (pinned copies), h->ev[13..14] = copy-stream joins,
+  // h->ev[16..17] = first site parts of a partitioned group final
   cudaEvent_t ev_keys[3] = {}, ev_done[3] = {};
   // profiling timeline: per group Williamson done, keys on host, Sigma done, DP done
   cudaEvent_t tl0 = nullptr, tl[3][4] = {};
@@ -1657,17 +1658,46 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
         rc = BSG_ERR_CUDA;
       }
     }
-    if (!in.empty() && rc == BSG_OK)
-      rc = run_sites(h, in, d, chi, precision, out_dtype, h->slot[G.slot], G.dp_stream);
+    // Host outputs: the left group finishes last, so its DP runs in three site
+    // parts (own plan / item / scratch slots) and each part's Gammas download
+    // while the next part computes; everything else runs as one launch set.
+    const size_t gb = (size_t)chi * chi * d * (out_dtype == BSG_OUT_C128 ? 16 : 8);
+    int copied = G.s0;  // sites of this group whose download is queued
+    if (!in.empty() && rc == BSG_OK) {
+      const int n_in = int(in.size());
+      const int parts = (gammas_pinned && ng > 1 && g == 1) ? std::min(3, n_in) : 1;
+      const int per = (n_in + parts - 1) / parts;
+      for (int q = 0; q < parts && rc == BSG_OK; ++q) {
+        const int i0 = q * per, i1 = std::min(n_in, i0 + per);
+        if (i0 >= i1) break;
+        if (parts == 1) {
+          rc = run_sites(h, in, d, chi, precision, out_dtype, h->slot[G.slot], G.dp_stream);
+          break;
+        }
+        const std::vector<SiteInput> sub(in.begin() + i0, in.begin() + i1);
+        rc = run_sites(h, sub, d, chi, precision, out_dtype, h->slot[q == 0 ? G.slot : 2 + q], G.dp_stream);
+        if (rc == BSG_OK && q + 1 < parts) {
+          cudaStream_t cp = h->copy[g & 1];
+          cudaError_t e = cudaEventRecord(h->ev[16 + q], G.dp_stream);
+          if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[16 + q], 0);
+          for (int i = G.s0 + i0; i < G.s0 + i1 && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(gammas_pinned[i], gammas_host[i], gb, cudaMemcpyDeviceToHost, cp);
+          if (e != cudaSuccess) {
+            set_error("bsg_build_mps: %s", cudaGetErrorString(e));
+            rc = BSG_ERR_CUDA;
+          }
+          copied = G.s0 + i1;
+        }
+      }
+    }
     if (tl0 && rc == BSG_OK) cudaEventRecord(tl[g][3], G.dp_stream);
     h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
     if (gammas_pinned && rc == BSG_OK) {
-      // this group's Gammas are final once its DP stream gets here
+      // the rest of this group's Gammas are final once its DP stream gets here
       cudaStream_t cp = h->copy[g & 1];
-      const size_t gb = (size_t)chi * chi * d * (out_dtype == BSG_OUT_C128 ? 16 : 8);
       cudaError_t e = cudaEventRecord(h->ev[10 + g], G.dp_stream);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[10 + g], 0);
-      for (int i = G.s0; i < G.s1 && e == cudaSuccess; ++i)
+      for (int i = copied; i < G.s1 && e == cudaSuccess; ++i)
         e = cudaMemcpyAsync(gammas_pinned[i], gammas_host[i], gb, cudaMemcpyDeviceToHost, cp);
       if (e != cudaSuccess) {
         set_error("bsg_build_mps: %s", cudaGetErrorString(e));

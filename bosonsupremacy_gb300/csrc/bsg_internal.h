@@ -235,14 +235,16 @@ struct bsg_handle_s {
   // groups, dp_lo[3] low-priority streams of the groups' DP
   cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[3] = {}, copy[2] = {};
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
-  cudaEvent_t ev[16] = {};
+  cudaEvent_t ev[20] = {};
   int ensure_aux();
   // per-group buffers of the site DP (plan tables, item slots, per-warp
-  // scratch, pinned plan staging); slot 0 serves the single-site calls
+  // scratch, pinned plan staging); slot 0 serves the single-site calls,
+  // slots 3 and 4 the later site parts of a build group whose Gammas are
+  // downloaded part by part
   struct SiteSlot {
     bsg::DevBuf plan, items, scratch;
     bsg::HostBuf stage;
-  } slot[3];
+  } slot[5];
   int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1, 2};
 };
 

@@ -173,31 +173,38 @@ struct SitePlanDev {
   int ngl, ngr, kl, kr, d;
 };
 
-__global__ void site_scatter_kernel(SitePlanDev p) {
-  const int64_t total = (int64_t)p.d * p.kr * p.kl;
+// One launch per set of sites (blockIdx.y = site).  A thread takes one (right
+// row, left row) pair in key-sorted order and scatters its even-order items
+// over j, so the row lookups happen once per pair and consecutive lanes
+// usually share a bucket (one aggregated atomic per bucket and j).
+__global__ void site_scatter_kernel(const SitePlanDev* __restrict__ plans) {
+  const SitePlanDev p = plans[blockIdx.y];
+  const int64_t total = (int64_t)p.kr * p.kl;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
-    int64_t i = base + threadIdx.x;
-    int bucket = -1;
-    int32_t item = 0;
-    if (i < total) {
-      int bs = int(i % p.kl);
-      int64_t rest = i / p.kl;
-      int as = int(rest % p.kr);
-      int j = int(rest / p.kr);
-      bucket = p.bucket_of[((size_t)j * p.ngl + p.grp_l[bs]) * p.ngr + p.grp_r[as]];
-      item = (p.perm_r[as] << 20) | (p.perm_l[bs] << 8) | j;
+    const int64_t i = base + threadIdx.x;
+    const bool in = i < total;
+    int gl = 0, gr = 0;
+    int32_t ab = 0;
+    if (in) {
+      const int bs = int(i % p.kl), as = int(i / p.kl);
+      gl = p.grp_l[bs];
+      gr = p.grp_r[as];
+      ab = (p.perm_r[as] << 20) | (p.perm_l[bs] << 8);
     }
-    unsigned active = __ballot_sync(0xffffffffu, bucket >= 0);
-    if (bucket >= 0) {
-      unsigned peers = __match_any_sync(active, bucket);
-      int leader = __ffs(peers) - 1;
-      int rank = __popc(peers & ((1u << lane) - 1));
-      int slot0 = 0;
-      if (lane == leader) slot0 = atomicAdd(&p.cursor[bucket], __popc(peers));
-      slot0 = __shfl_sync(peers, slot0, leader);
-      p.items[p.bucket_off[bucket] + slot0 + rank] = item;
+    for (int j = 0; j < p.d; ++j) {
+      const int bucket = in ? p.bucket_of[((size_t)j * p.ngl + gl) * p.ngr + gr] : -1;
+      const unsigned active = __ballot_sync(0xffffffffu, bucket >= 0);
+      if (bucket >= 0) {
+        const unsigned peers = __match_any_sync(active, bucket);
+        const int leader = __ffs(peers) - 1;
+        const int rank = __popc(peers & ((1u << lane) - 1));
+        int slot0 = 0;
+        if (lane == leader) slot0 = atomicAdd(&p.cursor[bucket], __popc(peers));
+        slot0 = __shfl_sync(peers, slot0, leader);
+        p.items[p.bucket_off[bucket] + slot0 + rank] = ab | j;
+      }
     }
   }
 }
@@ -354,8 +361,13 @@ __device__ int acquire_dp_slot(int* flags, int n) {
   return -1;
 }
 
+// DP block size; the launch bound keeps 40 warps resident per SM (128- and
+// 64-thread blocks measured slower)
+constexpr int kDPThreads = 256;
+constexpr int kDPWarps = kDPThreads / 32;
+
 template <class P, int MODE>
-__global__ void __launch_bounds__(256, 5) dp_kernel(DPArgs a) {
+__global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArgs a) {
   using C = typename P::C;
   using CA = typename P::CA;
   using CF = typename P::CF;
@@ -699,7 +711,7 @@ struct DPLaunch {
 // Otherwise a persistent launch: every warp drains the queue.
 template <class P>
 static void dp_shape(bsg_handle_t h, int blocks_per_sm, int occupancy, DPLaunch& L) {
-  const int threads = 256;
+  const int threads = kDPThreads;
   L.per_warp = (size_t)L.pmax * 32 * sizeof(typename P::CA) + (size_t)L.smax * 32 * sizeof(typename P::CF);
   const size_t budget = (size_t)h->tune[BSG_TUNE_DP_SCRATCH_MIB] << 20;  // per-warp tables of one launch
   const int64_t q = (int64_t)h->tune[BSG_TUNE_DP_QUANTUM] * 256;
@@ -766,11 +778,11 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
   BSG_CUDA(cudaFuncSetAttribute(dp_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 h->tune[BSG_TUNE_DP_L1_CARVEOUT]));
   int occ = 0;
-  if (!helper) BSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dp_kernel<P, MODE>, 256, 0));
+  if (!helper) BSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dp_kernel<P, MODE>, kDPThreads, 0));
   dp_shape<P>(h, h->tune[BSG_TUNE_DP_SMALL_BLOCKS], occ, Ls);
   dp_shape<P>(h, h->tune[BSG_TUNE_DP_BLOCKS_PER_SM], occ, Lb);
   const bool run_b = Lb.c1 > Lb.c0, run_s = Ls.c1 > Ls.c0 || !run_b;
-  auto tables = [](const DPLaunch& L) { return (size_t)(L.quantum > 0 ? L.slots : L.blocks) * 8 * L.per_warp; };
+  auto tables = [](const DPLaunch& L) { return (size_t)(L.quantum > 0 ? L.slots : L.blocks) * kDPWarps * L.per_warp; };
   size_t need = 0;
   if (run_s) need = std::max(need, tables(Ls));
   if (run_b) need = std::max(need, tables(Lb));
@@ -785,8 +797,8 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     Hb.blocks = std::min(Hb.blocks, h->num_sms * helper_bps);
     helper_off = (need + 255) & ~size_t(255);
     size_t hneed = 0;
-    if (run_s) hneed = std::max(hneed, (size_t)Hs.blocks * 8 * Hs.per_warp);
-    if (run_b) hneed = std::max(hneed, (size_t)Hb.blocks * 8 * Hb.per_warp);
+    if (run_s) hneed = std::max(hneed, (size_t)Hs.blocks * kDPWarps * Hs.per_warp);
+    if (run_b) hneed = std::max(hneed, (size_t)Hb.blocks * kDPWarps * Hb.per_warp);
     need = helper_off + hneed;
   }
   BSG_TRY(scratch.ensure(need));
@@ -818,20 +830,20 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
     a.slot_flags = flags;
     a.n_slots = L->slots;
     if (helper) {
-      dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a);
+      dp_kernel<P, MODE><<<L->blocks, kDPThreads, 0, st>>>(a);
       BSG_CUDA(cudaGetLastError());
       DPArgs ha = a;
       ha.scratch = reinterpret_cast<char*>(scratch.ptr) + helper_off;
-      dp_kernel<PrecF64, MODE><<<H_or_b[i]->blocks, 256, 0, aux>>>(ha);
+      dp_kernel<PrecF64, MODE><<<H_or_b[i]->blocks, kDPThreads, 0, aux>>>(ha);
       BSG_CUDA(cudaGetLastError());
     } else {
-      BSG_PROFILED(h, BSG_K_DP, st, L->work, (dp_kernel<P, MODE><<<L->blocks, 256, 0, st>>>(a)));
+      BSG_PROFILED(h, BSG_K_DP, st, L->work, (dp_kernel<P, MODE><<<L->blocks, kDPThreads, 0, st>>>(a)));
       if (L->quantum > 0) {
         // drain: a persistent launch over the table slots finishes any chunk
         // left behind by a block that found no slot (normally none: it exits at once)
         DPArgs da = a;
         da.quantum = 0;
-        dp_kernel<P, MODE><<<std::min(L->slots, h->num_sms), 256, 0, st>>>(da);
+        dp_kernel<P, MODE><<<std::min(L->slots, h->num_sms), kDPThreads, 0, st>>>(da);
         BSG_CUDA(cudaGetLastError());
       }
     }
@@ -1114,7 +1126,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   }
   const size_t o_boff = carve((size_t)nb * 4 + 4), o_cur = carve((size_t)nb * 4 + 4);
   const size_t o_bch = carve((size_t)nb * 4 + 4), o_bpr = carve((size_t)nb * 4 + 4),
-               o_bsi = carve((size_t)nb * 4 + 4), o_ctr = carve(16);
+               o_bsi = carve((size_t)nb * 4 + 4), o_ctr = carve(16), o_sp = carve(sizeof(SitePlanDev) * ns);
   const size_t plan_bytes = off;
   BSG_TRY(slot.plan.ensure(plan_bytes));
   BSG_TRY(slot.stage.ensure(plan_bytes));
@@ -1168,6 +1180,19 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     std::memcpy(hp + o_bsi, bk.sites.data(), (size_t)nb * 4);
   }
   std::memset(hp + o_ctr, 0, 16);
+  BSG_TRY(slot.items.ensure(std::max<size_t>((size_t)bk.slots * 4, 4)));
+  int32_t* d_items = reinterpret_cast<int32_t*>(slot.items.ptr);
+  SitePlanDev* hsp = reinterpret_cast<SitePlanDev*>(hp + o_sp);
+  int64_t max_pairs = 1;
+  for (int s = 0; s < ns; ++s) {
+    const SitePlanHost& p = plans[s];
+    hsp[s] = SitePlanDev{reinterpret_cast<int32_t*>(dp + o_pl[s]), reinterpret_cast<int32_t*>(dp + o_gl[s]),
+                         reinterpret_cast<int32_t*>(dp + o_pr[s]), reinterpret_cast<int32_t*>(dp + o_gr[s]),
+                         reinterpret_cast<int32_t*>(dp + o_bo[s]), reinterpret_cast<int32_t*>(dp + o_boff),
+                         reinterpret_cast<int32_t*>(dp + o_cur),   d_items,
+                         p.ngl, p.ngr, p.KL, p.KR, p.d};
+    max_pairs = std::max<int64_t>(max_pairs, (int64_t)p.KL * p.KR);
+  }
   BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
   BSG_PROFILED(h, BSG_K_PREP, st, (double)ns * max_kl,
                (left_scale_kernel<<<dim3((max_kl + 127) / 128, ns), 128, 0, st>>>(
@@ -1175,19 +1200,15 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   const size_t esz = out_c128 ? 16 : 8;
   for (int s = 0; s < ns; ++s) BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, (size_t)chi * chi * d * esz, st));
   if (bk.slots == 0) return BSG_OK;
-  BSG_TRY(slot.items.ensure((size_t)bk.slots * 4));
-  int32_t* d_items = reinterpret_cast<int32_t*>(slot.items.ptr);
   BSG_CUDA(cudaMemsetAsync(d_items, 0xff, (size_t)bk.slots * 4, st));
-  for (int s = 0; s < ns; ++s) {
-    const SitePlanHost& p = plans[s];
-    SitePlanDev sp{reinterpret_cast<int32_t*>(dp + o_pl[s]), reinterpret_cast<int32_t*>(dp + o_gl[s]),
-                   reinterpret_cast<int32_t*>(dp + o_pr[s]), reinterpret_cast<int32_t*>(dp + o_gr[s]),
-                   reinterpret_cast<int32_t*>(dp + o_bo[s]), reinterpret_cast<int32_t*>(dp + o_boff),
-                   reinterpret_cast<int32_t*>(dp + o_cur),   d_items,
-                   p.ngl, p.ngr, p.KL, p.KR, p.d};
-    const int64_t total = (int64_t)p.d * p.KL * p.KR;
-    const int sblocks = int(std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)h->num_sms * 8)));
-    BSG_PROFILED(h, BSG_K_PREP, st, (double)total, (site_scatter_kernel<<<sblocks, 256, 0, st>>>(sp)));
+  {
+    // all sites in one launch: blocks per site so the launch covers ~8 blocks per SM
+    const int64_t per_site = std::max<int64_t>(1, ((int64_t)h->num_sms * 8 + ns - 1) / ns);
+    const int bx = int(std::max<int64_t>(1, std::min<int64_t>((max_pairs + 255) / 256, per_site)));
+    double pairs = 0.0;
+    for (int s = 0; s < ns; ++s) pairs += (double)plans[s].KL * plans[s].KR * plans[s].d;
+    BSG_PROFILED(h, BSG_K_PREP, st, pairs,
+                 (site_scatter_kernel<<<dim3(bx, ns), 256, 0, st>>>(reinterpret_cast<const SitePlanDev*>(dp + o_sp))));
   }
   DPArgs a{};
   a.prog = prog_dev(ps);

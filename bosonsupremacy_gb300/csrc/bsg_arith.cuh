@@ -16,6 +16,11 @@ struct PrecF64 {
     acc.x = fma(a.x, f.x, fma(-a.y, f.y, acc.x));
     acc.y = fma(a.x, f.y, fma(a.y, f.x, acc.y));
   }
+  // acc = a f (the first term of a sum)
+  static __device__ __forceinline__ void mac_init(Acc& acc, const C& a, const C& f) {
+    acc = zero();
+    mac(acc, a, f);
+  }
   // scaled by 1/r (r small positive integer)
   static __device__ __forceinline__ C finish(const Acc& acc, int r, const double* inv_d, const float2*) {
     if (r == 1) return acc;
@@ -37,6 +42,10 @@ struct PrecF32 {
   static __device__ __forceinline__ void mac(Acc& acc, const C& a, const C& f) {
     acc.x = fmaf(a.x, f.x, fmaf(-a.y, f.y, acc.x));
     acc.y = fmaf(a.x, f.y, fmaf(a.y, f.x, acc.y));
+  }
+  static __device__ __forceinline__ void mac_init(Acc& acc, const C& a, const C& f) {
+    acc = zero();
+    mac(acc, a, f);
   }
   static __device__ __forceinline__ C finish(const Acc& acc, int r, const double*, const float2* inv_f) {
     if (r == 1) return acc;
@@ -73,6 +82,17 @@ __device__ __forceinline__ void split_mac1(float& s, float& t, float xh, float x
   t += err + e;
 }
 
+// s + t = (xh + xl) * (yh + yl): the first term of a sum, where the two-sum
+// with a zero accumulator would be the identity
+__device__ __forceinline__ void split_mul1(float& s, float& t, float xh, float xl, float yh, float yl) {
+  const float p = xh * yh;
+  float e = fmaf(xh, yh, -p);
+  e = fmaf(xh, yl, e);
+  e = fmaf(xl, yh, e);
+  s = p;
+  t = e;
+}
+
 struct PrecSplit {
   using C = float4;  // (re_hi, re_lo, im_hi, im_lo)
   using CA = C;
@@ -84,6 +104,13 @@ struct PrecSplit {
     split_mac1(acc.rs, acc.rt, a.x, a.y, f.x, f.y);
     split_mac1(acc.rs, acc.rt, -a.z, -a.w, f.z, f.w);
     split_mac1(acc.is, acc.it, a.x, a.y, f.z, f.w);
+    split_mac1(acc.is, acc.it, a.z, a.w, f.x, f.y);
+  }
+  // acc = a f: the first product of each part starts the pair directly
+  static __device__ __forceinline__ void mac_init(Acc& acc, const C& a, const C& f) {
+    split_mul1(acc.rs, acc.rt, a.x, a.y, f.x, f.y);
+    split_mac1(acc.rs, acc.rt, -a.z, -a.w, f.z, f.w);
+    split_mul1(acc.is, acc.it, a.x, a.y, f.z, f.w);
     split_mac1(acc.is, acc.it, a.z, a.w, f.x, f.y);
   }
   static __device__ __forceinline__ void renorm(float s, float t, float& h, float& l) {

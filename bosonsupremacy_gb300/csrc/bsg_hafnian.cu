@@ -432,8 +432,24 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
       done += cnt;
       typename P::Acc acc = P::zero();
       // two transitions per step: both pairs of table loads are in flight
-      // before the first multiply-add (states average ~2.4 transitions)
+      // before the first multiply-add (states average ~2.4 transitions); the
+      // first product starts the sum (mac_init) instead of adding to zero
       int t = 0;
+      if (cnt >= 2) {
+        const uint32_t w0 = __ldg(a.prog.trans + off);
+        const uint32_t w1 = __ldg(a.prog.trans + off + 1);
+        const CA av0 = Ab[(size_t)(w0 & 0xfffu) * 32 + lane];
+        const CF fv0 = Fb[(size_t)(w0 >> 12) * 32 + lane];
+        const CA av1 = Ab[(size_t)(w1 & 0xfffu) * 32 + lane];
+        const CF fv1 = Fb[(size_t)(w1 >> 12) * 32 + lane];
+        P::mac_init(acc, av0, fv0);
+        P::mac(acc, av1, fv1);
+        t = 2;
+      } else if (cnt == 1) {
+        const uint32_t w = __ldg(a.prog.trans + off);
+        P::mac_init(acc, Ab[(size_t)(w & 0xfffu) * 32 + lane], Fb[(size_t)(w >> 12) * 32 + lane]);
+        t = 1;
+      }
       for (; t + 1 < cnt; t += 2) {
         const uint32_t w0 = __ldg(a.prog.trans + off + t);
         const uint32_t w1 = __ldg(a.prog.trans + off + t + 1);

@@ -1,0 +1,77 @@
+"""Size-independent properties of the whole-MPS build at the headline size
+(M=144 modes, d=8, chi=1024 -- the reference's largest single-GPU workload,
+9.7 GB of Gamma), where no CPU oracle finishes:
+
+* the split-precision build agrees with the plain FP64 build: identical
+  Schmidt values and cut labels (both run the same FP64 factorisations), and
+  every Gamma entry within a few FP32 ulps (the two DP arithmetics differ by
+  ~2^-44 relative before the complex64 rounding);
+* the host-output build (per-group downloads, the left group's DP in three
+  site parts) lands exactly the device build's Gammas and Lambdas;
+* every Gamma is finite and not identically zero, every cut keeps at least
+  one row, and the Schmidt weights of each cut are positive and sorted.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+WORKLOAD = "M144_d8_chi1024"
+
+
+@pytest.fixture(scope="module")
+def full_builds(cuda):
+    import torch
+    from bosonsupremacy_gb300 import synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps
+    cfg = synthetic.NAMED[WORKLOAD]
+    _, sq = synthetic.lossy_covariances(cfg)
+    split = build_mps(sq, cfg.d, cfg.chi, precision="split")
+    fp64 = build_mps(sq, cfg.d, cfg.chi, precision="fp64")
+    yield cfg, sq, split, fp64
+    del split, fp64
+    torch.cuda.empty_cache()
+
+
+def test_split_matches_fp64_at_full_size(full_builds):
+    import torch
+    cfg, _, split, fp64 = full_builds
+    assert np.array_equal(split.kept, fp64.kept)
+    assert torch.equal(split.Lambdas, fp64.Lambdas)
+    assert torch.equal(split.num, fp64.num)
+    worst = 0.0
+    for i, (a, b) in enumerate(zip(split.Gammas, fp64.Gammas)):
+        scale = b.abs().max().item()
+        assert scale > 0.0, i
+        assert torch.isfinite(torch.view_as_real(a)).all(), i
+        # elementwise: a few complex64 ulps of the entry, or of 1e-6 of the site's largest entry
+        tol = 4.0 * 2.0 ** -23 * torch.maximum(b.abs(), torch.full_like(b.abs(), 1e-6 * scale))
+        err = (a - b).abs()
+        assert bool((err <= tol).all()), (i, (err / tol).max().item())
+        worst = max(worst, (err.max() / scale).item())
+    assert worst <= 1e-6
+
+
+def test_cut_structure_at_full_size(full_builds):
+    cfg, _, split, _ = full_builds
+    res = split.res.cpu().numpy()
+    for c in range(cfg.M - 1):
+        k = int(split.kept[c])
+        assert 1 <= k <= cfg.chi, c
+        w = res[c, :k]
+        assert (w > 0).all() and (np.diff(w) <= 0).all(), c
+        assert w.sum() <= 1.0 + 1e-9, c
+
+
+def test_host_output_build_matches_device_build_at_full_size(full_builds):
+    import torch
+    from bosonsupremacy_gb300.pipeline import build_mps_host
+    cfg, sq, split, _ = full_builds
+    M, d, chi = cfg.M, cfg.d, cfg.chi
+    sqh = torch.as_tensor(sq).pin_memory()
+    gh = [torch.empty(chi, chi, d, dtype=torch.complex64, pin_memory=True) for _ in range(M)]
+    lh = torch.empty(M - 1, chi, dtype=torch.float64, pin_memory=True)
+    build_mps_host(sqh, d, chi, gh, lh, precision="split")
+    assert torch.equal(split.Lambdas.cpu(), lh)
+    for i in range(M):
+        assert torch.equal(split.Gammas[i], gh[i].to(split.Gammas[i].device, non_blocking=False)), i

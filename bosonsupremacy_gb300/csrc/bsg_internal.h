@@ -239,12 +239,12 @@ struct bsg_handle_s {
   int ensure_aux();
   // per-group buffers of the site DP (plan tables, item slots, per-warp
   // scratch, pinned plan staging); slot 0 serves the single-site calls,
-  // slots 3 and 4 the later site parts of a build group whose Gammas are
+  // slots 3 to 5 the later site parts of a build group whose Gammas are
   // downloaded part by part
   struct SiteSlot {
     bsg::DevBuf plan, items, scratch;
     bsg::HostBuf stage;
-  } slot[5];
+  } slot[6];
   int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1, 2};
 };
 

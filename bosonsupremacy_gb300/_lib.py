@@ -46,6 +46,8 @@ SIGNATURES = {
     "bsg_build_site": (_I, [_P, _I, _P, _I, _P, _I, _I, _P, _P, _I, _I, _P, _I, _I, _I, _I, _P, _P]),
     "bsg_cut_spectra": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _P, _P, _P, _P, _P]),
     "bsg_pattern_amplitudes": (_I, [_P, _P, _P, _I, _I, _I, _P, _L, _I, _P, _P]),
+    "bsg_contract_patterns": (_I, [_P, _P, _P, _I, _I, _I, _P, _L, _I, _P, _P]),
+    "bsg_cut_spectrum": (_I, [_P, _P, _I, _I, _I, _I, _D, _L, _P, _P, _P, _P, _P]),
     "bsg_build_mps": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_build_mps_to_host": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_profile_enable": (_I, [_P, _I]),

@@ -428,3 +428,9 @@ extern "C" int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas,
   return run_contraction<float>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, precision == BSG_PREC_SPLIT,
                                 nullptr, st);
 }
+
+extern "C" int bsg_contract_patterns(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi,
+                                     int d, const int32_t* patterns, int64_t P, int precision, double* amp,
+                                     bsg_stream_t stream) {
+  return bsg_pattern_amplitudes(h, Gammas, Lambdas, M, chi, d, patterns, P, precision, amp, stream);
+}

@@ -981,3 +981,13 @@ extern "C" int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int 
   BSG_TRY(cut_read_phases(h, a, st));
   return cut_check_status(h, a, 0, n_cuts, status.data());
 }
+
+extern "C" int bsg_cut_spectrum(bsg_handle_t h, const double* sq_cov, int M, int L, int d, int chi, double err_tol,
+                                int64_t max_dim, double* res, int8_t* num, double* S, int32_t* kept,
+                                bsg_stream_t stream) {
+  BSG_CHECK_ARG(max_dim >= chi,
+                "bsg_cut_spectrum: max_dim=%lld is below chi=%d (the per-step top-chi selection reproduces the "
+                "reference's candidate cap only when max_dim >= chi)",
+                (long long)max_dim, chi);
+  return bsg_cut_spectra(h, sq_cov, M, L, 1, d, chi, err_tol, res, num, S, kept, stream);
+}

@@ -160,6 +160,16 @@ int bsg_build_site(bsg_handle_t h, int kind, const double* Sigma, int M_r, const
 int bsg_cut_spectra(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                     double* res, int8_t* num, double* S, int32_t* kept, bsg_stream_t stream);
 
+/* One cut L, the per-cut form of kron_cpu.py's loop body (kron_cpu.py:147-153,
+ * get_cumsum_kron(nbar, d, max_dim, err_tol) at kron_cpu.py:92-127): res
+ * float64 [chi], num int8 [chi, M-1], S float64 [2(M-1), 2(M-1)] (leading
+ * 2(M-L) block), *kept.  max_dim is the reference's per-step candidate cap
+ * (1e5 there); keeping the top chi products per step selects the same final
+ * set whenever max_dim >= chi, so a smaller max_dim is rejected.  Same as
+ * bsg_cut_spectra with L0 = L, n_cuts = 1. */
+int bsg_cut_spectrum(bsg_handle_t h, const double* sq_cov, int M, int L, int d, int chi, double err_tol,
+                     int64_t max_dim, double* res, int8_t* num, double* S, int32_t* kept, bsg_stream_t stream);
+
 /* ---- the whole MPS ---------------------------------------------------------
  * kron_cpu.py (all M-1 cuts, kron_cpu.py:147-153) followed by MPS_cpu.py
  * (all M sites, MPS_cpu.py:384-525) in one call, device-resident:
@@ -201,6 +211,12 @@ int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, in
  * host). */
 int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                            const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
+
+/* The same contraction under the name the reference-side bindings use for
+ * the pattern-probability consumer (sampling_cpu.py:75-81): identical
+ * arguments and results to bsg_pattern_amplitudes. */
+int bsg_contract_patterns(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
+                          const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
 
 /* ---- sampling ------------------------------------------------------------
  * Photon-number samples of the lossy state from the MPS, replacing

@@ -47,3 +47,26 @@ def test_contraction_of_gpu_mps_medium_sample(cuda):
     Lam = mps.Lambdas.cpu().numpy()
     ref = R.pattern_amplitudes(G, list(Lam), pats)
     assert np.abs(amp - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_contract_patterns_alias(cuda, golden):
+    """bsg_contract_patterns returns exactly bsg_pattern_amplitudes' result."""
+    import ctypes
+    import torch
+    from bosonsupremacy_gb300 import _lib, ops
+    t = golden("tiny_M8.npz")
+    M, d = int(t["M"]), int(t["d"])
+    G = [torch.as_tensor(t[f"Gamma_{i}"]).to(torch.complex128).cuda().contiguous() for i in range(M)]
+    chi = G[0].shape[0]
+    L = np.stack([t[f"Lambda_{c}"] for c in range(M - 1)]).astype(np.float64)
+    want = ops.pattern_amplitudes(G, L, t["patterns"], precision="fp64")
+    Lt = torch.as_tensor(L).cuda().contiguous()
+    pats = torch.as_tensor(np.asarray(t["patterns"], np.int32)).cuda().contiguous()
+    out = torch.empty(pats.shape[0], dtype=torch.complex128, device="cuda")
+    ptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in G])
+    h = _lib.Handle.get(0)
+    _lib.check(_lib.load().bsg_contract_patterns(h.h, ptrs, Lt.data_ptr(), M, chi, d, pats.data_ptr(),
+                                                 pats.shape[0], _lib.PREC_FP64, out.data_ptr(), _lib.stream_ptr()),
+               "bsg_contract_patterns")
+    torch.cuda.synchronize()
+    assert torch.equal(out, want.to(out.device))

@@ -92,3 +92,36 @@ def test_cut_spectra_full_size_medium(cuda):
         untied[:-1] &= ~gap
         k = M - 1 - c
         assert np.array_equal(num[c, : kept[c], :k].sum(1)[untied], ref_num.reshape(len(ref_res), -1).sum(1)[untied])
+
+
+def test_single_cut_entry_point(cuda, golden):
+    """bsg_cut_spectrum (one cut, the reference's max_dim argument) equals
+    the slab of that cut from bsg_cut_spectra, bit for bit; a max_dim below
+    chi is rejected."""
+    import torch
+    from bosonsupremacy_gb300 import _lib, ops
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    res_all, num_all, S_all, kept_all = ops.cut_spectra(t["sq_cov"], d, chi)
+    sq = torch.as_tensor(t["sq_cov"], dtype=torch.float64).cuda()
+    h = _lib.Handle.get(0)
+    lib = _lib.load()
+    for L in (1, M // 2, M - 1):
+        res = torch.empty(chi, dtype=torch.float64, device="cuda")
+        num = torch.empty(chi, M - 1, dtype=torch.int8, device="cuda")
+        S = torch.empty(2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device="cuda")
+        kept = torch.empty(1, dtype=torch.int32, device="cuda")
+        _lib.check(lib.bsg_cut_spectrum(h.h, sq.data_ptr(), M, L, d, chi, 1e-12, 100000, res.data_ptr(),
+                                        num.data_ptr(), S.data_ptr(), kept.data_ptr(), _lib.stream_ptr()),
+                   "bsg_cut_spectrum")
+        c = L - 1
+        k = int(kept_all[c])
+        assert int(kept.item()) == k
+        assert torch.equal(res[:k], res_all[c, :k])
+        assert torch.equal(num[:k], num_all[c, :k])
+        n = 2 * (M - L)
+        assert torch.equal(S[:n, :n], S_all[c, :n, :n])
+    with pytest.raises(_lib.BSGError, match="max_dim"):
+        _lib.check(lib.bsg_cut_spectrum(h.h, sq.data_ptr(), M, 1, d, chi, 1e-12, chi - 1, res.data_ptr(),
+                                        num.data_ptr(), S.data_ptr(), kept.data_ptr(), _lib.stream_ptr()),
+                   "bsg_cut_spectrum")

@@ -6,10 +6,13 @@
   Schmidt values and cut labels (both run the same FP64 factorisations), and
   every Gamma entry within a few FP32 ulps (the two DP arithmetics differ by
   ~2^-44 relative before the complex64 rounding);
-* the host-output build (per-group downloads, the left group's DP in three
+* the host-output build (per-group downloads, the left group's DP in four
   site parts) lands exactly the device build's Gammas and Lambdas;
 * every Gamma is finite and not identically zero, every cut keeps at least
   one row, and the Schmidt weights of each cut are positive and sorted.
+
+The largest banded workload (M=216, d=10, chi=2048) and instances of the
+64-instance uneven workload get the same kind of checks.
 """
 import numpy as np
 import pytest
@@ -75,3 +78,51 @@ def test_host_output_build_matches_device_build_at_full_size(full_builds):
     assert torch.equal(split.Lambdas.cpu(), lh)
     for i in range(M):
         assert torch.equal(split.Gammas[i], gh[i].to(split.Gammas[i].device, non_blocking=False)), i
+
+
+def test_largest_banded_workload_properties(cuda):
+    """M=216, d=10, chi=2048, banded interferometer (72 GB of Gamma): the build
+    completes, every Gamma is finite and non-zero, every cut keeps between 1
+    and chi rows with positive, sorted weights summing to <= 1, and Lambda is
+    the square root of the kept weights above the site tolerance."""
+    import torch
+    from bosonsupremacy_gb300 import synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps
+    cfg = synthetic.LARGEST
+    _, sq = synthetic.lossy_covariances(cfg)
+    m = build_mps(sq, cfg.d, cfg.chi, precision="split")
+    try:
+        for i, g in enumerate(m.Gammas):
+            assert torch.isfinite(torch.view_as_real(g)).all(), i
+            assert g.abs().max().item() > 0.0, i
+        res = m.res.cpu().numpy()
+        lam = m.Lambdas.cpu().numpy()
+        for c in range(cfg.M - 1):
+            k = int(m.kept[c])
+            assert 1 <= k <= cfg.chi, c
+            w = res[c, :k]
+            assert (w > 0).all() and (np.diff(w) <= 0).all() and w.sum() <= 1.0 + 1e-9, c
+            big = w > 1e-10
+            assert np.allclose(lam[c, :k][big], np.sqrt(w[big]), rtol=1e-12, atol=0.0), c
+    finally:
+        del m
+        torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("k", [0, 17, 42, 63])
+def test_uneven_batch_instances_split_vs_fp64(cuda, k):
+    """Instances of the 64-instance uneven workload (M 8-48, d 4-8, chi
+    32-256): split and FP64 builds agree in Lambda exactly and in every Gamma
+    entry to a few complex64 ulps."""
+    import torch
+    from bosonsupremacy_gb300 import synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps
+    cfg = synthetic.batch_configs(64)[k]
+    _, sq = synthetic.lossy_covariances(cfg)
+    a = build_mps(sq, cfg.d, cfg.chi, precision="split")
+    b = build_mps(sq, cfg.d, cfg.chi, precision="fp64")
+    assert torch.equal(a.Lambdas, b.Lambdas)
+    for i, (x, y) in enumerate(zip(a.Gammas, b.Gammas)):
+        scale = y.abs().max().item()
+        tol = 4.0 * 2.0 ** -23 * torch.maximum(y.abs(), torch.full_like(y.abs(), 1e-6 * scale))
+        assert bool(((x - y).abs() <= tol).all()), (cfg.name, i)

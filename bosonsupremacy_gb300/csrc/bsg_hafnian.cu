@@ -216,9 +216,6 @@ struct ProgDev {
   const int32_t* k;
   const int32_t* nstates;
   const int32_t* state_off;
-  const int32_t* st_trans_off;
-  const int32_t* st_trans_cnt;
-  const int32_t* st_ra;
   const uint32_t* trans;
   const uint4* st_pack;  // {first transition, count | r_a << 16, F slot, 0} per state
 };
@@ -702,8 +699,7 @@ static void group_rows(const uint64_t* key, int rows, std::vector<int32_t>& perm
 }
 
 static ProgDev prog_dev(const bsg::ProgramSet& ps) {
-  return ProgDev{ps.d_k,  ps.d_nstates, ps.d_state_off, ps.d_st_trans_off, ps.d_st_trans_cnt,
-                 ps.d_st_ra, ps.d_trans, ps.d_st_pack};
+  return ProgDev{ps.d_k, ps.d_nstates, ps.d_state_off, ps.d_trans, ps.d_st_pack};
 }
 
 // Launch shape for chunks [c0, c1) whose programs need at most (pmax, smax)

@@ -55,6 +55,7 @@ struct ProgramSet {
   std::vector<int32_t> nstates;        // states per program (>= 1)
   std::vector<int32_t> state_off;      // first state (global index) per program
   std::vector<int32_t> mult;           // [prog * BSG_MAX_CLASSES + c] ascending multiplicities
+  // host-only per-state tables (planning, statistics); the device reads st_pack
   std::vector<int32_t> st_trans_off;   // per global state: first transition
   std::vector<int32_t> st_trans_cnt;   // per global state: number of transitions
   std::vector<int32_t> st_ra;          // per global state: r_a (0 for the empty state)
@@ -66,9 +67,6 @@ struct ProgramSet {
   int32_t* d_k = nullptr;
   int32_t* d_nstates = nullptr;
   int32_t* d_state_off = nullptr;
-  int32_t* d_st_trans_off = nullptr;
-  int32_t* d_st_trans_cnt = nullptr;
-  int32_t* d_st_ra = nullptr;
   uint32_t* d_trans = nullptr;
   uint4* d_st_pack = nullptr;
   size_t dev_states_cap = 0, dev_trans_cap = 0, dev_prog_cap = 0;

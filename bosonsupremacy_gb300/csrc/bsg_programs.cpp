@@ -170,12 +170,8 @@ int programs_upload(ProgramSet& ps, cudaStream_t stream) {
   BSG_TRY(upload(ps.d_state_off, pc3, ps.dev_prog_n, ps.state_off, stream));
   ps.dev_prog_cap = pc;
   ps.dev_prog_n = ps.k.size();
-  size_t sc = ps.dev_states_cap, sc2 = ps.dev_states_cap, sc3 = ps.dev_states_cap;
-  BSG_TRY(upload(ps.d_st_trans_off, sc, ps.dev_states_n, ps.st_trans_off, stream));
-  BSG_TRY(upload(ps.d_st_trans_cnt, sc2, ps.dev_states_n, ps.st_trans_cnt, stream));
-  BSG_TRY(upload(ps.d_st_ra, sc3, ps.dev_states_n, ps.st_ra, stream));
-  size_t sc4 = ps.dev_states_cap;
-  BSG_TRY(upload(ps.d_st_pack, sc4, ps.dev_states_n, ps.st_pack, stream));
+  size_t sc = ps.dev_states_cap;
+  BSG_TRY(upload(ps.d_st_pack, sc, ps.dev_states_n, ps.st_pack, stream));
   ps.dev_states_cap = sc;
   ps.dev_states_n = ps.st_trans_off.size();
   BSG_TRY(upload(ps.d_trans, ps.dev_trans_cap, ps.dev_trans_n, ps.trans, stream));
@@ -190,9 +186,6 @@ void programs_free(ProgramSet& ps) {
   cudaFree(ps.d_k);
   cudaFree(ps.d_nstates);
   cudaFree(ps.d_state_off);
-  cudaFree(ps.d_st_trans_off);
-  cudaFree(ps.d_st_trans_cnt);
-  cudaFree(ps.d_st_ra);
   cudaFree(ps.d_st_pack);
   cudaFree(ps.d_trans);
   ps = ProgramSet();

@@ -4,11 +4,12 @@
 // Every work item is one hafnian of Sigma restricted to a target index list
 // with repeats.  Items are bucketed by the multiplicity partition of their
 // target; a warp takes 32 items of one bucket and runs that bucket's
-// partition program (bsg_programs.cpp) in lock-step, one item per lane, with
-// the per-lane A (class pair) table and F (DP state) table in a per-warp
-// scratch slice laid out [entry][lane] so every access is one coalesced line.
-// Buckets of all sites of an MPS share one persistent launch with an atomic
-// work counter; each 32-slot chunk carries its site and program.
+// partition program (bsg_programs.cpp) in lock-step, one item per lane.  The
+// class-pair values are read from the site's Sigma at each transition; the
+// DP states (F) live in a per-warp ring slice laid out [entry][lane] so every
+// access is one coalesced line.  The buckets of a set of sites share
+// yielding launches with an atomic work counter; each 32-slot chunk finds its
+// bucket (site and program) in a per-bucket prefix sum.
 #include <algorithm>
 #include <chrono>
 #include <atomic>
@@ -26,6 +27,7 @@ namespace bsg {
 
 constexpr int kMaxInv = 64;
 __constant__ double c_inv_d[kMaxInv];
+__constant__ uint16_t c_pair_ab[BSG_MAX_CLASSES * (BSG_MAX_CLASSES + 1) / 2];  // pair index -> a | b << 8
 __constant__ float2 c_inv_f[kMaxInv];
 __constant__ double c_sqrt_fact[kMaxInv];  // sqrt(n!)
 __constant__ double c_fact[kMaxInv];       // n! (as double)
@@ -50,6 +52,10 @@ static int ensure_tables() {
   BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact2, sf2, sizeof(sf2)));
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_d, inv_d, sizeof(inv_d)));
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_f, inv_f, sizeof(inv_f)));
+  uint16_t pab[BSG_MAX_CLASSES * (BSG_MAX_CLASSES + 1) / 2];
+  for (int b = 0; b < BSG_MAX_CLASSES; ++b)
+    for (int a = 0; a <= b; ++a) pab[pair_index(a, b)] = uint16_t(a | (b << 8));
+  BSG_CUDA(cudaMemcpyToSymbol(c_pair_ab, pab, sizeof(pab)));
   BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact, sf, sizeof(sf)));
   BSG_CUDA(cudaMemcpyToSymbol(c_fact, f, sizeof(f)));
   dev_done = dev;
@@ -253,7 +259,7 @@ struct DPArgs {
   int64_t n_chunks;    // chunks of this launch
   unsigned long long* counter;
   void* scratch;
-  int pairs_max, states_max;
+  int states_max;  // F ring entries of a warp's slice
   // yielding launches (quantum > 0): a warp leaves after `quantum` program
   // transitions, its block after all its warps; blocks take a per-warp table
   // slot from `slot_flags` [n_slots] and give it back before exiting.
@@ -378,9 +384,8 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
     if (bslot < 0) return;  // no slot: this block takes no work (a later launch drains the queue)
   }
   const int warp = bslot * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const size_t slice = (size_t)a.pairs_max * 32 * sizeof(CA) + (size_t)a.states_max * 32 * sizeof(CF);
-  CA* Ab = reinterpret_cast<CA*>(reinterpret_cast<char*>(a.scratch) + (size_t)warp * slice);
-  CF* Fb = reinterpret_cast<CF*>(Ab + (size_t)a.pairs_max * 32);
+  const size_t slice = (size_t)a.states_max * 32 * sizeof(CF);
+  CF* Fb = reinterpret_cast<CF*>(reinterpret_cast<char*>(a.scratch) + (size_t)warp * slice);
   int64_t done = 0;  // program transitions this warp has run
   while (true) {
     if (a.quantum > 0 && done >= a.quantum) break;
@@ -415,11 +420,13 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
     } else {
       for (int q = 0; q < kp; ++q) cls[q] = 0;
     }
-    // gather the class-pair table (diagonal included)
-    for (int bq = 0; bq < kp; ++bq) {
-      const int64_t rowb = sb + (int64_t)cls[bq] * n_len;
-      for (int aq = 0; aq <= bq; ++aq) Ab[(size_t)pair_index(aq, bq) * 32 + lane] = sig[rowb + cls[aq]];
-    }
+    // class-pair values are read straight from Sigma at each transition
+    // (Sigma is shared by every item of the site and stays in L1 / L2; a
+    // per-item copy would double the warp's table footprint)
+    auto A_at = [&](uint32_t w) -> CA {
+      const int ab = c_pair_ab[w & 0xfffu];
+      return sig[sb + (int64_t)cls[ab >> 8] * n_len + cls[ab & 0xff]];
+    };
     // run the program (the final coefficient stays in a register)
     Fb[lane] = P::one();
     CF fin = P::one();
@@ -435,31 +442,31 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
       if (cnt >= 2) {
         const uint32_t w0 = __ldg(a.prog.trans + off);
         const uint32_t w1 = __ldg(a.prog.trans + off + 1);
-        const CA av0 = Ab[(size_t)(w0 & 0xfffu) * 32 + lane];
+        const CA av0 = A_at(w0);
         const CF fv0 = Fb[(size_t)(w0 >> 12) * 32 + lane];
-        const CA av1 = Ab[(size_t)(w1 & 0xfffu) * 32 + lane];
+        const CA av1 = A_at(w1);
         const CF fv1 = Fb[(size_t)(w1 >> 12) * 32 + lane];
         P::mac_init(acc, av0, fv0);
         P::mac(acc, av1, fv1);
         t = 2;
       } else if (cnt == 1) {
         const uint32_t w = __ldg(a.prog.trans + off);
-        P::mac_init(acc, Ab[(size_t)(w & 0xfffu) * 32 + lane], Fb[(size_t)(w >> 12) * 32 + lane]);
+        P::mac_init(acc, A_at(w), Fb[(size_t)(w >> 12) * 32 + lane]);
         t = 1;
       }
       for (; t + 1 < cnt; t += 2) {
         const uint32_t w0 = __ldg(a.prog.trans + off + t);
         const uint32_t w1 = __ldg(a.prog.trans + off + t + 1);
-        const CA av0 = Ab[(size_t)(w0 & 0xfffu) * 32 + lane];
+        const CA av0 = A_at(w0);
         const CF fv0 = Fb[(size_t)(w0 >> 12) * 32 + lane];
-        const CA av1 = Ab[(size_t)(w1 & 0xfffu) * 32 + lane];
+        const CA av1 = A_at(w1);
         const CF fv1 = Fb[(size_t)(w1 >> 12) * 32 + lane];
         P::mac(acc, av0, fv0);
         P::mac(acc, av1, fv1);
       }
       if (t < cnt) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
-        const CA av = Ab[(size_t)(w & 0xfffu) * 32 + lane];
+        const CA av = A_at(w);
         const CF fv = Fb[(size_t)(w >> 12) * 32 + lane];
         P::mac(acc, av, fv);
       }
@@ -608,7 +615,7 @@ struct Buckets {
   std::vector<int32_t> offsets;  // bucket -> first slot (multiple of 32)
   std::vector<int32_t> chunk_start;  // bucket -> first chunk (nb + 1 entries)
   int64_t slots = 0;
-  int pairs_max = 1, states_max = 1;
+  int states_max = 1;
   double work = 0.0;             // complex multiply-adds of all items
 };
 
@@ -658,8 +665,6 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
     const int64_t ch = (out.counts[b] + 31) / 32;
     off += ch * 32;
     const int p = out.progs[b];
-    const int kk = ps.k[p];
-    out.pairs_max = std::max(out.pairs_max, kk * (kk + 1) / 2);
     out.states_max = std::max(out.states_max, ps.fslots[p]);
     out.work += (double)out.counts[b] * (double)prog_trans(ps, p);
     if (off > INT32_MAX) {
@@ -702,11 +707,11 @@ static ProgDev prog_dev(const bsg::ProgramSet& ps) {
   return ProgDev{ps.d_k, ps.d_nstates, ps.d_state_off, ps.d_trans, ps.d_st_pack};
 }
 
-// Launch shape for chunks [c0, c1) whose programs need at most (pmax, smax)
+// Launch shape for chunks [c0, c1) whose programs need at most smax F entries
 // table entries per warp.
 struct DPLaunch {
   int64_t c0 = 0, c1 = 0;
-  int pmax = 1, smax = 1;
+  int smax = 1;
   double work = 0.0;
   double wtrans = 0.0;  // program transitions of all chunks (one warp runs a chunk's program once)
   int blocks = 0;
@@ -724,7 +729,7 @@ struct DPLaunch {
 template <class P>
 static void dp_shape(bsg_handle_t h, int blocks_per_sm, int occupancy, DPLaunch& L) {
   const int threads = kDPThreads;
-  L.per_warp = (size_t)L.pmax * 32 * sizeof(typename P::CA) + (size_t)L.smax * 32 * sizeof(typename P::CF);
+  L.per_warp = (size_t)L.smax * 32 * sizeof(typename P::CF);
   const size_t budget = (size_t)h->tune[BSG_TUNE_DP_SCRATCH_MIB] << 20;  // per-warp tables of one launch
   const int64_t q = (int64_t)h->tune[BSG_TUNE_DP_QUANTUM] * 256;
   const int64_t slots = (int64_t)h->num_sms * occupancy;
@@ -766,7 +771,6 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
   for (int b = 0; b < nb; ++b) {
     const int p = bk.progs[b];
     DPLaunch& L = b < first_small ? Lb : Ls;
-    L.pmax = std::max(L.pmax, ps.k[p] * (ps.k[p] + 1) / 2);
     L.smax = std::max(L.smax, ps.fslots[p]);
     L.work += (double)bk.counts[b] * (double)prog_trans(ps, p);
     L.wtrans += (double)(bk.chunk_start[b + 1] - bk.chunk_start[b]) * (double)prog_trans(ps, p);
@@ -832,7 +836,6 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
   for (int i = 0; i < 2; ++i) {
     const DPLaunch* L = Ls_or_b[i];
     if (!L) continue;
-    a.pairs_max = L->pmax;
     a.states_max = L->smax;
     a.chunk_base = L->c0;
     a.n_chunks = L->c1 - L->c0;

@@ -213,7 +213,7 @@ struct bsg_handle_s {
   int num_sms = 0;
   bsg::ProgramSet programs;
   // scratch reused across calls
-  bsg::DevBuf warp_scratch;   // per-warp A/F tables of the DP kernel
+  bsg::DevBuf warp_scratch;   // per-warp F rings of the DP kernel
   bsg::DevBuf items;          // bucketed item ids
   bsg::DevBuf plan;           // per-call plan tables
   bsg::DevBuf keys;           // per-row / per-item partition keys

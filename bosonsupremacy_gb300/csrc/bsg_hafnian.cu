@@ -27,7 +27,6 @@ namespace bsg {
 
 constexpr int kMaxInv = 64;
 __constant__ double c_inv_d[kMaxInv];
-__constant__ uint16_t c_pair_ab[BSG_MAX_CLASSES * (BSG_MAX_CLASSES + 1) / 2];  // pair index -> a | b << 8
 __constant__ float2 c_inv_f[kMaxInv];
 __constant__ double c_sqrt_fact[kMaxInv];  // sqrt(n!)
 __constant__ double c_fact[kMaxInv];       // n! (as double)
@@ -52,10 +51,6 @@ static int ensure_tables() {
   BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact2, sf2, sizeof(sf2)));
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_d, inv_d, sizeof(inv_d)));
   BSG_CUDA(cudaMemcpyToSymbol(c_inv_f, inv_f, sizeof(inv_f)));
-  uint16_t pab[BSG_MAX_CLASSES * (BSG_MAX_CLASSES + 1) / 2];
-  for (int b = 0; b < BSG_MAX_CLASSES; ++b)
-    for (int a = 0; a <= b; ++a) pab[pair_index(a, b)] = uint16_t(a | (b << 8));
-  BSG_CUDA(cudaMemcpyToSymbol(c_pair_ab, pab, sizeof(pab)));
   BSG_CUDA(cudaMemcpyToSymbol(c_sqrt_fact, sf, sizeof(sf)));
   BSG_CUDA(cudaMemcpyToSymbol(c_fact, f, sizeof(f)));
   dev_done = dev;
@@ -423,10 +418,8 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
     // class-pair values are read straight from Sigma at each transition
     // (Sigma is shared by every item of the site and stays in L1 / L2; a
     // per-item copy would double the warp's table footprint)
-    auto A_at = [&](uint32_t w) -> CA {
-      const int ab = c_pair_ab[w & 0xfffu];
-      return sig[sb + (int64_t)cls[ab >> 8] * n_len + cls[ab & 0xff]];
-    };
+    // transition word: (source F slot << 10) | (b << 5) | a
+    auto A_at = [&](uint32_t w) -> CA { return sig[sb + (int64_t)cls[(w >> 5) & 31u] * n_len + cls[w & 31u]]; };
     // run the program (the final coefficient stays in a register)
     Fb[lane] = P::one();
     CF fin = P::one();
@@ -443,31 +436,31 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
         const uint32_t w0 = __ldg(a.prog.trans + off);
         const uint32_t w1 = __ldg(a.prog.trans + off + 1);
         const CA av0 = A_at(w0);
-        const CF fv0 = Fb[(size_t)(w0 >> 12) * 32 + lane];
+        const CF fv0 = Fb[(size_t)(w0 >> 10) * 32 + lane];
         const CA av1 = A_at(w1);
-        const CF fv1 = Fb[(size_t)(w1 >> 12) * 32 + lane];
+        const CF fv1 = Fb[(size_t)(w1 >> 10) * 32 + lane];
         P::mac_init(acc, av0, fv0);
         P::mac(acc, av1, fv1);
         t = 2;
       } else if (cnt == 1) {
         const uint32_t w = __ldg(a.prog.trans + off);
-        P::mac_init(acc, A_at(w), Fb[(size_t)(w >> 12) * 32 + lane]);
+        P::mac_init(acc, A_at(w), Fb[(size_t)(w >> 10) * 32 + lane]);
         t = 1;
       }
       for (; t + 1 < cnt; t += 2) {
         const uint32_t w0 = __ldg(a.prog.trans + off + t);
         const uint32_t w1 = __ldg(a.prog.trans + off + t + 1);
         const CA av0 = A_at(w0);
-        const CF fv0 = Fb[(size_t)(w0 >> 12) * 32 + lane];
+        const CF fv0 = Fb[(size_t)(w0 >> 10) * 32 + lane];
         const CA av1 = A_at(w1);
-        const CF fv1 = Fb[(size_t)(w1 >> 12) * 32 + lane];
+        const CF fv1 = Fb[(size_t)(w1 >> 10) * 32 + lane];
         P::mac(acc, av0, fv0);
         P::mac(acc, av1, fv1);
       }
       if (t < cnt) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
         const CA av = A_at(w);
-        const CF fv = Fb[(size_t)(w >> 12) * 32 + lane];
+        const CF fv = Fb[(size_t)(w >> 10) * 32 + lane];
         P::mac(acc, av, fv);
       }
       fin = P::finish(acc, ra, c_inv_d, c_inv_f);

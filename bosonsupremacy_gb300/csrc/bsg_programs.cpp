@@ -9,6 +9,10 @@
 
 namespace bsg {
 
+// transition words pack (F slot << 10) | (b << 5) | a
+static_assert(BSG_MAX_CLASSES <= 32, "class indices take 5 bits of a transition word");
+static_assert(2 * BSG_MAX_STATES < (1 << 22), "F ring slots take 22 bits of a transition word");
+
 int key_order(uint64_t key) {
   int n = 0;
   for (int v = 1; v <= kKeyMaxMult; ++v) n += v * int((key >> (kKeyBits * (v - 1))) & 63);
@@ -124,7 +128,7 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
         t[a]--;
         t[b]--;
         const uint32_t src = uint32_t(slot[local[seen.at(t)]]);
-        ps.trans.push_back((src << 12) | uint32_t(pair_index(a, b)));
+        ps.trans.push_back((src << 10) | (uint32_t(b) << 5) | uint32_t(a));
         ++cnt;
       }
     }

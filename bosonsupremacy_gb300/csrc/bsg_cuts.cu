@@ -35,6 +35,21 @@ namespace bsg {
 constexpr int kMaxCutModes = 256;  // modes in one cut's right block
 
 
+__device__ double block_max(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) s = fmax(s, red[i]);
+    red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
 __device__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -176,8 +191,15 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
   double anorm = 0.0;
   for (size_t t = tid; t < mm; t += nt) anorm += Hm[t] * Hm[t];
   anorm = sqrt(block_sum(anorm, red));
-  constexpr int kRefine = 3;
-  for (int it = 0; it < kRefine; ++it) {
+  // Ogita-Aishima steps until a step's largest off-diagonal correction is
+  // at most 1e-8: each step squares the eigenvector error of every eigenvalue
+  // gap above its cluster threshold, so after such a step the error is at
+  // rounding level.  The FP32 start mixes nearly degenerate eigenvalues
+  // (relative gaps ~1e-6, near-vacuum modes of middle cuts) by a few percent,
+  // which three fixed steps left at ~1e-6.
+  constexpr int kRefineMax = 8;
+  int refined = 0;
+  for (int it = 0; it < kRefineMax; ++it) {
     // s1 = R = I - QT QT^T ; s2 = T = Hm QT^T
     for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
@@ -212,12 +234,15 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     rr = block_sum(rr, red);
     const double delta = 2.0 * (sqrt(so) + anorm * sqrt(rr));
     // s1 <- E (in place: E_ij reads s1_ij and s3_ij only)
+    double emax = 0.0;
     for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
       const double r = s1[t], gap = lam[j] - lam[i];
-      s1[t] = (i != j && fabs(gap) > delta) ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
+      const double e = (i != j && fabs(gap) > delta) ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
+      s1[t] = e;
+      if (i != j) emax = fmax(emax, fabs(e));
     }
-    __syncthreads();
+    emax = block_max(emax, red);
     // s2 = QT + E^T QT, then QT = s2
     for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
@@ -228,11 +253,13 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     __syncthreads();
     for (size_t t = tid; t < mm; t += nt) QT[t] = s2[t];
     __syncthreads();
+    refined = it + 1;
+    if (emax <= 1e-8) break;  // the remaining error is ~emax^2
   }
   for (int i = tid; i < m; i += nt) Hm[(size_t)i * m + i] = lam[i];
   if (sweep_log && tid == 0) {
     sweep_log[0] = (unsigned long long)(sw32 < 0 ? 99 : sw32);
-    sweep_log[1] = (unsigned long long)kRefine;
+    sweep_log[1] = (unsigned long long)refined;
   }
   __syncthreads();
   return sw32 < 0 ? -1 : sw32;

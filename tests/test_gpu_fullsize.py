@@ -126,3 +126,30 @@ def test_uneven_batch_instances_split_vs_fp64(cuda, k):
         scale = y.abs().max().item()
         tol = 4.0 * 2.0 ** -23 * torch.maximum(y.abs(), torch.full_like(y.abs(), 1e-6 * scale))
         assert bool(((x - y).abs() <= tol).all()), (cfg.name, i)
+
+
+@pytest.mark.parametrize("cut", [0, 1, 20, 47, 60, 65, 71, 76, 100, 141])
+def test_williamson_symplectics_at_full_size(full_builds, cut):
+    """Cut symplectics of the M=144 build (left cuts carry a vacuum cluster of
+    up to 284 modes): S Omega S^T = Omega and S^-1 V S^-T = diag(nu, nu) with
+    nu >= 1, V the sub-covariance of the cut's right block."""
+    cfg, sq, split, _ = full_builds
+    M = cfg.M
+    L = cut + 1
+    k = M - L
+    sel = np.concatenate([np.arange(L, M), np.arange(L, M) + M])
+    V = sq[np.ix_(sel, sel)]
+    S = split.S[cut, : 2 * k, : 2 * k].cpu().numpy()
+    om = np.block([[np.zeros((k, k)), np.eye(k)], [-np.eye(k), np.zeros((k, k))]])
+    scale = max(1.0, np.abs(S).max() ** 2)
+    sym_err = np.abs(S @ om @ S.T - om).max() / scale
+    assert sym_err <= 1e-10, sym_err
+    Si = -om @ S.T @ om  # the inverse of a symplectic matrix
+    D = Si @ V @ Si.T
+    dg = np.diag(D)
+    nu = dg[:k]
+    off = np.abs(D - np.diag(dg)) / np.sqrt(np.outer(np.abs(dg), np.abs(dg)))
+    assert off.max() <= 1e-9, off.max()
+    pair_err = np.abs(dg[k:] - nu).max() / nu.max()
+    assert pair_err <= 1e-9, pair_err
+    assert nu.min() >= 1.0 - 1e-9, nu.min()

@@ -525,8 +525,8 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   // already taken (pivoted Gram-Schmidt), so a degenerate eigenspace of any
   // dimension (e.g. the nu = 1 vacuum modes) is always completed.  The
   // candidates' residuals are tracked in FP32 (pivot choice only); the chosen
-  // FP64 eigenvector (not its FP32 copy) and y are cleaned by one FP64
-  // projection against the accepted vectors of the cluster.
+  // FP64 eigenvector (not its FP32 copy) is cleaned by one FP64 projection
+  // against the accepted vectors of the cluster.
   // 1/nu of each pair is |G x| (x a unit eigenvector: |G x|^2 = mu).
   double* Xacc = H;  // accepted vectors as rows
   float* c32 = reinterpret_cast<float*>(X2 + nn);       // FP32 candidates of the cluster
@@ -645,11 +645,15 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       const double ix = 1.0 / sqrt(nx);
       for (int i = tid; i < n; i += nt) x[i] *= ix;
       __syncthreads();
+      // y = G x / |G x| needs no projection: G maps the span of the accepted
+      // pairs into itself (G x_j = |G x_j| y_j, G y_j = -|G x_j| x_j for
+      // eigenvectors x_j of G^T G), so x orthogonal to that span makes G x
+      // orthogonal to it up to rounding (checked to 1e-10 on every kind of
+      // cut by the symplectic tests)
       apply_G(x, y);
       double gx = 0.0;
       for (int i = tid; i < n; i += nt) gx += y[i] * y[i];
       gx = block_sum(gx, red);  // |G x|^2 = 1/nu^2
-      project_out(y, acc0, acc + 1);
       double ny = 0.0;
       for (int i = tid; i < n; i += nt) ny += y[i] * y[i];
       ny = block_sum(ny, red);

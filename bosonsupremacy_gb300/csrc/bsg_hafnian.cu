@@ -1563,7 +1563,7 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   const int ng = int(groups.size());
   // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[4..9] = final joins,
   // h->ev[10..12] = Gammas final (pinned copies), h->ev[13..14] = copy-stream joins,
-  // h->ev[16..18] = first site parts of a partitioned group final
+  // h->ev[16 + 3 g + q] (q < 3) = site part q of group g final (host outputs)
   cudaEvent_t ev_keys[3] = {}, ev_done[3] = {};
   // profiling timeline: per group Williamson done, keys on host, Sigma done, DP done
   cudaEvent_t tl0 = nullptr, tl[3][4] = {};
@@ -1687,17 +1687,18 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
         rc = BSG_ERR_CUDA;
       }
     }
-    // Host outputs: the left group finishes last, so its DP runs in four site
-    // parts (34 / 34 / 22 / 10 % of its sites, own plan / item / scratch
-    // slots) and each part's Gammas download while the next part computes;
-    // the small last part keeps the download left after the build short
-    // (the device-to-host link moves ~190 GB/s).  Everything else runs as one
-    // launch set.
+    // Host outputs: every group's DP runs in four site parts (34 / 34 / 22 /
+    // 10 % of its sites, each part with its own plan / item / scratch slot)
+    // and each part's Gammas download while the next part computes.  The
+    // device-to-host link moves ~190 GB/s, so the 50 ms of downloads of the
+    // largest workload must start early to stay off the end of the build; the
+    // small last parts keep what is left after the build short.  The
+    // device-resident build runs one launch set per group.
     const size_t gb = (size_t)chi * chi * d * (out_dtype == BSG_OUT_C128 ? 16 : 8);
     int copied = G.s0;  // sites of this group whose download is queued
     if (!in.empty() && rc == BSG_OK) {
       const int n_in = int(in.size());
-      const bool split_parts = gammas_pinned && ng > 1 && g == 1 && n_in >= 4;
+      const bool split_parts = gammas_pinned && ng > 1 && n_in >= 4;
       const int parts = split_parts ? 4 : 1;
       const double cut_at[5] = {0.0, 0.34, 0.68, 0.90, 1.0};
       for (int q = 0; q < parts && rc == BSG_OK; ++q) {
@@ -1709,11 +1710,11 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
         const int i1 = q + 1 == parts ? n_in : std::max(q + 1, int(cut_at[q + 1] * n_in + 0.5));
         if (i0 >= i1) continue;
         const std::vector<SiteInput> sub(in.begin() + i0, in.begin() + i1);
-        rc = run_sites(h, sub, d, chi, precision, out_dtype, h->slot[q == 0 ? G.slot : 2 + q], G.dp_stream);
+        rc = run_sites(h, sub, d, chi, precision, out_dtype, h->slot[q == 0 ? G.slot : 2 + 3 * g + q], G.dp_stream);
         if (rc == BSG_OK && q + 1 < parts) {
           cudaStream_t cp = h->copy[g & 1];
-          cudaError_t e = cudaEventRecord(h->ev[16 + q], G.dp_stream);
-          if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[16 + q], 0);
+          cudaError_t e = cudaEventRecord(h->ev[16 + 3 * g + q], G.dp_stream);
+          if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, h->ev[16 + 3 * g + q], 0);
           for (int i = G.s0 + i0; i < G.s0 + i1 && e == cudaSuccess; ++i)
             e = cudaMemcpyAsync(gammas_pinned[i], gammas_host[i], gb, cudaMemcpyDeviceToHost, cp);
           if (e != cudaSuccess) {

@@ -233,16 +233,16 @@ struct bsg_handle_s {
   // groups, dp_lo[3] low-priority streams of the groups' DP
   cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[3] = {}, copy[2] = {};
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
-  cudaEvent_t ev[20] = {};
+  cudaEvent_t ev[25] = {};
   int ensure_aux();
   // per-group buffers of the site DP (plan tables, item slots, per-warp
   // scratch, pinned plan staging); slot 0 serves the single-site calls,
-  // slots 3 to 5 the later site parts of a build group whose Gammas are
-  // downloaded part by part
+  // slots 3 + 3 g .. 5 + 3 g the later site parts of build group g when the
+  // Gammas are downloaded part by part
   struct SiteSlot {
     bsg::DevBuf plan, items, scratch;
     bsg::HostBuf stage;
-  } slot[6];
+  } slot[12];
   int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1, 2};
 };
 

@@ -6,8 +6,9 @@
   Schmidt values and cut labels (both run the same FP64 factorisations), and
   every Gamma entry within a few FP32 ulps (the two DP arithmetics differ by
   ~2^-44 relative before the complex64 rounding);
-* the host-output build (per-group downloads, the left group's DP in four
-  site parts) lands exactly the device build's Gammas and Lambdas;
+* the host-output build (every group's DP in four site parts, each part
+  downloaded as it finishes) lands exactly the device build's Gammas and
+  Lambdas;
 * every Gamma is finite and not identically zero, every cut keeps at least
   one row, and the Schmidt weights of each cut are positive and sorted.
 

@@ -173,18 +173,27 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
 // scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
 // the start tolerance of the refinement.
 __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
-                            double* cs, double* sn, int* pos, unsigned long long* sweep_log) {
+                            double* cs, double* sn, int* pos, float* jsm, unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t mm = (size_t)m * m;
-  float* H32 = reinterpret_cast<float*>(s1);
-  float* Q32 = H32 + mm;  // s1 holds 2 m^2 floats
+  // the FP32 copies: in shared memory when the launch reserved room for them
+  // (the rotation rounds touch scattered rows and columns), else in s1
+  float* H32 = jsm ? jsm : reinterpret_cast<float*>(s1);
+  float* Q32 = H32 + mm;  // 2 m^2 floats
   for (size_t t = tid; t < mm; t += nt) {
     H32[t] = float(Hm[t]);
     Q32[t] = (t / m == t % m) ? 1.f : 0.f;
   }
   __syncthreads();
+  unsigned long long t32 = 0;
+  if (sweep_log && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t32));
   const int sw32 =
       block_jacobi<float>(H32, m, Q32, 24, 1e-10, red, reinterpret_cast<float*>(cs), reinterpret_cast<float*>(sn), pos);
+  if (sweep_log && tid == 0) {
+    unsigned long long t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    sweep_log[2] = t1 - t32;
+  }
   for (size_t t = tid; t < mm; t += nt) QT[t] = double(Q32[t]);
   __syncthreads();
   double* lam = reinterpret_cast<double*>(cs);  // m doubles (cs and sn are adjacent: 2 kMaxCutModes)
@@ -330,6 +339,8 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n (also Householder taus)
   double* vec = dots + 2 * kMaxCutModes;                               // n
   double* vec2 = vec + 2 * kMaxCutModes;                               // n
+  // FP32 Jacobi matrices (2 m^2 floats) when the launch reserved them
+  float* jsm = a.jac_smem_m > 0 ? reinterpret_cast<float*>(vec2 + 2 * kMaxCutModes) : nullptr;
   __shared__ int s_flag;
   __shared__ double s_scalar;
 
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     }
     __syncthreads();
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos,
+    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
@@ -479,7 +490,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     __syncthreads();
     // Gm is free in this path (G is applied through W = L^{-1}, which the pairing still needs)
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos,
+    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos, jsm,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
@@ -901,7 +912,21 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
   if (c1 <= c0) return BSG_OK;
   CutArgs a = args;
   a.c0 = c0;
-  const size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
+  size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
+  // eigen-problem size of cut c: 2 min(L, k) (full path m = 2k, low-rank path m = 2L)
+  int m_max = 0;
+  for (int c = c0; c < c1; ++c) {
+    const int L = a.L0 + c, k = a.M - L;
+    m_max = std::max(m_max, 2 * std::min(L, k));
+  }
+  int smem_optin = 0;
+  BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+  const size_t jac = (size_t)2 * m_max * m_max * sizeof(float);
+  a.jac_smem_m = 0;
+  if (wsm + jac <= (size_t)smem_optin) {
+    a.jac_smem_m = m_max;
+    wsm += jac;
+  }
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
   BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0,
                (williamson_kernel<<<c1 - c0, h->tune[BSG_TUNE_FACTOR_THREADS], wsm, st>>>(a)));
@@ -940,6 +965,7 @@ int cut_read_phases(bsg_handle_t h, const CutArgs& a, cudaStream_t st) {
     }
     for (int i = kCutTimedPhases; i < kCutPhases; ++i)
       h->prof.cut_phases[(size_t)c * kCutPhases + i] = double(t[(size_t)c * kCutPhases + i]);
+    h->prof.cut_phases[(size_t)c * kCutPhases + kCutPhases - 1] *= 1e-6;  // ns -> ms
   }
   return BSG_OK;
 }

@@ -166,10 +166,11 @@ struct CutArgs {
   double* mu;          // [n_cuts, 2 kmax] eigenvalues of G^T G, then 1/nu per pair
   int max_sweeps;
   int c0;              // first cut of this launch (block b handles cut c0 + b)
+  int jac_smem_m;      // > 0: the FP32 Jacobi matrices of eigen-problems up to this size live in shared memory
   unsigned long long* phase_t;  // [n_cuts, kCutPhases] phase timestamps (profiling) or null
 };
 constexpr int kCutTimedPhases = 11;  // stamps 0..10
-constexpr int kCutPhases = 13;       // + FP32 and FP64 Jacobi sweep counts
+constexpr int kCutPhases = 14;       // + FP32 sweeps, FP64 refinement steps, FP32 sweep time (ns)
 
 int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                 double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);

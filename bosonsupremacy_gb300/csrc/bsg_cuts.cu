@@ -87,10 +87,10 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
     dia = block_sum(dia, red);
     if (off <= tol * dia) return sweep;
     for (int step = 0; step < m - 1; ++step) {
-      for (int i = tid; i < m; i += nt) pos[i] = i == 0 ? 0 : ((i - 1 + step) % (m - 1)) + 1;
-      __syncthreads();
+      // round-robin pairing of this step: slot i holds index pos(i)
+      auto pos_at = [&](int i) { return i == 0 ? 0 : ((i - 1 + step) % (m - 1)) + 1; };
       for (int q0 = tid; q0 < P; q0 += nt) {
-        int p = pos[q0], q = pos[m - 1 - q0];
+        int p = pos_at(q0), q = pos_at(m - 1 - q0);
         if (p > q) {
           const int x = p;
           p = q;
@@ -108,14 +108,19 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
         }
         cs[q0] = T(c_);
         sn[q0] = T(s_);
+        pos[q0] = p;
+        pos[P + q0] = q;
       }
       __syncthreads();
-      for (int t = tid; t < P * P; t += nt) {
-        const int m1 = t / P, m2 = t % P;
-        if (m1 > m2) continue;
-        int p1 = pos[m1], q1 = pos[m - 1 - m1], p2 = pos[m2], q2 = pos[m - 1 - m2];
-        if (p1 > q1) { const int x = p1; p1 = q1; q1 = x; }
-        if (p2 > q2) { const int x = p2; p2 = q2; q2 = x; }
+      // 2 x 2 blocks (m1 <= m2) of the two-sided update, upper triangle of pairs
+      const int PT = P * (P + 1) / 2;
+      for (int t = tid; t < PT; t += nt) {
+        // t -> (m1, m2), m1 <= m2: row m2 of the triangle starts at m2 (m2 + 1) / 2
+        int m2 = int((sqrtf(8.f * float(t) + 1.f) - 1.f) * 0.5f);
+        while (m2 * (m2 + 1) / 2 > t) --m2;
+        while ((m2 + 1) * (m2 + 2) / 2 <= t) ++m2;
+        const int m1 = t - m2 * (m2 + 1) / 2;
+        const int p1 = pos[m1], q1 = pos[P + m1], p2 = pos[m2], q2 = pos[P + m2];
         const T c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
         const T b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
         const T b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
@@ -142,8 +147,7 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
       }
       for (int t = tid; t < P * m; t += nt) {
         const int q0 = t / m, j = t % m;
-        int p = pos[q0], q = pos[m - 1 - q0];
-        if (p > q) { const int x = p; p = q; q = x; }
+        const int p = pos[q0], q = pos[P + q0];
         const T c_ = cs[q0], s_ = sn[q0];
         const T hp = QT[(size_t)p * m + j], hq = QT[(size_t)q * m + j];
         QT[(size_t)p * m + j] = c_ * hp - s_ * hq;

@@ -91,9 +91,6 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out);
 int programs_upload(ProgramSet& ps, cudaStream_t stream);
 void programs_free(ProgramSet& ps);
 
-// pair index of classes a <= b in the packed upper triangle
-__host__ __device__ inline int pair_index(int a, int b) { return b * (b + 1) / 2 + a; }
-
 // ---- device buffer helper ---------------------------------------------------
 struct DevBuf {
   void* ptr = nullptr;

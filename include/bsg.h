@@ -130,9 +130,9 @@ int bsg_first_sigma(bsg_handle_t h, const double* S_0, int M, const double* sq_c
  *   Gamma[a, b, j] = haf(Sigma[T(j, b, a)]) / (sqrt(j!) sqrt(prod num_l[b]!)
  *                     sqrt(prod num_r[a]!)) / Z / lambda_l[b]
  * with T = j copies of index 0, mode q of label num_l[b] at index 1 + q, mode
- * q of label num_r[a] at index M_r + q.  Every (a, b, j) of the bond grid is
- * one work item of one persistent launch; items are bucketed by the
- * multiplicity partition of T so that a warp runs one program.
+ * q of label num_r[a] at index M_r + q.  Every even-order (a, b, j) of the
+ * bond grid is one work item of the site's DP launches; items are bucketed by
+ * the multiplicity partition of T so that a warp runs one program.
  *   kind FIRST : num_r ignored (one empty right label), Gamma[0, b, j]
  *   kind MIDDLE: Gamma[a, b, j]
  *   kind LAST  : num_l ignored (one empty left label), lambda_l ignored, Gamma[a, 0, j]

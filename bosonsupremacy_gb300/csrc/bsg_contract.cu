@@ -39,15 +39,37 @@ __global__ void final_dot_kernel(const typename Cx<R>::T* __restrict__ L, const 
                                  const double* __restrict__ lam, int chi, int64_t P, double2* __restrict__ amp) {
   const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (p >= P) return;
-  const typename Cx<R>::T* l = L + (int64_t)li[p] * chi;
-  const typename Cx<R>::T* r = Rt + (int64_t)ri[p] * chi;
   double sr = 0.0, si = 0.0;
-  for (int a = lane; a < chi; a += 32) {
-    const double w = lam ? lam[a] : 1.0;
-    const double lx = double(l[a].x) * w, ly = double(l[a].y) * w;
-    sr += lx * double(r[a].x) - ly * double(r[a].y);
-    si += lx * double(r[a].y) + ly * double(r[a].x);
+  if constexpr (std::is_same<R, float>::value) {
+    // FP32 environments: each lane's few products accumulate in FP32 FMAs
+    // (their TF32x3 rounding dominates), the 32 lane sums in FP64; the
+    // bond weights are converted once per block
+    extern __shared__ float lam_f[];
+    for (int a = threadIdx.x; a < chi; a += blockDim.x) lam_f[a] = lam ? float(lam[a]) : 1.f;
+    __syncthreads();
+    if (p >= P) return;  // after the block barrier
+    const float2* l = reinterpret_cast<const float2*>(L) + (int64_t)li[p] * chi;
+    const float2* r = reinterpret_cast<const float2*>(Rt) + (int64_t)ri[p] * chi;
+    float fr = 0.f, fi = 0.f;
+    for (int a = lane; a < chi; a += 32) {
+      const float2 lv = l[a], rv = r[a];
+      const float w = lam_f[a];
+      const float lx = lv.x * w, ly = lv.y * w;
+      fr = fmaf(lx, rv.x, fmaf(-ly, rv.y, fr));
+      fi = fmaf(lx, rv.y, fmaf(ly, rv.x, fi));
+    }
+    sr = fr;
+    si = fi;
+  } else {
+    if (p >= P) return;
+    const typename Cx<R>::T* l = L + (int64_t)li[p] * chi;
+    const typename Cx<R>::T* r = Rt + (int64_t)ri[p] * chi;
+    for (int a = lane; a < chi; a += 32) {
+      const double w = lam ? lam[a] : 1.0;
+      const double lx = double(l[a].x) * w, ly = double(l[a].y) * w;
+      sr += lx * double(r[a].x) - ly * double(r[a].y);
+      si += lx * double(r[a].y) + ly * double(r[a].x);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
@@ -189,6 +211,89 @@ __global__ void __launch_bounds__(1024) plan_scan_kernel(PlanArgs a, int level, 
   }
 }
 
+// Multi-CTA form of plan_scan_kernel for large levels, in three launches over
+// 1024-key tiles (the grid covers d * P keys, the bound of d * prev; tiles past
+// the level's keys do nothing): per-tile flag counts, one CTA turning the
+// counts into tile offsets (and the level's row count), then each tile's
+// exclusive scan plus its offset.
+__device__ __forceinline__ int block_incl_scan_1024(int x, int32_t* warp_sums) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int v = warp_sums[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    warp_sums[lane] = v;
+  }
+  __syncthreads();
+  const int r = x + (w ? warp_sums[w - 1] : 0);
+  __syncthreads();  // warp_sums may be reused
+  return r;
+}
+
+__global__ void __launch_bounds__(1024) plan_count_kernel(PlanArgs a, int level, int32_t* tile_sum) {
+  __shared__ int32_t warp_sums[32];
+  const int prev = level == 0 ? 1 : a.meta[(level - 1) * (a.d + 2)];
+  const int64_t size = (int64_t)a.d * prev;
+  const int64_t q = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  if ((int64_t)blockIdx.x * 1024 >= size) {  // block-uniform
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = 0;
+    return;
+  }
+  const int incl = block_incl_scan_1024(q < size ? a.flags[q] : 0, warp_sums);
+  if (threadIdx.x == 1023) tile_sum[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(1024) plan_offsets_kernel(PlanArgs a, int level, int32_t* tile_sum, int n_tiles) {
+  __shared__ int32_t warp_sums[32];
+  __shared__ int32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n_tiles; base += 1024) {
+    const int t = base + threadIdx.x;
+    const int v = t < n_tiles ? tile_sum[t] : 0;
+    const int incl = block_incl_scan_1024(v, warp_sums);
+    const int c0 = carry;
+    if (t < n_tiles) tile_sum[t] = c0 + incl - v;  // exclusive offset of tile t
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = c0 + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int32_t* meta = a.meta + level * (a.d + 2);
+    meta[0] = carry;
+    meta[1 + a.d] = carry;
+  }
+}
+
+__global__ void __launch_bounds__(1024) plan_place_kernel(PlanArgs a, int level, const int32_t* tile_off,
+                                                          int32_t* parent, int32_t* nval) {
+  __shared__ int32_t warp_sums[32];
+  const int prev = level == 0 ? 1 : a.meta[(level - 1) * (a.d + 2)];
+  const int64_t size = (int64_t)a.d * prev;
+  if ((int64_t)blockIdx.x * 1024 >= size) return;  // block-uniform
+  int32_t* meta = a.meta + level * (a.d + 2);
+  const int64_t q = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  const int f = q < size ? a.flags[q] : 0;
+  const int excl = tile_off[blockIdx.x] + block_incl_scan_1024(f, warp_sums) - f;
+  if (q < size) {
+    a.idx[q] = excl;
+    a.flags[q] = 0;
+    if (q % prev == 0) meta[1 + q / prev] = excl;  // first row of photon number q / prev
+    if (f) {
+      parent[excl] = int32_t(q % prev);
+      nval[excl] = int32_t(q / prev);
+    }
+  }
+}
+
 __global__ void plan_assign_kernel(PlanArgs a) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.P) return;
@@ -213,7 +318,7 @@ static int plan_side_device(bsg_handle_t h, const int32_t* pat, int64_t P, int M
   sp.sites = sites;
   sp.P = P;
   sp.d = d;
-  // work: cur, keys [P] | flags, idx [d P] | meta [nl (d + 2)] | parent, nval [nl P]
+  // work: cur, keys [P] | flags, idx [d P] | meta [nl (d + 2)] | parent, nval [nl P] | tile sums
   PlanArgs a{};
   a.pat = pat;
   a.P = P;
@@ -227,13 +332,28 @@ static int plan_side_device(bsg_handle_t h, const int32_t* pat, int64_t P, int M
   a.err = err;
   sp.parent = a.meta + (size_t)nl * (d + 2);
   sp.nval = sp.parent + (size_t)nl * P;
+  int32_t* tile_sum = sp.nval + (size_t)nl * P;  // [ceil(d P / 1024)]
   sp.final_row = a.cur;
   BSG_CUDA(cudaMemsetAsync(a.flags, 0, (size_t)d * P * 4, st));
   const unsigned blocks = unsigned((P + 255) / 256);
+  // level l has at most d * min(P, d^l) keys: small levels use the one-CTA
+  // scan, large ones the three-launch multi-CTA scan over d * P keys
+  const int n_tiles = int(((int64_t)d * P + 1023) / 1024);
+  int64_t bound = 1;  // d^l, capped
   for (int l = 0; l < nl; ++l) {
+    bound = std::min<int64_t>(bound * d, (int64_t)d * P);
+    int32_t* par = sp.parent + (size_t)l * P;
+    int32_t* nv = sp.nval + (size_t)l * P;
     BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_mark_kernel<<<blocks, 256, 0, st>>>(a, sites[l], l)));
-    BSG_PROFILED(h, BSG_K_PREP, st, (double)P,
-                 (plan_scan_kernel<<<1, 1024, 0, st>>>(a, l, sp.parent + (size_t)l * P, sp.nval + (size_t)l * P)));
+    if (bound <= 8192 || n_tiles <= 8) {
+      BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_scan_kernel<<<1, 1024, 0, st>>>(a, l, par, nv)));
+    } else {
+      BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_count_kernel<<<n_tiles, 1024, 0, st>>>(a, l, tile_sum)));
+      BSG_PROFILED(h, BSG_K_PREP, st, (double)P,
+                   (plan_offsets_kernel<<<1, 1024, 0, st>>>(a, l, tile_sum, n_tiles)));
+      BSG_PROFILED(h, BSG_K_PREP, st, (double)P,
+                   (plan_place_kernel<<<n_tiles, 1024, 0, st>>>(a, l, tile_sum, par, nv)));
+    }
     BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_assign_kernel<<<blocks, 256, 0, st>>>(a)));
   }
   sp.meta.resize((size_t)nl * (d + 2));
@@ -242,7 +362,8 @@ static int plan_side_device(bsg_handle_t h, const int32_t* pat, int64_t P, int M
 }
 
 static size_t plan_side_words(int64_t P, int d, int levels) {
-  return (size_t)2 * P + (size_t)2 * d * P + (size_t)levels * (d + 2) + (size_t)2 * levels * P;
+  return (size_t)2 * P + (size_t)2 * d * P + (size_t)levels * (d + 2) + (size_t)2 * levels * P +
+         (size_t)((int64_t)d * P + 1023) / 1024;
 }
 
 template <class R>
@@ -366,7 +487,8 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   T* Rend = side(right, E[2], E[3], false);
   if (!Rend) return BSG_ERR_CUDA;
   const int mid = left.sites.back();
-  final_dot_kernel<R><<<unsigned((P * 32 + 255) / 256), 256, 0, st>>>(
+  final_dot_kernel<R><<<unsigned((P * 32 + 255) / 256), 256, std::is_same<R, float>::value ? chi * sizeof(float) : 0,
+                        st>>>(
       Lend, left.final_row, Rend, right.final_row, lam + (size_t)mid * chi, chi, P, reinterpret_cast<double2*>(amp));
   BSG_CUDA(cudaGetLastError());
   if (h->prof.on) BSG_TRY(h->prof.end(BSG_K_CONTRACT, st, ev, flops + 8.0 * P * chi));

@@ -129,12 +129,13 @@ __global__ void build_a_kernel(const float2* __restrict__ E, const int32_t* __re
 // Level l of a side keys every pattern by (n, parent row) with n its photon
 // number at the level's site; the distinct keys, in n-major order, are the
 // level's rows, so rows of one n are contiguous (one GEMM per n).  Per level:
-// mark the keys, one CTA scans them into row ids (writing each row's parent
-// and n and the level's group bounds), then every pattern takes its row.
+// mark the keys (each pattern first taking its row of the previous level),
+// scan them into row ids (writing each row's parent and n and the level's
+// group bounds); the patterns take their rows of the last level at the end.
 constexpr int kMaxLevels = 1024;
 
 struct PlanArgs {
-  const int32_t* pat;  // [P, M]
+  const int32_t* pat;  // [M, P]: photon number of pattern p at site s is pat[s * P + p]
   int64_t P;
   int M, d;
   int32_t* cur;        // [P] row at the previous level (0 before level 0)
@@ -145,16 +146,42 @@ struct PlanArgs {
   int* err;
 };
 
+// Patterns [P, M] -> [M, P] (32 x 32 tiles through shared memory), so the
+// per-level kernels read one site's photon numbers contiguously.
+__global__ void transpose_patterns_kernel(const int32_t* __restrict__ pat, int64_t P, int M, int32_t* __restrict__ patT) {
+  __shared__ int32_t tile[32][33];
+  const int64_t p0 = (int64_t)blockIdx.x * 32;
+  const int s0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t p = p0 + r;
+    const int s = s0 + threadIdx.x;
+    if (p < P && s < M) tile[r][threadIdx.x] = pat[p * M + s];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int s = s0 + r;
+    const int64_t p = p0 + threadIdx.x;
+    if (p < P && s < M) patT[(int64_t)s * P + p] = tile[threadIdx.x][r];
+  }
+}
+
+// Level `level` keys every pattern; for level > 0 the pattern first takes
+// its row of level - 1 (the scan of that level is done).
 __global__ void plan_mark_kernel(PlanArgs a, int site, int level) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.P) return;
-  const int prev = level == 0 ? 1 : a.meta[(level - 1) * (a.d + 2)];
-  int n = a.pat[p * a.M + site];
+  int prev = 1, row = 0;
+  if (level > 0) {
+    prev = a.meta[(level - 1) * (a.d + 2)];
+    row = a.idx[a.keys[p]];
+    a.cur[p] = row;
+  }
+  int n = a.pat[(int64_t)site * a.P + p];
   if (n < 0 || n >= a.d) {
     atomicExch(a.err, 1);
     n = 0;
   }
-  const int key = n * prev + (level == 0 ? 0 : a.cur[p]);
+  const int key = n * prev + row;
   a.keys[p] = key;
   a.flags[key] = 1;
 }
@@ -354,8 +381,9 @@ static int plan_side_device(bsg_handle_t h, const int32_t* pat, int64_t P, int M
       BSG_PROFILED(h, BSG_K_PREP, st, (double)P,
                    (plan_place_kernel<<<n_tiles, 1024, 0, st>>>(a, l, tile_sum, par, nv)));
     }
-    BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_assign_kernel<<<blocks, 256, 0, st>>>(a)));
   }
+  // rows of the last level
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)P, (plan_assign_kernel<<<blocks, 256, 0, st>>>(a)));
   sp.meta.resize((size_t)nl * (d + 2));
   BSG_CUDA(cudaMemcpyAsync(sp.meta.data(), a.meta, sp.meta.size() * 4, cudaMemcpyDeviceToHost, st));
   return BSG_OK;
@@ -527,13 +555,17 @@ extern "C" int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas,
   BSG_CHECK_ARG((int64_t)d * P < INT32_MAX, "bsg_pattern_amplitudes: d * P = %lld too large", (long long)d * P);
   // planning workspace (both sides) + an error word
   const size_t wl = plan_side_words(P, d, int(ls.size())), wr = plan_side_words(P, d, int(rs.size()));
-  BSG_TRY(h->sample_ws.ensure((wl + wr) * 4 + 256));
+  BSG_TRY(h->sample_ws.ensure((wl + wr) * 4 + 256 + (size_t)M * P * 4));
   int32_t* work = reinterpret_cast<int32_t*>(h->sample_ws.ptr);
   int* perr = reinterpret_cast<int*>(work + wl + wr);
+  int32_t* patT = work + wl + wr + 64;  // [M, P]
   BSG_CUDA(cudaMemsetAsync(perr, 0, 4, st));
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)P * M,
+               (transpose_patterns_kernel<<<dim3(unsigned((P + 31) / 32), unsigned((M + 31) / 32)), dim3(32, 8), 0,
+                                            st>>>(patterns, P, M, patT)));
   SidePlan left, right;
-  BSG_TRY(plan_side_device(h, patterns, P, M, d, ls, left, work, perr, st));
-  BSG_TRY(plan_side_device(h, patterns, P, M, d, rs, right, work + wl, perr, st));
+  BSG_TRY(plan_side_device(h, patT, P, M, d, ls, left, work, perr, st));
+  BSG_TRY(plan_side_device(h, patT, P, M, d, rs, right, work + wl, perr, st));
   int herr = 0;
   BSG_CUDA(cudaMemcpyAsync(&herr, perr, 4, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaStreamSynchronize(st));  // level sizes for the GEMM launches

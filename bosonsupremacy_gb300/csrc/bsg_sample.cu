@@ -239,7 +239,10 @@ struct SampleArgs {
   float* a_lo;                 //        and lo
 };
 
-template <class R, bool SPLIT>
+// DDM: compile-time bound of dd (4, 8, 12 or 16) for the per-lane arrays and
+// the unrolled dd x d products (a bound of 16 for dd = 8 ran 4x the
+// instructions under predication)
+template <class R, bool SPLIT, int DDM>
 __global__ void __launch_bounds__(32 * kSampleWarps) sample_kernel(SampleArgs<R> a) {
   using T = typename Cx<R>::T;
   __shared__ T ex[kSampleWarps][kMaxDD], ph[kSampleWarps][32], D[kSampleWarps][kMaxDD * kMaxDD];
@@ -252,13 +255,13 @@ __global__ void __launch_bounds__(32 * kSampleWarps) sample_kernel(SampleArgs<R>
   const T* tb = a.T + b * a.t_stride;
   const T* Dw = D[wib];
   const bool last = a.lam == nullptr;
-  R p[kMaxDD];
+  R p[DDM];
 #pragma unroll
-  for (int k = 0; k < kMaxDD; ++k) p[k] = R(0);
+  for (int k = 0; k < DDM; ++k) p[k] = R(0);
   for (int m = lane; m < (last ? 1 : chi); m += 32) {
-    T t[kMaxDD];
+    T t[DDM];
 #pragma unroll
-    for (int j = 0; j < kMaxDD; ++j) {
+    for (int j = 0; j < DDM; ++j) {
       if (j < jmax) {
         t[j] = tb[(size_t)m * d + j];
       } else {
@@ -268,11 +271,11 @@ __global__ void __launch_bounds__(32 * kSampleWarps) sample_kernel(SampleArgs<R>
     }
     const R w = last ? R(1) : R(a.lam[m]) * R(a.lam[m]);
 #pragma unroll
-    for (int k = 0; k < kMaxDD; ++k) {
+    for (int k = 0; k < DDM; ++k) {
       if (k < dd) {
         R zr = R(0), zi = R(0);
 #pragma unroll
-        for (int j = 0; j < kMaxDD; ++j) {
+        for (int j = 0; j < DDM; ++j) {
           if (j < jmax) {
             const T dk = Dw[k * kMaxDD + j];
             zr += dk.x * t[j].x - dk.y * t[j].y;
@@ -284,18 +287,18 @@ __global__ void __launch_bounds__(32 * kSampleWarps) sample_kernel(SampleArgs<R>
     }
   }
 #pragma unroll
-  for (int k = 0; k < kMaxDD; ++k)
+  for (int k = 0; k < DDM; ++k)
     for (int o = 16; o > 0; o >>= 1) p[k] += __shfl_xor_sync(0xffffffffu, p[k], o);
   // inverse CDF, as the reference: normalise, cumulative sum, count thresholds above
   R tot = R(0);
 #pragma unroll
-  for (int k = 0; k < kMaxDD; ++k)
+  for (int k = 0; k < DDM; ++k)
     if (k < dd) tot += p[k];
   const R u = R(a.u[b]);
   R cum = R(0);
   int cnt = 0;
 #pragma unroll
-  for (int k = 0; k < kMaxDD; ++k) {
+  for (int k = 0; k < DDM; ++k) {
     if (k < dd) {
       cum += p[k] / tot;
       cnt += u > cum ? 1 : 0;
@@ -438,8 +441,18 @@ static int run_sampler(bsg_handle_t h, const void* const* Gd, const double* lam,
       sa.pre = pre;
       sa.a_hi = a_hi;
       sa.a_lo = a_lo;
-      BSG_PROFILED(h, BSG_K_SAMPLE, st, (double)nb * chi * dd * d,
-                   (sample_kernel<R, SPLIT><<<sblocks, 32 * kSampleWarps, 0, st>>>(sa)));
+      if (dd <= 4)
+        BSG_PROFILED(h, BSG_K_SAMPLE, st, (double)nb * chi * dd * d,
+                     (sample_kernel<R, SPLIT, 4><<<sblocks, 32 * kSampleWarps, 0, st>>>(sa)));
+      else if (dd <= 8)
+        BSG_PROFILED(h, BSG_K_SAMPLE, st, (double)nb * chi * dd * d,
+                     (sample_kernel<R, SPLIT, 8><<<sblocks, 32 * kSampleWarps, 0, st>>>(sa)));
+      else if (dd <= 12)
+        BSG_PROFILED(h, BSG_K_SAMPLE, st, (double)nb * chi * dd * d,
+                     (sample_kernel<R, SPLIT, 12><<<sblocks, 32 * kSampleWarps, 0, st>>>(sa)));
+      else
+        BSG_PROFILED(h, BSG_K_SAMPLE, st, (double)nb * chi * dd * d,
+                     (sample_kernel<R, SPLIT, kMaxDD><<<sblocks, 32 * kSampleWarps, 0, st>>>(sa)));
     }
   }
   int err = 0;

@@ -22,7 +22,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib, ops
+from . import _lib, dist, ops
 
 ERR_TOL = 10 ** (-10)  # MPS_cpu.py:390
 
@@ -70,16 +70,17 @@ def push_to_end(array):
     return out
 
 
-def get_Sigma_Z(S_l, S_r, sq_cov=None):
+def get_Sigma_Z(S_l, S_r, sq_cov=None, device: int = 0):
     """Sigma and Z of a site from the Williamson symplectics of its two cuts
     (MPS_cpu.py:357-372 + 305-312 + 483).  Site 0 passes ``sq_cov`` (the pure
     covariance) instead of the full-state Williamson S (MPS_cpu.py:395)."""
     if sq_cov is not None:
-        return ops.first_sigma(S_l, sq_cov)
-    return ops.site_sigma(S_l, S_r)
+        return ops.first_sigma(S_l, sq_cov, device=device)
+    return ops.site_sigma(S_l, S_r, device=device)
 
 
-def build_site(site, M, d, chi, sq_cov, path, precision="split", out_dtype=torch.complex64, err_tol=ERR_TOL):
+def build_site(site, M, d, chi, sq_cov, path, precision="split", out_dtype=torch.complex64, err_tol=ERR_TOL,
+               device: int = 0):
     """Gamma and Lambda of one site from the cut files in ``path``
     (the three branches of MPS_cpu.py:402-520)."""
     lam = np.zeros(chi, dtype=np.float64)
@@ -90,16 +91,17 @@ def build_site(site, M, d, chi, sq_cov, path, precision="split", out_dtype=torch
         keep = res > err_tol
         num = num[keep].reshape(int(keep.sum()), -1)
         res = res[keep]
-        Sig, Z = get_Sigma_Z(S_l, None, sq_cov=sq_cov)
+        Sig, Z = get_Sigma_Z(S_l, None, sq_cov=sq_cov, device=device)
         lam[: len(res)] = np.sqrt(res)
-        G = ops.build_site(_lib.SITE_FIRST, Sig, num, np.sqrt(res), None, Z, d, chi, precision, out_dtype)
+        G = ops.build_site(_lib.SITE_FIRST, Sig, num, np.sqrt(res), None, Z, d, chi, precision, out_dtype,
+                           device=device)
         return G, lam
     if site == M - 1:
         num_pre = np.load(path + f"num_{site - 1}.npy")
         num_pre = num_pre.reshape(num_pre.shape[0], -1)
         S_r = np.load(path + f"S_{site - 1}.npy")
-        Sig, Z = get_Sigma_Z(None, S_r)
-        G = ops.build_site(_lib.SITE_LAST, Sig, None, None, num_pre, Z, d, chi, precision, out_dtype)
+        Sig, Z = get_Sigma_Z(None, S_r, device=device)
+        G = ops.build_site(_lib.SITE_LAST, Sig, None, None, num_pre, Z, d, chi, precision, out_dtype, device=device)
         return G, None
     num_pre = np.load(path + f"num_{site - 1}.npy")
     num_pre = num_pre.reshape(num_pre.shape[0], -1)
@@ -110,9 +112,10 @@ def build_site(site, M, d, chi, sq_cov, path, precision="split", out_dtype=torch
     keep = res > err_tol
     num = num[keep].reshape(int(keep.sum()), -1)
     res = res[keep]
-    Sig, Z = get_Sigma_Z(S_l, S_r)
+    Sig, Z = get_Sigma_Z(S_l, S_r, device=device)
     lam[: len(res)] = np.sqrt(res)
-    G = ops.build_site(_lib.SITE_MIDDLE, Sig, num, np.sqrt(res), num_pre, Z, d, chi, precision, out_dtype)
+    G = ops.build_site(_lib.SITE_MIDDLE, Sig, num, np.sqrt(res), num_pre, Z, d, chi, precision, out_dtype,
+                       device=device)
     return G, lam
 
 
@@ -131,9 +134,13 @@ def main(argv=None):
     M = len(cov) // 2
     gdt = torch.complex128 if args.fp64_out else torch.complex64
     ldt = "float64" if args.fp64_out else "float32"
-    for site in range(M):
+    # under torchrun each rank writes the files of its own contiguous site range
+    rank, world, local = dist.rank_world()
+    device = local % max(1, torch.cuda.device_count())
+    s0, s1 = dist.shard_sites(M, world)[rank] if world > 1 else (0, M)
+    for site in range(s0, s1):
         t0 = time.time()
-        G, lam = build_site(site, M, d, chi, sq_cov, path, args.precision, gdt)
+        G, lam = build_site(site, M, d, chi, sq_cov, path, args.precision, gdt, device=device)
         G = G.cpu().numpy()
         print(f"mode: {site} Total {time.time() - t0:.4f}")
         np.save(path + f"Gamma_{site}.npy", G)

@@ -20,6 +20,29 @@ def test_shard_sites_cover_every_site_once():
             assert all(r[i][1] == r[i + 1][0] for i in range(world - 1))
 
 
+def test_shard_cuts_cover_every_cut_once():
+    from bosonsupremacy_gb300.dist import shard_cuts
+    for M in (3, 8, 16, 50, 144, 216):
+        for world in (1, 2, 3, 4, 8):
+            if world > M - 1:
+                continue
+            r = shard_cuts(M, world)
+            assert len(r) == world and r[0][0] == 0 and r[-1][1] == M - 1
+            assert all(a < b for a, b in r) and all(r[i][1] == r[i + 1][0] for i in range(world - 1))
+
+
+def test_rank_world_from_environment(monkeypatch):
+    from bosonsupremacy_gb300.dist import rank_world
+    monkeypatch.delenv("RANK", raising=False)
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    monkeypatch.delenv("LOCAL_RANK", raising=False)
+    assert rank_world() == (0, 1, 0)
+    monkeypatch.setenv("RANK", "3")
+    monkeypatch.setenv("WORLD_SIZE", "4")
+    monkeypatch.setenv("LOCAL_RANK", "1")
+    assert rank_world() == (3, 4, 1)
+
+
 def test_cuts_needed():
     assert cuts_needed((0, 5), 10) == (0, 5)
     assert cuts_needed((5, 10), 10) == (4, 9)

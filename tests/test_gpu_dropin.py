@@ -79,3 +79,32 @@ def test_oracle_on_our_cut_files_matches_our_gamma(cuda, golden, tmp_path):
         G = G.cpu().numpy()
         G_ref, _ = R.build_site(site, M, d, chi, t["sq_cov"], cuts)
         assert np.abs(G - G_ref).max() <= 1e-9 * np.abs(G_ref).max(), site
+
+
+def test_cli_steps_sharded_over_ranks(cuda, golden, tmp_path):
+    """Both CLI steps under a torchrun-style environment with two ranks (run
+    one after the other here, on the one GPU): every rank writes the files of
+    its own cut / site range, and together they are the single-rank files."""
+    import subprocess
+    import sys
+    t = golden("small_M16.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = {}
+    for world in (1, 2):
+        root = str(tmp_path / f"w{world}") + "/"
+        os.makedirs(root)
+        _write_inputs(t, root)
+        args = ["--d", str(d), "--chi", str(chi), "--dir", root]
+        for step in ("kron", "mps"):
+            for rank in range(world):
+                env = dict(os.environ, RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK="0")
+                r = subprocess.run([sys.executable, "-m", f"bosonsupremacy_gb300.{step}"] + args,
+                                   cwd=repo, env=env, capture_output=True, text=True, timeout=600)
+                assert r.returncode == 0, r.stderr[-2000:]
+        path = root + f"d_{d}_chi_{chi}/"
+        outs[world] = {name: np.load(path + name) for name in sorted(os.listdir(path)) if name.endswith(".npy")}
+    assert outs[1].keys() == outs[2].keys()
+    assert len([n for n in outs[1] if n.startswith("Gamma_")]) == M
+    for name, v in outs[1].items():
+        assert np.array_equal(v, outs[2][name]), name

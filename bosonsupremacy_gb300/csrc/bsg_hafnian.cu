@@ -218,7 +218,7 @@ struct ProgDev {
   const int32_t* nstates;
   const int32_t* state_off;
   const uint32_t* trans;
-  const uint4* st_pack;  // {first transition, count | r_a << 16, F slot, 0} per state
+  const uint4* st_pack;  // {first transition, count | r_a << 16, F slot, class a} per state
 };
 
 enum { MODE_SITE = 0, MODE_TARGETS = 1, MODE_MATRICES = 2 };
@@ -417,16 +417,36 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
     }
     // class-pair values are read straight from Sigma at each transition
     // (Sigma is shared by every item of the site and stays in L1 / L2; a
-    // per-item copy would double the warp's table footprint)
-    // transition word: (source F slot << 10) | (b << 5) | a
-    auto A_at = [&](uint32_t w) -> CA { return sig[sb + (int64_t)cls[(w >> 5) & 31u] * n_len + cls[w & 31u]]; };
+    // per-item copy would double the warp's table footprint).  Sigma is
+    // symmetric: in site mode each pair is read with the larger key as the
+    // row, key = Sigma index - 1 as an unsigned word (the site mode, index 0,
+    // ranks last).  The site mode and the right label's modes are usually
+    // shared by the warp's lanes (one right row, consecutive left rows of one
+    // key group), so the lanes read along one row of Sigma instead of down a
+    // column.
+    const int kb = MODE == MODE_SITE ? 1 : 0;
+    for (int q = 0; q < kp; ++q) cls[q] -= kb;
+    const C* sigp = sig + sb + (int64_t)kb * (n_len + 1);
+    // transition word: (source F slot << 9) | (b << 2); every transition of a
+    // state pairs its b with the state's first class a
+    constexpr unsigned kFShift = sizeof(CF) == 16 ? 0u : sizeof(CF) == 8 ? 1u : 0u;
+    static_assert(sizeof(CF) == 16 || sizeof(CF) == 8, "F entries of 8 or 16 bytes");
+    const char* cls_b = reinterpret_cast<const char*>(cls);
+    const char* Fl = reinterpret_cast<const char*>(Fb + lane);
+    auto F_at = [&](uint32_t w) -> CF { return *reinterpret_cast<const CF*>(Fl + ((w & ~511u) >> kFShift)); };
     // run the program (the final coefficient stays in a register)
     Fb[lane] = P::one();
     CF fin = P::one();
     for (int s = 1; s < ns; ++s) {
       const uint4 pk = __ldg(a.prog.st_pack + so + s);
       const int off = int(pk.x), cnt = int(pk.y & 0xffffu), ra = int(pk.y >> 16);
+      const uint32_t ya = uint32_t(cls[pk.w]);
       done += cnt;
+      auto A_at = [&](uint32_t w) -> CA {
+        const uint32_t x = uint32_t(*reinterpret_cast<const int*>(cls_b + (w & 0x7cu)));
+        if (MODE == MODE_SITE) return sigp[int(max(x, ya) * uint32_t(n_len) + min(x, ya))];
+        return sigp[int(x * uint32_t(n_len) + ya)];
+      };
       typename P::Acc acc = P::zero();
       // two transitions per step: both pairs of table loads are in flight
       // before the first multiply-add (states average ~2.4 transitions); the
@@ -436,31 +456,31 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
         const uint32_t w0 = __ldg(a.prog.trans + off);
         const uint32_t w1 = __ldg(a.prog.trans + off + 1);
         const CA av0 = A_at(w0);
-        const CF fv0 = Fb[(size_t)(w0 >> 10) * 32 + lane];
+        const CF fv0 = F_at(w0);
         const CA av1 = A_at(w1);
-        const CF fv1 = Fb[(size_t)(w1 >> 10) * 32 + lane];
+        const CF fv1 = F_at(w1);
         P::mac_init(acc, av0, fv0);
         P::mac(acc, av1, fv1);
         t = 2;
       } else if (cnt == 1) {
         const uint32_t w = __ldg(a.prog.trans + off);
-        P::mac_init(acc, A_at(w), Fb[(size_t)(w >> 10) * 32 + lane]);
+        P::mac_init(acc, A_at(w), F_at(w));
         t = 1;
       }
       for (; t + 1 < cnt; t += 2) {
         const uint32_t w0 = __ldg(a.prog.trans + off + t);
         const uint32_t w1 = __ldg(a.prog.trans + off + t + 1);
         const CA av0 = A_at(w0);
-        const CF fv0 = Fb[(size_t)(w0 >> 10) * 32 + lane];
+        const CF fv0 = F_at(w0);
         const CA av1 = A_at(w1);
-        const CF fv1 = Fb[(size_t)(w1 >> 10) * 32 + lane];
+        const CF fv1 = F_at(w1);
         P::mac(acc, av0, fv0);
         P::mac(acc, av1, fv1);
       }
       if (t < cnt) {
         const uint32_t w = __ldg(a.prog.trans + off + t);
         const CA av = A_at(w);
-        const CF fv = Fb[(size_t)(w >> 10) * 32 + lane];
+        const CF fv = F_at(w);
         P::mac(acc, av, fv);
       }
       fin = P::finish(acc, ra, c_inv_d, c_inv_f);

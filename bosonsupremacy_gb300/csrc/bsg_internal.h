@@ -59,9 +59,9 @@ struct ProgramSet {
   std::vector<int32_t> st_trans_off;   // per global state: first transition
   std::vector<int32_t> st_trans_cnt;   // per global state: number of transitions
   std::vector<int32_t> st_ra;          // per global state: r_a (0 for the empty state)
-  std::vector<uint32_t> trans;         // packed (src F slot << 10) | (b << 5) | a, classes a <= b
+  std::vector<uint32_t> trans;         // packed (src F slot << 9) | (b << 2), b >= the state's class a
   std::vector<int32_t> fslots;         // F table entries per program (two levels of states)
-  std::vector<uint4> st_pack;          // per global state: {first transition, count | r_a << 16, F slot, 0}
+  std::vector<uint4> st_pack;          // per global state: {first transition, count | r_a << 16, F slot, a}
   std::unordered_map<uint64_t, int32_t> index;
   // device copies (valid when dev_valid)
   int32_t* d_k = nullptr;

@@ -9,9 +9,12 @@
 
 namespace bsg {
 
-// transition words pack (F slot << 10) | (b << 5) | a
-static_assert(BSG_MAX_CLASSES <= 32, "class indices take 5 bits of a transition word");
-static_assert(2 * BSG_MAX_STATES < (1 << 22), "F ring slots take 22 bits of a transition word");
+// transition words pack (F slot << 9) | (b << 2): the byte offset of class b
+// in a lane's int class array and, for 16-byte F entries, the byte offset of
+// the source slot's [32 lanes] row.  Every transition of a state shares its
+// first class a, which the state's pack word carries.
+static_assert(BSG_MAX_CLASSES <= 32, "class byte offsets take bits 2..6 of a transition word");
+static_assert(2 * BSG_MAX_STATES < (1 << 23), "F ring slots take 23 bits of a transition word");
 
 int key_order(uint64_t key) {
   int n = 0;
@@ -128,14 +131,14 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
         t[a]--;
         t[b]--;
         const uint32_t src = uint32_t(slot[local[seen.at(t)]]);
-        ps.trans.push_back((src << 10) | (uint32_t(b) << 5) | uint32_t(a));
+        ps.trans.push_back((src << 9) | (uint32_t(b) << 2));
         ++cnt;
       }
     }
     ps.st_trans_cnt.push_back(cnt);
     ps.st_ra.push_back(a < k ? int(s[a]) : 0);
     ps.st_pack.push_back(make_uint4(uint32_t(ps.st_trans_off.back()), uint32_t(cnt) | (uint32_t(a < k ? s[a] : 0) << 16),
-                                    uint32_t(slot[i]), 0u));
+                                    uint32_t(slot[i]), uint32_t(a < k ? a : 0)));
   }
   ps.index.emplace(key, prog);
   ps.max_states = std::max(ps.max_states, int(states.size()));

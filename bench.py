@@ -407,19 +407,20 @@ def main():
         roof = {"kernel": "dp_kernel<PrecF64> (hafnian DP)", "bound": "fp64-pipe", "achieved": achieved / 1e12,
                 "peak": pk64.value / 1e12, "unit": "TFLOP/s", "frac": achieved / pk64.value, "traffic": None}
     else:
-        # FP32-pipe instructions issued per complex multiply-add (split: four
-        # products of hi/lo pairs, 12 instructions each; plain FP32: 4 FMAs)
-        instr = {"split": 48.0, "fp32": 4.0}[args.precision]
+        # FP32 operations per complex multiply-add (split: four products of
+        # hi/lo pairs, 12 operations each, issued as 24 packed f32x2
+        # instructions; plain FP32: 4 FMAs)
+        ops = {"split": 48.0, "fp32": 4.0}[args.precision]
         roof = {"kernel": f"dp_kernel<Prec{'Split' if args.precision == 'split' else 'F32'}> (hafnian DP)",
                 "bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": pk32.value / 1e12, "unit": "TFLOP/s",
                 "frac": achieved / pk32.value, "traffic": None,
-                # the pipe issues one instruction per lane and cycle: half the FMA flop peak
-                "fp32_issue_frac": instr * (achieved / 8.0) / (pk32.value / 2.0),
+                # the pipe runs one operation per lane and cycle: half the FMA flop peak
+                "fp32_ops_frac": ops * (achieved / 8.0) / (pk32.value / 2.0),
                 "fp64_equivalent_frac": achieved / pk64.value,
-                "note": ("split arithmetic issues 48 FP32-pipe instructions per complex multiply-add; "
-                         "fp32_issue_frac = those instructions per second over the pipe's instruction rate "
-                         "(live launch durations, which overlap other kernels); fp64_equivalent_frac compares "
-                         "the FP64-accurate result rate with the FP64 pipe's peak")}
+                "note": ("split arithmetic runs 48 FP32 operations per complex multiply-add (24 packed f32x2 "
+                         "instructions); fp32_ops_frac = those operations per second over the FP32 pipe's "
+                         "operation rate (live launch durations, which overlap other kernels); "
+                         "fp64_equivalent_frac compares the FP64-accurate result rate with the FP64 pipe's peak")}
     roof["peak_source"] = "measured on this GPU by bsg_fma_peak (register FMA loop on every SM)"
     roof["work"] = ("8 flops per complex multiply-add of the repetition-aware partition programs "
                     f"({prof[dom]['work'] / args.steps:.4g} per build)")

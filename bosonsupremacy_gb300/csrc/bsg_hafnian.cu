@@ -494,13 +494,13 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
       if constexpr (std::is_same<P, PrecSplit>::value) {
         if (!sd->out_c128) {
         // epilogue on the FP32 pipe: (hi + lo) * sqrt(j!) * l_scale * r_rowfact as FP32 pairs
-        const float4 q = fin;  // (re_h, re_l, im_h, im_l)
+        const float4 q = fin;  // (re_h, im_h, re_l, im_l)
         const float2 js = c_sqrt_fact2[j], ls = sd->l_scale2[beta], rs = sd->r_rowfact2[alpha];
         float sh, sl, th, tl, re_h, re_l, im_h, im_l;
         PrecSplit::mul(js.x, js.y, ls.x, ls.y, sh, sl);
         PrecSplit::mul(sh, sl, rs.x, rs.y, th, tl);
-        PrecSplit::mul(q.x, q.y, th, tl, re_h, re_l);
-        PrecSplit::mul(q.z, q.w, th, tl, im_h, im_l);
+        PrecSplit::mul(q.x, q.z, th, tl, re_h, re_l);
+        PrecSplit::mul(q.y, q.w, th, tl, im_h, im_l);
         __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(re_h + re_l, im_h + im_l));
         done = true;
         }
@@ -584,7 +584,7 @@ __global__ void convert_kernel(const double2* __restrict__ src, C* __restrict__ 
 }
 
 static size_t prec_bytes(int precision) {
-  return precision == BSG_PREC_FP64 ? sizeof(double2) : precision == BSG_PREC_SPLIT ? sizeof(float4) : sizeof(float2);
+  return precision == BSG_PREC_FP64 ? sizeof(double2) : precision == BSG_PREC_SPLIT ? sizeof(PrecSplit::C) : sizeof(float2);
 }
 
 // Converts n c128 values at src into the precision's storage type at dst.
@@ -596,8 +596,8 @@ static int convert_into(bsg_handle_t h, const double* src, int64_t n, int precis
     BSG_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * 16, cudaMemcpyDeviceToDevice, st));
   } else if (precision == BSG_PREC_SPLIT) {
     BSG_PROFILED(h, BSG_K_PREP, st, (double)n,
-                 (convert_kernel<float4><<<(unsigned)blocks, threads, 0, st>>>(
-                     reinterpret_cast<const double2*>(src), reinterpret_cast<float4*>(dst), n)));
+                 (convert_kernel<PrecSplit::C><<<(unsigned)blocks, threads, 0, st>>>(
+                     reinterpret_cast<const double2*>(src), reinterpret_cast<PrecSplit::C*>(dst), n)));
   } else {
     BSG_PROFILED(h, BSG_K_PREP, st, (double)n,
                  (convert_kernel<float2><<<(unsigned)blocks, threads, 0, st>>>(
@@ -803,7 +803,7 @@ static int launch_dp_t(bsg_handle_t h, DPArgs a, const Buckets& bk, bsg::DevBuf&
   // pipe takes a share of the items while the FP32 pipe runs the split DP.
   const int helper_bps = h->tune[BSG_TUNE_DP_FP64_BLOCKS];
   const bool helper = MODE == MODE_SITE && std::is_same<P, PrecSplit>::value && helper_bps > 0;
-  static_assert(sizeof(typename PrecF64::CA) == sizeof(typename P::CA) || !std::is_same<P, PrecSplit>::value, "");
+  static_assert(sizeof(typename PrecF64::CF) == sizeof(typename P::CF) || !std::is_same<P, PrecSplit>::value, "");
   BSG_CUDA(cudaFuncSetAttribute(dp_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 h->tune[BSG_TUNE_DP_L1_CARVEOUT]));
   int occ = 0;

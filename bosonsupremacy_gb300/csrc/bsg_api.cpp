@@ -126,7 +126,15 @@ int bsg_handle_s::ensure_aux() {
   BSG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
   BSG_CUDA(cudaStreamCreateWithFlags(&aux_stream, cudaStreamNonBlocking));
   for (auto& s : grp) BSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest));
-  for (auto& s : dp_lo) BSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least));
+  // the DP streams of the whole-MPS build's groups (right, left, middle)
+  // rank below the factorisation streams and among themselves in the order
+  // the groups should finish (right, middle, left): with one shared level
+  // the middle group's later launches queue behind the left group's blocks
+  // and both groups finish at the end of the build, which bunches up their
+  // host downloads
+  const int dp_prio[3] = {std::min(least, std::max(greatest + 1, least - 2)), least,
+                          std::min(least, std::max(greatest + 1, least - 1))};
+  for (int g = 0; g < 3; ++g) BSG_CUDA(cudaStreamCreateWithPriority(&dp_lo[g], cudaStreamNonBlocking, dp_prio[g]));
   for (auto& s : copy) BSG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   BSG_CUDA(cudaEventCreateWithFlags(&aux_fork, cudaEventDisableTiming));
   BSG_CUDA(cudaEventCreateWithFlags(&aux_join, cudaEventDisableTiming));

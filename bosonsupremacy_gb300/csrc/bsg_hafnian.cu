@@ -1459,9 +1459,13 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // still in flight take SMs within about one quantum instead of waiting for
   // a whole DP launch.  No kernel waits on another; streams are ordered by
   // events only.
+  // Host outputs take a smaller left group (a quarter of the cuts instead of
+  // a third): it finishes last, and what it leaves to download after the
+  // build is the tail of the end-to-end time (M=144: 115.4 -> 113.5 ms, the
+  // device-resident build 108.3 -> 109.2 ms, so it keeps a third).
   int T1 = 0, T2 = nc;
   if (nc >= 6) {
-    T1 = nc / 3;
+    T1 = gammas_pinned ? nc / 4 : nc / 3;
     T2 = nc - nc / 4;
   }
   struct Group {

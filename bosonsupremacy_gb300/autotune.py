@@ -1,7 +1,8 @@
 """Autotuner for the launch parameters of the hafnian DP kernel.
 
-Each DP warp keeps its items' class-pair (A) and DP-state (F) tables in a
-per-warp scratch slice sized for the largest program of its launch.  The
+Each DP warp keeps its items' DP-state (F) ring in a per-warp scratch slice
+sized for the largest program of its launch (the class-pair values come
+straight from the site's Sigma).  The
 items are split into two launches by table size (programs with at most
 `small_entries` table entries run with small slices), and the number of
 resident warps is capped by a scratch budget.  The best split point,

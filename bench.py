@@ -411,16 +411,23 @@ def main():
         # hi/lo pairs, 12 operations each, issued as 24 packed f32x2
         # instructions; plain FP32: 4 FMAs)
         ops = {"split": 48.0, "fp32": 4.0}[args.precision]
+        # The arithmetic's own ceiling: the FP32 pipe runs one operation per
+        # lane and cycle (half its FMA flop peak), and a complex multiply-add
+        # (8 algorithmic flops) costs `ops` of them, so the most this
+        # arithmetic can deliver is 8 * (pk32 / 2) / ops algorithmic flop/s.
+        ceiling = 8.0 * (pk32.value / 2.0) / ops
         roof = {"kernel": f"dp_kernel<Prec{'Split' if args.precision == 'split' else 'F32'}> (hafnian DP)",
-                "bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": pk32.value / 1e12, "unit": "TFLOP/s",
-                "frac": achieved / pk32.value, "traffic": None,
-                # the pipe runs one operation per lane and cycle: half the FMA flop peak
-                "fp32_ops_frac": ops * (achieved / 8.0) / (pk32.value / 2.0),
+                "bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": ceiling / 1e12, "unit": "TFLOP/s",
+                "frac": achieved / ceiling, "traffic": None,
+                "fp32_flop_peak": pk32.value / 1e12,
+                "frac_of_fp32_flop_peak": achieved / pk32.value,
                 "fp64_equivalent_frac": achieved / pk64.value,
-                "note": ("split arithmetic runs 48 FP32 operations per complex multiply-add (24 packed f32x2 "
-                         "instructions); fp32_ops_frac = those operations per second over the FP32 pipe's "
-                         "operation rate (live launch durations, which overlap other kernels); "
-                         "fp64_equivalent_frac compares the FP64-accurate result rate with the FP64 pipe's peak")}
+                "note": (f"{'split arithmetic runs 48 FP32 operations (24 packed f32x2 instructions)' if args.precision == 'split' else 'FP32 arithmetic runs 4 FMAs'} "
+                         "per complex multiply-add; peak = the FP32 pipe's measured operation rate (half its FMA flop "
+                         "peak) / those operations x 8 algorithmic flops, so frac is the FP32 pipe's busy fraction; "
+                         "achieved uses live launch durations, which overlap other kernels; frac_of_fp32_flop_peak "
+                         "divides the 8-flop work by the FMA flop peak; fp64_equivalent_frac compares the "
+                         "FP64-accurate result rate with the FP64 pipe's peak")}
     roof["peak_source"] = "measured on this GPU by bsg_fma_peak (register FMA loop on every SM)"
     roof["work"] = ("8 flops per complex multiply-add of the repetition-aware partition programs "
                     f"({prof[dom]['work'] / args.steps:.4g} per build)")

@@ -406,6 +406,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     for (size_t t = tid; t < nn; t += nt) {
       const int i = int(t / n), j = int(t % n);
       double s = 0.0;
+#pragma unroll 8
       for (int r = 0; r < n; ++r) s += Gm[(size_t)r * n + i] * Gm[(size_t)r * n + j];
       H[t] = s;
     }
@@ -451,6 +452,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     for (size_t t = tid; t < (size_t)n * nA; t += nt) {
       const int i = int(t / nA), j = int(t % nA);
       double s = 0.0;
+#pragma unroll 8
       for (int r = 0; r <= i; ++r) s += W[(size_t)i * n + r] * X2[(size_t)j * n + r];
       H[t] = s;
     }
@@ -565,6 +567,10 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     } else {
       for (int j = tid; j < n; j += nt) {  // t = W^T x (W lower triangular)
         double s = 0.0;
+        // unrolled: the FMA chain is serial, so the loads of the next 8
+        // terms must be in flight (the workspace lives in L2 / DRAM while the
+        // DP runs); the summation order, and so the result, is unchanged
+#pragma unroll 8
         for (int i = j; i < n; ++i) s = fma(W[(size_t)i * n + j], x[i], s);
         tv[j] = s;
       }
@@ -592,6 +598,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
     __syncthreads();
     for (int i = tid; i < n; i += nt) {
       double s = v[i];
+#pragma unroll 8
       for (int av = a0; av < a1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
       v[i] = s;
     }

@@ -159,8 +159,12 @@ __global__ void lambda_kernel(const double* __restrict__ res, int chi, double er
 
 // ---------------------------------------------------------------------------
 // Site classification: scatter every even-order (a, b, j) item into the
-// bucket of its partition program.  Rows are visited in key-sorted order so
-// that a warp usually shares one bucket (one aggregated atomic).
+// bucket of its partition program.  Rows are visited in key-sorted order, so
+// the items of one (j, left key group, right key group) combination are the
+// |gl| x |gr| row pairs of two contiguous ranges: the host gives each
+// combination its offset inside its bucket and an item's slot follows from
+// the ranks of its rows inside their groups (no atomics; consecutive left
+// rows land in consecutive slots).
 // ---------------------------------------------------------------------------
 struct SitePlanDev {
   const int32_t* perm_l;     // sorted position -> left row
@@ -168,44 +172,31 @@ struct SitePlanDev {
   const int32_t* perm_r;
   const int32_t* grp_r;
   const int32_t* bucket_of;  // [d][ngl][ngr] -> global bucket or -1 (odd order)
+  const int32_t* combo_off;  // [d][ngl][ngr] -> first slot of the combination inside its bucket
+  const int32_t* gstart_l;   // [ngl] sorted position of the group's first row
+  const int32_t* gcnt_l;     // [ngl] rows of the group
+  const int32_t* gstart_r;   // [ngr]
   const int32_t* bucket_off; // [nb] first slot
-  int32_t* cursor;           // [nb]
   int32_t* items;            // slots
   int ngl, ngr, kl, kr, d;
 };
 
 // One launch per set of sites (blockIdx.y = site).  A thread takes one (right
-// row, left row) pair in key-sorted order and scatters its even-order items
-// over j, so the row lookups happen once per pair and consecutive lanes
-// usually share a bucket (one aggregated atomic per bucket and j).
+// row, left row) pair in key-sorted order and writes its even-order items
+// over j, so the row lookups happen once per pair.
 __global__ void site_scatter_kernel(const SitePlanDev* __restrict__ plans) {
   const SitePlanDev p = plans[blockIdx.y];
   const int64_t total = (int64_t)p.kr * p.kl;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
-    const int64_t i = base + threadIdx.x;
-    const bool in = i < total;
-    int gl = 0, gr = 0;
-    int32_t ab = 0;
-    if (in) {
-      const int bs = int(i % p.kl), as = int(i / p.kl);
-      gl = p.grp_l[bs];
-      gr = p.grp_r[as];
-      ab = (p.perm_r[as] << 20) | (p.perm_l[bs] << 8);
-    }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const int bs = int(i % p.kl), as = int(i / p.kl);
+    const int gl = p.grp_l[bs], gr = p.grp_r[as];
+    const int32_t within = (as - p.gstart_r[gr]) * p.gcnt_l[gl] + (bs - p.gstart_l[gl]);
+    const int32_t ab = (p.perm_r[as] << 20) | (p.perm_l[bs] << 8);
     for (int j = 0; j < p.d; ++j) {
-      const int bucket = in ? p.bucket_of[((size_t)j * p.ngl + gl) * p.ngr + gr] : -1;
-      const unsigned active = __ballot_sync(0xffffffffu, bucket >= 0);
-      if (bucket >= 0) {
-        const unsigned peers = __match_any_sync(active, bucket);
-        const int leader = __ffs(peers) - 1;
-        const int rank = __popc(peers & ((1u << lane) - 1));
-        int slot0 = 0;
-        if (lane == leader) slot0 = atomicAdd(&p.cursor[bucket], __popc(peers));
-        slot0 = __shfl_sync(peers, slot0, leader);
-        p.items[p.bucket_off[bucket] + slot0 + rank] = ab | j;
-      }
+      const size_t o = ((size_t)j * p.ngl + gl) * p.ngr + gr;
+      const int bucket = p.bucket_of[o];
+      if (bucket >= 0) p.items[p.bucket_off[bucket] + p.combo_off[o] + within] = ab | j;
     }
   }
 }
@@ -695,7 +686,7 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
 // of every (j, left group, right group) combination.
 struct SitePlanHost {
   int KL = 0, KR = 0, ngl = 0, ngr = 0, d = 0;
-  std::vector<int32_t> perm_l, grp_l, perm_r, grp_r, bucket_of;
+  std::vector<int32_t> perm_l, grp_l, perm_r, grp_r, bucket_of, combo_off, gstart_l, gcnt_l, gstart_r;
 };
 
 static void group_rows(const uint64_t* key, int rows, std::vector<int32_t>& perm, std::vector<int32_t>& grp,
@@ -1049,6 +1040,15 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
     const SiteCombos& c = cb[s];
     std::unordered_map<int32_t, int32_t> local;
     sp.bucket_of.assign(c.keys.size(), -1);
+    sp.combo_off.assign(c.keys.size(), 0);
+    sp.gstart_l.assign(sp.ngl, 0);
+    sp.gcnt_l.assign(sp.ngl, 0);
+    sp.gstart_r.assign(sp.ngr, 0);
+    for (int g = 0, at = 0; g < sp.ngl; at += int(c.gc_l[g]), ++g) {
+      sp.gstart_l[g] = at;
+      sp.gcnt_l[g] = int32_t(c.gc_l[g]);
+    }
+    for (int g = 0, at = 0; g < sp.ngr; at += int(c.gc_r[g]), ++g) sp.gstart_r[g] = at;
     for (int j = 0; j < d; ++j)
       for (int gl = 0; gl < sp.ngl; ++gl)
         for (int gr = 0; gr < sp.ngr; ++gr) {
@@ -1066,6 +1066,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
           } else {
             b = it->second;
           }
+          sp.combo_off[o] = int32_t(lcount[s][b]);
           lcount[s][b] += c.gc_l[gl] * c.gc_r[gr];
           sp.bucket_of[o] = b;
         }
@@ -1130,7 +1131,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   BSG_TRY(programs_upload(ps, st));
   const int nb = int(bk.progs.size());
 
-  // one plan buffer: site descs, per-site tables, bucket offsets/cursors/chunks/programs/sites, counters
+  // one plan buffer: site descs, per-site tables, bucket offsets/chunks/programs/sites, counters
   auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
   size_t off = 0;
   auto carve = [&](size_t bytes) {
@@ -1140,7 +1141,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   };
   const size_t o_desc = carve(sizeof(SiteDesc) * ns);
   const size_t o_lsj = carve(sizeof(LeftScaleJob) * ns);
-  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns), o_lsd(ns), o_lsf(ns);
+  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns), o_co(ns), o_gsl(ns), o_gcl(ns), o_gsr(ns),
+      o_lsd(ns), o_lsf(ns);
   int max_kl = 1;
   for (int s = 0; s < ns; ++s) {
     o_lsd[s] = carve((size_t)in[s].KL * 8);
@@ -1151,8 +1153,12 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     o_pr[s] = carve(plans[s].perm_r.size() * 4);
     o_gr[s] = carve(plans[s].grp_r.size() * 4);
     o_bo[s] = carve(plans[s].bucket_of.size() * 4);
+    o_co[s] = carve(plans[s].combo_off.size() * 4);
+    o_gsl[s] = carve(plans[s].gstart_l.size() * 4);
+    o_gcl[s] = carve(plans[s].gcnt_l.size() * 4);
+    o_gsr[s] = carve(plans[s].gstart_r.size() * 4);
   }
-  const size_t o_boff = carve((size_t)nb * 4 + 4), o_cur = carve((size_t)nb * 4 + 4);
+  const size_t o_boff = carve((size_t)nb * 4 + 4);
   const size_t o_bch = carve((size_t)nb * 4 + 4), o_bpr = carve((size_t)nb * 4 + 4),
                o_bsi = carve((size_t)nb * 4 + 4), o_ctr = carve(16), o_sp = carve(sizeof(SitePlanDev) * ns);
   const size_t plan_bytes = off;
@@ -1199,9 +1205,12 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     std::memcpy(hp + o_pr[s], plans[s].perm_r.data(), plans[s].perm_r.size() * 4);
     std::memcpy(hp + o_gr[s], plans[s].grp_r.data(), plans[s].grp_r.size() * 4);
     std::memcpy(hp + o_bo[s], plans[s].bucket_of.data(), plans[s].bucket_of.size() * 4);
+    std::memcpy(hp + o_co[s], plans[s].combo_off.data(), plans[s].combo_off.size() * 4);
+    std::memcpy(hp + o_gsl[s], plans[s].gstart_l.data(), plans[s].gstart_l.size() * 4);
+    std::memcpy(hp + o_gcl[s], plans[s].gcnt_l.data(), plans[s].gcnt_l.size() * 4);
+    std::memcpy(hp + o_gsr[s], plans[s].gstart_r.data(), plans[s].gstart_r.size() * 4);
   }
   std::memcpy(hp + o_boff, bk.offsets.data(), (size_t)nb * 4);
-  std::memset(hp + o_cur, 0, (size_t)nb * 4 + 4);
   if (nb) {
     std::memcpy(hp + o_bch, bk.chunk_start.data(), (size_t)(nb + 1) * 4);
     std::memcpy(hp + o_bpr, bk.progs.data(), (size_t)nb * 4);
@@ -1214,11 +1223,11 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   int64_t max_pairs = 1;
   for (int s = 0; s < ns; ++s) {
     const SitePlanHost& p = plans[s];
-    hsp[s] = SitePlanDev{reinterpret_cast<int32_t*>(dp + o_pl[s]), reinterpret_cast<int32_t*>(dp + o_gl[s]),
-                         reinterpret_cast<int32_t*>(dp + o_pr[s]), reinterpret_cast<int32_t*>(dp + o_gr[s]),
-                         reinterpret_cast<int32_t*>(dp + o_bo[s]), reinterpret_cast<int32_t*>(dp + o_boff),
-                         reinterpret_cast<int32_t*>(dp + o_cur),   d_items,
-                         p.ngl, p.ngr, p.KL, p.KR, p.d};
+    auto dptr = [&](size_t o) { return reinterpret_cast<int32_t*>(dp + o); };
+    hsp[s] = SitePlanDev{dptr(o_pl[s]),  dptr(o_gl[s]),  dptr(o_pr[s]), dptr(o_gr[s]), dptr(o_bo[s]),
+                         dptr(o_co[s]),  dptr(o_gsl[s]), dptr(o_gcl[s]), dptr(o_gsr[s]), dptr(o_boff),
+                         d_items,        p.ngl,          p.ngr,          p.KL,           p.KR,
+                         p.d};
     max_pairs = std::max<int64_t>(max_pairs, (int64_t)p.KL * p.KR);
   }
   BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));

@@ -201,6 +201,17 @@ __global__ void site_scatter_kernel(const SitePlanDev* __restrict__ plans) {
   }
 }
 
+// The padding slots of each bucket (from its last item to its chunk end,
+// fewer than 32) hold -1, which the DP reads as "no item"; a warp per bucket.
+__global__ void pad_items_kernel(const int32_t* __restrict__ bucket_end, const int32_t* __restrict__ bucket_chunk,
+                                 int nb, int32_t* __restrict__ items) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = int(t >> 5);
+  if (b >= nb) return;
+  const int64_t slot = (int64_t)bucket_end[b] + (t & 31);
+  if (slot < (int64_t)bucket_chunk[b + 1] * 32) items[slot] = -1;
+}
+
 // ---------------------------------------------------------------------------
 // The DP kernel
 // ---------------------------------------------------------------------------
@@ -1158,7 +1169,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     o_gcl[s] = carve(plans[s].gcnt_l.size() * 4);
     o_gsr[s] = carve(plans[s].gstart_r.size() * 4);
   }
-  const size_t o_boff = carve((size_t)nb * 4 + 4);
+  const size_t o_boff = carve((size_t)nb * 4 + 4), o_bend = carve((size_t)nb * 4 + 4);
   const size_t o_bch = carve((size_t)nb * 4 + 4), o_bpr = carve((size_t)nb * 4 + 4),
                o_bsi = carve((size_t)nb * 4 + 4), o_ctr = carve(16), o_sp = carve(sizeof(SitePlanDev) * ns);
   const size_t plan_bytes = off;
@@ -1211,6 +1222,10 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     std::memcpy(hp + o_gsr[s], plans[s].gstart_r.data(), plans[s].gstart_r.size() * 4);
   }
   std::memcpy(hp + o_boff, bk.offsets.data(), (size_t)nb * 4);
+  {
+    int32_t* hend = reinterpret_cast<int32_t*>(hp + o_bend);
+    for (int b = 0; b < nb; ++b) hend[b] = bk.offsets[b] + int32_t(bk.counts[b]);
+  }
   if (nb) {
     std::memcpy(hp + o_bch, bk.chunk_start.data(), (size_t)(nb + 1) * 4);
     std::memcpy(hp + o_bpr, bk.progs.data(), (size_t)nb * 4);
@@ -1237,7 +1252,10 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   const size_t esz = out_c128 ? 16 : 8;
   for (int s = 0; s < ns; ++s) BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, (size_t)chi * chi * d * esz, st));
   if (bk.slots == 0) return BSG_OK;
-  BSG_CUDA(cudaMemsetAsync(d_items, 0xff, (size_t)bk.slots * 4, st));
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)nb * 32,
+               (pad_items_kernel<<<unsigned(((int64_t)nb * 32 + 255) / 256), 256, 0, st>>>(
+                   reinterpret_cast<const int32_t*>(dp + o_bend), reinterpret_cast<const int32_t*>(dp + o_bch), nb,
+                   d_items)));
   {
     // all sites in one launch: blocks per site so the launch covers ~8 blocks per SM
     const int64_t per_site = std::max<int64_t>(1, ((int64_t)h->num_sms * 8 + ns - 1) / ns);

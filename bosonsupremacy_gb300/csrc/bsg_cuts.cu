@@ -541,9 +541,9 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   // the candidate with the largest residual after projecting out the pairs
   // already taken (pivoted Gram-Schmidt), so a degenerate eigenspace of any
   // dimension (e.g. the nu = 1 vacuum modes) is always completed.  The
-  // candidates' residuals are tracked in FP32 (pivot choice only); the chosen
-  // FP64 eigenvector (not its FP32 copy) is cleaned by one FP64 projection
-  // against the accepted vectors of the cluster.
+  // candidates' squared residuals are tracked in FP32 by subtraction (pivot
+  // choice only); the chosen FP64 eigenvector (not its FP32 copy) is cleaned
+  // by one FP64 projection against the accepted vectors of the cluster.
   // 1/nu of each pair is |G x| (x a unit eigenvector: |G x|^2 = mu).
   double* Xacc = H;  // accepted vectors as rows
   float* c32 = reinterpret_cast<float*>(X2 + nn);       // FP32 candidates of the cluster
@@ -687,10 +687,12 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       }
       if (tid == 0) MU[acc / 2] = sqrt(gx);  // 1/nu of pair acc/2 (MU no longer needed by candidates)
       __syncthreads();
-      // FP32 tracking: project x and y out of the remaining candidates
+      // FP32 tracking: the candidates stay as they are (orthonormal); a
+      // candidate's squared residual against the accepted orthonormal pairs
+      // is |u|^2 - sum (a . u)^2, so each step subtracts (x . u)^2 + (y . u)^2
       for (int r = tid >> 5; r < C; r += nt >> 5) {
         if (used[cb + r]) continue;
-        float* w = c32 + (size_t)r * n;
+        const float* w = c32 + (size_t)r * n;
         float sx = 0.f, sy = 0.f;
         for (int i = tid & 31; i < n; i += 32) {
           sx = fmaf(xy32[i], w[i], sx);
@@ -700,14 +702,7 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
           sx += __shfl_xor_sync(0xffffffffu, sx, o);
           sy += __shfl_xor_sync(0xffffffffu, sy, o);
         }
-        float rn = 0.f;
-        for (int i = tid & 31; i < n; i += 32) {
-          const float v = w[i] - sx * xy32[i] - sy * xy32[n + i];
-          w[i] = v;
-          rn = fmaf(v, v, rn);
-        }
-        for (int o = 16; o > 0; o >>= 1) rn += __shfl_xor_sync(0xffffffffu, rn, o);
-        if ((tid & 31) == 0) r32[r] = rn;
+        if ((tid & 31) == 0) r32[r] -= sx * sx + sy * sy;
       }
       __syncthreads();
       acc += 2;

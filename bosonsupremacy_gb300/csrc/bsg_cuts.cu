@@ -550,6 +550,12 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
   float* r32 = reinterpret_cast<float*>(X2 + 2 * nn);   // their squared residuals
   float* xy32 = r32 + n;                                 // FP32 copies of x and y
   double* tv = X2;                                       // 2n doubles: W^T x and Omega W^T x
+  // The triangular W^T x and the projection update are sums per output of up
+  // to n terms: with one thread per output only n of the CTA's threads would
+  // work, so each sum is split into `segs` ranges whose partial sums (part,
+  // segs x n doubles after tv in X2) are added in range order.
+  const int segs = n >= 6 ? max(1, min(4, nt / n)) : 1;
+  double* part = X2 + 2 * (size_t)n;
   for (int i = tid; i < n; i += nt) vec2[i] = MU[order[i]];
   __syncthreads();
   int* used = reinterpret_cast<int*>(vec);  // n flags (vec reused as int storage)
@@ -565,16 +571,27 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
         if ((tid & 31) == 0) y[i] = s;
       }
     } else {
-      for (int j = tid; j < n; j += nt) {  // t = W^T x (W lower triangular)
+      for (int u = tid; u < n * segs; u += nt) {  // t = W^T x (W lower triangular)
+        const int j = u % n, g = u / n;
+        const int len = (n - j + segs - 1) / segs, i0 = j + g * len, i1 = min(n, i0 + len);
         double s = 0.0;
         // unrolled: the FMA chain is serial, so the loads of the next 8
         // terms must be in flight (the workspace lives in L2 / DRAM while the
-        // DP runs); the summation order, and so the result, is unchanged
+        // DP runs)
 #pragma unroll 8
-        for (int i = j; i < n; ++i) s = fma(W[(size_t)i * n + j], x[i], s);
-        tv[j] = s;
+        for (int i = i0; i < i1; ++i) s = fma(W[(size_t)i * n + j], x[i], s);
+        if (segs == 1) tv[j] = s;
+        else part[(size_t)g * n + j] = s;
       }
       __syncthreads();
+      if (segs > 1) {
+        for (int j = tid; j < n; j += nt) {
+          double s = part[j];
+          for (int g = 1; g < segs; ++g) s += part[(size_t)g * n + j];
+          tv[j] = s;
+        }
+        __syncthreads();
+      }
       for (int j = tid; j < n; j += nt) tv[n + j] = j < k ? tv[j + k] : -tv[j - k];  // Omega t
       __syncthreads();
       for (int i = tid >> 5; i < n; i += nt >> 5) {  // y = W (Omega t)
@@ -596,11 +613,29 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       if ((t & 31) == 0) dots[av - a0] = s;
     }
     __syncthreads();
-    for (int i = tid; i < n; i += nt) {
-      double s = v[i];
+    if (segs == 1) {
+      for (int i = tid; i < n; i += nt) {
+        double s = v[i];
 #pragma unroll 8
-      for (int av = a0; av < a1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
-      v[i] = s;
+        for (int av = a0; av < a1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
+        v[i] = s;
+      }
+    } else {
+      const int len = (a1 - a0 + segs - 1) / segs;
+      for (int u = tid; u < n * segs; u += nt) {
+        const int i = u % n, g = u / n;
+        const int b0 = a0 + g * len, b1 = min(a1, b0 + len);
+        double s = 0.0;
+#pragma unroll 8
+        for (int av = b0; av < b1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
+        part[(size_t)g * n + i] = s;
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += nt) {
+        double s = v[i];
+        for (int g = 0; g < segs; ++g) s += part[(size_t)g * n + i];
+        v[i] = s;
+      }
     }
     __syncthreads();
   };

@@ -176,6 +176,19 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
 // eigenvalues (the rest of Hm is overwritten).  s1, s2, s3: m*m doubles of
 // scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
 // the start tolerance of the refinement.
+// (i, j), i <= j, of entry p of an m x m upper triangle stored row by row
+// (row r holds m - r entries and starts at r m - r (r - 1) / 2)
+__device__ __forceinline__ void upper_index(int64_t p, int m, int& i, int& j) {
+  const double b = 2.0 * m + 1.0;
+  int r = int((b - sqrt(b * b - 8.0 * (double)p)) * 0.5);
+  auto start = [m](int64_t q) { return q * m - q * (q - 1) / 2; };
+  r = max(0, min(r, m - 1));
+  while (r > 0 && start(r) > p) --r;
+  while (r + 1 < m && start(r + 1) <= p) ++r;
+  i = r;
+  j = r + int(p - start(r));
+}
+
 __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
                             double* cs, double* sn, int* pos, float* jsm, unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -211,27 +224,36 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
   // (relative gaps ~1e-6, near-vacuum modes of middle cuts) by a few percent,
   // which three fixed steps left at ~1e-6.
   constexpr int kRefineMax = 8;
+  const size_t tri = (size_t)m * (m + 1) / 2;  // entries of an upper triangle (diagonal included)
   int refined = 0;
   for (int it = 0; it < kRefineMax; ++it) {
-    // s1 = R = I - QT QT^T ; s2 = T = Hm QT^T
-    for (size_t t = tid; t < mm; t += nt) {
-      const int i = int(t / m), j = int(t % m);
-      double r = 0.0, h = 0.0;
-      for (int q = 0; q < m; ++q) {
-        const double xj = QT[(size_t)j * m + q];
-        r = fma(QT[(size_t)i * m + q], xj, r);
-        h = fma(Hm[(size_t)i * m + q], xj, h);
+    // s2 = T = Hm QT^T (all m^2 entries) and s1 = R = I - QT QT^T (symmetric:
+    // its upper triangle, mirrored), one pass over both index sets
+    for (size_t t = tid; t < mm + tri; t += nt) {
+      if (t < mm) {
+        const int i = int(t / m), j = int(t % m);
+        double h = 0.0;
+        for (int q = 0; q < m; ++q) h = fma(Hm[(size_t)i * m + q], QT[(size_t)j * m + q], h);
+        s2[t] = h;
+      } else {
+        int i, j;
+        upper_index(int64_t(t - mm), m, i, j);
+        double r = 0.0;
+        for (int q = 0; q < m; ++q) r = fma(QT[(size_t)i * m + q], QT[(size_t)j * m + q], r);
+        r = (i == j ? 1.0 : 0.0) - r;
+        s1[(size_t)i * m + j] = r;
+        s1[(size_t)j * m + i] = r;
       }
-      s1[t] = (i == j ? 1.0 : 0.0) - r;
-      s2[t] = h;
     }
     __syncthreads();
-    // s3 = S = QT T
-    for (size_t t = tid; t < mm; t += nt) {
-      const int i = int(t / m), j = int(t % m);
+    // s3 = S = QT T = QT Hm QT^T (symmetric: its upper triangle, mirrored)
+    for (size_t t = tid; t < tri; t += nt) {
+      int i, j;
+      upper_index(int64_t(t), m, i, j);
       double acc = 0.0;
       for (int q = 0; q < m; ++q) acc = fma(QT[(size_t)i * m + q], s2[(size_t)q * m + j], acc);
-      s3[t] = acc;
+      s3[(size_t)i * m + j] = acc;
+      s3[(size_t)j * m + i] = acc;
     }
     __syncthreads();
     for (int i = tid; i < m; i += nt) lam[i] = s3[(size_t)i * m + i] / (1.0 - s1[(size_t)i * m + i]);

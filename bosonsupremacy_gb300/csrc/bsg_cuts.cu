@@ -470,12 +470,20 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       }
       __syncthreads();
     }
-    // F = W (L_A^{-1} C)^T  [n, nA] into H
+    // F = W (L_A^{-1} C)^T  [n, nA] into H.  The lanes of a warp take
+    // consecutive j, so L_A^{-1} C is read through its transpose (in Gm, free
+    // in this path) to keep the loads coalesced; same products, same order.
+    double* X2T = Gm;  // [n, nA]
+    for (size_t t = tid; t < (size_t)n * nA; t += nt) {
+      const int r = int(t / nA), j = int(t % nA);
+      X2T[t] = X2[(size_t)j * n + r];
+    }
+    __syncthreads();
     for (size_t t = tid; t < (size_t)n * nA; t += nt) {
       const int i = int(t / nA), j = int(t % nA);
       double s = 0.0;
 #pragma unroll 8
-      for (int r = 0; r <= i; ++r) s += W[(size_t)i * n + r] * X2[(size_t)j * n + r];
+      for (int r = 0; r <= i; ++r) s += W[(size_t)i * n + r] * X2T[(size_t)r * nA + j];
       H[t] = s;
     }
     __syncthreads();
@@ -508,11 +516,19 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
       }
       __syncthreads();
     }
-    // K = I - R R^T into X1, eigenvector rows of K (identity) into X2
+    // K = I - R R^T into X1, eigenvector rows of K (identity) into X2; R is
+    // read through its transpose (in Gm) for the j-consecutive lanes
+    double* RT = Gm;  // [nA, nA]
+    for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
+      const int q = int(t / nA), j = int(t % nA);
+      RT[t] = H[(size_t)j * nA + q];
+    }
+    __syncthreads();
     for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
       const int i = int(t / nA), j = int(t % nA);
       double s = 0.0;
-      for (int q = (i > j ? i : j); q < nA; ++q) s += H[(size_t)i * nA + q] * H[(size_t)j * nA + q];
+#pragma unroll 8
+      for (int q = (i > j ? i : j); q < nA; ++q) s += H[(size_t)i * nA + q] * RT[(size_t)q * nA + j];
       X1[t] = (i == j ? 1.0 : 0.0) - s;
     }
     __syncthreads();

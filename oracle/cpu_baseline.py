@@ -49,8 +49,14 @@ def recursion_macs(n: int) -> int:
 
 def group_sizes(cuts: Sequence[tuple], M: int, d: int, err_tol: float = 1e-10) -> List[Tuple[int, int]]:
     """(n, B) of every A_elem call the reference's site loop makes."""
-    out = []
+    return [g for site in site_group_sizes(cuts, M, d, err_tol) for g in site]
+
+
+def site_group_sizes(cuts: Sequence[tuple], M: int, d: int, err_tol: float = 1e-10) -> List[List[Tuple[int, int]]]:
+    """Per site, (n, B) of every A_elem call of that site (MPS_cpu.py:486-519)."""
+    per_site = []
     for site in range(M):
+        out: List[Tuple[int, int]] = []
         if site == 0:
             res, num, _ = cuts[0]
             keep = res > err_tol
@@ -77,7 +83,8 @@ def group_sizes(cuts: Sequence[tuple], M: int, d: int, err_tol: float = 1e-10) -
                     tot[int(a + b)] = tot.get(int(a + b), 0) + int(ca * cb)
             for j in range(d):
                 out += [(j + s, c) for s, c in tot.items() if not (j == 0 and s == 0)]
-    return out
+        per_site.append(out)
+    return per_site
 
 
 def _time_group(Sigma, n: int, B: int, rng) -> float:
@@ -149,5 +156,98 @@ def estimate_full_build(sq_cov: np.ndarray, d: int, chi: int, cuts: Sequence[tup
         "groups": len(groups),
         "items": int(sum(B for _, B in groups)),
         "sample_s": time.perf_counter() - t_sample0,
+        "sites_per_s": M / total,
+    }
+
+
+# ---- all host cores ----------------------------------------------------------
+# The reference's multi-process form (distributed_kron.py / distributed_MPS.py)
+# gives each rank whole cuts and whole sites.  Here every host core runs the
+# same timed sample at once (so the per-core costs include the memory and
+# clock contention of a fully loaded host), and the cuts, then the sites, are
+# spread over the cores longest first; the build time is the sum of the two
+# makespans.
+
+
+def _sample_worker(args) -> Dict[str, float]:
+    sq_cov, S_l, S_r, d, chi, budget_s, seed = args
+    rng = np.random.default_rng(seed)
+    M = sq_cov.shape[0] // 2
+    Lm = max(1, M // 2)
+    t0 = time.perf_counter()
+    R.get_cumsum_kron(sq_cov, Lm, chi=chi, max_dim=10 ** 5, cutoff=d)
+    t_cut = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    R.williamson(sq_cov)
+    t_will = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    U2, sq, U1 = R.get_U2_sq_U1(S_l, S_r)
+    Sigma = R.get_Sigma(U2, sq, U1)
+    t_bm = time.perf_counter() - t0
+    model = fit_site_model(Sigma, rng, budget_s=budget_s)
+    return dict(model, t_cut_step=t_cut / max(1, M - Lm - 1), t_will=t_will, t_bm=t_bm)
+
+
+def _makespan(costs: Sequence[float], procs: int) -> float:
+    """Longest-processing-time-first assignment of independent tasks."""
+    load = [0.0] * max(1, procs)
+    for c in sorted(costs, reverse=True):
+        i = min(range(len(load)), key=load.__getitem__)
+        load[i] += c
+    return max(load)
+
+
+def estimate_full_build_parallel(sq_cov: np.ndarray, d: int, chi: int, cuts: Sequence[tuple], procs: int,
+                                 budget_s: float = 20.0, seed: int = 0, timeout_s: float = 600.0) -> Dict[str, float]:
+    """Extrapolated wall time of the reference's build on `procs` host cores
+    (one process per core, one thread each).  Raises if a sample process
+    fails or the samples exceed `timeout_s`."""
+    import multiprocessing as mp
+    import os
+    from concurrent.futures import ProcessPoolExecutor
+
+    M = sq_cov.shape[0] // 2
+    site = max(1, min(M - 2, M // 2))
+    jobs = [(sq_cov, cuts[site][2], cuts[site - 1][2], d, chi, budget_s, seed + 1000 * w) for w in range(procs)]
+    saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    for k in saved:
+        os.environ[k] = "1"  # one thread per sample process (inherited at spawn)
+    ex = ProcessPoolExecutor(max_workers=procs, mp_context=mp.get_context("spawn"))
+    try:
+        futs = [ex.submit(_sample_worker, j) for j in jobs]
+        res = [f.result(timeout=timeout_s) for f in futs]
+        ex.shutdown(wait=True)
+    except BaseException:
+        # do not wait for a stuck sample process: stop this pool's own workers
+        procs_left = list(getattr(ex, "_processes", {}).values())
+        ex.shutdown(wait=False, cancel_futures=True)
+        for p in procs_left:
+            if p.is_alive():
+                p.kill()
+        raise
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    med = {k: float(np.median([r[k] for r in res])) for k in res[0]}
+    cut_costs = [med["t_cut_step"] * max(0, M - L - 1) for L in range(1, M)]
+    site_costs = []
+    for groups in site_group_sizes(cuts, M, d):
+        t = med["t_will"] + med["t_bm"]
+        for n, B in groups:
+            C = recursion_macs(n)
+            t += med["a"] * C + med["b"] * C * B + med["g"] * B * n * n + med["o"]
+        site_costs.append(t)
+    kron_s, mps_s = _makespan(cut_costs, procs), _makespan(site_costs, procs)
+    total = kron_s + mps_s
+    return {
+        "build_s": total,
+        "kron_s": kron_s,
+        "mps_s": mps_s,
+        "serial_s": float(sum(cut_costs) + sum(site_costs)),
+        "largest_site_s": float(max(site_costs)),
+        "procs": procs,
         "sites_per_s": M / total,
     }

@@ -186,11 +186,11 @@ int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, d
                   int precision, int out_dtype, void* const* gammas_host, double* Lambdas, double* res, int8_t* num,
                   double* S, int32_t* kept, bsg_stream_t stream);
 
-/* bsg_build_mps plus the download of its outputs: each group's Gammas are
- * copied from gammas_dev[i] (device) to gammas_pinned[i] (pinned host) as soon
- * as that group's DP is done, overlapping the copies with the rest of the
- * build, and the Lambdas to lambdas_pinned [M-1, chi] float64.  Returns after
- * every copy has landed. */
+/* bsg_build_mps plus the download of its outputs: each group's DP runs in four
+ * site parts and each part's Gammas are copied from gammas_dev[i] (device) to
+ * gammas_pinned[i] (pinned host) as soon as that part is done, overlapping the
+ * copies with the rest of the build, and the Lambdas to lambdas_pinned
+ * [M-1, chi] float64.  Returns after every copy has landed. */
 int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
                           double site_tol, int precision, int out_dtype, void* const* gammas_dev,
                           void* const* gammas_pinned, double* Lambdas, double* lambdas_pinned, double* res,
@@ -207,8 +207,9 @@ int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, in
  * every (level, photon number) group is one batched complex GEMM.
  * precision: BSG_PREC_FP64 (FP64 CUDA cores), BSG_PREC_FP32 (FP32 CUDA cores)
  * or BSG_PREC_SPLIT (3-way split TF32 products on the tcgen05 tensor cores,
- * FP32 accumulation).  Synchronises `stream` (plans the prefix tries on the
- * host). */
+ * FP32 accumulation).  Synchronises `stream`: the prefix tries are planned on
+ * the GPU, and the host reads each level's row counts to size its GEMM
+ * launches. */
 int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                            const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
 

@@ -9,9 +9,10 @@
 // Each level is a set of GEMMs, one per photon number n of the new site:
 //   left : L_i[rows(n)] = (L_{i-1}[parents] * Lambda_{i-1}) @ Gamma_i[:, :, n]
 //   right: R_i[rows(n)] = (R_{i+1}[parents] * Lambda_i)     @ Gamma_i[:, :, n]^T
-// Rows of a level are grouped by n on the host so every GEMM writes a
-// contiguous block.  The GEMM gathers its A rows by parent index and applies
-// Lambda on the fly.
+// Rows of a level are keyed n-major on the GPU (photon number, then parent
+// row), so every GEMM writes a contiguous block; the host reads the level's
+// row counts to size the launches.  The GEMM gathers its A rows by parent
+// index and applies Lambda on the fly.
 #include <algorithm>
 #include <cstring>
 #include <type_traits>

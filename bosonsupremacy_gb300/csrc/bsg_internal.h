@@ -228,7 +228,8 @@ struct bsg_handle_s {
   bsg::Profiler prof;
   // side streams for concurrent launches (created on first use) and events:
   // aux_stream (FP64 helper), grp[3] high-priority streams of the build
-  // groups, dp_lo[3] low-priority streams of the groups' DP
+  // groups, dp_lo[3] lower-priority streams of the groups' DP (ranked right >
+  // middle > left among themselves)
   cudaStream_t aux_stream = nullptr, grp[3] = {}, dp_lo[3] = {}, copy[2] = {};
   cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
   cudaEvent_t ev[25] = {};

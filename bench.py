@@ -30,6 +30,10 @@ if REPO not in sys.path:
 
 METRIC = "full-MPS build throughput (sites/s), split-precision batched kernels"
 UNIT = "sites/s"
+# DRAM bytes (read + write) per complex multiply-add of the split hafnian DP,
+# from the ncu capture of the M=144, d=8, chi=1024 build's DP launches
+# (profiles/dp_kernel_M144_d8_chi1024_traffic.md); None until captured.
+DP_DRAM_BYTES_PER_CMAC = None
 
 
 def parse():
@@ -47,6 +51,7 @@ def parse():
     p.add_argument("--no-contract", action="store_true")
     p.add_argument("--contract-workload", default="M50_d6_chi256")
     p.add_argument("--contract-photons", type=int, default=4)
+    p.add_argument("--no-largest", action="store_true")
     p.add_argument("--no-sampler", action="store_true")
     p.add_argument("--sampler-workload", default="M50_d6_chi256")
     p.add_argument("--sampler-n", type=int, default=100000)
@@ -135,6 +140,23 @@ def measured_peaks():
         with open(path) as f:
             return json.load(f)
     return {}
+
+
+def link_probe(dev_bufs, host_bufs, reps=2):
+    """Device-to-host link rate (GB/s): the best of `reps` bare copies of
+    every device buffer into its pinned host twin."""
+    import torch
+
+    nbytes = sum(b.numel() * b.element_size() for b in dev_bufs)
+    best = 0.0
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for h, d in zip(host_bufs, dev_bufs):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+        best = max(best, nbytes / (time.perf_counter() - t0) / 1e9)
+    return best
 
 
 def measure_contraction(args, lib, handle, peaks):
@@ -255,6 +277,68 @@ def measure_sampler(args, lib, handle, peaks):
     }
 
 
+def measure_largest(args, lib, handle):
+    """The largest single-GPU workload (M=216 banded, d=10, chi=2048; 72 GB
+    of complex64 Gamma): full-build time of the split build (CUDA events,
+    one untimed build first), the plain-FP64 build's time, and per cut /
+    site the error of the first 32: Lambda against the reference's FP64
+    kron_cpu.py weights (tests/golden/largest_M216.npz) and Gamma of the
+    split build against the FP64 build (max |difference| over the site's
+    largest entry)."""
+    import numpy as np
+    import torch
+
+    from bosonsupremacy_gb300 import synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps
+
+    cfg = synthetic.LARGEST
+    M, d, chi = cfg.M, cfg.d, cfg.chi
+    _, sq = synthetic.lossy_covariances(cfg)
+    fx = os.path.join(REPO, "tests", "golden", "largest_M216.npz")
+    ref = np.load(fx) if os.path.exists(fx) else None
+    if ref is not None:
+        sq = ref["sq_cov"]
+    sq_dev = torch.as_tensor(sq).cuda()
+    stream = torch.cuda.current_stream()
+
+    def timed(prec, out):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m = build_mps(sq_dev, d, chi, precision=prec, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), m
+
+    split = [torch.empty(chi, chi, d, dtype=torch.complex64, device="cuda") for _ in range(M)]
+    timed(args.precision, split)
+    ms, m = timed(args.precision, split)
+    n = 32
+    lam_err = None
+    if ref is not None:
+        res = m.res.cpu().numpy()
+        lam_err = []
+        for c in range(n):
+            k = int(ref["kept"][c])
+            a = np.sort(res[c, :k])[::-1]
+            b = ref["res"][c, :k]
+            big = b > 1e-10
+            lam_err.append(float((np.abs(np.sqrt(a[big]) - np.sqrt(b[big])) / np.sqrt(b[big])).max()))
+    # the FP64 build writes its first 32 sites to their own buffers and the
+    # rest over the split build's (not compared)
+    fp64 = [torch.empty(chi, chi, d, dtype=torch.complex64, device="cuda") for _ in range(n)] + split[n:]
+    ms64, _ = timed("fp64", fp64)
+    g_err = [float((split[i] - fp64[i]).abs().max().item() / fp64[i].abs().max().item()) for i in range(n)]
+    out = {"workload": cfg.label(), "build_ms": ms, "sites_per_s": M / (ms / 1e3), "fp64_build_ms": ms64,
+           "split_speedup": ms64 / ms,
+           "lambda_rel_err_vs_reference_kron_first32": lam_err,
+           "lambda_source": "tests/golden/largest_M216.npz (kron_cpu.py FP64-promoted, cuts 0-31)" if lam_err else None,
+           "gamma_err_split_vs_fp64_first32": g_err,
+           "note": "Gamma errors: max |split - fp64| / max |fp64| per site, both complex64"}
+    del split, fp64, m
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args, ws, rank):
     """The reference's own CPU MPS construction (oracle port of kron_cpu.py +
     MPS_cpu.py) on all the host's cores: each step runs one bounded timed
@@ -277,7 +361,9 @@ def run_reference(args, ws, rank):
     vals = []
     est = None
     note = None
+    step_s = []
     for i in range(args.warmup + args.steps):
+        t_step = time.perf_counter()
         try:
             est = cpu_baseline.estimate_full_build_parallel(sq, cfg.d, cfg.chi, cuts, procs,
                                                             budget_s=args.cpu_budget / 2, seed=i,
@@ -288,20 +374,23 @@ def run_reference(args, ws, rank):
             est = cpu_baseline.estimate_full_build(sq, cfg.d, cfg.chi, cuts, budget_s=args.cpu_budget / 2, seed=i)
         if i >= args.warmup:
             vals.append(est["sites_per_s"])
+            step_s.append(time.perf_counter() - t_step)
     v = statistics.median(vals)
     sample = (f"oracle (FP64 restatement of kron_cpu.py + MPS_cpu.py) on {procs} host cores, one process per "
               f"core: each timed one middle cut at max_dim=1e5, one williamson(sq_cov) + Bloch-Messiah and "
               f"~20 A_elem batches (n=6..12) fitted to the per-group cost model; the workload's cuts and "
-              f"sites (exact (j, size) groups) spread over the cores longest first; extrapolated, not a full run")
+              f"sites (exact (j, size) groups) spread over the cores longest first; value is the extrapolated "
+              f"full build, ms_per_step the wall time of one step's timed sample")
     if note:
         sample = note + "; " + sample
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * cfg.M / v, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(step_s), "higher_is_better": True,
+        "scaling": "weak",
         "vs_baseline": None, "dtype": "c128/f64", "data": "synthetic",
         "config": {"workload": cfg.label(), "M": cfg.M, "d": cfg.d, "chi": cfg.chi},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample,
-                         "extrapolated_build_s": est["build_s"],
+                         "extrapolated_build_s": est["build_s"], "extrapolated_ms_per_build": 1e3 * cfg.M / v,
                          "one_core_equivalent_s": est.get("serial_s", est["build_s"])},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -378,14 +467,32 @@ def main():
         fp64 = {"build_ms": t64, "sites_per_s": M / (t64 / 1e3), "split_speedup": t64 / ms}
         build_mps(sq_dev, d, chi, precision=args.precision, out=outs)  # restore outputs
 
+    # first build on a fresh handle: partition programs generated, scratch
+    # allocated and every table uploaded inside the timed region
+    cold = None
+    if rank == 0:
+        fresh = _lib.Handle(local)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs, handle=fresh)
+        torch.cuda.synchronize()
+        cold = {"ms": (time.perf_counter() - t0) * 1e3,
+                "note": "one build on a new library handle (empty program cache, no scratch yet), host clock"}
+        fresh.close()
+        del fresh
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
+
     # end to end through the public host API
     e2e = None
     if not args.no_e2e:
         host_sq = torch.as_tensor(sq).pin_memory()
         host_out = [torch.empty(chi, chi, d, dtype=torch.complex64, pin_memory=True) for _ in range(M)]
         host_lam = torch.empty(M - 1, chi, dtype=torch.float64, pin_memory=True)
-        build_mps_host(host_sq, d, chi, host_out, host_lam, precision=args.precision, device_out=outs)
+        # every pinned page touched twice before timing (first-touch / pinning costs stay outside)
+        for _ in range(2):
+            build_mps_host(host_sq, d, chi, host_out, host_lam, precision=args.precision, device_out=outs)
         torch.cuda.synchronize()
+        link_before = link_probe(outs, host_out)
         et = []
         for _ in range(args.steps):
             flush.fill_(1.0)
@@ -400,9 +507,16 @@ def main():
             t = torch.tensor([es], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             es = float(t.item())
+        link_after = link_probe(outs, host_out)
+        d2h = int(sum(o.numel() * 8 for o in host_out) + host_lam.numel() * 8)
         e2e = {"value": ws * M / es, "unit": UNIT, "h2d_bytes_per_step": int(host_sq.numel() * 8),
-               "d2h_bytes_per_step": int(sum(o.numel() * 8 for o in host_out) + host_lam.numel() * 8),
-               "ms_per_step": es * 1e3}
+               "d2h_bytes_per_step": d2h, "ms_per_step": es * 1e3,
+               "step_ms": {"min": min(et) * 1e3, "median": statistics.median(et) * 1e3, "max": max(et) * 1e3},
+               "link_d2h_gbs": {"before": link_before, "after": link_after,
+                                "note": "bare device-to-host copy of the same Gamma bytes into the same pinned "
+                                        "buffers (one cudaMemcpyAsync per site), timed just before and after the "
+                                        "e2e steps; the e2e floor is max(build, bytes / link rate)"},
+               "pinned": "torch pin_memory buffers, one per site, touched by two untimed e2e builds"}
 
     # roofline of the hafnian DP (the dominant kernel by SM-time: it is
     # ~15k of the ~19k SM-milliseconds of a build; the Williamson / Sigma
@@ -430,18 +544,23 @@ def main():
         # arithmetic can deliver is 8 * (pk32 / 2) / ops algorithmic flop/s.
         ceiling = 8.0 * (pk32.value / 2.0) / ops
         roof = {"kernel": f"dp_kernel<Prec{'Split' if args.precision == 'split' else 'F32'}> (hafnian DP)",
-                "bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": ceiling / 1e12, "unit": "TFLOP/s",
-                "frac": achieved / ceiling, "traffic": None,
-                "fp32_flop_peak": pk32.value / 1e12,
-                "frac_of_fp32_flop_peak": achieved / pk32.value,
+                "bound": "fp32-pipe", "achieved": achieved / 1e12, "peak": pk32.value / 1e12, "unit": "TFLOP/s",
+                "frac": achieved / pk32.value, "traffic": (DP_DRAM_BYTES_PER_CMAC * prof[dom]["work"] / max(1, prof[dom]["launches"])
+                            if DP_DRAM_BYTES_PER_CMAC else None),
+                "fp32_op_busy_frac": achieved / ceiling,
                 "fp64_equivalent_frac": achieved / pk64.value,
-                "note": (f"{'split arithmetic runs 48 FP32 operations (24 packed f32x2 instructions)' if args.precision == 'split' else 'FP32 arithmetic runs 4 FMAs'} "
-                         "per complex multiply-add; peak = the FP32 pipe's measured operation rate (half its FMA flop "
-                         "peak) / those operations x 8 algorithmic flops, so frac is the FP32 pipe's busy fraction; "
-                         "achieved uses live launch durations, which overlap other kernels; frac_of_fp32_flop_peak "
-                         "divides the 8-flop work by the FMA flop peak; fp64_equivalent_frac compares the "
-                         "FP64-accurate result rate with the FP64 pipe's peak")}
-    roof["peak_source"] = "measured on this GPU by bsg_fma_peak (register FMA loop on every SM)"
+                "note": ("achieved = 8 algorithmic flops per complex multiply-add of the partition programs over the "
+                         "live (CUDA-event) DP launch durations, which overlap the factorisations' kernels; peak = "
+                         "the FP32 FMA flop rate measured on this GPU by bsg_fma_peak (MEASURED_PEAKS.json has no "
+                         "CUDA-core peak); "
+                         f"{'the split arithmetic spends 48 FP32 operations (24 packed f32x2 instructions)' if args.precision == 'split' else 'FP32 arithmetic spends 4 FMAs'} "
+                         "per complex multiply-add, so fp32_op_busy_frac = achieved / (8 x half the FMA flop peak / "
+                         "those operations) is the FP32 pipe's busy fraction; fp64_equivalent_frac compares the "
+                         "FP64-accurate result rate with the FP64 pipe's measured peak; traffic = DRAM bytes per "
+                         "DP launch from the ncu capture of the M=144 build's DP launches, per complex "
+                         "multiply-add, times this launch's work (profiles/dp_kernel_M144_d8_chi1024_traffic.md)")}
+    roof["peak_source"] = "FMA peak measured on this GPU by bsg_fma_peak (register FMA loop on every SM)"
+    roof["launch_ms_mean"] = prof[dom]["ms"] / max(1, prof[dom]["launches"])
     roof["work"] = ("8 flops per complex multiply-add of the repetition-aware partition programs "
                     f"({prof[dom]['work'] / args.steps:.4g} per build)")
     roof["launches_per_build"] = prof[dom]["launches"] / args.steps
@@ -475,6 +594,12 @@ def main():
                           f"({est['items']} items); extrapolated full build {est['build_s']:.0f} s"),
                "extrapolated_build_s": est["build_s"]}
 
+    largest = None
+    if rank == 0 and not args.no_largest:
+        del outs
+        torch.cuda.empty_cache()
+        largest = measure_largest(args, lib, handle)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -487,7 +612,8 @@ def main():
             "clocks": clk, "gpu_launches": launches, "kernels": {k: {"ms": v["ms"], "launches": v["launches"]}
                                                                  for k, v in prof.items()},
             "host": {k: {"ms": v["ms"], "calls": v["launches"]} for k, v in host_prof.items()},
-            "roofline": roof, "fp64_path": fp64, "e2e": e2e, "cpu_baseline": cpu, "contraction": contraction, "sampler": sampler,
+            "roofline": roof, "fp64_path": fp64, "cold_build": cold, "e2e": e2e, "cpu_baseline": cpu, "contraction": contraction, "sampler": sampler,
+            "largest": largest,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

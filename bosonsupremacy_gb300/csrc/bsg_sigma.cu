@@ -54,8 +54,9 @@ __device__ __forceinline__ double apply_L(const SigmaJob& jb, int r, int c, cons
   return acc;
 }
 
-__global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob* __restrict__ jobs) {
-  const SigmaJob jb = jobs[blockIdx.x];
+// One CTA per call: the whole Sigma construction of one site (the
+// descriptor travels as a kernel parameter, so no host-to-device copy).
+__global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob jb) {
   const int Mr = jb.Mr, n2 = 2 * Mr;
   const int tid = threadIdx.x, nt = blockDim.x;
   double* P = jb.ws;                                     // [n2, n2]
@@ -560,15 +561,17 @@ extern "C" int bsg_first_sigma(bsg_handle_t h, const double* S_0, int M, const d
 // serving runtime that owns all of HBM), latency-critical loops that must not
 // pay the implicit device synchronisation of cudaMalloc/cudaFree, and plug-in
 // hosts that forbid raw device allocation.  bsg_site_sigma_noalloc serves
-// them: its scratch (the job descriptor, a status word and the Gauss-Jordan
-// workspace) is the file-scope device array below, sized for M_r <= 160
-// modes.  Every GPU that loads this library holds the array until the
-// process exits.
+// them: its scratch (a status word and the Gauss-Jordan workspace) is the
+// file-scope device array below, sized for M_r <= 160 modes; the job
+// descriptor is a kernel parameter.  Every GPU that loads this library holds
+// the array until the process exits.  The array's device address is looked
+// up once per device and kept, so the entry point does not survive a
+// cudaDeviceReset of that device (the array may move).
 // ---------------------------------------------------------------------------
 namespace bsg {
 constexpr int kNoAllocMaxModes = 160;
-constexpr size_t kNoAllocStatusOff = 256;
-constexpr size_t kNoAllocWsOff = 512;
+constexpr size_t kNoAllocStatusOff = 0;
+constexpr size_t kNoAllocWsOff = 256;
 constexpr size_t kNoAllocBytes = kNoAllocWsOff + 112ull * kNoAllocMaxModes * kNoAllocMaxModes + 256;  // ~2.75 MiB
 constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_sigma_scratch[kNoAllocBytes];
@@ -620,8 +623,7 @@ extern "C" int bsg_site_sigma_noalloc(const double* S_l, int m_l, const double* 
   jb.status = reinterpret_cast<int*>(base + kNoAllocStatusOff);
   // the status word must start at zero; the workspace is fully overwritten
   BSG_CUDA(cudaMemsetAsync(base + kNoAllocStatusOff, 0, 4, st));
-  BSG_CUDA(cudaMemcpyToSymbolAsync(g_noalloc_sigma_scratch, &jb, sizeof(SigmaJob), 0, cudaMemcpyHostToDevice, st));
-  sigma_kernel<<<1, 1024, 0, st>>>(reinterpret_cast<const SigmaJob*>(base));
+  sigma_kernel<<<1, 1024, 0, st>>>(jb);
   BSG_CUDA(cudaGetLastError());
   return BSG_OK;
 }

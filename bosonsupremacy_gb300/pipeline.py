@@ -32,9 +32,12 @@ class MPS:
 
 
 def build_mps(sq_cov, d: int, chi: int, precision="split", out_dtype=torch.complex64, err_tol: float = 1e-10,
-              cut_tol: float = 1e-12, device: int = 0, out: Optional[List[torch.Tensor]] = None) -> MPS:
+              cut_tol: float = 1e-12, device: int = 0, out: Optional[List[torch.Tensor]] = None,
+              handle: Optional[_lib.Handle] = None) -> MPS:
     """Whole MPS in one library call (bsg_build_mps).  ``out`` may supply the
-    M Gamma tensors to fill (reused across calls)."""
+    M Gamma tensors to fill (reused across calls); ``handle`` a library
+    handle other than the device's shared one (its own program cache and
+    scratch)."""
     dev = torch.device("cuda", device)
     sq = torch.as_tensor(sq_cov, dtype=torch.float64).to(dev).contiguous()
     M = sq.shape[0] // 2
@@ -48,7 +51,7 @@ def build_mps(sq_cov, d: int, chi: int, precision="split", out_dtype=torch.compl
     S = torch.empty(nc, 2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device=dev)
     kept = torch.empty(nc, dtype=torch.int32, device=dev)
     ptrs = (ctypes.c_void_p * M)(*[g.data_ptr() for g in out])
-    h = _lib.Handle.get(device)
+    h = handle if handle is not None else _lib.Handle.get(device)
     t0 = time.perf_counter()
     _lib.check(_lib.load().bsg_build_mps(h.h, sq.data_ptr(), M, d, chi, float(cut_tol), float(err_tol),
                                          ops._prec(precision), odt, ptrs, lam.data_ptr(), res.data_ptr(),

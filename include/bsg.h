@@ -97,7 +97,9 @@ int bsg_hafnian_matrices(bsg_handle_t h, const double* A, int n, int64_t B, int 
  * reference reaches through Bloch-Messiah, without the SVDs.
  * S_l: float64 [2 m_l, 2 m_l] with m_l = M_r - 1 (ignored when m_l == 0, the
  * last site); S_r: float64 [2 M_r, 2 M_r]; Sigma: c128 [2 M_r, 2 M_r];
- * Z: float64 [1].  Asynchronous. */
+ * Z: float64 [1].  Asynchronous: a singular A (impossible for a symplectic
+ * S, whose A satisfies A A^dag = I + B B^dag) is not reported by this call;
+ * bsg_build_mps checks it on its own status words. */
 int bsg_site_sigma(bsg_handle_t h, const double* S_l, int m_l, const double* S_r, int M_r, double* Sigma,
                    double* Z, bsg_stream_t stream);
 
@@ -111,8 +113,9 @@ int bsg_site_sigma(bsg_handle_t h, const double* S_l, int m_l, const double* S_r
  * M_r <= 160; larger M_r returns BSG_ERR_LIMIT.  The first call on a device
  * looks up that array's device address (make it before any stream capture).
  * Every call shares the array: calls that overlap on the GPU race, so issue
- * them on one stream or serialise them.  Same arguments and results as
- * bsg_site_sigma.  Asynchronous. */
+ * them on one stream or serialise them.  The array's address is kept per
+ * device, so a cudaDeviceReset of that device ends its use in this process.
+ * Same arguments and results as bsg_site_sigma.  Asynchronous. */
 int bsg_site_sigma_noalloc(const double* S_l, int m_l, const double* S_r, int M_r, double* Sigma, double* Z,
                            bsg_stream_t stream);
 

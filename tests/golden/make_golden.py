@@ -11,7 +11,7 @@ changes, the same ones the oracle's header names:
   * ``sys.argv`` set before exec (module-level argparse) and np.random seeded
     before the sampler (it is unseeded, sampling_cpu.py:37, 52, 92).
 
-Usage:  python tests/golden/make_golden.py [path/to/reference]
+Usage:  python tests/golden/make_golden.py REFERENCE_DIR
 The fixtures are small .npz files committed next to this script; the GPU machine
 never needs the reference itself.
 """
@@ -38,23 +38,26 @@ FP64 = [("'complex64'", "'complex128'"), ("'float32'", "'float64'"),
 TINY = GBSConfig("M8_d4_chi24", 8, 4, 24, 0.5, 1.0, 0.3, seed=7)
 
 
-def _source(ref: str, name: str) -> str:
+def _source(ref: str, name: str, extra=()) -> str:
     with open(os.path.join(ref, name)) as f:
         src = f.read()
-    for a, b in FP64:
+    for a, b in list(FP64) + list(extra):
+        if a not in src and (a, b) in extra:
+            raise ValueError(f"{name}: substitution target not found: {a!r}")
         src = src.replace(a, b)
     return src
 
 
-def run_ref(ref: str, name: str, argv, as_main: bool):
-    """exec one reference script; returns its namespace."""
+def run_ref(ref: str, name: str, argv, as_main: bool, extra=()):
+    """exec one reference script; returns its namespace.  ``extra`` holds
+    further (old, new) source substitutions (e.g. a site filter)."""
     np.product = np.prod  # numpy 2.x shim
     ns = {"__name__": "__main__" if as_main else "ref_" + name[:-3]}
     old = sys.argv
     sys.argv = [name] + list(argv)
     try:
         with contextlib.redirect_stdout(io.StringIO()):
-            exec(compile(_source(ref, name), os.path.join(ref, name), "exec"), ns)
+            exec(compile(_source(ref, name, extra), os.path.join(ref, name), "exec"), ns)
     finally:
         sys.argv = old
     return ns
@@ -159,7 +162,9 @@ def pipeline(ref: str, cfg: GBSConfig, full_gamma: bool, n_samples: int, out: st
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py REFERENCE_DIR")
+    ref = sys.argv[1]
     hafnian_kat(ref, os.path.join(HERE, "hafnian_kat.npz"))
     pipeline(ref, TINY, full_gamma=True, n_samples=2000, out=os.path.join(HERE, "tiny_M8.npz"))
     pipeline(ref, SMALL, full_gamma=False, n_samples=10000, out=os.path.join(HERE, "small_M16.npz"), n_big=100000)

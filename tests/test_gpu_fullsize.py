@@ -81,16 +81,20 @@ def test_host_output_build_matches_device_build_at_full_size(full_builds):
         assert torch.equal(split.Gammas[i], gh[i].to(split.Gammas[i].device, non_blocking=False)), i
 
 
-def test_largest_banded_workload_properties(cuda):
+def test_largest_banded_workload_properties(cuda, golden):
     """M=216, d=10, chi=2048, banded interferometer (72 GB of Gamma): the build
     completes, every Gamma is finite and non-zero, every cut keeps between 1
     and chi rows with positive, sorted weights summing to <= 1, and Lambda is
-    the square root of the kept weights above the site tolerance."""
+    the square root of the kept weights above the site tolerance.  The first
+    32 cuts' Schmidt values match the reference's FP64 kron_cpu.py
+    (tests/golden/largest_M216.npz) to 1e-8 relative, with the same kept
+    counts."""
     import torch
     from bosonsupremacy_gb300 import synthetic
     from bosonsupremacy_gb300.pipeline import build_mps
     cfg = synthetic.LARGEST
-    _, sq = synthetic.lossy_covariances(cfg)
+    ref = golden("largest_M216.npz")
+    sq = ref["sq_cov"]
     m = build_mps(sq, cfg.d, cfg.chi, precision="split")
     try:
         for i, g in enumerate(m.Gammas):
@@ -105,6 +109,15 @@ def test_largest_banded_workload_properties(cuda):
             assert (w > 0).all() and (np.diff(w) <= 0).all() and w.sum() <= 1.0 + 1e-9, c
             big = w > 1e-10
             assert np.allclose(lam[c, :k][big], np.sqrt(w[big]), rtol=1e-12, atol=0.0), c
+        errs = []
+        for c in range(len(ref["kept"])):
+            k = int(ref["kept"][c])
+            assert int(m.kept[c]) == k, (c, int(m.kept[c]), k)
+            a, b = np.sort(res[c, :k])[::-1], ref["res"][c, :k]
+            big = b > 1e-10
+            errs.append(float((np.abs(np.sqrt(a[big]) - np.sqrt(b[big])) / np.sqrt(b[big])).max()))
+        print(f"M=216 first 32 cuts: Lambda rel err max {max(errs):.3e}")
+        assert max(errs) <= 1e-8, errs
     finally:
         del m
         torch.cuda.empty_cache()

@@ -76,3 +76,46 @@ def test_sampler_first_batch_of_1e5_matches_reference(golden):
     rng = np.random.RandomState(int(t["big_sample_seed"]))
     s = R.sample(G, Lam, sqrtW, d + 2, int(t["big_sample_batch"]), rng)
     assert np.array_equal(s[:256], t["big_sample_head"])
+
+
+def test_large_config_cut_spectra(golden):
+    """The oracle's truncation to chi against kron_cpu.py on the M=144, d=8,
+    chi=1024 workload (tests/golden/large_M144.npz): weights of the first,
+    two middle and the last cut to 1e-10 relative (LAPACK's thread count
+    moves the near-vacuum nu in their last bits, ~1e-11 in the weights),
+    and the label rows of the two middle cuts
+    the site-71 fixture was built from.  Rows of equal weight may come in
+    another order (argsort ties, kron_cpu.py:113, 122), so the labels are
+    compared as sets.  The Williamson symplectics differ by a rotation inside
+    the near-degenerate (nu ~ 1) blocks, whose basis LAPACK leaves free, so
+    S is checked for what fixes it: S Omega S^T = Omega and S^-1 V S^-T
+    diagonal."""
+    t = golden("large_M144.npz")
+    M, d, chi = int(t["M"]), int(t["d"]), int(t["chi"])
+    for c in (0, 70, 71, 142):
+        res, num, S = R.get_cumsum_kron(t["sq_cov"], c + 1, chi=chi, cutoff=d)
+        k = int(t["kept"][c])
+        assert len(res) == k, c
+        assert np.allclose(res, t["res"][c, :k], rtol=1e-10, atol=0), c  # LAPACK threading: ~1e-11
+        if c in (70, 71):
+            ref = t[f"num_{c}"]
+            assert num.shape == ref.shape and set(map(bytes, num)) == set(map(bytes, ref)), c
+            kk = M - c - 1
+            sel = np.concatenate([np.arange(c + 1, M), np.arange(c + 1, M) + M])
+            V = t["sq_cov"][np.ix_(sel, sel)]
+            om = np.block([[np.zeros((kk, kk)), np.eye(kk)], [-np.eye(kk), np.zeros((kk, kk))]])
+            for Sx in (S, t[f"S_{c}"]):
+                assert np.abs(Sx @ om @ Sx.T - om).max() < 1e-9, c
+                Si = -om @ Sx.T @ om
+                D = Si @ V @ Si.T
+                assert np.abs(D - np.diag(np.diag(D))).max() < 1e-9, c
+
+
+def test_medium_config_cut_spectra(golden):
+    """Same on the M=50, d=6, chi=256 workload (tests/golden/medium_M50.npz)."""
+    t = golden("medium_M50.npz")
+    d, chi = int(t["d"]), int(t["chi"])
+    for c in (0, 24, 48):
+        res, _, _ = R.get_cumsum_kron(t["sq_cov"], c + 1, chi=chi, cutoff=d)
+        k = int(t["kept"][c])
+        assert len(res) == k and np.allclose(res, t["res"][c, :k], rtol=1e-10, atol=0), c

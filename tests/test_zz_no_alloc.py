@@ -48,6 +48,26 @@ def test_noalloc_sigma_matches_allocating_entry_point(cuda, golden):
         assert abs(Zg - Zr) <= 1e-12 * Zr
 
 
+def test_noalloc_sigma_at_its_largest_size(cuda):
+    """M_r = 160, the most modes the fixed scratch array holds: the two cuts
+    next to site 1 of a synthetic 161-mode covariance (320 x 320 and
+    318 x 318 Williamson symplectics), two calls in a row against
+    bsg_site_sigma."""
+    from bosonsupremacy_gb300 import _lib, ops, synthetic
+    lib = _lib.load()
+    h = _lib.Handle.get(0)
+    cfg = synthetic.GBSConfig("M161_d4_chi8", 161, 4, 8, 0.5, 1.0, 0.4, seed=161)
+    _, sq = synthetic.lossy_covariances(cfg)
+    _, _, S, _ = ops.cut_spectra(sq, cfg.d, cfg.chi, L0=1, n_cuts=2)
+    S = S.cpu().numpy()
+    S_r, S_l = S[0, :320, :320], S[1, :318, :318]
+    ref, Zr = _call(lib, lib.bsg_site_sigma, S_l, S_r, handle=h.h)
+    for _ in range(2):
+        got, Zg = _call(lib, lib.bsg_site_sigma_noalloc, S_l, S_r)
+        assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+        assert abs(Zg - Zr) <= 1e-12 * Zr
+
+
 def test_noalloc_sigma_rejects_oversize(cuda):
     import torch
     from bosonsupremacy_gb300 import _lib

@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--contract-workload", default="M50_d6_chi256")
     p.add_argument("--contract-photons", type=int, default=4)
     p.add_argument("--no-largest", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-sampler", action="store_true")
     p.add_argument("--sampler-workload", default="M50_d6_chi256")
     p.add_argument("--sampler-n", type=int, default=100000)
@@ -197,10 +198,30 @@ def measure_contraction(args, lib, handle, peaks):
     e1.record(stream)
     torch.cuda.synchronize()
     t64 = e0.elapsed_time(e1)
+    # the sliced tensor-core path: complex128 Gamma, FP64 environments, BF16
+    # fixed-point slice products with exact FP32 accumulation per level
+    ops.pattern_amplitudes(mps64.Gammas, mps64.Lambdas, pats, precision="sliced")
+    torch.cuda.synchronize()
+    lib.bsg_profile_reset(handle.h)
+    lib.bsg_profile_enable(handle.h, 1)
+    sl_times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        amp_sl = ops.pattern_amplitudes(mps64.Gammas, mps64.Lambdas, pats, precision="sliced")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sl_times.append(e0.elapsed_time(e1))
+    lib.bsg_profile_enable(handle.h, 0)
+    prof_sl = profile_read(lib, handle.h)["contract"]
     p = (amp.abs() ** 2).cpu().numpy()
     p64 = (amp64.abs() ** 2).cpu().numpy()
+    psl = (amp_sl.abs() ** 2).cpu().numpy()
     big = p64 > 1e-10 * p64.max()
     rel = np.abs(p - p64)[big] / p64[big]
+    rel_sl = np.abs(psl - p64)[big] / p64[big]
+    sl_ms = statistics.mean(sl_times)
+    sl_useful = prof_sl["work"] / max(1, prof_sl["launches"])
     ms = statistics.mean(times)
     useful = prof["work"] / max(1, prof["launches"])  # real flops of one contraction
     kern_ms = prof["ms"] / max(1, prof["launches"])
@@ -210,6 +231,12 @@ def measure_contraction(args, lib, handle, peaks):
         "workload": cfg.label(), "patterns": int(pats.shape[0]), "max_photons": args.contract_photons,
         "ms": ms, "patterns_per_s": pats.shape[0] / (ms / 1e3), "fp64_ms": t64, "speedup_vs_fp64": t64 / ms,
         "prob_rel_err_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel))},
+        "sliced": {"ms": sl_ms, "patterns_per_s": pats.shape[0] / (sl_ms / 1e3), "speedup_vs_fp64": t64 / sl_ms,
+                   "prob_rel_err_vs_fp64": {"max": float(rel_sl.max()), "median": float(np.median(rel_sl))},
+                   "useful_tflops": sl_useful / (prof_sl["ms"] / max(1, prof_sl["launches"]) / 1e3) / 1e12,
+                   "note": "complex128 Gamma, FP64 environments; every level's complex GEMM as BF16 fixed-point "
+                           "slice products (tcgen05 kind::f16) summed exactly per slice level in TMEM; useful = 8 "
+                           "flops per complex MAC of the contraction over the contraction's CUDA-event time"},
         "roofline": {"kernel": "umma_gemm_kernel (3xTF32 tcgen05) + gather/env kernels", "bound": "tensor",
                      "achieved": achieved, "unit": "TFLOP/s",
                      "peak": tf32_peak / 2 if tf32_peak else None,
@@ -277,6 +304,51 @@ def measure_sampler(args, lib, handle, peaks):
     }
 
 
+def measure_batch(args, lib, handle):
+    """The 64-instance uneven workload (M ~ U{8..48}, d ~ U{4..8}, chi in
+    {32..256}): one bsg_build_mps_batch call (one launch per phase, one DP
+    launch set over every instance's items) against 64 bsg_build_mps calls
+    back to back; CUDA events on the launching stream, one untimed run of
+    each first."""
+    import torch
+
+    from bosonsupremacy_gb300 import synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps, build_mps_batch
+
+    cfgs = synthetic.batch_configs(64)
+    sqs = [torch.as_tensor(synthetic.lossy_covariances(c)[1]).cuda() for c in cfgs]
+    ds, chis = [c.d for c in cfgs], [c.chi for c in cfgs]
+    outs = [[torch.empty(c.chi, c.chi, c.d, dtype=torch.complex64, device="cuda") for _ in range(c.M)] for c in cfgs]
+    stream = torch.cuda.current_stream()
+
+    def batched():
+        build_mps_batch(sqs, ds, chis, precision=args.precision, outs=outs)
+
+    def looped():
+        for c, q, o in zip(cfgs, sqs, outs):
+            build_mps(q, c.d, c.chi, precision=args.precision, out=o)
+
+    res = {}
+    for name, fn in (("batched", batched), ("looped", looped)):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        res[name] = statistics.mean(ts)
+    sites = sum(c.M for c in cfgs)
+    return {"workload": "batch64: 64 instances, M~U{8..48}, d~U{4..8}, chi in {32,64,128,256}, r~U[0.5,1.4], "
+                        "eta~U[0.2,0.6]", "instances": len(cfgs), "sites": sites,
+            "batched_ms": res["batched"], "looped_ms": res["looped"],
+            "batched_sites_per_s": sites / (res["batched"] / 1e3), "looped_sites_per_s": sites / (res["looped"] / 1e3),
+            "speedup_vs_looped": res["looped"] / res["batched"]}
+
+
 def measure_largest(args, lib, handle):
     """The largest single-GPU workload (M=216 banded, d=10, chi=2048; 72 GB
     of complex64 Gamma): full-build time of the split build (CUDA events,
@@ -313,16 +385,17 @@ def measure_largest(args, lib, handle):
     timed(args.precision, split)
     ms, m = timed(args.precision, split)
     n = 32
-    lam_err = None
+    lam_err, lam_err_hi = None, None
     if ref is not None:
         res = m.res.cpu().numpy()
-        lam_err = []
+        lam_err, lam_err_hi = [], []
         for c in range(n):
             k = int(ref["kept"][c])
             a = np.sort(res[c, :k])[::-1]
             b = ref["res"][c, :k]
-            big = b > 1e-10
-            lam_err.append(float((np.abs(np.sqrt(a[big]) - np.sqrt(b[big])) / np.sqrt(b[big])).max()))
+            rel = np.abs(np.sqrt(a) - np.sqrt(b)) / np.sqrt(b)
+            lam_err.append(float(rel[b > 1e-10].max()))
+            lam_err_hi.append(float(rel[b > 1e-6].max()))
     # the FP64 build writes its first 32 sites to their own buffers and the
     # rest over the split build's (not compared)
     fp64 = [torch.empty(chi, chi, d, dtype=torch.complex64, device="cuda") for _ in range(n)] + split[n:]
@@ -331,6 +404,7 @@ def measure_largest(args, lib, handle):
     out = {"workload": cfg.label(), "build_ms": ms, "sites_per_s": M / (ms / 1e3), "fp64_build_ms": ms64,
            "split_speedup": ms64 / ms,
            "lambda_rel_err_vs_reference_kron_first32": lam_err,
+           "lambda_rel_err_vs_reference_kron_first32_weights_above_1e-6": lam_err_hi if lam_err else None,
            "lambda_source": "tests/golden/largest_M216.npz (kron_cpu.py FP64-promoted, cuts 0-31)" if lam_err else None,
            "gamma_err_split_vs_fp64_first32": g_err,
            "note": "Gamma errors: max |split - fp64| / max |fp64| per site, both complex64"}
@@ -594,6 +668,10 @@ def main():
                           f"({est['items']} items); extrapolated full build {est['build_s']:.0f} s"),
                "extrapolated_build_s": est["build_s"]}
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = measure_batch(args, lib, handle)
+
     largest = None
     if rank == 0 and not args.no_largest:
         del outs
@@ -613,7 +691,7 @@ def main():
                                                                  for k, v in prof.items()},
             "host": {k: {"ms": v["ms"], "calls": v["launches"]} for k, v in host_prof.items()},
             "roofline": roof, "fp64_path": fp64, "cold_build": cold, "e2e": e2e, "cpu_baseline": cpu, "contraction": contraction, "sampler": sampler,
-            "largest": largest,
+            "batch64": batch, "largest": largest,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -14,8 +14,8 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbsg.so")
 
-PREC_FP64, PREC_SPLIT, PREC_FP32 = 0, 1, 2
-PRECISIONS = {"fp64": PREC_FP64, "split": PREC_SPLIT, "fp32": PREC_FP32}
+PREC_FP64, PREC_SPLIT, PREC_FP32, PREC_SLICED = 0, 1, 2, 3
+PRECISIONS = {"fp64": PREC_FP64, "split": PREC_SPLIT, "fp32": PREC_FP32, "sliced": PREC_SLICED}
 SITE_FIRST, SITE_MIDDLE, SITE_LAST = 0, 1, 2
 K_DP, K_WILLIAMSON, K_THERMAL, K_SIGMA, K_PREP, K_CONTRACT, K_HOST_PLAN, K_HOST_WAIT, K_SAMPLE = range(9)
 KERNEL_CLASSES = {K_DP: "hafnian_dp", K_WILLIAMSON: "williamson", K_THERMAL: "thermal_topk", K_SIGMA: "site_sigma",
@@ -50,11 +50,13 @@ SIGNATURES = {
     "bsg_cut_spectrum": (_I, [_P, _P, _I, _I, _I, _I, _D, _L, _P, _P, _P, _P, _P]),
     "bsg_build_mps": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_build_mps_to_host": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "bsg_build_mps_batch": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_profile_enable": (_I, [_P, _I]),
     "bsg_profile_read": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_L), C.POINTER(_D)]),
     "bsg_profile_reset": (_I, [_P]),
     "bsg_fma_peak": (_I, [_P, _I, C.POINTER(_D), _P]),
     "bsg_gemm_tf32x3": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
+    "bsg_gemm_sliced": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "bsg_tune_set": (_I, [_P, _I, _I]),
     "bsg_tune_get": (_I, [_P, _I, C.POINTER(_I)]),
     "bsg_sample": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _L, _I, _P, _P]),

@@ -398,7 +398,7 @@ static size_t plan_side_words(int64_t P, int d, int levels) {
 template <class R>
 static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* lam, int M, int chi, int d,
                            const SidePlan& left, const SidePlan& right, int64_t P, double* amp, bool umma,
-                           char* ws, cudaStream_t st) {
+                           bool sliced, char* ws, cudaStream_t st) {
   using T = typename Cx<R>::T;
   // device memory: two env buffers per side (ping-pong)
   int64_t max_rows = 1;
@@ -408,7 +408,13 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   const size_t env_bytes = al((size_t)max_rows * chi * sizeof(T));
   const size_t a_bytes = umma ? al((size_t)max_rows * 2 * chi * 4) : 0;
   const size_t b_bytes = umma ? al((size_t)d * 4 * chi * chi * 4) : 0;
-  const size_t need = 4 * env_bytes + 2 * a_bytes + 2 * b_bytes + 256;
+  // sliced: S BF16 slices of the level's A rows and of all d B blocks, row exponents
+  int S = 0, bits = 0;
+  if (sliced) sliced_params(2 * chi, &S, &bits);
+  const size_t sa_bytes = sliced ? al(sliced_operand_bytes(max_rows, 2 * chi, S)) : 0;
+  const size_t sb_bytes = sliced ? al(sliced_operand_bytes((int64_t)d * 2 * chi, 2 * chi, S)) : 0;
+  const size_t se_bytes = sliced ? al((size_t)(max_rows + (int64_t)d * 2 * chi) * 4) : 0;
+  const size_t need = 4 * env_bytes + 2 * a_bytes + 2 * b_bytes + sa_bytes + sb_bytes + se_bytes + 256;
   BSG_TRY(h->contract_ws.ensure(need));
   char* base = reinterpret_cast<char*>(h->contract_ws.ptr);
   char* sp_base = base + 4 * env_bytes;
@@ -416,8 +422,13 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   float* Alo = reinterpret_cast<float*>(sp_base + a_bytes);
   float* Bhi = reinterpret_cast<float*>(sp_base + 2 * a_bytes);
   float* Blo = reinterpret_cast<float*>(sp_base + 2 * a_bytes + b_bytes);
-  int* d_err = reinterpret_cast<int*>(sp_base + 2 * a_bytes + 2 * b_bytes);
-  if (umma) BSG_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
+  char* sl_base = sp_base + 2 * a_bytes + 2 * b_bytes;
+  void* Asl = sl_base;
+  void* Bsl = sl_base + sa_bytes;
+  int* ea = reinterpret_cast<int*>(sl_base + sa_bytes + sb_bytes);
+  int* eb = ea + max_rows;
+  int* d_err = reinterpret_cast<int*>(sl_base + sa_bytes + sb_bytes + se_bytes);
+  if (umma || sliced) BSG_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
   T* E[4] = {reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + env_bytes),
              reinterpret_cast<T*>(base + 2 * env_bytes), reinterpret_cast<T*>(base + 3 * env_bytes)};
   (void)ws;
@@ -426,7 +437,7 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   const int K2 = 2 * chi;
   std::vector<int4> tiles;
   std::vector<int> tile_off[2];
-  if (umma) {
+  if (umma || sliced) {
     const SidePlan* sps[2] = {&left, &right};
     for (int sd = 0; sd < 2; ++sd) {
       tile_off[sd].assign(sps[sd]->sites.size() + 1, 0);
@@ -441,7 +452,7 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
     }
   }
   int4* d_tiles = nullptr;
-  if (umma && !tiles.empty()) {
+  if ((umma || sliced) && !tiles.empty()) {
     BSG_TRY(h->plan.ensure(tiles.size() * sizeof(int4)));
     BSG_TRY(h->host_stage2.ensure(tiles.size() * sizeof(int4)));
     std::memcpy(h->host_stage2.ptr, tiles.data(), tiles.size() * sizeof(int4));
@@ -469,6 +480,24 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
       const int32_t* parent = sp.parent + l * sp.P;
       // left uses Lambda_{s-1}, right uses Lambda_s
       const double* lm = lam + (size_t)(is_left ? s - 1 : s) * chi;
+      if constexpr (std::is_same<R, double>::value) {
+        if (sliced) {
+          // all photon numbers of the level in one grouped sliced GEMM
+          const int rows = sp.rows(int(l));
+          const int sd = is_left ? 0 : 1;
+          const int t0 = tile_off[sd][l], nt = tile_off[sd][l + 1] - t0;
+          if (sliced_slice_gamma(reinterpret_cast<const double2*>(G), chi, d, is_left, S, bits, Bsl, eb, st) !=
+                  BSG_OK ||
+              sliced_slice_env(reinterpret_cast<const double2*>(prev), parent, lm, rows, chi, S, bits, Asl, ea, st) !=
+                  BSG_OK ||
+              sliced_gemm(h, Asl, rows, ea, Bsl, d * K2, eb, reinterpret_cast<double*>(curb), rows, K2, K2, K2, S,
+                          bits, d_err, st, false, d_tiles + t0, nt) != BSG_OK)
+            return nullptr;
+          flops += 8.0 * rows * (double)chi * chi;
+          std::swap(prev, curb);
+          continue;
+        }
+      }
       if constexpr (std::is_same<R, float>::value) {
         if (umma) {
           // all photon numbers of the level in one grouped GEMM
@@ -522,7 +551,7 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   BSG_CUDA(cudaGetLastError());
   if (h->prof.on) BSG_TRY(h->prof.end(BSG_K_CONTRACT, st, ev, flops + 8.0 * P * chi));
   int err = 0;
-  if (umma) BSG_CUDA(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, st));
+  if (umma || sliced) BSG_CUDA(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaStreamSynchronize(st));
   if (err) {
     set_error("bsg_pattern_amplitudes: a tensor-core pipeline wait timed out");
@@ -542,8 +571,11 @@ extern "C" int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas,
   BSG_CHECK_ARG(Gammas && Lambdas && amp && (patterns || P == 0), "bsg_pattern_amplitudes: null pointer");
   BSG_CHECK_ARG(M >= 2 && chi >= 1 && d >= 1 && P >= 0, "bsg_pattern_amplitudes: bad sizes M=%d chi=%d d=%d", M, chi,
                 d);
-  BSG_CHECK_ARG(precision == BSG_PREC_FP64 || precision == BSG_PREC_SPLIT || precision == BSG_PREC_FP32,
+  BSG_CHECK_ARG(precision == BSG_PREC_FP64 || precision == BSG_PREC_SPLIT || precision == BSG_PREC_FP32 ||
+                    precision == BSG_PREC_SLICED,
                 "bsg_pattern_amplitudes: bad precision %d", precision);
+  BSG_CHECK_ARG(precision != BSG_PREC_SLICED || chi % 4 == 0,
+                "bsg_pattern_amplitudes: the sliced tensor-core path needs chi %% 4 == 0 (chi=%d)", chi);
   for (int i = 0; i < M; ++i) BSG_CHECK_ARG(Gammas[i], "bsg_pattern_amplitudes: Gamma %d is NULL", i);
   BSG_CUDA(cudaSetDevice(h->device));
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -574,14 +606,15 @@ extern "C" int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas,
     set_error("bsg_pattern_amplitudes: a photon number is outside [0, d=%d)", d);
     return BSG_ERR_INVALID;
   }
-  if (precision == BSG_PREC_FP64)
-    return run_contraction<double>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, false, nullptr, st);
+  if (precision == BSG_PREC_FP64 || precision == BSG_PREC_SLICED)
+    return run_contraction<double>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, false,
+                                   precision == BSG_PREC_SLICED, nullptr, st);
   if (precision == BSG_PREC_SPLIT && chi % 2 != 0) {
     set_error("bsg_pattern_amplitudes: the tensor-core path needs an even chi");
     return BSG_ERR_INVALID;
   }
   return run_contraction<float>(h, Gammas, Lambdas, M, chi, d, left, right, P, amp, precision == BSG_PREC_SPLIT,
-                                nullptr, st);
+                                false, nullptr, st);
 }
 
 extern "C" int bsg_contract_patterns(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi,

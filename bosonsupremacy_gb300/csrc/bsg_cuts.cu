@@ -226,6 +226,7 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
   constexpr int kRefineMax = 8;
   const size_t tri = (size_t)m * (m + 1) / 2;  // entries of an upper triangle (diagonal included)
   int refined = 0;
+  bool converged = false;
   for (int it = 0; it < kRefineMax; ++it) {
     // s2 = T = Hm QT^T (all m^2 entries) and s1 = R = I - QT QT^T (symmetric:
     // its upper triangle, mirrored), one pass over both index sets
@@ -268,16 +269,22 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     so = block_sum(so, red);
     rr = block_sum(rr, red);
     const double delta = 2.0 * (sqrt(so) + anorm * sqrt(rr));
-    // s1 <- E (in place: E_ij reads s1_ij and s3_ij only)
-    double emax = 0.0;
+    // s1 <- E (in place: E_ij reads s1_ij and s3_ij only).  cnum: the largest
+    // numerator s_ij + lambda_j r_ij of a clustered pair -- rounding level for
+    // an exactly degenerate pair, about gap x mixing for distinct eigenvalues
+    // the clustering leaves unresolved
+    double emax = 0.0, cnum = 0.0;
     for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
       const double r = s1[t], gap = lam[j] - lam[i];
-      const double e = (i != j && fabs(gap) > delta) ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
+      const bool sep = i != j && fabs(gap) > delta;
+      const double e = sep ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
       s1[t] = e;
       if (i != j) emax = fmax(emax, fabs(e));
+      if (i != j && !sep) cnum = fmax(cnum, fabs(s3[t] + lam[j] * r));
     }
     emax = block_max(emax, red);
+    cnum = block_max(cnum, red);
     // s2 = QT + E^T QT, then QT = s2
     for (size_t t = tid; t < mm; t += nt) {
       const int i = int(t / m), j = int(t % m);
@@ -289,7 +296,29 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     for (size_t t = tid; t < mm; t += nt) QT[t] = s2[t];
     __syncthreads();
     refined = it + 1;
-    if (emax <= 1e-8) break;  // the remaining error is ~emax^2
+    if (emax <= 1e-8) {  // the remaining error is ~emax^2
+      converged = cnum <= 1e-12 * anorm;
+      break;
+    }
+  }
+  if (!converged) {
+    // Eigenvalues closer than the FP32 start can separate (gaps ~1e-7 of the
+    // norm: near-vacuum modes of cuts far from where the interferometer
+    // couples, e.g. the banded M=216 workload's cuts 12 and up) come out of
+    // the FP32 sweeps mixed by O(1): either the steps stop converging once
+    // delta drops below their gap, or the mixed pair keeps delta above its
+    // gap and stays a cluster (cnum above rounding).  Such a cut restarts from
+    // the identity with FP64 Jacobi sweeps on Hm (still the input matrix),
+    // which resolve any gap above the FP64 rounding of Hm.
+    for (size_t t = tid; t < mm; t += nt) QT[t] = (t / m == t % m) ? 1.0 : 0.0;
+    __syncthreads();
+    const int sw64 = block_jacobi<double>(Hm, m, QT, 60, 1e-26, red, cs, sn, pos);
+    if (sweep_log && tid == 0) {
+      sweep_log[0] = (unsigned long long)(sw32 < 0 ? 99 : sw32);
+      sweep_log[1] = 100 + (unsigned long long)(sw64 < 0 ? 99 : sw64);  // 100 + FP64 sweeps: the restart
+    }
+    __syncthreads();
+    return sw64 < 0 ? -1 : (sw32 < 0 ? 0 : sw32);
   }
   for (int i = tid; i < m; i += nt) Hm[(size_t)i * m + i] = lam[i];
   if (sweep_log && tid == 0) {
@@ -342,8 +371,8 @@ __device__ __forceinline__ void phase_stamp(const CutArgs& a, int c, int i) {
   }
 }
 
-__global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
-  const int c = a.c0 + blockIdx.x;
+// The Williamson decomposition of cut c of `a` by the whole CTA.
+__device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   const int L = a.L0 + c, M = a.M;
   const int k = M - L, n = 2 * k, nA = 2 * L;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -758,7 +787,12 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
         xy32[i] = float(x[i]);
         xy32[n + i] = float(y[i] );
       }
-      if (tid == 0) MU[acc / 2] = sqrt(gx);  // 1/nu of pair acc/2 (MU no longer needed by candidates)
+      // 1/nu of pair acc/2 (MU no longer needed by candidates): |G x| in the
+      // full path; in the low-rank path the eigenvalue of K = I - R R^T
+      // itself, whose 1 - mu = sigma^2 carries the small nbar of weakly
+      // coupled modes to ~1e-16 absolute, where |G x| (through L^-1 twice)
+      // loses cond(V) of it
+      if (tid == 0) MU[acc / 2] = g_dense ? sqrt(gx) : sqrt(vec2[cb + best]);
       __syncthreads();
       // FP32 tracking: the candidates stay as they are (orthonormal); a
       // candidate's squared residual against the accepted orthonormal pairs
@@ -819,8 +853,8 @@ __global__ void __launch_bounds__(1024) williamson_kernel(CutArgs a) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 
-__global__ void __launch_bounds__(1024) thermal_kernel(CutArgs a) {
-  const int c = a.c0 + blockIdx.x;
+// The top-chi weights of cut c of `a` by the whole CTA.
+__device__ __forceinline__ void thermal_cut(const CutArgs& a, const int c) {
   if (a.status[c] != 0) return;
   const int L = a.L0 + c, k = a.M - L, d = a.d, chi = a.chi;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -920,15 +954,54 @@ __global__ void __launch_bounds__(1024) thermal_kernel(CutArgs a) {
   if (tid == 0) a.kept[c] = Kout;
 }
 
+// One CTA per cut: cuts c0 + blockIdx.x of one call.
+__global__ void __launch_bounds__(1024) williamson_kernel(const __grid_constant__ CutArgs a) {
+  williamson_cut(a, a.c0 + blockIdx.x);
+}
+__global__ void __launch_bounds__(1024) thermal_kernel(const __grid_constant__ CutArgs a) {
+  thermal_cut(a, a.c0 + blockIdx.x);
+}
+// Batched over independent instances: block b handles cut map[b].y of instance map[b].x.
+__global__ void __launch_bounds__(1024) williamson_batch_kernel(const CutArgs* __restrict__ args,
+                                                                const int2* __restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  williamson_cut(args[m.x], m.y);
+}
+__global__ void __launch_bounds__(1024) thermal_batch_kernel(const CutArgs* __restrict__ args,
+                                                             const int2* __restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  thermal_cut(args[m.x], m.y);
+}
+
 }  // namespace bsg
 
 using namespace bsg;
 
 namespace bsg {
 
-// Workspace, output clearing and the launch arguments of a cut-spectra call.
+static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Bytes of cut workspace for n_cuts cuts of an M-mode state (cut_prepare_at).
+size_t cut_ws_bytes(int M, int L0, int n_cuts, int chi) {
+  const int kmax = M - L0, nmax = 2 * kmax;
+  return al256((size_t)8 * nmax * nmax * 8 * n_cuts) + al256((size_t)n_cuts * kmax * 8) +
+         al256((size_t)n_cuts * kmax * chi * 4) + al256((size_t)n_cuts * 8) + al256((size_t)n_cuts * 2 * kmax * 8) +
+         al256((size_t)n_cuts * kCutPhases * 8);
+}
+
 int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                 double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st) {
+  BSG_CHECK_ARG(M >= 2 && L0 >= 1 && n_cuts >= 1 && L0 + n_cuts <= M, "bsg_cut_spectra: cuts [%d, %d) outside [1, M=%d)",
+                L0, L0 + n_cuts, M);
+  BSG_TRY(h->cut_ws.ensure(cut_ws_bytes(M, L0, n_cuts, chi)));
+  return cut_prepare_at(h, reinterpret_cast<char*>(h->cut_ws.ptr), sq_cov, M, L0, n_cuts, d, chi, err_tol, res, num,
+                        S, kept, out, st);
+}
+
+// Workspace (at `base`, cut_ws_bytes of it), output clearing and the launch
+// arguments of a cut-spectra call.
+int cut_prepare_at(bsg_handle_t h, char* base, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
+                   double err_tol, double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st) {
   BSG_CHECK_ARG(M >= 2 && L0 >= 1 && n_cuts >= 1 && L0 + n_cuts <= M, "bsg_cut_spectra: cuts [%d, %d) outside [1, M=%d)",
                 L0, L0 + n_cuts, M);
   BSG_CHECK_ARG(M - L0 <= kMaxCutModes, "bsg_cut_spectra: %d modes in a cut exceeds %d", M - L0, kMaxCutModes);
@@ -962,9 +1035,6 @@ int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts,
   const size_t st_bytes = (size_t)n_cuts * 8;
   const size_t ph_bytes = (size_t)n_cuts * kCutPhases * 8;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  BSG_TRY(h->cut_ws.ensure(al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes) + al(mu_bytes) +
-                           al(ph_bytes)));
-  char* base = reinterpret_cast<char*>(h->cut_ws.ptr);
   a.ws = reinterpret_cast<double*>(base);
   a.nbar = reinterpret_cast<double*>(base + al(ws_bytes));
   a.rec = reinterpret_cast<uint32_t*>(base + al(ws_bytes) + al(nbar_bytes));
@@ -1009,6 +1079,67 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
   BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0,
                (williamson_kernel<<<c1 - c0, h->tune[BSG_TUNE_FACTOR_THREADS], wsm, st>>>(a)));
+  return BSG_OK;
+}
+
+// Dynamic shared memory of a Williamson launch whose largest eigen-problem
+// is m_max (the FP32 Jacobi matrices in shared memory when they fit).
+static int williamson_smem(bsg_handle_t h, int m_max, size_t* wsm, int* jac_m) {
+  *wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
+  int smem_optin = 0;
+  BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+  const size_t jac = (size_t)2 * m_max * m_max * sizeof(float);
+  *jac_m = 0;
+  if (*wsm + jac <= (size_t)smem_optin) {
+    *jac_m = m_max;
+    *wsm += jac;
+  }
+  return BSG_OK;
+}
+
+// Williamson, then top-chi selection, of every cut of n independent
+// instances (their CutArgs, from cut_prepare_at), one launch each: block b
+// takes one (instance, cut).  dev: device room for n CutArgs and the block
+// map (batch_dev_bytes); stage: pinned host room of the same size.
+size_t cut_batch_bytes(const CutArgs* args, int n) {
+  size_t cuts = 0;
+  for (int i = 0; i < n; ++i) cuts += (size_t)args[i].n_cuts;
+  return al256(sizeof(CutArgs) * n) + al256(sizeof(int2) * cuts);
+}
+
+int cut_launch_batch(bsg_handle_t h, CutArgs* args, int n, void* dev, void* stage, cudaStream_t st) {
+  int m_max = 0, total = 0, thermal_smem_max = 0;
+  double ranked = 0.0;
+  for (int i = 0; i < n; ++i) {
+    CutArgs& a = args[i];
+    a.c0 = 0;
+    for (int c = 0; c < a.n_cuts; ++c) {
+      const int L = a.L0 + c, k = a.M - L;
+      m_max = std::max(m_max, 2 * std::min(L, k));
+      ranked += (double)(a.M - a.L0 - c) * a.chi * a.d;
+    }
+    total += a.n_cuts;
+    thermal_smem_max = std::max(thermal_smem_max, a.d * a.chi * 8 + 2 * a.chi * 8 + 64 * 8);
+  }
+  if (total == 0) return BSG_OK;
+  size_t wsm = 0;
+  int jac_m = 0;
+  BSG_TRY(williamson_smem(h, m_max, &wsm, &jac_m));
+  for (int i = 0; i < n; ++i) args[i].jac_smem_m = jac_m;
+  char* hs = reinterpret_cast<char*>(stage);
+  std::memcpy(hs, args, sizeof(CutArgs) * n);
+  int2* map = reinterpret_cast<int2*>(hs + al256(sizeof(CutArgs) * n));
+  int b = 0;
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < args[i].n_cuts; ++c) map[b++] = make_int2(i, c);
+  BSG_CUDA(cudaMemcpyAsync(dev, stage, al256(sizeof(CutArgs) * n) + sizeof(int2) * total, cudaMemcpyHostToDevice, st));
+  const CutArgs* dargs = reinterpret_cast<const CutArgs*>(dev);
+  const int2* dmap = reinterpret_cast<const int2*>(reinterpret_cast<char*>(dev) + al256(sizeof(CutArgs) * n));
+  BSG_CUDA(cudaFuncSetAttribute(williamson_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0,
+               (williamson_batch_kernel<<<total, h->tune[BSG_TUNE_FACTOR_THREADS], wsm, st>>>(dargs, dmap)));
+  BSG_CUDA(cudaFuncSetAttribute(thermal_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, thermal_smem_max));
+  BSG_PROFILED(h, BSG_K_THERMAL, st, ranked, (thermal_batch_kernel<<<total, 1024, thermal_smem_max, st>>>(dargs, dmap)));
   return BSG_OK;
 }
 

@@ -1000,13 +1000,14 @@ struct SiteCombos {
 };
 
 static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, const int* KL,
-                               const uint64_t* const* kr, const int* KR, int ns, int d,
+                               const uint64_t* const* kr, const int* KR, int ns, const int* dv,
                                std::vector<SitePlanHost>& plans, Buckets& bk) {
   plans.assign(ns, SitePlanHost());
   std::vector<SiteCombos> cb(ns);
   parallel_for(ns, [&](int s) {
     SitePlanHost& sp = plans[s];
     SiteCombos& c = cb[s];
+    const int d = dv[s];
     sp.KL = KL[s];
     sp.KR = KR[s];
     sp.d = d;
@@ -1060,7 +1061,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
       sp.gcnt_l[g] = int32_t(c.gc_l[g]);
     }
     for (int g = 0, at = 0; g < sp.ngr; at += int(c.gc_r[g]), ++g) sp.gstart_r[g] = at;
-    for (int j = 0; j < d; ++j)
+    for (int j = 0; j < sp.d; ++j)
       for (int gl = 0; gl < sp.ngl; ++gl)
         for (int gr = 0; gr < sp.ngr; ++gr) {
           const size_t o = ((size_t)j * sp.ngl + gl) * sp.ngr + gr;
@@ -1114,6 +1115,7 @@ struct SiteInput {
   RowTable lt;            // device row tables (already offset to this cut)
   RowTable rt;
   void* gamma;
+  int d = 0, chi = 0;     // this site's cutoff and bond dimension (0: the call's)
 };
 
 // Plans, uploads and launches the scatter + DP for a set of sites.
@@ -1125,14 +1127,15 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   std::vector<SitePlanHost> plans;
   {
     std::vector<const uint64_t*> kl(ns), kr(ns);
-    std::vector<int> KL(ns), KR(ns);
+    std::vector<int> KL(ns), KR(ns), dv(ns);
     for (int s = 0; s < ns; ++s) {
       kl[s] = in[s].hkey_l;
       kr[s] = in[s].hkey_r;
       KL[s] = in[s].KL;
       KR[s] = in[s].KR;
+      dv[s] = in[s].d ? in[s].d : d;
     }
-    BSG_TRY(plan_sites_parallel(ps, kl.data(), KL.data(), kr.data(), KR.data(), ns, d, plans, bk));
+    BSG_TRY(plan_sites_parallel(ps, kl.data(), KL.data(), kr.data(), KR.data(), ns, dv.data(), plans, bk));
   }
   std::vector<int32_t> remap;
   BSG_TRY(layout_buckets(ps, h->tune[BSG_TUNE_DP_SMALL_ENTRIES], bk, remap));
@@ -1207,8 +1210,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     sd.l_scale2 = lj.out_f;
     sd.Z = si.Z;
     sd.gamma = si.gamma;
-    sd.chi = chi;
-    sd.d = d;
+    sd.chi = si.chi ? si.chi : chi;
+    sd.d = si.d ? si.d : d;
     sd.out_c128 = out_c128;
     hd[s] = sd;
     std::memcpy(hp + o_pl[s], plans[s].perm_l.data(), plans[s].perm_l.size() * 4);
@@ -1250,7 +1253,10 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
                (left_scale_kernel<<<dim3((max_kl + 127) / 128, ns), 128, 0, st>>>(
                    reinterpret_cast<const LeftScaleJob*>(dp + o_lsj))));
   const size_t esz = out_c128 ? 16 : 8;
-  for (int s = 0; s < ns; ++s) BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, (size_t)chi * chi * d * esz, st));
+  for (int s = 0; s < ns; ++s) {
+    const size_t cs = in[s].chi ? in[s].chi : chi, ds = in[s].d ? in[s].d : d;
+    BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, cs * cs * ds * esz, st));
+  }
   if (bk.slots == 0) return BSG_OK;
   BSG_PROFILED(h, BSG_K_PREP, st, (double)nb * 32,
                (pad_items_kernel<<<unsigned(((int64_t)nb * 32 + 255) / 256), 256, 0, st>>>(
@@ -1851,12 +1857,263 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   return BSG_OK;
 }
 
+// The whole MPS of n independent instances (each its own M, d, chi) with one
+// launch per phase for all of them: the Williamson and top-chi kernels over
+// every cut of every instance (cut_launch_batch), the Sigma phases over every
+// site of every instance (launch_sigma_jobs), one host wait, then one item
+// scatter and one set of DP launches over the items of every site of every
+// instance (run_sites with per-site d and chi).  Per-instance outputs as in
+// bsg_build_mps; gammas holds the instances' site pointers back to back.
+static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, const int* Ms, const int* ds,
+                                const int* chis, double cut_tol, double site_tol, int precision, int out_dtype,
+                                void* const* gammas, double* const* Lambdas, double* const* res,
+                                int8_t* const* num, double* const* S, int32_t* const* kept, cudaStream_t st) {
+  BSG_CHECK_ARG(n >= 1, "bsg_build_mps_batch: need at least one instance");
+  BSG_CHECK_ARG(sq && Ms && ds && chis && gammas && Lambdas && res && num && S && kept,
+                "bsg_build_mps_batch: null pointer");
+  BSG_CHECK_ARG(precision >= 0 && precision <= 2, "bsg_build_mps_batch: bad precision %d", precision);
+  BSG_CHECK_ARG(out_dtype == BSG_OUT_C64 || out_dtype == BSG_OUT_C128, "bsg_build_mps_batch: bad out_dtype");
+  std::vector<int> site0(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    const int M = Ms[i], d = ds[i], chi = chis[i];
+    BSG_CHECK_ARG(sq[i] && Lambdas[i] && res[i] && num[i] && S[i] && kept[i],
+                  "bsg_build_mps_batch: instance %d: null pointer", i);
+    BSG_CHECK_ARG(M >= 2, "bsg_build_mps_batch: instance %d: need M >= 2 modes (M=%d)", i, M);
+    BSG_CHECK_ARG(chi >= d && chi <= 2048, "bsg_build_mps_batch: instance %d: need d <= chi <= 2048", i);
+    BSG_CHECK_ARG(d >= 1 && d <= kKeyMaxMult + 1, "bsg_build_mps_batch: instance %d: d=%d outside [1, %d]", i, d,
+                  kKeyMaxMult + 1);
+    site0[i + 1] = site0[i] + M;
+  }
+  const int ns = site0[n];
+  for (int s = 0; s < ns; ++s) BSG_CHECK_ARG(gammas[s], "bsg_build_mps_batch: Gamma pointer %d is NULL", s);
+  BSG_CUDA(cudaSetDevice(h->device));
+  BSG_TRY(ensure_tables());
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = al(off + bytes);
+    return o;
+  };
+  struct Inst {
+    size_t o_cut, o_ent, o_nnz, o_sum, o_key, o_rf, o_rf2, o_above, o_err, o_Z, o_status;
+    size_t h_cut, h_keys, h_cnt, h_above, h_err;  // offsets in the pinned staging
+  };
+  std::vector<Inst> I(n);
+  std::vector<size_t> o_sig(ns), o_sigc(ns), o_sws(ns);
+  size_t hoff = 0;
+  auto hcarve = [&](size_t bytes) {
+    size_t o = hoff;
+    hoff = (hoff + bytes + 63) & ~size_t(63);
+    return o;
+  };
+  int total_cuts = 0;
+  for (int i = 0; i < n; ++i) {
+    const int M = Ms[i], chi = chis[i], nc = M - 1;
+    total_cuts += nc;
+    Inst& t = I[i];
+    t.o_cut = carve(cut_ws_bytes(M, 1, nc, chi));
+    t.o_ent = carve((size_t)nc * chi * kMaxNnz * 4);
+    t.o_nnz = carve((size_t)nc * chi * 4);
+    t.o_sum = carve((size_t)nc * chi * 4);
+    t.o_key = carve((size_t)nc * chi * 8);
+    t.o_rf = carve((size_t)nc * chi * 8);
+    t.o_rf2 = carve((size_t)nc * chi * 8);
+    t.o_above = carve((size_t)nc * 4);
+    t.o_err = carve(16);
+    t.o_Z = carve((size_t)M * 8);
+    t.o_status = carve((size_t)M * 4);
+    for (int j = 0; j < M; ++j) {
+      const int s = site0[i] + j, Mr = j == 0 ? M : M - j;
+      o_sig[s] = carve((size_t)(2 * Mr) * (2 * Mr) * 16);
+      o_sigc[s] = precision == BSG_PREC_FP64 ? o_sig[s] : carve((size_t)(2 * Mr) * (2 * Mr) * prec_bytes(precision));
+      o_sws[s] = carve(sigma_ws_bytes(Mr));
+    }
+    t.h_cut = hcarve((size_t)2 * nc * 4);
+    t.h_keys = hcarve((size_t)nc * chi * 8);
+    t.h_cnt = hcarve((size_t)nc * 4);
+    t.h_above = hcarve((size_t)nc * 4);
+    t.h_err = hcarve(4);
+  }
+  const size_t o_empty = carve(kMaxNnz * 4 + 64);
+  const size_t cargs_bytes = al(sizeof(CutArgs) * n) + al(sizeof(int2) * total_cuts);
+  const size_t o_cargs = carve(cargs_bytes);
+  const size_t o_jobs = carve(sizeof(SigmaJob) * ns);
+  const size_t h_cargs = hcarve(cargs_bytes), h_jobs = hcarve(sizeof(SigmaJob) * ns), h_sst = hcarve((size_t)ns * 4);
+  const size_t h_empty = hcarve(kMaxNnz * 4 + 64);
+  BSG_TRY(h->mps_ws.ensure(off));
+  BSG_TRY(h->host_stage.ensure(hoff));
+  char* wb = reinterpret_cast<char*>(h->mps_ws.ptr);
+  char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
+  auto table = [&](int i, int c) {
+    const Inst& t = I[i];
+    const size_t o = (size_t)c * chis[i];
+    return RowTable{reinterpret_cast<int32_t*>(wb + t.o_ent) + o * kMaxNnz, reinterpret_cast<int32_t*>(wb + t.o_nnz) + o,
+                    reinterpret_cast<int32_t*>(wb + t.o_sum) + o, reinterpret_cast<uint64_t*>(wb + t.o_key) + o,
+                    reinterpret_cast<double*>(wb + t.o_rf) + o, reinterpret_cast<float2*>(wb + t.o_rf2) + o};
+  };
+  RowTable empty{reinterpret_cast<int32_t*>(wb + o_empty), reinterpret_cast<int32_t*>(wb + o_empty + kMaxNnz * 4),
+                 nullptr, nullptr, reinterpret_cast<double*>(wb + o_empty + kMaxNnz * 4 + 8),
+                 reinterpret_cast<float2*>(wb + o_empty + kMaxNnz * 4 + 16)};
+  {
+    // empty row: nnz 0, rowfact 1 (and as the FP32 pair (1, 0))
+    char* e = hs + h_empty;
+    std::memset(e, 0, kMaxNnz * 4 + 64);
+    const double one = 1.0;
+    const float2 one2 = make_float2(1.f, 0.f);
+    std::memcpy(e + kMaxNnz * 4 + 8, &one, 8);
+    std::memcpy(e + kMaxNnz * 4 + 16, &one2, 8);
+    BSG_CUDA(cudaMemcpyAsync(wb + o_empty, e, kMaxNnz * 4 + 64, cudaMemcpyHostToDevice, st));
+  }
+  // 1. every cut of every instance: Williamson and top-chi, one launch each
+  std::vector<CutArgs> cargs(n);
+  for (int i = 0; i < n; ++i) {
+    const int M = Ms[i];
+    BSG_TRY(cut_prepare_at(h, wb + I[i].o_cut, sq[i], M, 1, M - 1, ds[i], chis[i], cut_tol, res[i], num[i], S[i],
+                           kept[i], &cargs[i], st));
+    BSG_CUDA(cudaMemsetAsync(wb + I[i].o_err, 0, 16, st));
+    BSG_CUDA(cudaMemsetAsync(wb + I[i].o_status, 0, (size_t)M * 4, st));
+  }
+  BSG_TRY(cut_launch_batch(h, cargs.data(), n, wb + o_cargs, hs + h_cargs, st));
+  // 2. per instance: Lambda, label rows, keys to the host
+  for (int i = 0; i < n; ++i) {
+    const int M = Ms[i], chi = chis[i], nc = M - 1;
+    const Inst& t = I[i];
+    BSG_TRY(cut_queue_status(cargs[i], 0, nc, reinterpret_cast<int*>(hs + t.h_cut), st));
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
+                 (lambda_kernel<<<nc, 256, 0, st>>>(res[i], chi, site_tol, Lambdas[i],
+                                                    reinterpret_cast<int32_t*>(wb + t.o_above))));
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
+                 (label_rows_kernel<<<dim3((chi + 127) / 128, nc), 128, 0, st>>>(
+                     num[i], (int64_t)chi * (M - 1), M - 1, kept[i], M - 1, 1, chi, table(i, 0),
+                     reinterpret_cast<int*>(wb + t.o_err))));
+    BSG_CUDA(cudaMemcpyAsync(hs + t.h_keys, wb + t.o_key, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
+    BSG_CUDA(cudaMemcpyAsync(hs + t.h_cnt, kept[i], (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+    BSG_CUDA(cudaMemcpyAsync(hs + t.h_above, wb + t.o_above, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+    BSG_CUDA(cudaMemcpyAsync(hs + t.h_err, wb + t.o_err, 4, cudaMemcpyDeviceToHost, st));
+  }
+  // 3. Sigma of every site of every instance in one set of launches
+  SigmaJob* jobs = reinterpret_cast<SigmaJob*>(hs + h_jobs);
+  for (int i = 0; i < n; ++i) {
+    const int M = Ms[i], ldS = 2 * (M - 1);
+    for (int j = 0; j < M; ++j) {
+      const int s = site0[i] + j;
+      SigmaJob jb{};
+      jb.Mr = j == 0 ? M : M - j;
+      if (j == 0) {
+        jb.S_l = S[i];
+        jb.ld_l = ldS;
+        jb.S_r = sq[i];
+        jb.ld_r = 2 * M;
+        jb.m_l = M - 1;
+        jb.first = 1;
+      } else {
+        jb.m_l = j == M - 1 ? 0 : M - 1 - j;
+        jb.S_l = jb.m_l ? S[i] + (size_t)j * ldS * ldS : nullptr;
+        jb.ld_l = ldS;
+        jb.S_r = S[i] + (size_t)(j - 1) * ldS * ldS;
+        jb.ld_r = ldS;
+        jb.first = 0;
+      }
+      jb.Sigma = reinterpret_cast<double2*>(wb + o_sig[s]);
+      jb.Z = reinterpret_cast<double*>(wb + I[i].o_Z) + j;
+      jb.ws = reinterpret_cast<double*>(wb + o_sws[s]);
+      jb.status = reinterpret_cast<int*>(wb + I[i].o_status) + j;
+      jobs[s] = jb;
+    }
+  }
+  BSG_TRY(launch_sigma_jobs(h, jobs, ns, wb + o_jobs, st));
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < Ms[i]; ++j) {
+      const int s = site0[i] + j, Mr = j == 0 ? Ms[i] : Ms[i] - j;
+      if (o_sigc[s] != o_sig[s])
+        BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[s]), (int64_t)(2 * Mr) * (2 * Mr), precision,
+                             wb + o_sigc[s], st));
+    }
+  // 4. one host wait: every instance's cut status and keys
+  BSG_CUDA(cudaStreamSynchronize(st));
+  static const uint64_t zero_key = 0;
+  std::vector<SiteInput> in(ns);
+  for (int i = 0; i < n; ++i) {
+    const int M = Ms[i], chi = chis[i], nc = M - 1;
+    const Inst& t = I[i];
+    BSG_TRY(cut_check_status(h, cargs[i], 0, nc, reinterpret_cast<const int*>(hs + t.h_cut)));
+    if (*reinterpret_cast<const int*>(hs + t.h_err)) {
+      set_error("bsg_build_mps_batch: instance %d: a label row has a multiplicity above %d or more than %d non-zeros",
+                i, kKeyMaxMult, kMaxNnz);
+      return BSG_ERR_LIMIT;
+    }
+    const uint64_t* hkeys = reinterpret_cast<const uint64_t*>(hs + t.h_keys);
+    const int32_t* hcnt = reinterpret_cast<const int32_t*>(hs + t.h_cnt);
+    const int32_t* habove = reinterpret_cast<const int32_t*>(hs + t.h_above);
+    for (int j = 0; j < M; ++j) {
+      const int s = site0[i] + j;
+      SiteInput& si = in[s];
+      si.kind = j == 0 ? BSG_SITE_FIRST : j == M - 1 ? BSG_SITE_LAST : BSG_SITE_MIDDLE;
+      si.Mr = j == 0 ? M : M - j;
+      si.sigma = wb + o_sigc[s];
+      si.sigma64 = reinterpret_cast<const double2*>(wb + o_sig[s]);
+      si.Z = reinterpret_cast<const double*>(wb + t.o_Z) + j;
+      si.gamma = gammas[s];
+      si.d = ds[i];
+      si.chi = chi;
+      if (si.kind != BSG_SITE_LAST) {
+        si.lt = table(i, j);
+        si.KL = habove[j];
+        si.hkey_l = hkeys + (size_t)j * chi;
+        si.lambda = Lambdas[i] + (size_t)j * chi;
+      } else {
+        si.lt = empty;
+        si.KL = 1;
+        si.hkey_l = &zero_key;
+        si.lambda = nullptr;
+      }
+      if (si.kind != BSG_SITE_FIRST) {
+        si.rt = table(i, j - 1);
+        si.KR = hcnt[j - 1];
+        si.hkey_r = hkeys + (size_t)(j - 1) * chi;
+      } else {
+        si.rt = empty;
+        si.KR = 1;
+        si.hkey_r = &zero_key;
+      }
+      if (si.KL == 0 || si.KR == 0) {
+        set_error("bsg_build_mps_batch: instance %d site %d has an empty bond", i, j);
+        return BSG_ERR_INVALID;
+      }
+    }
+  }
+  // 5. the items of every site of every instance: one scatter, one DP launch set
+  BSG_TRY(run_sites(h, in, ds[0], chis[0], precision, out_dtype, h->slot[0], st));
+  // Sigma status (singular A), read after the DP
+  int32_t* sst = reinterpret_cast<int32_t*>(hs + h_sst);
+  for (int i = 0; i < n; ++i)
+    BSG_CUDA(cudaMemcpyAsync(sst + site0[i], wb + I[i].o_status, (size_t)Ms[i] * 4, cudaMemcpyDeviceToHost, st));
+  BSG_CUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < Ms[i]; ++j)
+      if (sst[site0[i] + j]) {
+        set_error("bsg_build_mps_batch: instance %d site %d: the Gaussian unitary's A block is singular", i, j);
+        return BSG_ERR_NO_CONVERGE;
+      }
+  return BSG_OK;
+}
+
 extern "C" int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,
                              double site_tol, int precision, int out_dtype, void* const* gammas_host,
                              double* Lambdas, double* res, int8_t* num, double* S, int32_t* kept,
                              bsg_stream_t stream) {
   return build_mps_impl(h, sq_cov, M, d, chi, cut_tol, site_tol, precision, out_dtype, gammas_host, Lambdas, res,
                         num, S, kept, nullptr, nullptr, stream);
+}
+
+extern "C" int bsg_build_mps_batch(bsg_handle_t h, int n, const double* const* sq_covs, const int* M, const int* d,
+                                   const int* chi, double cut_tol, double site_tol, int precision, int out_dtype,
+                                   void* const* gammas, double* const* Lambdas, double* const* res,
+                                   int8_t* const* num, double* const* S, int32_t* const* kept, bsg_stream_t stream) {
+  BSG_CHECK_ARG(h, "bsg_build_mps_batch: null handle");
+  return build_mps_batch_impl(h, n, sq_covs, M, d, chi, cut_tol, site_tol, precision, out_dtype, gammas, Lambdas,
+                              res, num, S, kept, reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,

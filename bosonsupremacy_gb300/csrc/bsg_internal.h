@@ -171,6 +171,11 @@ constexpr int kCutPhases = 14;       // + FP32 sweeps, FP64 refinement steps, FP
 
 int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                 double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);
+size_t cut_ws_bytes(int M, int L0, int n_cuts, int chi);
+int cut_prepare_at(bsg_handle_t h, char* base, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
+                   double err_tol, double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);
+size_t cut_batch_bytes(const CutArgs* args, int n);
+int cut_launch_batch(bsg_handle_t h, CutArgs* args, int n, void* dev, void* stage, cudaStream_t st);
 int cut_launch_williamson(bsg_handle_t h, const CutArgs& a, int c0, int c1, cudaStream_t st);
 int cut_launch_thermal(bsg_handle_t h, const CutArgs& a, int c0, int c1, cudaStream_t st);
 // status of cuts [c0, c1) into hst[c0..c1) and their sweep counts into hst[n_cuts + c0 ..)
@@ -202,6 +207,20 @@ int gemm_tf32x3(bsg_handle_t h, const float* Ahi, const float* Alo, const float*
                 int M, int N, int K, int ldc, int* d_err, cudaStream_t st, bool profile,
                 const int4* mtiles = nullptr, int n_mtiles = 0, int b_rows = 0);
 int split_tf32(bsg_handle_t h, const float* x, float* hi, float* lo, int64_t n, cudaStream_t st);
+
+// Sliced GEMM (bsg_sliced.cu): C[M, N] fp64 (ldc) = A[M, K] B[N, K]^T from
+// S fixed-point BF16 slices of b bits per FP64 operand row, exact FP32
+// accumulation per slice level on the tcgen05 tensor cores.  Operands are
+// stacked [S, rows, K] bf16 with per-row exponents; grouped mode as for
+// gemm_tf32x3 (B rows of a tile group from mtiles[].z on).
+void sliced_params(int K, int* S, int* b);
+size_t sliced_operand_bytes(int64_t rows, int K, int S);
+int sliced_slice_env(const double2* E, const int32_t* pidx, const double* lam, int rows, int chi, int S, int b,
+                     void* A, int* ea, cudaStream_t st);
+int sliced_slice_gamma(const double2* G, int chi, int d, bool left, int S, int b, void* B, int* eb, cudaStream_t st);
+int sliced_gemm(bsg_handle_t h, const void* A, int a_rows, const int* ea, const void* B, int b_rows, const int* eb,
+                double* C, int M, int N, int K, int ldc, int S, int b, int* d_err, cudaStream_t st, bool profile,
+                const int4* mtiles, int n_mtiles);
 int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st);
 
 }  // namespace bsg

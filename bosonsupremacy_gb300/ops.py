@@ -145,12 +145,12 @@ def cut_spectra(sq_cov, d: int, chi: int, L0: int = 1, n_cuts: Optional[int] = N
 def pattern_amplitudes(Gammas: Sequence[torch.Tensor], Lambdas, patterns, precision="fp64", device: int = 0):
     """Amplitudes of photon patterns [P, M] of the MPS (sampling_cpu.py:75-80
     with fixed photon numbers).  Gammas: M device tensors [chi, chi, d]
-    (complex128 for fp64, complex64 otherwise); Lambdas [M-1, chi]."""
+    (complex128 for fp64 and sliced, complex64 otherwise); Lambdas [M-1, chi]."""
     import ctypes
     dev = torch.device("cuda", device)
     M = len(Gammas)
     chi, _, d = Gammas[0].shape
-    want = C128 if _prec(precision) == _lib.PREC_FP64 else torch.complex64
+    want = C128 if _prec(precision) in (_lib.PREC_FP64, _lib.PREC_SLICED) else torch.complex64
     G = [g.to(device=dev, dtype=want).contiguous() for g in Gammas]
     lam = _dev(Lambdas, torch.float64, dev)
     pat = _dev(patterns, torch.int32, dev)
@@ -161,6 +161,20 @@ def pattern_amplitudes(Gammas: Sequence[torch.Tensor], Lambdas, patterns, precis
     check(_lib.load().bsg_pattern_amplitudes(h.h, ptrs, ptr(lam), M, chi, d, ptr(pat), P, _prec(precision), ptr(amp),
                                              stream_ptr()), "bsg_pattern_amplitudes")
     return amp
+
+
+def gemm_sliced(A, B, device: int = 0) -> torch.Tensor:
+    """C = A B^T in FP64 from BF16 fixed-point slice products on the tensor
+    cores (bsg_gemm_sliced); A [M, K], B [N, K] float64, K % 8 == 0."""
+    dev = torch.device("cuda", device)
+    At = _dev(A, torch.float64, dev)
+    Bt = _dev(B, torch.float64, dev)
+    M, K = At.shape
+    N = Bt.shape[0]
+    C = torch.empty(M, N, dtype=torch.float64, device=dev)
+    h = Handle.get(device)
+    check(_lib.load().bsg_gemm_sliced(h.h, ptr(At), ptr(Bt), ptr(C), M, N, K, stream_ptr()), "bsg_gemm_sliced")
+    return C
 
 
 def displacements(alpha, dd: int, device: int = 0) -> torch.Tensor:

@@ -65,6 +65,49 @@ def build_mps(sq_cov, d: int, chi: int, precision="split", out_dtype=torch.compl
     return MPS(out, lam, res, num, S, kept_h, left_rows, t)
 
 
+def build_mps_batch(sq_covs, ds, chis, precision="split", out_dtype=torch.complex64, err_tol: float = 1e-10,
+                    cut_tol: float = 1e-12, device: int = 0, outs: Optional[List[List[torch.Tensor]]] = None,
+                    handle: Optional[_lib.Handle] = None) -> List[MPS]:
+    """Independent instances (their own M, d, chi) in one library call
+    (bsg_build_mps_batch): one launch per phase for all of them.  Returns
+    one MPS per instance, equal to build_mps of that instance."""
+    dev = torch.device("cuda", device)
+    sqs = [torch.as_tensor(q, dtype=torch.float64).to(dev).contiguous() for q in sq_covs]
+    n = len(sqs)
+    Ms = [q.shape[0] // 2 for q in sqs]
+    if outs is None:
+        outs = [[torch.empty(c, c, d, dtype=out_dtype, device=dev) for _ in range(M)] for M, d, c in zip(Ms, ds, chis)]
+    odt = _lib.OUT_C128 if outs[0][0].dtype == torch.complex128 else _lib.OUT_C64
+    lam = [torch.empty(M - 1, c, dtype=torch.float64, device=dev) for M, c in zip(Ms, chis)]
+    res = [torch.empty(M - 1, c, dtype=torch.float64, device=dev) for M, c in zip(Ms, chis)]
+    num = [torch.empty(M - 1, c, M - 1, dtype=torch.int8, device=dev) for M, c in zip(Ms, chis)]
+    S = [torch.empty(M - 1, 2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device=dev) for M in Ms]
+    kept = [torch.empty(M - 1, dtype=torch.int32, device=dev) for M in Ms]
+
+    def arr(ctype, xs):
+        return (ctype * len(xs))(*xs)
+
+    P = ctypes.c_void_p
+    gptr = arr(P, [g.data_ptr() for o in outs for g in o])
+    h = handle if handle is not None else _lib.Handle.get(device)
+    t0 = time.perf_counter()
+    _lib.check(_lib.load().bsg_build_mps_batch(
+        h.h, n, arr(P, [q.data_ptr() for q in sqs]), arr(ctypes.c_int, Ms), arr(ctypes.c_int, list(ds)),
+        arr(ctypes.c_int, list(chis)), float(cut_tol), float(err_tol), ops._prec(precision), odt, gptr,
+        arr(P, [x.data_ptr() for x in lam]), arr(P, [x.data_ptr() for x in res]), arr(P, [x.data_ptr() for x in num]),
+        arr(P, [x.data_ptr() for x in S]), arr(P, [x.data_ptr() for x in kept]), _lib.stream_ptr()),
+        "bsg_build_mps_batch")
+    torch.cuda.synchronize(dev)
+    t = {"total_s": time.perf_counter() - t0}
+    out = []
+    for i in range(n):
+        kh = kept[i].cpu().numpy()
+        rh = res[i].cpu().numpy()
+        left = np.array([int((rh[c, : kh[c]] > err_tol).sum()) for c in range(Ms[i] - 1)])
+        out.append(MPS(outs[i], lam[i], res[i], num[i], S[i], kh, left, t))
+    return out
+
+
 def build_mps_host(sq_cov_host: torch.Tensor, d: int, chi: int, gammas_host: List[torch.Tensor],
                    lambdas_host: torch.Tensor, precision="split", device: int = 0,
                    device_out: Optional[List[torch.Tensor]] = None, err_tol: float = 1e-10,

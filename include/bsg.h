@@ -46,6 +46,9 @@ typedef struct CUstream_st* bsg_stream_t; /* == cudaStream_t */
 #define BSG_PREC_SPLIT 1 /* split: FP32 products with exact error terms, sums kept as    */
                          /* FP32 pairs (~48-bit significand) -- FP32 pipe, FP64-class     */
 #define BSG_PREC_FP32 2  /* complex64 throughout (the reference's own working precision)  */
+#define BSG_PREC_SLICED 3 /* contraction only: FP64 operands cut into fixed-point BF16     */
+                          /* slices, tcgen05 products with exact FP32 accumulation per    */
+                          /* slice level, FP64 results (complex128 Gamma in)              */
 
 /* site kinds (MPS_cpu.py:402, 430, 461) */
 #define BSG_SITE_FIRST 0
@@ -189,6 +192,24 @@ int bsg_build_mps(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, d
                   int precision, int out_dtype, void* const* gammas_host, double* Lambdas, double* res, int8_t* num,
                   double* S, int32_t* kept, bsg_stream_t stream);
 
+/* The whole MPS of n independent instances, each with its own M[i], d[i] and
+ * chi[i] (the reference builds one state per run; its MPI driver spreads
+ * hafnian batches over idle ranks, distributed_MPS.py:214-240, and A_elem
+ * chunks them, MPS_cpu.py:339-354).  One launch per phase for all instances:
+ * the Williamson and top-chi kernels over every cut of every instance, the
+ * Sigma construction over every site of every instance, one host wait for
+ * the label keys, then one item scatter and one set of hafnian DP launches
+ * over the items of every site of every instance (work items of all
+ * instances bucketed together by partition program).  Results equal
+ * bsg_build_mps of each instance bit for bit.  sq_covs, M, d, chi, Lambdas,
+ * res, num, S, kept: host arrays of n (per-instance buffers as in
+ * bsg_build_mps); gammas: host array of sum(M) device pointers, instance 0's
+ * sites first.  Synchronises `stream`. */
+int bsg_build_mps_batch(bsg_handle_t h, int n, const double* const* sq_covs, const int* M, const int* d,
+                        const int* chi, double cut_tol, double site_tol, int precision, int out_dtype,
+                        void* const* gammas, double* const* Lambdas, double* const* res, int8_t* const* num,
+                        double* const* S, int32_t* const* kept, bsg_stream_t stream);
+
 /* bsg_build_mps plus the download of its outputs: each group's DP runs in four
  * site parts and each part's Gammas are copied from gammas_dev[i] (device) to
  * gammas_pinned[i] (pinned host) as soon as that part is done, overlapping the
@@ -208,11 +229,14 @@ int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, in
  * meet-in-the-middle: left environments of every distinct prefix up to site
  * (M-1)/2, right environments of every distinct suffix, one dot per pattern;
  * every (level, photon number) group is one batched complex GEMM.
- * precision: BSG_PREC_FP64 (FP64 CUDA cores), BSG_PREC_FP32 (FP32 CUDA cores)
- * or BSG_PREC_SPLIT (3-way split TF32 products on the tcgen05 tensor cores,
- * FP32 accumulation).  Synchronises `stream`: the prefix tries are planned on
- * the GPU, and the host reads each level's row counts to size its GEMM
- * launches. */
+ * precision: BSG_PREC_FP64 (FP64 CUDA cores), BSG_PREC_FP32 (FP32 CUDA cores),
+ * BSG_PREC_SPLIT (3-way split TF32 products on the tcgen05 tensor cores,
+ * FP32 accumulation; complex64 Gamma, ~1e-4 relative in the probabilities)
+ * or BSG_PREC_SLICED (complex128 Gamma and FP64 environments, every level's
+ * GEMM as fixed-point BF16 slice products on the tcgen05 tensor cores with
+ * exact FP32 accumulation, see bsg_gemm_sliced; needs chi % 4 == 0).
+ * Synchronises `stream`: the prefix tries are planned on the GPU, and the
+ * host reads each level's row counts to size its GEMM launches. */
 int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                            const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
 
@@ -221,6 +245,17 @@ int bsg_pattern_amplitudes(bsg_handle_t h, const void* const* Gammas, const doub
  * arguments and results to bsg_pattern_amplitudes. */
 int bsg_contract_patterns(bsg_handle_t h, const void* const* Gammas, const double* Lambdas, int M, int chi, int d,
                           const int32_t* patterns, int64_t P, int precision, double* amp, bsg_stream_t stream);
+
+/* FP64 GEMM from BF16 tensor-core products (no counterpart in the reference;
+ * the primitive of BSG_PREC_SLICED): C[M, N] = A[M, K] B[N, K]^T, all three
+ * row-major float64 on the device.  Every row of A and of B is scaled by a
+ * power of two and cut into S fixed-point slices of b bits (b such that
+ * 3 K 2^(2b) < 2^23, S = ceil(42 / b)); the slice products of each level
+ * s + t <= 2 sum exactly in FP32 in TMEM, the rest below 2^-40 of the
+ * result, so C carries ~42 bits of each row's scale.  0 < K <= 32768,
+ * K % 8 == 0.  Synchronises `stream`. */
+int bsg_gemm_sliced(bsg_handle_t h, const double* A, const double* B, double* C, int M, int N, int K,
+                    bsg_stream_t stream);
 
 /* ---- sampling ------------------------------------------------------------
  * Photon-number samples of the lossy state from the MPS, replacing

@@ -8,7 +8,9 @@ from oracle import reference_mps as R
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 2e-5), ("split", 2e-5)])
+# sliced: ~42 bits of each operand row's scale (fixed point per row), so a
+# probability 1e-6 of the largest keeps ~1e-10 relative
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 2e-5), ("split", 2e-5), ("sliced", 1e-9)])
 def test_pattern_probabilities_on_reference_mps(cuda, golden, prec, tol):
     import torch
     from bosonsupremacy_gb300 import ops

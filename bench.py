@@ -31,9 +31,10 @@ if REPO not in sys.path:
 METRIC = "full-MPS build throughput (sites/s), split-precision batched kernels"
 UNIT = "sites/s"
 # DRAM bytes (read + write) per complex multiply-add of the split hafnian DP,
-# from the ncu capture of the M=144, d=8, chi=1024 build's DP launches
-# (profiles/dp_kernel_M144_d8_chi1024_traffic.md); None until captured.
-DP_DRAM_BYTES_PER_CMAC = None
+# from the ncu capture of the M=50, d=6, chi=256 build's DP launches (725 MB
+# for 3.182e8 multiply-adds, profiles/dp_kernel_traffic_M50_d6_chi256.md),
+# scaled to each launch's work.
+DP_DRAM_BYTES_PER_CMAC = 725e6 / 3.182e8
 
 
 def parse():
@@ -631,8 +632,9 @@ def main():
                          "per complex multiply-add, so fp32_op_busy_frac = achieved / (8 x half the FMA flop peak / "
                          "those operations) is the FP32 pipe's busy fraction; fp64_equivalent_frac compares the "
                          "FP64-accurate result rate with the FP64 pipe's measured peak; traffic = DRAM bytes per "
-                         "DP launch from the ncu capture of the M=144 build's DP launches, per complex "
-                         "multiply-add, times this launch's work (profiles/dp_kernel_M144_d8_chi1024_traffic.md)")}
+                         "DP launch: 2.28 bytes per complex multiply-add measured by ncu on the M=50 build's DP "
+                         "launches, times this workload's multiply-adds per launch "
+                         "(profiles/dp_kernel_traffic_M50_d6_chi256.md)")}
     roof["peak_source"] = "FMA peak measured on this GPU by bsg_fma_peak (register FMA loop on every SM)"
     roof["launch_ms_mean"] = prof[dom]["ms"] / max(1, prof[dom]["launches"])
     roof["work"] = ("8 flops per complex multiply-add of the repetition-aware partition programs "

@@ -51,6 +51,7 @@ SIGNATURES = {
     "bsg_build_mps": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_build_mps_to_host": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_build_mps_batch": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "bsg_build_sites": (_I, [_P, _P, _I, _I, _I, _D, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "bsg_profile_enable": (_I, [_P, _I]),
     "bsg_profile_read": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_L), C.POINTER(_D)]),
     "bsg_profile_reset": (_I, [_P]),

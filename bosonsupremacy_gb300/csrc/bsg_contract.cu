@@ -414,7 +414,8 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   const size_t sa_bytes = sliced ? al(sliced_operand_bytes(max_rows, 2 * chi, S)) : 0;
   const size_t sb_bytes = sliced ? al(sliced_operand_bytes((int64_t)d * 2 * chi, 2 * chi, S)) : 0;
   const size_t se_bytes = sliced ? al((size_t)(max_rows + (int64_t)d * 2 * chi) * 4) : 0;
-  const size_t need = 4 * env_bytes + 2 * a_bytes + 2 * b_bytes + sa_bytes + sb_bytes + se_bytes + 256;
+  const size_t st_bytes = sliced ? al(sliced_gamma_scratch_bytes(chi, d)) : 0;
+  const size_t need = 4 * env_bytes + 2 * a_bytes + 2 * b_bytes + sa_bytes + sb_bytes + se_bytes + st_bytes + 256;
   BSG_TRY(h->contract_ws.ensure(need));
   char* base = reinterpret_cast<char*>(h->contract_ws.ptr);
   char* sp_base = base + 4 * env_bytes;
@@ -427,7 +428,8 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
   void* Bsl = sl_base + sa_bytes;
   int* ea = reinterpret_cast<int*>(sl_base + sa_bytes + sb_bytes);
   int* eb = ea + max_rows;
-  int* d_err = reinterpret_cast<int*>(sl_base + sa_bytes + sb_bytes + se_bytes);
+  void* Tsl = sl_base + sa_bytes + sb_bytes + se_bytes;  // transposed Gamma block of the level's site
+  int* d_err = reinterpret_cast<int*>(sl_base + sa_bytes + sb_bytes + se_bytes + st_bytes);
   if (umma || sliced) BSG_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
   T* E[4] = {reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + env_bytes),
              reinterpret_cast<T*>(base + 2 * env_bytes), reinterpret_cast<T*>(base + 3 * env_bytes)};
@@ -486,7 +488,7 @@ static int run_contraction(bsg_handle_t h, const void* const* Gd, const double* 
           const int rows = sp.rows(int(l));
           const int sd = is_left ? 0 : 1;
           const int t0 = tile_off[sd][l], nt = tile_off[sd][l + 1] - t0;
-          if (sliced_slice_gamma(reinterpret_cast<const double2*>(G), chi, d, is_left, S, bits, Bsl, eb, st) !=
+          if (sliced_slice_gamma(reinterpret_cast<const double2*>(G), chi, d, is_left, S, bits, Bsl, eb, Tsl, st) !=
                   BSG_OK ||
               sliced_slice_env(reinterpret_cast<const double2*>(prev), parent, lm, rows, chi, S, bits, Asl, ea, st) !=
                   BSG_OK ||

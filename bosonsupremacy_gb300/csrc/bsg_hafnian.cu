@@ -1864,16 +1864,20 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
 // scatter and one set of DP launches over the items of every site of every
 // instance (run_sites with per-site d and chi).  Per-instance outputs as in
 // bsg_build_mps; gammas holds the instances' site pointers back to back.
+// With cuts_given the cut data (res, num, S, kept) are inputs -- the kron
+// step's files -- and only sites [lo[i], hi[i]) of instance i are built
+// (their Lambda rows and label tables from the cuts they read).
 static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, const int* Ms, const int* ds,
                                 const int* chis, double cut_tol, double site_tol, int precision, int out_dtype,
                                 void* const* gammas, double* const* Lambdas, double* const* res,
-                                int8_t* const* num, double* const* S, int32_t* const* kept, cudaStream_t st) {
+                                int8_t* const* num, double* const* S, int32_t* const* kept, cudaStream_t st,
+                                bool cuts_given = false, const int* lo = nullptr, const int* hi = nullptr) {
   BSG_CHECK_ARG(n >= 1, "bsg_build_mps_batch: need at least one instance");
   BSG_CHECK_ARG(sq && Ms && ds && chis && gammas && Lambdas && res && num && S && kept,
                 "bsg_build_mps_batch: null pointer");
   BSG_CHECK_ARG(precision >= 0 && precision <= 2, "bsg_build_mps_batch: bad precision %d", precision);
   BSG_CHECK_ARG(out_dtype == BSG_OUT_C64 || out_dtype == BSG_OUT_C128, "bsg_build_mps_batch: bad out_dtype");
-  std::vector<int> site0(n + 1, 0);
+  std::vector<int> site0(n + 1, 0), slo(n), shi(n), clo(n), chi_(n);
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i], d = ds[i], chi = chis[i];
     BSG_CHECK_ARG(sq[i] && Lambdas[i] && res[i] && num[i] && S[i] && kept[i],
@@ -1882,7 +1886,14 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     BSG_CHECK_ARG(chi >= d && chi <= 2048, "bsg_build_mps_batch: instance %d: need d <= chi <= 2048", i);
     BSG_CHECK_ARG(d >= 1 && d <= kKeyMaxMult + 1, "bsg_build_mps_batch: instance %d: d=%d outside [1, %d]", i, d,
                   kKeyMaxMult + 1);
-    site0[i + 1] = site0[i] + M;
+    slo[i] = lo ? lo[i] : 0;
+    shi[i] = hi ? hi[i] : M;
+    BSG_CHECK_ARG(0 <= slo[i] && slo[i] < shi[i] && shi[i] <= M, "bsg_build_mps_batch: instance %d: sites [%d, %d) "
+                  "outside [0, %d)", i, slo[i], shi[i], M);
+    // cuts the sites read: [lo - 1, hi) within [0, M - 1)
+    clo[i] = std::max(0, slo[i] - 1);
+    chi_[i] = std::min(shi[i], M - 1);
+    site0[i + 1] = site0[i] + (shi[i] - slo[i]);
   }
   const int ns = site0[n];
   for (int s = 0; s < ns; ++s) BSG_CHECK_ARG(gammas[s], "bsg_build_mps_batch: Gamma pointer %d is NULL", s);
@@ -1912,7 +1923,7 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     const int M = Ms[i], chi = chis[i], nc = M - 1;
     total_cuts += nc;
     Inst& t = I[i];
-    t.o_cut = carve(cut_ws_bytes(M, 1, nc, chi));
+    t.o_cut = cuts_given ? carve(0) : carve(cut_ws_bytes(M, 1, nc, chi));
     t.o_ent = carve((size_t)nc * chi * kMaxNnz * 4);
     t.o_nnz = carve((size_t)nc * chi * 4);
     t.o_sum = carve((size_t)nc * chi * 4);
@@ -1923,8 +1934,8 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     t.o_err = carve(16);
     t.o_Z = carve((size_t)M * 8);
     t.o_status = carve((size_t)M * 4);
-    for (int j = 0; j < M; ++j) {
-      const int s = site0[i] + j, Mr = j == 0 ? M : M - j;
+    for (int j = slo[i]; j < shi[i]; ++j) {
+      const int s = site0[i] + j - slo[i], Mr = j == 0 ? M : M - j;
       o_sig[s] = carve((size_t)(2 * Mr) * (2 * Mr) * 16);
       o_sigc[s] = precision == BSG_PREC_FP64 ? o_sig[s] : carve((size_t)(2 * Mr) * (2 * Mr) * prec_bytes(precision));
       o_sws[s] = carve(sigma_ws_bytes(Mr));
@@ -1969,35 +1980,42 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
   std::vector<CutArgs> cargs(n);
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i];
-    BSG_TRY(cut_prepare_at(h, wb + I[i].o_cut, sq[i], M, 1, M - 1, ds[i], chis[i], cut_tol, res[i], num[i], S[i],
-                           kept[i], &cargs[i], st));
+    if (!cuts_given)
+      BSG_TRY(cut_prepare_at(h, wb + I[i].o_cut, sq[i], M, 1, M - 1, ds[i], chis[i], cut_tol, res[i], num[i], S[i],
+                             kept[i], &cargs[i], st));
     BSG_CUDA(cudaMemsetAsync(wb + I[i].o_err, 0, 16, st));
     BSG_CUDA(cudaMemsetAsync(wb + I[i].o_status, 0, (size_t)M * 4, st));
   }
-  BSG_TRY(cut_launch_batch(h, cargs.data(), n, wb + o_cargs, hs + h_cargs, st));
-  // 2. per instance: Lambda, label rows, keys to the host
+  if (!cuts_given) BSG_TRY(cut_launch_batch(h, cargs.data(), n, wb + o_cargs, hs + h_cargs, st));
+  // 2. per instance: Lambda, label rows, keys to the host (the cuts its sites read)
   for (int i = 0; i < n; ++i) {
-    const int M = Ms[i], chi = chis[i], nc = M - 1;
+    const int M = Ms[i], chi = chis[i], nc = M - 1, c0 = clo[i], nci = chi_[i] - clo[i];
     const Inst& t = I[i];
-    BSG_TRY(cut_queue_status(cargs[i], 0, nc, reinterpret_cast<int*>(hs + t.h_cut), st));
-    BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
-                 (lambda_kernel<<<nc, 256, 0, st>>>(res[i], chi, site_tol, Lambdas[i],
-                                                    reinterpret_cast<int32_t*>(wb + t.o_above))));
-    BSG_PROFILED(h, BSG_K_PREP, st, (double)nc * chi,
-                 (label_rows_kernel<<<dim3((chi + 127) / 128, nc), 128, 0, st>>>(
-                     num[i], (int64_t)chi * (M - 1), M - 1, kept[i], M - 1, 1, chi, table(i, 0),
-                     reinterpret_cast<int*>(wb + t.o_err))));
-    BSG_CUDA(cudaMemcpyAsync(hs + t.h_keys, wb + t.o_key, (size_t)nc * chi * 8, cudaMemcpyDeviceToHost, st));
-    BSG_CUDA(cudaMemcpyAsync(hs + t.h_cnt, kept[i], (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
-    BSG_CUDA(cudaMemcpyAsync(hs + t.h_above, wb + t.o_above, (size_t)nc * 4, cudaMemcpyDeviceToHost, st));
+    if (!cuts_given) BSG_TRY(cut_queue_status(cargs[i], 0, nc, reinterpret_cast<int*>(hs + t.h_cut), st));
+    if (nci > 0) {
+      BSG_PROFILED(h, BSG_K_PREP, st, (double)nci * chi,
+                   (lambda_kernel<<<nci, 256, 0, st>>>(res[i] + (size_t)c0 * chi, chi, site_tol,
+                                                       Lambdas[i] + (size_t)c0 * chi,
+                                                       reinterpret_cast<int32_t*>(wb + t.o_above) + c0)));
+      BSG_PROFILED(h, BSG_K_PREP, st, (double)nci * chi,
+                   (label_rows_kernel<<<dim3((chi + 127) / 128, nci), 128, 0, st>>>(
+                       num[i] + (size_t)c0 * chi * (M - 1), (int64_t)chi * (M - 1), M - 1, kept[i] + c0, M - 1 - c0,
+                       1, chi, table(i, c0), reinterpret_cast<int*>(wb + t.o_err))));
+      BSG_CUDA(cudaMemcpyAsync(hs + t.h_keys + (size_t)c0 * chi * 8, wb + t.o_key + (size_t)c0 * chi * 8,
+                               (size_t)nci * chi * 8, cudaMemcpyDeviceToHost, st));
+      BSG_CUDA(cudaMemcpyAsync(hs + t.h_cnt + (size_t)c0 * 4, kept[i] + c0, (size_t)nci * 4, cudaMemcpyDeviceToHost,
+                               st));
+      BSG_CUDA(cudaMemcpyAsync(hs + t.h_above + (size_t)c0 * 4, wb + t.o_above + (size_t)c0 * 4, (size_t)nci * 4,
+                               cudaMemcpyDeviceToHost, st));
+    }
     BSG_CUDA(cudaMemcpyAsync(hs + t.h_err, wb + t.o_err, 4, cudaMemcpyDeviceToHost, st));
   }
   // 3. Sigma of every site of every instance in one set of launches
   SigmaJob* jobs = reinterpret_cast<SigmaJob*>(hs + h_jobs);
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i], ldS = 2 * (M - 1);
-    for (int j = 0; j < M; ++j) {
-      const int s = site0[i] + j;
+    for (int j = slo[i]; j < shi[i]; ++j) {
+      const int s = site0[i] + j - slo[i];
       SigmaJob jb{};
       jb.Mr = j == 0 ? M : M - j;
       if (j == 0) {
@@ -2024,8 +2042,8 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
   }
   BSG_TRY(launch_sigma_jobs(h, jobs, ns, wb + o_jobs, st));
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < Ms[i]; ++j) {
-      const int s = site0[i] + j, Mr = j == 0 ? Ms[i] : Ms[i] - j;
+    for (int j = slo[i]; j < shi[i]; ++j) {
+      const int s = site0[i] + j - slo[i], Mr = j == 0 ? Ms[i] : Ms[i] - j;
       if (o_sigc[s] != o_sig[s])
         BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[s]), (int64_t)(2 * Mr) * (2 * Mr), precision,
                              wb + o_sigc[s], st));
@@ -2037,7 +2055,7 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i], chi = chis[i], nc = M - 1;
     const Inst& t = I[i];
-    BSG_TRY(cut_check_status(h, cargs[i], 0, nc, reinterpret_cast<const int*>(hs + t.h_cut)));
+    if (!cuts_given) BSG_TRY(cut_check_status(h, cargs[i], 0, nc, reinterpret_cast<const int*>(hs + t.h_cut)));
     if (*reinterpret_cast<const int*>(hs + t.h_err)) {
       set_error("bsg_build_mps_batch: instance %d: a label row has a multiplicity above %d or more than %d non-zeros",
                 i, kKeyMaxMult, kMaxNnz);
@@ -2046,8 +2064,8 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     const uint64_t* hkeys = reinterpret_cast<const uint64_t*>(hs + t.h_keys);
     const int32_t* hcnt = reinterpret_cast<const int32_t*>(hs + t.h_cnt);
     const int32_t* habove = reinterpret_cast<const int32_t*>(hs + t.h_above);
-    for (int j = 0; j < M; ++j) {
-      const int s = site0[i] + j;
+    for (int j = slo[i]; j < shi[i]; ++j) {
+      const int s = site0[i] + j - slo[i];
       SiteInput& si = in[s];
       si.kind = j == 0 ? BSG_SITE_FIRST : j == M - 1 ? BSG_SITE_LAST : BSG_SITE_MIDDLE;
       si.Mr = j == 0 ? M : M - j;
@@ -2088,11 +2106,12 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
   // Sigma status (singular A), read after the DP
   int32_t* sst = reinterpret_cast<int32_t*>(hs + h_sst);
   for (int i = 0; i < n; ++i)
-    BSG_CUDA(cudaMemcpyAsync(sst + site0[i], wb + I[i].o_status, (size_t)Ms[i] * 4, cudaMemcpyDeviceToHost, st));
+    BSG_CUDA(cudaMemcpyAsync(sst + site0[i], reinterpret_cast<int32_t*>(wb + I[i].o_status) + slo[i],
+                             (size_t)(shi[i] - slo[i]) * 4, cudaMemcpyDeviceToHost, st));
   BSG_CUDA(cudaStreamSynchronize(st));
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < Ms[i]; ++j)
-      if (sst[site0[i] + j]) {
+    for (int j = slo[i]; j < shi[i]; ++j)
+      if (sst[site0[i] + j - slo[i]]) {
         set_error("bsg_build_mps_batch: instance %d site %d: the Gaussian unitary's A block is singular", i, j);
         return BSG_ERR_NO_CONVERGE;
       }
@@ -2114,6 +2133,21 @@ extern "C" int bsg_build_mps_batch(bsg_handle_t h, int n, const double* const* s
   BSG_CHECK_ARG(h, "bsg_build_mps_batch: null handle");
   return build_mps_batch_impl(h, n, sq_covs, M, d, chi, cut_tol, site_tol, precision, out_dtype, gammas, Lambdas,
                               res, num, S, kept, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bsg_build_sites(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double site_tol,
+                               int precision, int out_dtype, int s0, int s1, const double* res, const int8_t* num,
+                               const double* S, const int32_t* kept, void* const* gammas, double* Lambdas,
+                               bsg_stream_t stream) {
+  BSG_CHECK_ARG(h, "bsg_build_sites: null handle");
+  const double* sq[1] = {sq_cov};
+  double* lam[1] = {Lambdas};
+  double* rs[1] = {const_cast<double*>(res)};
+  int8_t* nm[1] = {const_cast<int8_t*>(num)};
+  double* Ss[1] = {const_cast<double*>(S)};
+  int32_t* kp[1] = {const_cast<int32_t*>(kept)};
+  return build_mps_batch_impl(h, 1, sq, &M, &d, &chi, 0.0, site_tol, precision, out_dtype, gammas, lam, rs, nm, Ss,
+                              kp, reinterpret_cast<cudaStream_t>(stream), true, &s0, &s1);
 }
 
 extern "C" int bsg_build_mps_to_host(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double cut_tol,

@@ -217,7 +217,9 @@ void sliced_params(int K, int* S, int* b);
 size_t sliced_operand_bytes(int64_t rows, int K, int S);
 int sliced_slice_env(const double2* E, const int32_t* pidx, const double* lam, int rows, int chi, int S, int b,
                      void* A, int* ea, cudaStream_t st);
-int sliced_slice_gamma(const double2* G, int chi, int d, bool left, int S, int b, void* B, int* eb, cudaStream_t st);
+size_t sliced_gamma_scratch_bytes(int chi, int d);
+int sliced_slice_gamma(const double2* G, int chi, int d, bool left, int S, int b, void* B, int* eb, void* scratch,
+                       cudaStream_t st);
 int sliced_gemm(bsg_handle_t h, const void* A, int a_rows, const int* ea, const void* B, int b_rows, const int* eb,
                 double* C, int M, int N, int K, int ldc, int S, int b, int* d_err, cudaStream_t st, bool profile,
                 const int4* mtiles, int n_mtiles);

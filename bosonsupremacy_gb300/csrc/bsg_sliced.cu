@@ -262,25 +262,35 @@ __global__ void __launch_bounds__(192, 1)
       const int row = m0 + q * 32 + lane;
       const bool live = row < m_end;
       const int er = live ? g.ea[row] : 0;
+      // The levels are summed exactly as an int64 in units of 2^-G (G = b x the
+      // last exact level): level a < 7 holds an integer times 2^(-b a), so
+      // acc_a 2^(b a) converts to an int64 exactly; the combined levels 7+ are
+      // rounded to the unit (below 2^-50 of the level-0 scale).  One
+      // conversion and one power-of-two product per output reach FP64, the
+      // FP64 pipe being ~1/64 of the FP32 one on this GPU.
+      const int G = g.b * (g.S - 1 < kAcc - 2 ? g.S - 1 : kAcc - 2);
       for (int c = 0; c < TN; c += 16) {
-        // smallest levels first; every level but the last is an exact FP32 sum
-        double v[16];
+        long long v[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = 0.0;
+        for (int j = 0; j < 16; ++j) v[j] = 0;
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c;
-        for (int a = n_acc - 1; a >= 0; --a) {
+        for (int a = 0; a < n_acc; ++a) {
           uint32_t r[16];
           tmem_ld16(lane_base + a * TN, r);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          const bool exact = a < kAcc - 1;
+          const int up = exact ? g.b * a : G;                      // to an integer
+          const float pw = __int_as_float((127 + up) << 23);      // 2^up (up <= 126)
+          const int sh = exact ? G - g.b * a : 0;                  // to units of 2^-G
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] += (double)__uint_as_float(r[j]);
+          for (int j = 0; j < 16; ++j) v[j] += __float2ll_rn(__uint_as_float(r[j]) * pw) << sh;
         }
         if (live) {
           double* out = g.C + (int64_t)row * g.ldc + n0 + c;
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int col = n0 + c + j;
-            if (col < g.N) out[j] = ldexp(v[j], er + g.eb[b_row0 + col] - 2 * g.b);
+            if (col < g.N) out[j] = ldexp(__ll2double_rn(v[j]), er + g.eb[b_row0 + col] - 2 * g.b - G);
           }
         }
       }
@@ -298,27 +308,57 @@ __global__ void __launch_bounds__(192, 1)
   if (threadIdx.x == 0 && *fail) atomicExch(g.err, 1);
 }
 
-// One warp per row: the row's power-of-two scale and its S slices.
-// x(q) is produced by `src`; slices land at out[s * slice_stride + row * K + q].
+// Row exponent of a row whose largest magnitude has the IEEE bits `mx`:
+// the e with max |x| < 2^e (frexp's exponent), 0 for an all-zero row.
+__device__ __forceinline__ int row_exponent(unsigned long long mx) {
+  const int ex = int((mx >> 52) & 0x7ff);
+  return mx == 0 ? 0 : (ex == 0 ? -1022 : ex - 1022);
+}
+
+// The S balanced b-bit digits of x 2^-e (|x| < 2^e) by integer arithmetic:
+// x 2^-e = X 2^-62 with X an int64 (the 53-bit significand shifted into
+// place; bits below 2^-62 of the row scale dropped), then digit s is X
+// rounded to a multiple of 2^(62 - b (s + 1)), taken off X.  Slice s holds
+// m_s 2^(-b s) (exact in BF16: |m_0| <= 2^b, |m_s| <= 2^(b-1) for s > 0).
+__device__ __forceinline__ void slice_value(double x, int e, int b, int S, __nv_bfloat16* out, int64_t stride) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int ex = int((bits >> 52) & 0x7ff);
+  long long X = 0;
+  if (ex != 0) {  // zero and subnormals (below 2^-1022) contribute nothing
+    const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1075 + 62 - e;  // <= 9 since |x| < 2^e
+    const unsigned long long m = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> -sh) : 0ull);
+    X = (bits >> 63) ? -(long long)m : (long long)m;
+  }
+  for (int s = 0; s < S; ++s) {
+    const int shift = 62 - b * (s + 1);
+    const long long m = (X + (1ll << (shift - 1))) >> shift;  // nearest multiple of 2^shift (ties up)
+    X -= m << shift;
+    // m_s 2^(-b s): the power of two built from its exponent bits (b s <= 126)
+    out[(int64_t)s * stride] = __float2bfloat16_rn(__int2float_rn((int)m) * __int_as_float((127 - b * s) << 23));
+  }
+}
+
+// One warp per row: the row's power-of-two scale (from the IEEE bits of its
+// largest magnitude, an integer max) and its S slices.  x(q) is produced by
+// `src`; slices land at out[s * slice_stride + row * K + q].
 template <class Src>
 __device__ __forceinline__ void slice_row(const Src& src, int row, int K, int S, int b, __nv_bfloat16* out,
                                           int64_t slice_stride, int* e_out) {
   const int lane = threadIdx.x & 31;
-  double mx = 0.0;
-  for (int q = lane; q < K; q += 32) mx = fmax(mx, fabs(src(q)));
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1): |x| < 2^e
-  if (lane == 0) e_out[row] = e;
+  unsigned long long mx = 0;
   for (int q = lane; q < K; q += 32) {
-    double x = ldexp(src(q), -e);  // |x| < 1
-    for (int s = 0; s < S; ++s) {
-      const double t = ldexp(x, b);
-      const double m = rint(t);
-      out[(int64_t)s * slice_stride + (int64_t)row * K + q] = __float2bfloat16_rn((float)ldexp(m, -b * s));
-      x = t - m;
-    }
+    const unsigned long long a = (unsigned long long)__double_as_longlong(src(q)) & 0x7fffffffffffffffull;
+    mx = a > mx ? a : mx;
   }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = v > mx ? v : mx;
+  }
+  const int e = row_exponent(mx);
+  if (lane == 0) e_out[row] = e;
+  __nv_bfloat16* o = out + (int64_t)row * K;
+  for (int q = lane; q < K; q += 32) slice_value(src(q), e, b, S, o + q, slice_stride);
 }
 
 // A rows of a contraction level: x(r, q) = E[parent[r]][q / 2].{re, im} * lam[q / 2].
@@ -327,25 +367,49 @@ __global__ void slice_env_kernel(const double2* __restrict__ E, const int32_t* _
                                  __nv_bfloat16* __restrict__ A, int a_rows, int* __restrict__ ea) {
   const int row = int(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (row >= rows) return;  // warp-uniform
-  const double2* e = E + (int64_t)pidx[row] * chi;
-  auto src = [&](int q) {
-    const double2 v = e[q >> 1];
-    return ((q & 1) ? v.y : v.x) * lam[q >> 1];
-  };
+  const double* e = reinterpret_cast<const double*>(E + (int64_t)pidx[row] * chi);
+  auto src = [&](int q) { return e[q] * lam[q >> 1]; };
   slice_row(src, row, 2 * chi, S, b, A, (int64_t)a_rows * 2 * chi, ea);
 }
 
+// T[n][c][k] = Gamma[k, c, n] (left) or Gamma[c, k, n] (right): 16 x 16 (c, k)
+// tiles of all d photon numbers through shared memory, so both the reads
+// (d-element runs of Gamma) and the writes (k-contiguous rows of T) coalesce.
+constexpr int kTT = 16;
+__global__ void transpose_gamma_kernel(const double2* __restrict__ G, int chi, int d, int left,
+                                       double2* __restrict__ T) {
+  extern __shared__ double2 tile[];  // [kTT][kTT][d]: (a, b, n) with a the slower Gamma index
+  const int c0 = blockIdx.y * kTT, k0 = blockIdx.x * kTT;
+  // Gamma index of tile entry (a, b): left a = k, b = c; right a = c, b = k
+  const int a0 = left ? k0 : c0, b0 = left ? c0 : k0;
+  const int per = kTT * d;  // contiguous elements of one a-row of the tile
+  for (int t = threadIdx.x; t < kTT * per; t += blockDim.x) {
+    const int a = t / per, r = t % per;
+    const int ga = a0 + a, gb = b0 + r / d;
+    if (ga < chi && gb < chi) tile[t] = G[((int64_t)ga * chi + gb) * d + (r % d)];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < d * kTT * kTT; t += blockDim.x) {
+    const int n = t / (kTT * kTT), cc = (t / kTT) % kTT, kk = t % kTT;
+    const int c = c0 + cc, k = k0 + kk;
+    if (c >= chi || k >= chi) continue;
+    const int a = left ? kk : cc, bb = left ? cc : kk;
+    T[((int64_t)n * chi + c) * chi + k] = tile[(a * kTT + bb) * d + n];
+  }
+}
+
 // B rows of photon number n: Bt[n 2chi + 2c + eo][2k + ei] = {{Re, Im}, {-Im, Re}}[ei][eo] of
-// G(k, c) = Gamma[k, c, n] (left) or Gamma[c, k, n] (right).
-__global__ void slice_gamma_kernel(const double2* __restrict__ G, int chi, int d, int left, int S, int b,
+// T[n][c][k] (the transposed Gamma block).
+__global__ void slice_gamma_kernel(const double2* __restrict__ T, int chi, int d, int S, int b,
                                    __nv_bfloat16* __restrict__ B, int b_rows, int* __restrict__ eb) {
   const int row = int(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int K2 = 2 * chi;
   if (row >= d * K2) return;  // warp-uniform
   const int n = row / K2, rc = row % K2, c = rc >> 1, eo = rc & 1;
+  const double2* t = T + ((int64_t)n * chi + c) * chi;
   auto src = [&](int q) {
-    const int k = q >> 1, ei = q & 1;
-    const double2 v = left ? G[((int64_t)k * chi + c) * d + n] : G[((int64_t)c * chi + k) * d + n];
+    const double2 v = t[q >> 1];
+    const int ei = q & 1;
     return ei == 0 ? (eo == 0 ? v.x : v.y) : (eo == 0 ? -v.y : v.x);
   };
   slice_row(src, row, K2, S, b, B, (int64_t)b_rows * K2, eb);
@@ -417,10 +481,20 @@ int sliced_slice_env(const double2* E, const int32_t* pidx, const double* lam, i
   return BSG_OK;
 }
 
-int sliced_slice_gamma(const double2* G, int chi, int d, bool left, int S, int b, void* B, int* eb, cudaStream_t st) {
+size_t sliced_gamma_scratch_bytes(int chi, int d) { return (size_t)d * chi * chi * 16; }
+
+int sliced_slice_gamma(const double2* G, int chi, int d, bool left, int S, int b, void* B, int* eb, void* scratch,
+                       cudaStream_t st) {
   const int rows = d * 2 * chi;
+  double2* T = reinterpret_cast<double2*>(scratch);
+  const unsigned nt = unsigned((chi + sliced::kTT - 1) / sliced::kTT);
+  const size_t smem = (size_t)sliced::kTT * sliced::kTT * d * sizeof(double2);
+  if (smem > 48 * 1024)
+    BSG_CUDA(cudaFuncSetAttribute(sliced::transpose_gamma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  sliced::transpose_gamma_kernel<<<dim3(nt, nt), 256, smem, st>>>(G, chi, d, left ? 1 : 0, T);
   sliced::slice_gamma_kernel<<<unsigned(((int64_t)rows * 32 + 255) / 256), 256, 0, st>>>(
-      G, chi, d, left ? 1 : 0, S, b, reinterpret_cast<__nv_bfloat16*>(B), rows, eb);
+      T, chi, d, S, b, reinterpret_cast<__nv_bfloat16*>(B), rows, eb);
   BSG_CUDA(cudaGetLastError());
   return BSG_OK;
 }

@@ -11,8 +11,10 @@ by bosonsupremacy_gb300.kron -- and the same outputs: Gamma_i.npy complex64
 Function-level mirror of the reference's operator API (same names, argument
 meaning and errors): ``hafnian(A)``, ``A_elem(Sigma, target, denominator,
 max_memory_in_gb)``, ``get_target(num)``, ``push_to_end(array)``,
-``get_Sigma_Z(S_l, S_r)`` (replaces get_U2_sq_U1 + get_Sigma) and
-``build_site(...)``.  All arithmetic runs in libbsg; there is no CPU path.
+``get_Sigma_Z(S_l, S_r)`` (replaces get_U2_sq_U1 + get_Sigma),
+``build_site(...)`` (one site) and ``build_sites(...)`` (a site range in one
+pipelined call, what the script runs).  All arithmetic runs in libbsg; there
+is no CPU path.
 """
 from __future__ import annotations
 
@@ -119,6 +121,56 @@ def build_site(site, M, d, chi, sq_cov, path, precision="split", out_dtype=torch
     return G, lam
 
 
+def load_cuts(path, M, chi, cuts, device: int = 0):
+    """Device arrays of the given cuts' files (res_c, num_c, S_c as kron_cpu.py
+    writes them; res may be float16 or float64) in bsg_cut_spectra's layout:
+    res [M-1, chi] float64, num [M-1, chi, M-1] int8, S [M-1, 2(M-1), 2(M-1)]
+    float64, kept [M-1] int32; the other cuts' rows stay zero."""
+    nc = M - 1
+    res = np.zeros((nc, chi))
+    num = np.zeros((nc, chi, nc), dtype=np.int8)
+    S = np.zeros((nc, 2 * nc, 2 * nc))
+    kept = np.zeros(nc, dtype=np.int32)
+    for c in cuts:
+        r = np.load(path + f"res_{c}.npy").astype(np.float64)
+        n_ = np.load(path + f"num_{c}.npy").reshape(len(r), -1)
+        s_ = np.load(path + f"S_{c}.npy")
+        k, m = len(r), nc - c
+        if k > chi or n_.shape[1] != m or s_.shape != (2 * m, 2 * m):
+            raise ValueError(f"cut {c}: files do not match M={M}, chi={chi}")
+        res[c, :k] = r
+        num[c, :k, :m] = n_
+        S[c, : 2 * m, : 2 * m] = s_
+        kept[c] = k
+    dev = torch.device("cuda", device)
+    return (torch.as_tensor(res).to(dev), torch.as_tensor(num).to(dev), torch.as_tensor(S).to(dev),
+            torch.as_tensor(kept).to(dev))
+
+
+def build_sites(s0, s1, M, d, chi, sq_cov, path, precision="split", out_dtype=torch.complex64, err_tol=ERR_TOL,
+                device: int = 0):
+    """Gamma of sites [s0, s1) and the Lambdas of the cuts they read, from the
+    cut files in ``path``, in one pipelined library call (bsg_build_sites):
+    Sigma of every site in one set of launches, one host wait, one DP launch
+    set over all their items.  Returns (list of Gamma tensors, Lambdas
+    [M-1, chi] float64 on the device)."""
+    import ctypes
+    dev = torch.device("cuda", device)
+    cuts = range(max(0, s0 - 1), min(s1, M - 1))
+    res, num, S, kept = load_cuts(path, M, chi, cuts, device)
+    sq = torch.as_tensor(np.asarray(sq_cov, dtype=np.float64)).to(dev).contiguous()
+    gam = [torch.empty(chi, chi, d, dtype=out_dtype, device=dev) for _ in range(s0, s1)]
+    lam = torch.zeros(M - 1, chi, dtype=torch.float64, device=dev)
+    odt = _lib.OUT_C128 if out_dtype == torch.complex128 else _lib.OUT_C64
+    ptrs = (ctypes.c_void_p * len(gam))(*[g.data_ptr() for g in gam])
+    h = _lib.Handle.get(device)
+    _lib.check(_lib.load().bsg_build_sites(h.h, sq.data_ptr(), M, d, chi, float(err_tol), ops._prec(precision), odt,
+                                           s0, s1, res.data_ptr(), num.data_ptr(), S.data_ptr(), kept.data_ptr(), ptrs,
+                                           lam.data_ptr(), _lib.stream_ptr()),
+               "bsg_build_sites")
+    return gam, lam
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--d", type=int, help="Maximum number of photons per mode before displacement - 1.")
@@ -137,15 +189,16 @@ def main(argv=None):
     # under torchrun each rank writes the files of its own contiguous site range
     rank, world, local = dist.rank_world()
     device = local % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(device)
     s0, s1 = dist.shard_sites(M, world)[rank] if world > 1 else (0, M)
+    t0 = time.time()
+    gam, lam = build_sites(s0, s1, M, d, chi, sq_cov, path, args.precision, gdt, device=device)
+    lam = lam.cpu().numpy()
+    print(f"modes {s0}..{s1 - 1}: build {time.time() - t0:.4f} s")
     for site in range(s0, s1):
-        t0 = time.time()
-        G, lam = build_site(site, M, d, chi, sq_cov, path, args.precision, gdt, device=device)
-        G = G.cpu().numpy()
-        print(f"mode: {site} Total {time.time() - t0:.4f}")
-        np.save(path + f"Gamma_{site}.npy", G)
+        np.save(path + f"Gamma_{site}.npy", gam[site - s0].cpu().numpy())
         if site < M - 1:
-            np.save(path + f"Lambda_{site}.npy", lam.astype(ldt))
+            np.save(path + f"Lambda_{site}.npy", lam[site].astype(ldt))
 
 
 if __name__ == "__main__":

@@ -210,6 +210,22 @@ int bsg_build_mps_batch(bsg_handle_t h, int n, const double* const* sq_covs, con
                         void* const* gammas, double* const* Lambdas, double* const* res, int8_t* const* num,
                         double* const* S, int32_t* const* kept, bsg_stream_t stream);
 
+/* Sites [s0, s1) of one MPS from given cut data -- the kron step's res_i /
+ * num_i / S_i files, as MPS_cpu.py reads them (MPS_cpu.py:384-525 restricted
+ * to a site range, the per-rank range of distributed_MPS.py:72) -- in one
+ * pipelined call: Lambda and label tables of the cuts the sites read
+ * (cuts max(0, s0 - 1) .. min(s1, M - 1) - 1), the Sigma of every site in
+ * one set of launches, one host wait, one item scatter and one set of DP
+ * launches.  res [M-1, chi] float64, num [M-1, chi, M-1] int8, S
+ * [M-1, 2(M-1), 2(M-1)] float64 and kept [M-1] int32 are device inputs laid
+ * out as bsg_cut_spectra writes them (only the rows of the cuts read need to
+ * be filled); gammas: host array of s1 - s0 device pointers; Lambdas
+ * [M-1, chi] float64 (rows of the cuts read are written).  Synchronises
+ * `stream`. */
+int bsg_build_sites(bsg_handle_t h, const double* sq_cov, int M, int d, int chi, double site_tol, int precision,
+                    int out_dtype, int s0, int s1, const double* res, const int8_t* num, const double* S,
+                    const int32_t* kept, void* const* gammas, double* Lambdas, bsg_stream_t stream);
+
 /* bsg_build_mps plus the download of its outputs: each group's DP runs in four
  * site parts and each part's Gammas are copied from gammas_dev[i] (device) to
  * gammas_pinned[i] (pinned host) as soon as that part is done, overlapping the

@@ -41,7 +41,7 @@ namespace bsg {
 namespace sliced {
 
 constexpr int TM = 128, TN = 64, TK = 64;        // TK bf16 = 128 bytes = one swizzle row
-constexpr int kStages = 6;
+constexpr int kStages = 9;                        // 216 KB of ring slots
 constexpr int kATile = TM * TK * 2;               // 16 KB
 constexpr int kBTile = TN * TK * 2;               // 8 KB
 constexpr int kStageBytes = kATile + kBTile;      // 24 KB
@@ -184,7 +184,79 @@ __global__ void __launch_bounds__(192, 1)
     }
   };
 
-  if (warp == 0 && lane == 0) {
+  // Slice-resident order (S <= kStages slots): a slot holds slice s of both
+  // operands for one K block, (A_s, B_s); all pairs of that K block are
+  // issued from the S resident slots, so each slice tile is loaded once per K
+  // block instead of once per pair (about a quarter of the L2 traffic per
+  // MMA).  Slot s is freed after slice max(s, S-1-s), its last use; fill f
+  // reuses the slot of fill f - kStages, freed no later than fill f - 1 since
+  // kStages >= S.  Otherwise (S > kStages) pairs stream one (A_s, B_t) K
+  // block per slot.
+  const bool resident = g.S <= kStages;
+  if (warp == 0 && lane == 0 && resident) {
+    uint32_t it = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < total && ok && !*(volatile int*)fail; tile += gridDim.x) {
+      int m0, m_end, b_row0, n0;
+      tile_rows(tile, m0, m_end, b_row0, n0);
+      for (int kb = 0; kb < nkb && ok; ++kb)
+        for (int sl = 0; sl < g.S; ++sl, ++it) {
+          const int st = it % kStages;
+          if (it >= kStages && !mbar_wait(&empty[st], ((it / kStages) - 1) & 1)) {
+            atomicExch(fail, 1);
+            ok = false;
+            break;
+          }
+          unsigned char* sp = base + st * kStageBytes;
+          mbar_expect_tx(&full[st], kStageBytes);
+          tma_load_2d(sp, &mA, &full[st], kb * TK, sl * g.a_rows + m0);
+          tma_load_2d(sp + kATile, &mB, &full[st], kb * TK, sl * g.b_rows + b_row0 + n0);
+        }
+    }
+  } else if (warp == 1 && lane == 0 && resident) {
+    constexpr uint32_t idesc = instr_desc_bf16();
+    uint32_t it = 0, t_local = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < total && ok && !*(volatile int*)fail; tile += gridDim.x, ++t_local) {
+      if (t_local >= 1 && !mbar_wait(acce, (t_local - 1) & 1)) {
+        atomicExch(fail, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      uint32_t written = 0;  // accumulators already started in this tile
+      for (int kb = 0; kb < nkb && ok; ++kb, it += g.S) {
+        for (int sl = 0; sl < g.S; ++sl) {
+          const uint32_t f = it + sl;
+          if (!mbar_wait(&full[f % kStages], (f / kStages) & 1)) {
+            atomicExch(fail, 1);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          // pairs whose later slice is sl: (sl, t) and (t, sl), t <= sl, sl + t <= S - 1
+          for (int t = 0; t <= sl && sl + t <= g.S - 1; ++t)
+            for (int sw = 0; sw < (t == sl ? 1 : 2); ++sw) {
+              const int pa = sw ? t : sl, pb = sw ? sl : t;
+              const int L = pa + pb, a = L < kAcc - 1 ? L : kAcc - 1;
+              const uint32_t dacc = tmem + a * TN;
+              const uint32_t sa = smem_u32(base + ((it + pa) % kStages) * kStageBytes);
+              const uint32_t sb = smem_u32(base + ((it + pb) % kStages) * kStageBytes + kATile);
+#pragma unroll
+              for (int kk = 0; kk < TK / 16; ++kk) {
+                const uint32_t acc_flag = (written >> a) & 1u;
+                umma_bf16(dacc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, acc_flag);
+                written |= 1u << a;
+              }
+            }
+          // free the slots whose last pair was just issued
+          if (sl >= g.S - 1 - sl) umma_commit(&empty[(it + sl) % kStages]);
+          if (g.S - 1 - sl < sl) umma_commit(&empty[(it + (g.S - 1 - sl)) % kStages]);
+        }
+      }
+      if (!ok) break;
+      umma_commit(accf);
+    }
+  } else if (warp == 0 && lane == 0) {
     // producer
     uint32_t it = 0;
     bool ok = true;

@@ -343,11 +343,25 @@ def measure_batch(args, lib, handle):
             ts.append(e0.elapsed_time(e1))
         res[name] = statistics.mean(ts)
     sites = sum(c.M for c in cfgs)
+    # the DP launch knobs searched for this workload (autotune.tune_batch),
+    # then the defaults restored for the rest of the line
+    from bosonsupremacy_gb300 import autotune
+
+    saved = autotune.get_knobs()
+    try:
+        best, table = autotune.tune_batch(sqs, ds, chis, precision=args.precision)
+    finally:
+        autotune.set_knobs(**saved)
+    names = ("small_entries", "dp_quantum", "blocks_per_sm")
     return {"workload": "batch64: 64 instances, M~U{8..48}, d~U{4..8}, chi in {32,64,128,256}, r~U[0.5,1.4], "
                         "eta~U[0.2,0.6]", "instances": len(cfgs), "sites": sites,
             "batched_ms": res["batched"], "looped_ms": res["looped"],
             "batched_sites_per_s": sites / (res["batched"] / 1e3), "looped_sites_per_s": sites / (res["looped"] / 1e3),
-            "speedup_vs_looped": res["looped"] / res["batched"]}
+            "speedup_vs_looped": res["looped"] / res["batched"],
+            "tuned": {"knobs": best, "batched_ms": min(table.values()),
+                      "speedup_vs_looped": res["looped"] / min(table.values()),
+                      "grid_ms": {"/".join(f"{n}={v}" for n, v in zip(names, k)): round(t, 3)
+                                  for k, t in table.items()}}}
 
 
 def measure_largest(args, lib, handle):

@@ -12,6 +12,7 @@ full builds and keeps the fastest setting on the handle.
 
     from bosonsupremacy_gb300 import autotune
     best, table = autotune.tune_dp(sq_cov, d, chi)   # sets the knobs
+    best, table = autotune.tune_batch(sq_covs, ds, chis)   # many instances per call
 """
 from __future__ import annotations
 
@@ -22,7 +23,7 @@ from typing import Dict, Iterable, Tuple
 import torch
 
 from . import _lib
-from .pipeline import build_mps
+from .pipeline import build_mps, build_mps_batch
 
 KNOBS = {
     "blocks_per_sm": _lib.TUNE_DP_BLOCKS_PER_SM,
@@ -90,6 +91,42 @@ def tune_dp(sq_cov, d: int, chi: int, precision: str = "split", device: int = 0,
     for values in itertools.product(*(tuple(grid[n]) for n in names)):
         set_knobs(device, **dict(zip(names, values)))
         table[values] = dp_time_ms(sq_cov, d, chi, precision, device, reps=reps, out=out)
+    best = min(table, key=table.get)
+    set_knobs(device, **dict(zip(names, best)))
+    return dict(zip(names, best)), table
+
+
+def tune_batch(sq_covs, ds, chis, precision: str = "split", device: int = 0,
+               grid: Dict[str, Iterable[int]] | None = None, reps: int = 2
+               ) -> Tuple[Dict[str, int], Dict[Tuple[int, ...], float]]:
+    """The same search for the batched build of many independent instances
+    (bsg_build_mps_batch), timed as whole batched builds with CUDA events:
+    the table-size split of the DP's two launches (`small_entries`: which
+    partition programs run with small per-warp tables), the work quantum of
+    its yielding launches (`dp_quantum`: how many program transitions a warp
+    runs before its block gives the SM back) and the resident blocks.  Leaves
+    the fastest setting on the handle and returns (best knobs, {values: ms})."""
+    if grid is None:
+        grid = {"small_entries": (0, 64, 256), "dp_quantum": (1, 2, 8), "blocks_per_sm": (4, 8)}
+    dev = torch.device("cuda", device)
+    Ms = [len(q) // 2 for q in sq_covs]
+    outs = [[torch.empty(c, c, d, dtype=torch.complex64, device=dev) for _ in range(M)]
+            for M, d, c in zip(Ms, ds, chis)]
+    sqs = [torch.as_tensor(q).to(dev) for q in sq_covs]
+    build_mps_batch(sqs, ds, chis, precision=precision, device=device, outs=outs)  # programs, workspaces
+    stream = torch.cuda.current_stream(dev)
+    names = list(grid)
+    table = {}
+    for values in itertools.product(*(tuple(grid[n]) for n in names)):
+        set_knobs(device, **dict(zip(names, values)))
+        build_mps_batch(sqs, ds, chis, precision=precision, device=device, outs=outs)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            build_mps_batch(sqs, ds, chis, precision=precision, device=device, outs=outs)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        table[values] = e0.elapsed_time(e1) / reps
     best = min(table, key=table.get)
     set_knobs(device, **dict(zip(names, best)))
     return dict(zip(names, best)), table

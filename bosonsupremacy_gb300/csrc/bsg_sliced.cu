@@ -115,6 +115,27 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "r"(taddr));
 }
 
+// I 2^x as an FP64 value, rounded to nearest even, assembled from integer
+// operations (the FP64 pipe runs at ~1/64 of the FP32 one on this GPU); the
+// rare result outside the normal range goes through ldexp.
+__device__ __forceinline__ double scaled_int_to_double(long long I, int x) {
+  if (I == 0) return 0.0;
+  const unsigned long long sign = I < 0 ? (1ull << 63) : 0ull;
+  unsigned long long a = I < 0 ? (unsigned long long)(-I) : (unsigned long long)I;
+  const int n = __clzll((long long)a);
+  a <<= n;                                   // leading one at bit 63
+  unsigned long long m = a >> 11;            // 53 bits
+  const unsigned long long rem = a & 0x7ffull;
+  if (rem > 0x400ull || (rem == 0x400ull && (m & 1ull))) ++m;
+  int E = 63 - n + x;                        // value = 1.m 2^E
+  if (m >> 53) {                             // the rounding carried into bit 53
+    m >>= 1;
+    ++E;
+  }
+  if (E < -1022 || E > 1023) return ldexp(__ll2double_rn(I), x);
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(E + 1023) << 52) | (m & ((1ull << 52) - 1))));
+}
+
 // (s, t) of pair p in level order: level L holds pairs (0, L), (1, L-1), ..., (L, 0).
 __device__ __forceinline__ void pair_of(int p, int& s, int& t, int& L) {
   L = 0;
@@ -337,9 +358,8 @@ __global__ void __launch_bounds__(192, 1)
       // The levels are summed exactly as an int64 in units of 2^-G (G = b x the
       // last exact level): level a < 7 holds an integer times 2^(-b a), so
       // acc_a 2^(b a) converts to an int64 exactly; the combined levels 7+ are
-      // rounded to the unit (below 2^-50 of the level-0 scale).  One
-      // conversion and one power-of-two product per output reach FP64, the
-      // FP64 pipe being ~1/64 of the FP32 one on this GPU.
+      // rounded to the unit (below 2^-50 of the level-0 scale).  The int64
+      // becomes the FP64 output by integer operations (scaled_int_to_double).
       const int G = g.b * (g.S - 1 < kAcc - 2 ? g.S - 1 : kAcc - 2);
       for (int c = 0; c < TN; c += 16) {
         long long v[16];
@@ -362,7 +382,7 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int col = n0 + c + j;
-            if (col < g.N) out[j] = ldexp(__ll2double_rn(v[j]), er + g.eb[b_row0 + col] - 2 * g.b - G);
+            if (col < g.N) out[j] = scaled_int_to_double(v[j], er + g.eb[b_row0 + col] - 2 * g.b - G);
           }
         }
       }

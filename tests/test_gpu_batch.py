@@ -39,3 +39,26 @@ def test_batched_build_rejects_bad_instance(cuda):
     sq = synthetic.lossy_covariances(cfg)[1]
     with pytest.raises(_lib.BSGError):
         build_mps_batch([sq, sq], [cfg.d, cfg.chi + 1], [cfg.chi, cfg.chi])  # d > chi for instance 1
+
+
+def test_batch_tuner_keeps_results(cuda):
+    """autotune.tune_batch over a small grid of the DP's launch knobs picks a
+    point of the grid, and the batched build after tuning gives the same
+    Gammas as before (every knob only changes which warp runs an item)."""
+    import torch
+    from bosonsupremacy_gb300 import autotune, synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps_batch
+    cfgs = synthetic.batch_configs(64)[:8]
+    sqs = [synthetic.lossy_covariances(c)[1] for c in cfgs]
+    ds, chis = [c.d for c in cfgs], [c.chi for c in cfgs]
+    before = build_mps_batch(sqs, ds, chis)
+    saved = autotune.get_knobs()
+    try:
+        best, table = autotune.tune_batch(sqs, ds, chis, grid={"small_entries": (0, 64), "dp_quantum": (1, 8)}, reps=1)
+        assert len(table) == 4 and tuple(best.values()) in table
+        after = build_mps_batch(sqs, ds, chis)
+    finally:
+        autotune.set_knobs(**saved)
+    for a, b in zip(before, after):
+        for x, y in zip(a.Gammas, b.Gammas):
+            assert torch.equal(x, y)

@@ -108,3 +108,34 @@ def test_cli_steps_sharded_over_ranks(cuda, golden, tmp_path):
     assert len([n for n in outs[1] if n.startswith("Gamma_")]) == M
     for name, v in outs[1].items():
         assert np.array_equal(v, outs[2][name]), name
+
+
+def test_site_range_build_equals_whole_build(cuda):
+    """bsg_build_sites (the drop-in MPS step's single call for a site range,
+    here sites 10..29 of the M=50 workload, and the two end sites) fed the
+    whole build's own cut data gives the whole build's Gammas and Lambdas
+    for that range bit for bit."""
+    import torch
+    from bosonsupremacy_gb300 import _lib, ops, synthetic
+    from bosonsupremacy_gb300.pipeline import build_mps
+    import ctypes
+    cfg = synthetic.MEDIUM
+    M, d, chi = cfg.M, cfg.d, cfg.chi
+    _, sq = synthetic.lossy_covariances(cfg)
+    whole = build_mps(sq, d, chi, precision="split")
+    sqd = torch.as_tensor(sq).cuda()
+    for s0, s1 in [(10, 30), (0, 1), (M - 1, M)]:
+        gam = [torch.empty(chi, chi, d, dtype=torch.complex64, device="cuda") for _ in range(s0, s1)]
+        lam = torch.zeros(M - 1, chi, dtype=torch.float64, device="cuda")
+        ptrs = (ctypes.c_void_p * len(gam))(*[g.data_ptr() for g in gam])
+        h = _lib.Handle.get(0)
+        kept = torch.as_tensor(whole.kept).to(torch.int32).cuda()
+        _lib.check(_lib.load().bsg_build_sites(h.h, sqd.data_ptr(), M, d, chi, 1e-10, _lib.PREC_SPLIT, _lib.OUT_C64,
+                                               s0, s1, whole.res.data_ptr(), whole.num.data_ptr(), whole.S.data_ptr(),
+                                               kept.data_ptr(), ptrs, lam.data_ptr(), _lib.stream_ptr()),
+                   "bsg_build_sites")
+        torch.cuda.synchronize()
+        for i in range(s0, s1):
+            assert torch.equal(gam[i - s0], whole.Gammas[i]), (s0, s1, i)
+            if i < M - 1:
+                assert torch.equal(lam[i], whole.Lambdas[i]), (s0, s1, i)

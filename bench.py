@@ -43,7 +43,8 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="M144_d8_chi1024")
+    p.add_argument("--workload", default="M144_d8_chi1024",
+                   help="M144_d8_chi1024 (default), M50_d6_chi256, M16_d4_chi64, M216_d10_chi2048_banded or batch64")
     p.add_argument("--precision", default="split", choices=["split", "fp64", "fp32"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
@@ -305,7 +306,7 @@ def measure_sampler(args, lib, handle, peaks):
     }
 
 
-def measure_batch(args, lib, handle):
+def measure_batch(args, lib, handle, steps: int = 3, warmup: int = 1):
     """The 64-instance uneven workload (M ~ U{8..48}, d ~ U{4..8}, chi in
     {32..256}): one bsg_build_mps_batch call (one launch per phase, one DP
     launch set over every instance's items) against 64 bsg_build_mps calls
@@ -331,10 +332,11 @@ def measure_batch(args, lib, handle):
 
     res = {}
     for name, fn in (("batched", batched), ("looped", looped)):
-        fn()
+        for _ in range(max(1, warmup)):
+            fn()
         torch.cuda.synchronize()
         ts = []
-        for _ in range(3):
+        for _ in range(max(1, steps)):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             fn()
@@ -502,6 +504,22 @@ def main():
     torch.cuda.set_device(dev)
     lib = _lib.load()
     handle = _lib.Handle.get(local)
+    if args.workload == "batch64":
+        # the 64 uneven instances alone: one line for the batched build
+        clocks = ClockSampler(local)
+        clocks.start()
+        b = measure_batch(args, lib, handle, steps=args.steps, warmup=args.warmup)
+        clk = clocks.stop()
+        if rank == 0:
+            print(json.dumps({
+                "metric": "batched full-MPS build throughput (sites/s), 64 independent uneven instances",
+                "value": b["batched_sites_per_s"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": b["batched_ms"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp32x2 (split) hafnian, f64 factorisations",
+                "data": "synthetic (64 seeded lossy GBS covariances)",
+                "config": {"workload": b["workload"], "precision": args.precision, "gamma_dtype": "complex64"},
+                "clocks": clk, "batch64": b}), flush=True)
+        return
     cfg = synthetic.NAMED[args.workload]
     _, sq = synthetic.lossy_covariances(cfg, seed=cfg.seed + rank)  # independent instance per rank
     sq_dev = torch.as_tensor(sq).to(dev)
@@ -543,34 +561,6 @@ def main():
         ms = float(t.item())
     value = ws * M / (ms / 1e3)
 
-    # plain-FP64 path of the same kernels, one build
-    fp64 = None
-    if not args.no_fp64 and args.precision != "fp64":
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        build_mps(sq_dev, d, chi, precision="fp64", out=outs)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        t64 = e0.elapsed_time(e1)
-        fp64 = {"build_ms": t64, "sites_per_s": M / (t64 / 1e3), "split_speedup": t64 / ms}
-        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)  # restore outputs
-
-    # first build on a fresh handle: partition programs generated, scratch
-    # allocated and every table uploaded inside the timed region
-    cold = None
-    if rank == 0:
-        fresh = _lib.Handle(local)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        build_mps(sq_dev, d, chi, precision=args.precision, out=outs, handle=fresh)
-        torch.cuda.synchronize()
-        cold = {"ms": (time.perf_counter() - t0) * 1e3,
-                "note": "one build on a new library handle (empty program cache, no scratch yet), host clock"}
-        fresh.close()
-        del fresh
-        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
-
     # end to end through the public host API
     e2e = None
     if not args.no_e2e:
@@ -606,6 +596,34 @@ def main():
                                         "buffers (one cudaMemcpyAsync per site), timed just before and after the "
                                         "e2e steps; the e2e floor is max(build, bytes / link rate)"},
                "pinned": "torch pin_memory buffers, one per site, touched by two untimed e2e builds"}
+
+    # plain-FP64 path of the same kernels, one build
+    fp64 = None
+    if not args.no_fp64 and args.precision != "fp64":
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        build_mps(sq_dev, d, chi, precision="fp64", out=outs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1)
+        fp64 = {"build_ms": t64, "sites_per_s": M / (t64 / 1e3), "split_speedup": t64 / ms}
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)  # restore outputs
+
+    # first build on a fresh handle: partition programs generated, scratch
+    # allocated and every table uploaded inside the timed region
+    cold = None
+    if rank == 0:
+        fresh = _lib.Handle(local)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs, handle=fresh)
+        torch.cuda.synchronize()
+        cold = {"ms": (time.perf_counter() - t0) * 1e3,
+                "note": "one build on a new library handle (empty program cache, no scratch yet), host clock"}
+        fresh.close()
+        del fresh
+        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
 
     # roofline of the hafnian DP (the dominant kernel by SM-time: it is
     # ~15k of the ~19k SM-milliseconds of a build; the Williamson / Sigma

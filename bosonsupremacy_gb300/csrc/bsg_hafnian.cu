@@ -608,6 +608,48 @@ static int convert_into(bsg_handle_t h, const double* src, int64_t n, int precis
   return BSG_OK;
 }
 
+// Many conversions in one launch: job y converts jobs[y].n values (blocks
+// along x cover the largest job).
+struct ConvJob {
+  const double2* src;
+  void* dst;
+  int64_t n;
+};
+
+template <class C>
+__global__ void convert_jobs_kernel(const ConvJob* __restrict__ jobs) {
+  const ConvJob jb = jobs[blockIdx.y];
+  C* dst = reinterpret_cast<C*>(jb.dst);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < jb.n; i += (int64_t)gridDim.x * blockDim.x) {
+    if constexpr (std::is_same<C, float2>::value) {
+      dst[i] = PrecF32::from_c128(jb.src[i]);
+    } else {
+      dst[i] = PrecSplit::from_c128(jb.src[i]);
+    }
+  }
+}
+
+// jobs_host: pinned; jobs_dev: device room for n_jobs ConvJobs.  FP64 needs no conversion.
+static int convert_many(bsg_handle_t h, const ConvJob* jobs_host, int n_jobs, void* jobs_dev, int precision,
+                        cudaStream_t st) {
+  if (n_jobs == 0 || precision == BSG_PREC_FP64) return BSG_OK;
+  int64_t nmax = 0;
+  double work = 0.0;
+  for (int i = 0; i < n_jobs; ++i) {
+    nmax = std::max(nmax, jobs_host[i].n);
+    work += (double)jobs_host[i].n;
+  }
+  BSG_CUDA(cudaMemcpyAsync(jobs_dev, jobs_host, sizeof(ConvJob) * n_jobs, cudaMemcpyHostToDevice, st));
+  const unsigned bx = unsigned(std::min<int64_t>((nmax + 255) / 256, 64));
+  const ConvJob* jd = reinterpret_cast<const ConvJob*>(jobs_dev);
+  if (precision == BSG_PREC_SPLIT) {
+    BSG_PROFILED(h, BSG_K_PREP, st, work, (convert_jobs_kernel<PrecSplit::C><<<dim3(bx, n_jobs), 256, 0, st>>>(jd)));
+  } else {
+    BSG_PROFILED(h, BSG_K_PREP, st, work, (convert_jobs_kernel<float2><<<dim3(bx, n_jobs), 256, 0, st>>>(jd)));
+  }
+  return BSG_OK;
+}
+
 static int convert_sigma(bsg_handle_t h, const double* src, int64_t n, int precision, bsg::DevBuf& buf,
                          const void** out, cudaStream_t st) {
   if (precision == BSG_PREC_FP64 || n == 0) {
@@ -1949,8 +1991,9 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
   const size_t o_empty = carve(kMaxNnz * 4 + 64);
   const size_t cargs_bytes = al(sizeof(CutArgs) * n) + al(sizeof(int2) * total_cuts);
   const size_t o_cargs = carve(cargs_bytes);
-  const size_t o_jobs = carve(sizeof(SigmaJob) * ns);
+  const size_t o_jobs = carve(sizeof(SigmaJob) * ns), o_conv = carve(sizeof(ConvJob) * ns);
   const size_t h_cargs = hcarve(cargs_bytes), h_jobs = hcarve(sizeof(SigmaJob) * ns), h_sst = hcarve((size_t)ns * 4);
+  const size_t h_conv = hcarve(sizeof(ConvJob) * ns);
   const size_t h_empty = hcarve(kMaxNnz * 4 + 64);
   BSG_TRY(h->mps_ws.ensure(off));
   BSG_TRY(h->host_stage.ensure(hoff));
@@ -2041,13 +2084,17 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     }
   }
   BSG_TRY(launch_sigma_jobs(h, jobs, ns, wb + o_jobs, st));
+  // every site's Sigma into the DP's storage type, one launch
+  ConvJob* conv = reinterpret_cast<ConvJob*>(hs + h_conv);
+  int n_conv = 0;
   for (int i = 0; i < n; ++i)
     for (int j = slo[i]; j < shi[i]; ++j) {
       const int s = site0[i] + j - slo[i], Mr = j == 0 ? Ms[i] : Ms[i] - j;
       if (o_sigc[s] != o_sig[s])
-        BSG_TRY(convert_into(h, reinterpret_cast<double*>(wb + o_sig[s]), (int64_t)(2 * Mr) * (2 * Mr), precision,
-                             wb + o_sigc[s], st));
+        conv[n_conv++] = ConvJob{reinterpret_cast<const double2*>(wb + o_sig[s]), wb + o_sigc[s],
+                                 (int64_t)(2 * Mr) * (2 * Mr)};
     }
+  BSG_TRY(convert_many(h, conv, n_conv, wb + o_conv, precision, st));
   // 4. one host wait: every instance's cut status and keys
   BSG_CUDA(cudaStreamSynchronize(st));
   static const uint64_t zero_key = 0;

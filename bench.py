@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--no-largest", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-sampler", action="store_true")
+    p.add_argument("--no-decomp", action="store_true")
+    p.add_argument("--decomp-M", type=int, default=50)
     p.add_argument("--sampler-workload", default="M50_d6_chi256")
     p.add_argument("--sampler-n", type=int, default=100000)
     return p.parse_args()
@@ -364,6 +366,43 @@ def measure_batch(args, lib, handle, steps: int = 3, warmup: int = 1):
                       "speedup_vs_looped": res["looped"] / min(table.values()),
                       "grid_ms": {"/".join(f"{n}={v}" for n, v in zip(names, k)): round(t, 3)
                                   for k, t in table.items()}}}
+
+
+def measure_decomposition(args):
+    """The covariance decomposition (get_decomposition.py:16-29 SDP) on the
+    GPU at M = args.decomp_M: a uniform-loss covariance of the medium
+    workload's parameters, whose optimum is known in closed form (error
+    reported), and a mode-dependent-loss covariance (loss between two
+    interferometers), whose optimum is certified by the duality gap and by
+    purity (every symplectic eigenvalue of X equal to 1).  Wall time of the
+    whole solve (one warm-up solve at M=4 first), iterations and gap."""
+    import dataclasses
+
+    import numpy as np
+    import torch
+
+    from bosonsupremacy_gb300 import decomposition, synthetic
+
+    M = args.decomp_M
+    decomposition.decompose(synthetic.nonuniform_lossy_covariance(4, seed=1))
+    cfg = dataclasses.replace(synthetic.MEDIUM, M=M)
+    cov_u, sq_u = synthetic.lossy_covariances(cfg)
+    cov_n = synthetic.nonuniform_lossy_covariance(M, seed=0)
+    out = {"M": M, "schur_order": M * (2 * M + 1), "precision": "fp64"}
+    for name, cov in (("uniform_loss", cov_u), ("mode_dependent_loss", cov_n)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X, meta = decomposition.decompose(cov)
+        ms = 1e3 * (time.perf_counter() - t0)
+        Om = np.kron(np.array([[0.0, 1.0], [-1.0, 0.0]]), np.eye(M))
+        nu = np.sort(np.abs(np.linalg.eigvals(1j * Om @ X).real))[::2]
+        r = {"ms": ms, "iterations": meta["iterations"], "rel_gap": meta["rel_gap"],
+             "primal_res": meta["primal_res"], "dual_res": meta["dual_res"], "trace": meta["primal_obj"],
+             "max_symplectic_eig_dev": float(np.abs(nu - 1.0).max())}
+        if name == "uniform_loss":
+            r["rel_err_vs_closed_form"] = float(np.abs(X - sq_u).max() / np.abs(sq_u).max())
+        out[name] = r
+    return out
 
 
 def measure_largest(args, lib, handle):
@@ -706,6 +745,10 @@ def main():
     if rank == 0 and not args.no_batch:
         batch = measure_batch(args, lib, handle)
 
+    decomp = None
+    if rank == 0 and not args.no_decomp:
+        decomp = measure_decomposition(args)
+
     largest = None
     if rank == 0 and not args.no_largest:
         del outs
@@ -725,7 +768,7 @@ def main():
                                                                  for k, v in prof.items()},
             "host": {k: {"ms": v["ms"], "calls": v["launches"]} for k, v in host_prof.items()},
             "roofline": roof, "fp64_path": fp64, "cold_build": cold, "e2e": e2e, "cpu_baseline": cpu, "contraction": contraction, "sampler": sampler,
-            "batch64": batch, "largest": largest,
+            "batch64": batch, "largest": largest, "decomposition": decomp,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -65,6 +65,9 @@ SIGNATURES = {
     "bsg_profile_build_timeline": (_I, [_P, _P, _I]),
     "bsg_profile_dp_buckets": (_I, [_P, _P, _I, C.POINTER(_I), _P, _I]),
     "bsg_displacements": (_I, [_P, _P, _L, _I, _P, _P]),
+    "bsg_cov_decomposition": (_I, [_P, _P, _I, _P, _D, _I, _P, _P]),
+    "bsg_potrf_f64": (_I, [_P, _P, _I, _P, _P]),
+    "bsg_profile_plan_phases": (_I, [_P, _P, _I]),
 }
 
 

@@ -21,7 +21,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbsg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["bsg_api.cpp", "bsg_programs.cpp", "bsg_hafnian.cu", "bsg_sigma.cu", "bsg_cuts.cu", "bsg_contract.cu",
-           "bsg_probe.cu", "bsg_umma.cu", "bsg_sliced.cu", "bsg_sample.cu"]
+           "bsg_probe.cu", "bsg_umma.cu", "bsg_sliced.cu", "bsg_sample.cu",
+           "bsg_decomp.cu"]
 
 
 def _nvcc() -> str:

@@ -160,6 +160,13 @@ int bsg_profile_reset(bsg_handle_t h) {
   }
   h->prof.dp_rows.clear();
   h->prof.dp_state_hist.clear();
+  for (double& x : h->prof.plan_ms) x = 0.0;
+  return BSG_OK;
+}
+
+int bsg_profile_plan_phases(bsg_handle_t h, double* ms, int n) {
+  BSG_CHECK_ARG(h && ms, "bsg_profile_plan_phases: null pointer");
+  for (int i = 0; i < n; ++i) ms[i] = i < 8 ? h->prof.plan_ms[i] : 0.0;
   return BSG_OK;
 }
 
@@ -290,6 +297,8 @@ int bsg_destroy(bsg_handle_t h) {
   h->mps_ws.release();
   h->sample_ws.release();
   h->disp_tab.release();
+  h->decomp_ws.release();
+  h->decomp_host.release();
   for (auto& sl : h->slot) {
     sl.plan.release();
     sl.items.release();

@@ -1001,7 +1001,8 @@ int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts,
 // Workspace (at `base`, cut_ws_bytes of it), output clearing and the launch
 // arguments of a cut-spectra call.
 int cut_prepare_at(bsg_handle_t h, char* base, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
-                   double err_tol, double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st) {
+                   double err_tol, double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st,
+                   std::vector<FillSpan>* defer) {
   BSG_CHECK_ARG(M >= 2 && L0 >= 1 && n_cuts >= 1 && L0 + n_cuts <= M, "bsg_cut_spectra: cuts [%d, %d) outside [1, M=%d)",
                 L0, L0 + n_cuts, M);
   BSG_CHECK_ARG(M - L0 <= kMaxCutModes, "bsg_cut_spectra: %d modes in a cut exceeds %d", M - L0, kMaxCutModes);
@@ -1042,16 +1043,21 @@ int cut_prepare_at(bsg_handle_t h, char* base, const double* sq_cov, int M, int 
   a.sweeps = a.status + n_cuts;
   a.mu = reinterpret_cast<double*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) + al(st_bytes));
   a.phase_t = nullptr;
-  if (h->prof.on) {
+  if (h->prof.on)
     a.phase_t = reinterpret_cast<unsigned long long*>(base + al(ws_bytes) + al(nbar_bytes) + al(rec_bytes) +
                                                       al(st_bytes) + al(mu_bytes));
-    BSG_CUDA(cudaMemsetAsync(a.phase_t, 0, ph_bytes, st));
+  // status -1: "did not finish" until the Williamson kernel writes it
+  const FillSpan clears[6] = {{a.phase_t, a.phase_t ? (int64_t)ph_bytes : 0, 0},
+                              {a.status, (int64_t)st_bytes, 0xff},
+                              {res, (int64_t)n_cuts * chi * 8, 0},
+                              {num, (int64_t)n_cuts * chi * (M - 1), 0},
+                              {S, (int64_t)n_cuts * a.ldS * a.ldS * 8, 0},
+                              {kept, (int64_t)n_cuts * 4, 0}};
+  for (const FillSpan& f : clears) {
+    if (f.bytes == 0) continue;
+    if (defer) defer->push_back(f);
+    else BSG_CUDA(cudaMemsetAsync(f.p, f.value, (size_t)f.bytes, st));
   }
-  BSG_CUDA(cudaMemsetAsync(a.status, 0xff, st_bytes, st));
-  BSG_CUDA(cudaMemsetAsync(res, 0, (size_t)n_cuts * chi * 8, st));
-  BSG_CUDA(cudaMemsetAsync(num, 0, (size_t)n_cuts * chi * (M - 1), st));
-  BSG_CUDA(cudaMemsetAsync(S, 0, (size_t)n_cuts * a.ldS * a.ldS * 8, st));
-  BSG_CUDA(cudaMemsetAsync(kept, 0, (size_t)n_cuts * 4, st));
   *out = a;
   return BSG_OK;
 }

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <thread>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <type_traits>
 #include <vector>
@@ -73,19 +74,14 @@ struct RowTable {  // arrays indexed [cut * rows_cap + row]
   float2* rowfact2;  // the same as an unevaluated FP32 pair (hi, lo)
 };
 
-__global__ void label_rows_kernel(const int8_t* __restrict__ num, int64_t cut_stride, int ld,
-                                  const int32_t* __restrict__ rows, int m_base, int m_step, int rows_cap, RowTable t,
-                                  int* __restrict__ err) {
-  const int cut = blockIdx.y;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows[cut]) return;
-  const int m = m_base - m_step * cut;
-  const size_t o = (size_t)cut * rows_cap + r;
+// One label row: its sorted (mode, multiplicity) entries, count, sum, key
+// and sqrt(prod num!) into entry o of the table.
+__device__ __forceinline__ void label_row(const int8_t* __restrict__ row, int m, const RowTable& t, size_t o,
+                                          int* __restrict__ err) {
   int ent[kMaxNnz];
   int cnt = 0, sum = 0;
   uint64_t key = 0;
   double rf = 1.0;
-  const int8_t* row = num + cut * cut_stride + (int64_t)r * ld;
   for (int q = 0; q < m; ++q) {
     int v = row[q];
     if (v == 0) continue;
@@ -111,6 +107,53 @@ __global__ void label_rows_kernel(const int8_t* __restrict__ num, int64_t cut_st
   t.rowfact[o] = rf;
   const float hi = float(rf);
   t.rowfact2[o] = make_float2(hi, float(rf - double(hi)));
+}
+
+__global__ void label_rows_kernel(const int8_t* __restrict__ num, int64_t cut_stride, int ld,
+                                  const int32_t* __restrict__ rows, int m_base, int m_step, int rows_cap, RowTable t,
+                                  int* __restrict__ err) {
+  const int cut = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows[cut]) return;
+  label_row(num + cut * cut_stride + (int64_t)r * ld, m_base - m_step * cut, t, (size_t)cut * rows_cap + r, err);
+}
+
+// The per-cut row work of many instances in one launch: Lambda = sqrt(res)
+// where res > tol (else 0) with the count of such rows, the label row tables
+// and a copy of the kept-row count next to the keys, so that the host reads
+// every instance's keys and counts with one copy.  blockIdx.y = (job, cut)
+// through `map`, 128 rows per block along x.
+struct CutRowsJob {
+  const int8_t* num;    // [cuts, chi, ld] from the job's first cut
+  const int32_t* kept;  // [cuts]
+  const double* res;    // [cuts, chi]
+  double* lambda;       // [cuts, chi]
+  RowTable t;           // row tables from the first cut (rows_cap = chi)
+  int32_t* above;       // [cuts] rows with res > tol (cleared before)
+  int32_t* cnt;         // [cuts] copy of kept
+  int* err;
+  double tol;
+  int chi, ld, m0;      // rows per cut, label row stride, modes right of the first cut
+};
+
+__global__ void cut_rows_batch_kernel(const CutRowsJob* __restrict__ jobs, const int2* __restrict__ map) {
+  const int2 jc = map[blockIdx.y];
+  const CutRowsJob& jb = jobs[jc.x];
+  const int c = jc.y, chi = jb.chi;
+  if ((int)(blockIdx.x * blockDim.x) >= chi) return;  // block-uniform
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  bool keep = false;
+  if (r < chi) {
+    const double v = jb.res[(size_t)c * chi + r];
+    keep = v > jb.tol;
+    jb.lambda[(size_t)c * chi + r] = keep ? sqrt(v) : 0.0;
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, keep);
+  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(jb.above + c, __popc(bal));
+  const int rows = jb.kept[c];
+  if (blockIdx.x == 0 && threadIdx.x == 0) jb.cnt[c] = rows;
+  if (r < rows)
+    label_row(jb.num + ((size_t)c * chi + r) * jb.ld, jb.m0 - c, jb.t, (size_t)c * chi + r, jb.err);
 }
 
 // Left-row scale of a site: sqrt(prod num!) / (Z * Lambda) in FP64 and as an
@@ -650,6 +693,43 @@ static int convert_many(bsg_handle_t h, const ConvJob* jobs_host, int n_jobs, vo
   return BSG_OK;
 }
 
+// Span y of the list is set to its byte value: the 16-byte-aligned body by
+// vector stores (blocks along x stride over it), the unaligned head and tail
+// bytes by the first threads.
+__global__ void fill_spans_kernel(const FillSpan* __restrict__ spans) {
+  const FillSpan f = spans[blockIdx.y];
+  if (f.bytes <= 0) return;
+  unsigned char* p = reinterpret_cast<unsigned char*>(f.p);
+  const int64_t mis = (16 - (int64_t)(reinterpret_cast<uintptr_t>(p) & 15)) & 15;
+  const int64_t head = mis < f.bytes ? mis : f.bytes;
+  const int64_t body = (f.bytes - head) / 16, tail0 = head + body * 16;
+  const unsigned char b = (unsigned char)f.value;
+  const unsigned w = 0x01010101u * b;
+  const uint4 v = make_uint4(w, w, w, w);
+  uint4* q = reinterpret_cast<uint4*>(p + head);
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = t; i < body; i += stride) q[i] = v;
+  if (t < head) p[t] = b;
+  if (t < f.bytes - tail0) p[tail0 + t] = b;
+}
+
+int fill_spans_dev(bsg_handle_t h, const FillSpan* dev_spans, int n, int64_t max_bytes, cudaStream_t st) {
+  if (n == 0 || max_bytes <= 0) return BSG_OK;
+  // about 8 vector stores per thread on the largest span, at most 64 blocks a span
+  const unsigned bx = unsigned(std::max<int64_t>(1, std::min<int64_t>((max_bytes / 16 + 2047) / 2048, 64)));
+  BSG_PROFILED(h, BSG_K_PREP, st, (double)n, (fill_spans_kernel<<<dim3(bx, n), 256, 0, st>>>(dev_spans)));
+  return BSG_OK;
+}
+
+int fill_spans(bsg_handle_t h, const FillSpan* spans, int n, void* dev, void* stage, cudaStream_t st) {
+  if (n == 0) return BSG_OK;
+  int64_t mx = 0;
+  for (int i = 0; i < n; ++i) mx = std::max(mx, spans[i].bytes);
+  std::memcpy(stage, spans, sizeof(FillSpan) * n);
+  BSG_CUDA(cudaMemcpyAsync(dev, stage, sizeof(FillSpan) * n, cudaMemcpyHostToDevice, st));
+  return fill_spans_dev(h, reinterpret_cast<const FillSpan*>(dev), n, mx, st);
+}
+
 static int convert_sigma(bsg_handle_t h, const double* src, int64_t n, int precision, bsg::DevBuf& buf,
                          const void** out, cudaStream_t st) {
   if (precision == BSG_PREC_FP64 || n == 0) {
@@ -695,13 +775,33 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
   const int nb = int(bk.progs.size());
   std::vector<int> order(nb);
   std::iota(order.begin(), order.end(), 0);
+  // stable order by descending cost, as a counting sort over the few
+  // distinct costs (a cost depends only on the bucket's program)
   std::vector<int64_t> cost(nb);
+  std::vector<int64_t> pcost(ps.k.size(), INT64_MIN);
   for (int b = 0; b < nb; ++b) {
     const int p = bk.progs[b];
-    const bool small = small_program(ps, p, small_entries);
-    cost[b] = small ? -(int64_t(1) << 40) - prog_trans(ps, p) : prog_trans(ps, p);
+    if (pcost[p] == INT64_MIN) {
+      const bool small = small_program(ps, p, small_entries);
+      pcost[p] = small ? -(int64_t(1) << 40) - prog_trans(ps, p) : prog_trans(ps, p);
+    }
+    cost[b] = pcost[p];
   }
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  {
+    std::vector<int64_t> uniq;
+    for (size_t p = 0; p < pcost.size(); ++p)
+      if (pcost[p] != INT64_MIN) uniq.push_back(pcost[p]);
+    std::sort(uniq.begin(), uniq.end(), std::greater<int64_t>());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    std::vector<int32_t> prank(pcost.size(), 0);
+    for (size_t p = 0; p < pcost.size(); ++p)
+      if (pcost[p] != INT64_MIN)
+        prank[p] = int32_t(std::lower_bound(uniq.begin(), uniq.end(), pcost[p], std::greater<int64_t>()) - uniq.begin());
+    std::vector<int> start(uniq.size() + 1, 0);
+    for (int b = 0; b < nb; ++b) start[prank[bk.progs[b]] + 1]++;
+    for (size_t r = 0; r < uniq.size(); ++r) start[r + 1] += start[r];
+    for (int b = 0; b < nb; ++b) order[start[prank[bk.progs[b]]]++] = b;
+  }
   Buckets out;
   remap.assign(nb, -1);
   out.progs.resize(nb);
@@ -1038,12 +1138,24 @@ struct SiteCombos {
   std::vector<uint64_t> gk_l, gk_r;
   std::vector<int64_t> gc_l, gc_r;
   std::vector<uint64_t> keys;   // per (j, gl, gr): full key, or ~0 for odd order
+  std::vector<int32_t> prog;    // its program, -1 until generated
+  std::vector<uint64_t> missing;  // keys without a program yet
   int err = 0;
 };
 
+using plan_clk = std::chrono::steady_clock;
+static double plan_ms_since(plan_clk::time_point& t) {
+  const auto now = plan_clk::now();
+  const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+  t = now;
+  return ms;
+}
+
+// ph: when non-null, host ms of phases A-D are added to ph[0..3]
 static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, const int* KL,
                                const uint64_t* const* kr, const int* KR, int ns, const int* dv,
-                               std::vector<SitePlanHost>& plans, Buckets& bk) {
+                               std::vector<SitePlanHost>& plans, Buckets& bk, double* ph = nullptr) {
+  auto t_ph = plan_clk::now();
   plans.assign(ns, SitePlanHost());
   std::vector<SiteCombos> cb(ns);
   parallel_for(ns, [&](int s) {
@@ -1058,6 +1170,8 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
     sp.ngl = int(c.gk_l.size());
     sp.ngr = int(c.gk_r.size());
     c.keys.assign((size_t)d * sp.ngl * sp.ngr, ~0ull);
+    c.prog.assign(c.keys.size(), -1);
+    // the program index is only read here (phase B adds to it afterwards)
     for (int j = 0; j < d; ++j) {
       const uint64_t kj = key_add_class(0, j);
       for (int gl = 0; gl < sp.ngl; ++gl) {
@@ -1069,7 +1183,12 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
             c.err = 1;
             continue;
           }
-          c.keys[((size_t)j * sp.ngl + gl) * sp.ngr + gr] = kj + c.gk_l[gl] + c.gk_r[gr];
+          const size_t o = ((size_t)j * sp.ngl + gl) * sp.ngr + gr;
+          const uint64_t k = kj + c.gk_l[gl] + c.gk_r[gr];
+          c.keys[o] = k;
+          auto it = ps.index.find(k);
+          if (it != ps.index.end()) c.prog[o] = it->second;
+          else c.missing.push_back(k);
         }
       }
     }
@@ -1079,13 +1198,14 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
       set_error("site %d: hafnian order exceeds BSG_MAX_ORDER", s);
       return BSG_ERR_LIMIT;
     }
-  // phase B: new programs, serially
+  if (ph) ph[0] += plan_ms_since(t_ph);
+  // phase B: new programs, serially (only the keys phase A did not find)
   for (int s = 0; s < ns; ++s)
-    for (uint64_t k : cb[s].keys)
-      if (k != ~0ull && !ps.index.count(k)) {
-        int32_t prog;
-        BSG_TRY(program_for_key(ps, k, &prog));
-      }
+    for (uint64_t k : cb[s].missing) {
+      int32_t prog;
+      BSG_TRY(program_for_key(ps, k, &prog));
+    }
+  if (ph) ph[1] += plan_ms_since(t_ph);
   // phase C: per-site buckets (read-only program index)
   std::vector<std::vector<int32_t>> lprog(ns);
   std::vector<std::vector<int64_t>> lcount(ns);
@@ -1109,7 +1229,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
           const size_t o = ((size_t)j * sp.ngl + gl) * sp.ngr + gr;
           const uint64_t k = c.keys[o];
           if (k == ~0ull) continue;
-          const int32_t prog = ps.index.find(k)->second;
+          const int32_t prog = c.prog[o] >= 0 ? c.prog[o] : ps.index.find(k)->second;
           auto it = local.find(prog);
           int32_t b;
           if (it == local.end()) {
@@ -1125,6 +1245,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
           sp.bucket_of[o] = b;
         }
   });
+  if (ph) ph[2] += plan_ms_since(t_ph);
   // phase D: global bucket list
   std::vector<int32_t> base(ns, 0);
   for (int s = 0; s < ns; ++s) {
@@ -1139,6 +1260,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
     for (auto& b : plans[s].bucket_of)
       if (b >= 0) b += base[s];
   });
+  if (ph) ph[3] += plan_ms_since(t_ph);
   return BSG_OK;
 }
 
@@ -1165,6 +1287,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
                      bsg_handle_s::SiteSlot& slot, cudaStream_t st) {
   auto& ps = h->programs;
   const int ns = int(in.size());
+  double* ph = h->prof.on ? h->prof.plan_ms : nullptr;
+  const auto t_all = plan_clk::now();
   Buckets bk;
   std::vector<SitePlanHost> plans;
   {
@@ -1177,14 +1301,18 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
       KR[s] = in[s].KR;
       dv[s] = in[s].d ? in[s].d : d;
     }
-    BSG_TRY(plan_sites_parallel(ps, kl.data(), KL.data(), kr.data(), KR.data(), ns, dv.data(), plans, bk));
+    BSG_TRY(plan_sites_parallel(ps, kl.data(), KL.data(), kr.data(), KR.data(), ns, dv.data(), plans, bk, ph));
   }
+  auto t_ph = plan_clk::now();
   std::vector<int32_t> remap;
   BSG_TRY(layout_buckets(ps, h->tune[BSG_TUNE_DP_SMALL_ENTRIES], bk, remap));
-  for (auto& p : plans)
-    for (auto& b : p.bucket_of)
+  parallel_for(ns, [&](int s) {
+    for (auto& b : plans[s].bucket_of)
       if (b >= 0) b = remap[b];
+  });
+  if (ph) ph[4] += plan_ms_since(t_ph);
   BSG_TRY(programs_upload(ps, st));
+  if (ph) ph[5] += plan_ms_since(t_ph);
   const int nb = int(bk.progs.size());
 
   // one plan buffer: site descs, per-site tables, bucket offsets/chunks/programs/sites, counters
@@ -1197,6 +1325,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   };
   const size_t o_desc = carve(sizeof(SiteDesc) * ns);
   const size_t o_lsj = carve(sizeof(LeftScaleJob) * ns);
+  const size_t o_fs = carve(sizeof(FillSpan) * ns);  // Gamma clears
   std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns), o_co(ns), o_gsl(ns), o_gcl(ns), o_gsr(ns),
       o_lsd(ns), o_lsf(ns);
   int max_kl = 1;
@@ -1224,8 +1353,18 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   char* dp = reinterpret_cast<char*>(slot.plan.ptr);
   SiteDesc* hd = reinterpret_cast<SiteDesc*>(hp + o_desc);
   LeftScaleJob* hl = reinterpret_cast<LeftScaleJob*>(hp + o_lsj);
+  FillSpan* hfs = reinterpret_cast<FillSpan*>(hp + o_fs);
   const int out_c128 = out_dtype == BSG_OUT_C128;
+  const size_t esz = out_c128 ? 16 : 8;
+  int64_t gamma_max = 0;
   for (int s = 0; s < ns; ++s) {
+    const size_t cs = in[s].chi ? in[s].chi : chi, ds = in[s].d ? in[s].d : d;
+    hfs[s] = FillSpan{in[s].gamma, (int64_t)(cs * cs * ds * esz), 0};
+    gamma_max = std::max(gamma_max, hfs[s].bytes);
+  }
+  // per-site descriptors and plan tables into the staging buffer (disjoint
+  // regions, filled by the planning threads)
+  parallel_for(ns, [&](int s) {
     const SiteInput& si = in[s];
     LeftScaleJob lj{};
     lj.rowfact = si.lt.rowfact;
@@ -1265,7 +1404,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     std::memcpy(hp + o_gsl[s], plans[s].gstart_l.data(), plans[s].gstart_l.size() * 4);
     std::memcpy(hp + o_gcl[s], plans[s].gcnt_l.data(), plans[s].gcnt_l.size() * 4);
     std::memcpy(hp + o_gsr[s], plans[s].gstart_r.data(), plans[s].gstart_r.size() * 4);
-  }
+  });
   std::memcpy(hp + o_boff, bk.offsets.data(), (size_t)nb * 4);
   {
     int32_t* hend = reinterpret_cast<int32_t*>(hp + o_bend);
@@ -1294,11 +1433,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   BSG_PROFILED(h, BSG_K_PREP, st, (double)ns * max_kl,
                (left_scale_kernel<<<dim3((max_kl + 127) / 128, ns), 128, 0, st>>>(
                    reinterpret_cast<const LeftScaleJob*>(dp + o_lsj))));
-  const size_t esz = out_c128 ? 16 : 8;
-  for (int s = 0; s < ns; ++s) {
-    const size_t cs = in[s].chi ? in[s].chi : chi, ds = in[s].d ? in[s].d : d;
-    BSG_CUDA(cudaMemsetAsync(in[s].gamma, 0, cs * cs * ds * esz, st));
-  }
+  BSG_TRY(fill_spans_dev(h, reinterpret_cast<const FillSpan*>(dp + o_fs), ns, gamma_max, st));
   if (bk.slots == 0) return BSG_OK;
   BSG_PROFILED(h, BSG_K_PREP, st, (double)nb * 32,
                (pad_items_kernel<<<unsigned(((int64_t)nb * 32 + 255) / 256), 256, 0, st>>>(
@@ -1322,7 +1457,12 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   a.nb = nb;
   a.counter = reinterpret_cast<unsigned long long*>(dp + o_ctr);
   a.sites = reinterpret_cast<SiteDesc*>(dp + o_desc);
-  return launch_dp<MODE_SITE>(h, precision, a, bk, slot.scratch, st);
+  const int rc = launch_dp<MODE_SITE>(h, precision, a, bk, slot.scratch, st);
+  if (ph) {
+    ph[6] += plan_ms_since(t_ph);
+    ph[7] += std::chrono::duration<double, std::milli>(plan_clk::now() - t_all).count();
+  }
+  return rc;
 }
 
 }  // namespace bsg
@@ -1914,12 +2054,18 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
                                 void* const* gammas, double* const* Lambdas, double* const* res,
                                 int8_t* const* num, double* const* S, int32_t* const* kept, cudaStream_t st,
                                 bool cuts_given = false, const int* lo = nullptr, const int* hi = nullptr) {
+  using clk = std::chrono::steady_clock;
+  auto ms_since = [](clk::time_point t0) {
+    return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+  };
   BSG_CHECK_ARG(n >= 1, "bsg_build_mps_batch: need at least one instance");
   BSG_CHECK_ARG(sq && Ms && ds && chis && gammas && Lambdas && res && num && S && kept,
                 "bsg_build_mps_batch: null pointer");
   BSG_CHECK_ARG(precision >= 0 && precision <= 2, "bsg_build_mps_batch: bad precision %d", precision);
   BSG_CHECK_ARG(out_dtype == BSG_OUT_C64 || out_dtype == BSG_OUT_C128, "bsg_build_mps_batch: bad out_dtype");
-  std::vector<int> site0(n + 1, 0), slo(n), shi(n), clo(n), chi_(n);
+  std::vector<int> site0(n + 1, 0), slo(n), shi(n), clo(n), chi_(n), cut0(n + 1, 0);
+  std::vector<int64_t> key0(n + 1, 0);
+  int chi_max = 0;
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i], d = ds[i], chi = chis[i];
     BSG_CHECK_ARG(sq[i] && Lambdas[i] && res[i] && num[i] && S[i] && kept[i],
@@ -1936,8 +2082,11 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     clo[i] = std::max(0, slo[i] - 1);
     chi_[i] = std::min(shi[i], M - 1);
     site0[i + 1] = site0[i] + (shi[i] - slo[i]);
+    cut0[i + 1] = cut0[i] + (M - 1);
+    key0[i + 1] = key0[i] + (int64_t)(M - 1) * chi;
+    chi_max = std::max(chi_max, chi);
   }
-  const int ns = site0[n];
+  const int ns = site0[n], total_cuts = cut0[n];
   for (int s = 0; s < ns; ++s) BSG_CHECK_ARG(gammas[s], "bsg_build_mps_batch: Gamma pointer %d is NULL", s);
   BSG_CUDA(cudaSetDevice(h->device));
   BSG_TRY(ensure_tables());
@@ -1949,8 +2098,7 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     return o;
   };
   struct Inst {
-    size_t o_cut, o_ent, o_nnz, o_sum, o_key, o_rf, o_rf2, o_above, o_err, o_Z, o_status;
-    size_t h_cut, h_keys, h_cnt, h_above, h_err;  // offsets in the pinned staging
+    size_t o_cut, o_ent, o_nnz, o_sum, o_rf, o_rf2, o_Z;
   };
   std::vector<Inst> I(n);
   std::vector<size_t> o_sig(ns), o_sigc(ns), o_sws(ns);
@@ -1960,50 +2108,53 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     hoff = (hoff + bytes + 63) & ~size_t(63);
     return o;
   };
-  int total_cuts = 0;
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i], chi = chis[i], nc = M - 1;
-    total_cuts += nc;
     Inst& t = I[i];
     t.o_cut = cuts_given ? carve(0) : carve(cut_ws_bytes(M, 1, nc, chi));
     t.o_ent = carve((size_t)nc * chi * kMaxNnz * 4);
     t.o_nnz = carve((size_t)nc * chi * 4);
     t.o_sum = carve((size_t)nc * chi * 4);
-    t.o_key = carve((size_t)nc * chi * 8);
     t.o_rf = carve((size_t)nc * chi * 8);
     t.o_rf2 = carve((size_t)nc * chi * 8);
-    t.o_above = carve((size_t)nc * 4);
-    t.o_err = carve(16);
     t.o_Z = carve((size_t)M * 8);
-    t.o_status = carve((size_t)M * 4);
     for (int j = slo[i]; j < shi[i]; ++j) {
       const int s = site0[i] + j - slo[i], Mr = j == 0 ? M : M - j;
       o_sig[s] = carve((size_t)(2 * Mr) * (2 * Mr) * 16);
       o_sigc[s] = precision == BSG_PREC_FP64 ? o_sig[s] : carve((size_t)(2 * Mr) * (2 * Mr) * prec_bytes(precision));
       o_sws[s] = carve(sigma_ws_bytes(Mr));
     }
-    t.h_cut = hcarve((size_t)2 * nc * 4);
-    t.h_keys = hcarve((size_t)nc * chi * 8);
-    t.h_cnt = hcarve((size_t)nc * 4);
-    t.h_above = hcarve((size_t)nc * 4);
-    t.h_err = hcarve(4);
   }
-  const size_t o_empty = carve(kMaxNnz * 4 + 64);
+  // Host-bound region, one device->host copy for all instances:
+  // [label error per instance | Sigma status per site | rows above tol per cut]  cleared to 0,
+  // [Williamson status per cut, then its sweeps, per instance]                   cleared to -1,
+  // [kept-row count per cut | row keys per (cut, row)].
+  const size_t hb_err = 0, hb_sst = hb_err + 4 * (size_t)n, hb_above = hb_sst + 4 * (size_t)ns;
+  const size_t hb_cst = hb_above + 4 * (size_t)total_cuts, hb_cnt = hb_cst + 8 * (size_t)total_cuts;
+  const size_t hb_keys = (hb_cnt + 4 * (size_t)total_cuts + 7) & ~size_t(7);
+  const size_t hb_bytes = hb_keys + 8 * (size_t)key0[n];
+  const size_t o_hb = carve(hb_bytes), h_hb = hcarve(hb_bytes);
+  const size_t o_empty = carve(kMaxNnz * 4 + 64), h_empty = hcarve(kMaxNnz * 4 + 64);
   const size_t cargs_bytes = al(sizeof(CutArgs) * n) + al(sizeof(int2) * total_cuts);
-  const size_t o_cargs = carve(cargs_bytes);
-  const size_t o_jobs = carve(sizeof(SigmaJob) * ns), o_conv = carve(sizeof(ConvJob) * ns);
-  const size_t h_cargs = hcarve(cargs_bytes), h_jobs = hcarve(sizeof(SigmaJob) * ns), h_sst = hcarve((size_t)ns * 4);
-  const size_t h_conv = hcarve(sizeof(ConvJob) * ns);
-  const size_t h_empty = hcarve(kMaxNnz * 4 + 64);
+  const size_t o_cargs = carve(cargs_bytes), h_cargs = hcarve(cargs_bytes);
+  const int max_spans = 6 * n + 2;
+  const size_t o_fill = carve(sizeof(FillSpan) * max_spans), h_fill = hcarve(sizeof(FillSpan) * max_spans);
+  const size_t rows_bytes = al(sizeof(CutRowsJob) * n) + sizeof(int2) * (size_t)total_cuts;
+  const size_t o_rows = carve(rows_bytes), h_rows = hcarve(rows_bytes);
+  const size_t o_jobs = carve(sizeof(SigmaJob) * ns), h_jobs = hcarve(sizeof(SigmaJob) * ns);
+  const size_t o_conv = carve(sizeof(ConvJob) * ns), h_conv = hcarve(sizeof(ConvJob) * ns);
   BSG_TRY(h->mps_ws.ensure(off));
   BSG_TRY(h->host_stage.ensure(hoff));
   char* wb = reinterpret_cast<char*>(h->mps_ws.ptr);
   char* hs = reinterpret_cast<char*>(h->host_stage.ptr);
+  char* hb = wb + o_hb;   // device
+  char* hbh = hs + h_hb;  // its host copy
   auto table = [&](int i, int c) {
     const Inst& t = I[i];
     const size_t o = (size_t)c * chis[i];
     return RowTable{reinterpret_cast<int32_t*>(wb + t.o_ent) + o * kMaxNnz, reinterpret_cast<int32_t*>(wb + t.o_nnz) + o,
-                    reinterpret_cast<int32_t*>(wb + t.o_sum) + o, reinterpret_cast<uint64_t*>(wb + t.o_key) + o,
+                    reinterpret_cast<int32_t*>(wb + t.o_sum) + o,
+                    reinterpret_cast<uint64_t*>(hb + hb_keys) + key0[i] + o,
                     reinterpret_cast<double*>(wb + t.o_rf) + o, reinterpret_cast<float2*>(wb + t.o_rf2) + o};
   };
   RowTable empty{reinterpret_cast<int32_t*>(wb + o_empty), reinterpret_cast<int32_t*>(wb + o_empty + kMaxNnz * 4),
@@ -2019,39 +2170,59 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     std::memcpy(e + kMaxNnz * 4 + 16, &one2, 8);
     BSG_CUDA(cudaMemcpyAsync(wb + o_empty, e, kMaxNnz * 4 + 64, cudaMemcpyHostToDevice, st));
   }
-  // 1. every cut of every instance: Williamson and top-chi, one launch each
+  // 1. every instance's output and status clears in one launch, then every
+  //    cut of every instance: Williamson and top-chi, one launch each
   std::vector<CutArgs> cargs(n);
-  for (int i = 0; i < n; ++i) {
-    const int M = Ms[i];
-    if (!cuts_given)
-      BSG_TRY(cut_prepare_at(h, wb + I[i].o_cut, sq[i], M, 1, M - 1, ds[i], chis[i], cut_tol, res[i], num[i], S[i],
-                             kept[i], &cargs[i], st));
-    BSG_CUDA(cudaMemsetAsync(wb + I[i].o_err, 0, 16, st));
-    BSG_CUDA(cudaMemsetAsync(wb + I[i].o_status, 0, (size_t)M * 4, st));
-  }
-  if (!cuts_given) BSG_TRY(cut_launch_batch(h, cargs.data(), n, wb + o_cargs, hs + h_cargs, st));
-  // 2. per instance: Lambda, label rows, keys to the host (the cuts its sites read)
-  for (int i = 0; i < n; ++i) {
-    const int M = Ms[i], chi = chis[i], nc = M - 1, c0 = clo[i], nci = chi_[i] - clo[i];
-    const Inst& t = I[i];
-    if (!cuts_given) BSG_TRY(cut_queue_status(cargs[i], 0, nc, reinterpret_cast<int*>(hs + t.h_cut), st));
-    if (nci > 0) {
-      BSG_PROFILED(h, BSG_K_PREP, st, (double)nci * chi,
-                   (lambda_kernel<<<nci, 256, 0, st>>>(res[i] + (size_t)c0 * chi, chi, site_tol,
-                                                       Lambdas[i] + (size_t)c0 * chi,
-                                                       reinterpret_cast<int32_t*>(wb + t.o_above) + c0)));
-      BSG_PROFILED(h, BSG_K_PREP, st, (double)nci * chi,
-                   (label_rows_kernel<<<dim3((chi + 127) / 128, nci), 128, 0, st>>>(
-                       num[i] + (size_t)c0 * chi * (M - 1), (int64_t)chi * (M - 1), M - 1, kept[i] + c0, M - 1 - c0,
-                       1, chi, table(i, c0), reinterpret_cast<int*>(wb + t.o_err))));
-      BSG_CUDA(cudaMemcpyAsync(hs + t.h_keys + (size_t)c0 * chi * 8, wb + t.o_key + (size_t)c0 * chi * 8,
-                               (size_t)nci * chi * 8, cudaMemcpyDeviceToHost, st));
-      BSG_CUDA(cudaMemcpyAsync(hs + t.h_cnt + (size_t)c0 * 4, kept[i] + c0, (size_t)nci * 4, cudaMemcpyDeviceToHost,
-                               st));
-      BSG_CUDA(cudaMemcpyAsync(hs + t.h_above + (size_t)c0 * 4, wb + t.o_above + (size_t)c0 * 4, (size_t)nci * 4,
-                               cudaMemcpyDeviceToHost, st));
+  std::vector<FillSpan> spans;
+  spans.reserve(max_spans);
+  spans.push_back(FillSpan{hb, (int64_t)hb_cst, 0});
+  spans.push_back(FillSpan{hb + hb_cst, (int64_t)(8 * (size_t)total_cuts), 0xff});
+  if (!cuts_given)
+    for (int i = 0; i < n; ++i) {
+      const int M = Ms[i], nc = M - 1;
+      BSG_TRY(cut_prepare_at(h, wb + I[i].o_cut, sq[i], M, 1, nc, ds[i], chis[i], cut_tol, res[i], num[i], S[i],
+                             kept[i], &cargs[i], st, &spans));
+      // the cut status lands in the host-bound region
+      cargs[i].status = reinterpret_cast<int*>(hb + hb_cst) + 2 * (size_t)cut0[i];
+      cargs[i].sweeps = cargs[i].status + nc;
     }
-    BSG_CUDA(cudaMemcpyAsync(hs + t.h_err, wb + t.o_err, 4, cudaMemcpyDeviceToHost, st));
+  BSG_TRY(fill_spans(h, spans.data(), int(spans.size()), wb + o_fill, hs + h_fill, st));
+  if (!cuts_given) BSG_TRY(cut_launch_batch(h, cargs.data(), n, wb + o_cargs, hs + h_cargs, st));
+  // 2. Lambda, label rows and keys of the cuts the sites read, one launch,
+  //    then the host-bound region in one copy
+  {
+    CutRowsJob* rj = reinterpret_cast<CutRowsJob*>(hs + h_rows);
+    int2* rmap = reinterpret_cast<int2*>(hs + h_rows + al(sizeof(CutRowsJob) * n));
+    int n_rows = 0;
+    double work = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const int M = Ms[i], chi = chis[i], c0 = clo[i], nci = chi_[i] - clo[i];
+      CutRowsJob jb{};
+      jb.num = num[i] + (size_t)c0 * chi * (M - 1);
+      jb.kept = kept[i] + c0;
+      jb.res = res[i] + (size_t)c0 * chi;
+      jb.lambda = Lambdas[i] + (size_t)c0 * chi;
+      jb.t = table(i, c0);
+      jb.above = reinterpret_cast<int32_t*>(hb + hb_above) + cut0[i] + c0;
+      jb.cnt = reinterpret_cast<int32_t*>(hb + hb_cnt) + cut0[i] + c0;
+      jb.err = reinterpret_cast<int*>(hb + hb_err) + i;
+      jb.tol = site_tol;
+      jb.chi = chi;
+      jb.ld = M - 1;
+      jb.m0 = M - 1 - c0;
+      rj[i] = jb;
+      for (int c = 0; c < nci; ++c) rmap[n_rows++] = make_int2(i, c);
+      work += (double)nci * chi;
+    }
+    if (n_rows > 0) {
+      BSG_CUDA(cudaMemcpyAsync(wb + o_rows, hs + h_rows, al(sizeof(CutRowsJob) * n) + sizeof(int2) * n_rows,
+                               cudaMemcpyHostToDevice, st));
+      BSG_PROFILED(h, BSG_K_PREP, st, work,
+                   (cut_rows_batch_kernel<<<dim3((chi_max + 127) / 128, n_rows), 128, 0, st>>>(
+                       reinterpret_cast<const CutRowsJob*>(wb + o_rows),
+                       reinterpret_cast<const int2*>(wb + o_rows + al(sizeof(CutRowsJob) * n)))));
+    }
+    BSG_CUDA(cudaMemcpyAsync(hbh, hb, hb_bytes, cudaMemcpyDeviceToHost, st));
   }
   // 3. Sigma of every site of every instance in one set of launches
   SigmaJob* jobs = reinterpret_cast<SigmaJob*>(hs + h_jobs);
@@ -2079,7 +2250,7 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
       jb.Sigma = reinterpret_cast<double2*>(wb + o_sig[s]);
       jb.Z = reinterpret_cast<double*>(wb + I[i].o_Z) + j;
       jb.ws = reinterpret_cast<double*>(wb + o_sws[s]);
-      jb.status = reinterpret_cast<int*>(wb + I[i].o_status) + j;
+      jb.status = reinterpret_cast<int*>(hb + hb_sst) + s;
       jobs[s] = jb;
     }
   }
@@ -2095,22 +2266,27 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
                                  (int64_t)(2 * Mr) * (2 * Mr)};
     }
   BSG_TRY(convert_many(h, conv, n_conv, wb + o_conv, precision, st));
-  // 4. one host wait: every instance's cut status and keys
-  BSG_CUDA(cudaStreamSynchronize(st));
+  // 4. one host wait: every instance's cut status, row counts and keys
+  {
+    auto t_wait = clk::now();
+    BSG_CUDA(cudaStreamSynchronize(st));
+    h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_wait), 0.0);
+  }
+  auto t_plan = clk::now();
   static const uint64_t zero_key = 0;
   std::vector<SiteInput> in(ns);
   for (int i = 0; i < n; ++i) {
     const int M = Ms[i], chi = chis[i], nc = M - 1;
-    const Inst& t = I[i];
-    if (!cuts_given) BSG_TRY(cut_check_status(h, cargs[i], 0, nc, reinterpret_cast<const int*>(hs + t.h_cut)));
-    if (*reinterpret_cast<const int*>(hs + t.h_err)) {
+    if (!cuts_given)
+      BSG_TRY(cut_check_status(h, cargs[i], 0, nc, reinterpret_cast<const int*>(hbh + hb_cst) + 2 * (size_t)cut0[i]));
+    if (reinterpret_cast<const int*>(hbh + hb_err)[i]) {
       set_error("bsg_build_mps_batch: instance %d: a label row has a multiplicity above %d or more than %d non-zeros",
                 i, kKeyMaxMult, kMaxNnz);
       return BSG_ERR_LIMIT;
     }
-    const uint64_t* hkeys = reinterpret_cast<const uint64_t*>(hs + t.h_keys);
-    const int32_t* hcnt = reinterpret_cast<const int32_t*>(hs + t.h_cnt);
-    const int32_t* habove = reinterpret_cast<const int32_t*>(hs + t.h_above);
+    const uint64_t* hkeys = reinterpret_cast<const uint64_t*>(hbh + hb_keys) + key0[i];
+    const int32_t* hcnt = reinterpret_cast<const int32_t*>(hbh + hb_cnt) + cut0[i];
+    const int32_t* habove = reinterpret_cast<const int32_t*>(hbh + hb_above) + cut0[i];
     for (int j = slo[i]; j < shi[i]; ++j) {
       const int s = site0[i] + j - slo[i];
       SiteInput& si = in[s];
@@ -2118,7 +2294,7 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
       si.Mr = j == 0 ? M : M - j;
       si.sigma = wb + o_sigc[s];
       si.sigma64 = reinterpret_cast<const double2*>(wb + o_sig[s]);
-      si.Z = reinterpret_cast<const double*>(wb + t.o_Z) + j;
+      si.Z = reinterpret_cast<const double*>(wb + I[i].o_Z) + j;
       si.gamma = gammas[s];
       si.d = ds[i];
       si.chi = chi;
@@ -2150,12 +2326,15 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
   }
   // 5. the items of every site of every instance: one scatter, one DP launch set
   BSG_TRY(run_sites(h, in, ds[0], chis[0], precision, out_dtype, h->slot[0], st));
+  h->prof.add_host(BSG_K_HOST_PLAN, ms_since(t_plan), 0.0);
   // Sigma status (singular A), read after the DP
-  int32_t* sst = reinterpret_cast<int32_t*>(hs + h_sst);
-  for (int i = 0; i < n; ++i)
-    BSG_CUDA(cudaMemcpyAsync(sst + site0[i], reinterpret_cast<int32_t*>(wb + I[i].o_status) + slo[i],
-                             (size_t)(shi[i] - slo[i]) * 4, cudaMemcpyDeviceToHost, st));
-  BSG_CUDA(cudaStreamSynchronize(st));
+  const int32_t* sst = reinterpret_cast<const int32_t*>(hbh + hb_sst);
+  BSG_CUDA(cudaMemcpyAsync(hbh + hb_sst, hb + hb_sst, 4 * (size_t)ns, cudaMemcpyDeviceToHost, st));
+  {
+    auto t_fin = clk::now();
+    BSG_CUDA(cudaStreamSynchronize(st));
+    h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_fin), 0.0);
+  }
   for (int i = 0; i < n; ++i)
     for (int j = slo[i]; j < shi[i]; ++j)
       if (sst[site0[i] + j - slo[i]]) {

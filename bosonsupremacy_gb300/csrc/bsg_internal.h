@@ -114,6 +114,7 @@ struct Profiler {
   double work[BSG_K_COUNT] = {0};
   std::vector<double> cut_phases;  // ms per (cut, Williamson phase) of the last profiled cut launch
   std::vector<double> timeline;    // last profiled whole-MPS build: ms per (group, milestone)
+  double plan_ms[8] = {0};         // host planning of the site DP since the last reset, ms per phase
   // DP launches since the last reset: one row per bucket (launch, chunks, classes,
   // F ring slots, states, transitions) and chunk-weighted states by transition count
   std::vector<double> dp_rows;
@@ -169,11 +170,28 @@ struct CutArgs {
 constexpr int kCutTimedPhases = 11;  // stamps 0..10
 constexpr int kCutPhases = 14;       // + FP32 sweeps, FP64 refinement steps, FP32 sweep time (ns)
 
+// A byte range to set to one byte value; many of them are cleared by one
+// launch (fill_spans).
+struct FillSpan {
+  void* p;
+  int64_t bytes;
+  int value;
+};
+// Fills every span in one launch.  stage: pinned host room and dev: device
+// room for n spans (the span list is copied up first).
+int fill_spans(bsg_handle_t h, const FillSpan* spans, int n, void* dev, void* stage, cudaStream_t st);
+// The same with the span list already on the device; max_bytes: the largest span.
+int fill_spans_dev(bsg_handle_t h, const FillSpan* dev_spans, int n, int64_t max_bytes, cudaStream_t st);
+
 int cut_prepare(bsg_handle_t h, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi, double err_tol,
                 double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);
 size_t cut_ws_bytes(int M, int L0, int n_cuts, int chi);
+// With `defer` non-null the output and status clears are appended to it
+// instead of being queued as memsets (the caller fills them, e.g. together
+// with other instances' in one launch).
 int cut_prepare_at(bsg_handle_t h, char* base, const double* sq_cov, int M, int L0, int n_cuts, int d, int chi,
-                   double err_tol, double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st);
+                   double err_tol, double* res, int8_t* num, double* S, int32_t* kept, CutArgs* out, cudaStream_t st,
+                   std::vector<FillSpan>* defer = nullptr);
 size_t cut_batch_bytes(const CutArgs* args, int n);
 int cut_launch_batch(bsg_handle_t h, CutArgs* args, int n, void* dev, void* stage, cudaStream_t st);
 int cut_launch_williamson(bsg_handle_t h, const CutArgs& a, int c0, int c1, cudaStream_t st);
@@ -243,6 +261,8 @@ struct bsg_handle_s {
   bsg::DevBuf mps_ws;         // whole-MPS build: Sigma, row tables, plans
   bsg::DevBuf sample_ws;      // sampler: chain GEMM operands and outputs
   bsg::DevBuf disp_tab;       // displacement eigen-tables for disp_dd
+  bsg::DevBuf decomp_ws;      // covariance decomposition: iterates, Schur complement, step tests
+  bsg::HostBuf decomp_host;   // its pinned scalars and index list
   int disp_dd = 0;
   bsg::HostBuf host_stage;    // pinned staging for plans
   bsg::HostBuf host_stage2;

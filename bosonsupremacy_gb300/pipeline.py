@@ -78,11 +78,18 @@ def build_mps_batch(sq_covs, ds, chis, precision="split", out_dtype=torch.comple
     if outs is None:
         outs = [[torch.empty(c, c, d, dtype=out_dtype, device=dev) for _ in range(M)] for M, d, c in zip(Ms, ds, chis)]
     odt = _lib.OUT_C128 if outs[0][0].dtype == torch.complex128 else _lib.OUT_C64
-    lam = [torch.empty(M - 1, c, dtype=torch.float64, device=dev) for M, c in zip(Ms, chis)]
-    res = [torch.empty(M - 1, c, dtype=torch.float64, device=dev) for M, c in zip(Ms, chis)]
-    num = [torch.empty(M - 1, c, M - 1, dtype=torch.int8, device=dev) for M, c in zip(Ms, chis)]
-    S = [torch.empty(M - 1, 2 * (M - 1), 2 * (M - 1), dtype=torch.float64, device=dev) for M in Ms]
-    kept = [torch.empty(M - 1, dtype=torch.int32, device=dev) for M in Ms]
+
+    # every instance's cut outputs are views of one buffer per kind
+    def views(dtype, shapes):
+        sizes = [int(np.prod(sh)) for sh in shapes]
+        flat = torch.empty(sum(sizes), dtype=dtype, device=dev)
+        return [v.view(sh) for v, sh in zip(torch.split(flat, sizes), shapes)], flat
+
+    lam, _ = views(torch.float64, [(M - 1, c) for M, c in zip(Ms, chis)])
+    res, res_flat = views(torch.float64, [(M - 1, c) for M, c in zip(Ms, chis)])
+    num, _ = views(torch.int8, [(M - 1, c, M - 1) for M, c in zip(Ms, chis)])
+    S, _ = views(torch.float64, [(M - 1, 2 * (M - 1), 2 * (M - 1)) for M in Ms])
+    kept, kept_flat = views(torch.int32, [(M - 1,) for M in Ms])
 
     def arr(ctype, xs):
         return (ctype * len(xs))(*xs)
@@ -97,13 +104,17 @@ def build_mps_batch(sq_covs, ds, chis, precision="split", out_dtype=torch.comple
         arr(P, [x.data_ptr() for x in lam]), arr(P, [x.data_ptr() for x in res]), arr(P, [x.data_ptr() for x in num]),
         arr(P, [x.data_ptr() for x in S]), arr(P, [x.data_ptr() for x in kept]), _lib.stream_ptr()),
         "bsg_build_mps_batch")
-    torch.cuda.synchronize(dev)
+    kept_all = kept_flat.cpu().numpy()
+    res_all = res_flat.cpu().numpy()
     t = {"total_s": time.perf_counter() - t0}
     out = []
+    k0 = r0 = 0
     for i in range(n):
-        kh = kept[i].cpu().numpy()
-        rh = res[i].cpu().numpy()
-        left = np.array([int((rh[c, : kh[c]] > err_tol).sum()) for c in range(Ms[i] - 1)])
+        nc, c = Ms[i] - 1, chis[i]
+        kh = kept_all[k0:k0 + nc]
+        rh = res_all[r0:r0 + nc * c].reshape(nc, c)
+        k0, r0 = k0 + nc, r0 + nc * c
+        left = np.array([int((rh[q, : kh[q]] > err_tol).sum()) for q in range(nc)])
         out.append(MPS(outs[i], lam[i], res[i], num[i], S[i], kh, left, t))
     return out
 

@@ -115,6 +115,25 @@ def lossy_covariances(cfg: GBSConfig, seed: Optional[int] = None) -> Tuple[np.nd
     return cov, sq
 
 
+def nonuniform_lossy_covariance(M: int, seed: int = 0, r_lo: float = 0.5, r_hi: float = 1.2, eta_lo: float = 0.2,
+                                eta_hi: float = 0.8) -> np.ndarray:
+    """Covariance (2M x 2M, xxpp) with mode-dependent loss between two
+    Haar-random interferometers: squeezed vacuum r_k ~ U[r_lo, r_hi] -> U1 ->
+    loss eta_k ~ U[eta_lo, eta_hi] on mode k -> U2.  Loss no longer commutes
+    with the interferometers, so the pure part has no closed form: this is
+    the input the covariance decomposition (an SDP) exists for."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(r_lo, r_hi, size=M)
+    O1 = passive_symplectic(haar_unitary(M, rng))
+    eta = rng.uniform(eta_lo, eta_hi, size=M)
+    O2 = passive_symplectic(haar_unitary(M, rng))
+    cov = O1 @ np.diag(np.concatenate([np.exp(2 * r), np.exp(-2 * r)])) @ O1.T
+    t = np.sqrt(np.concatenate([eta, eta]))
+    cov = t[:, None] * cov * t[None, :] + np.diag(1.0 - t * t)
+    cov = O2 @ cov @ O2.T
+    return 0.5 * (cov + cov.T)
+
+
 def write_inputs(cfg: GBSConfig, rootdir: str, seed: Optional[int] = None) -> None:
     """Write ``cov.npy`` and ``sq_cov.npy`` the way make_cov.py:135 and
     get_decomposition.py:30 leave them for kron_cpu.py / MPS_cpu.py."""

@@ -326,6 +326,15 @@ int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* m
  * absent.  n: entries to fill (12 covers every group). */
 int bsg_profile_build_timeline(bsg_handle_t h, double* ms, int n);
 
+/* Host wall time (ms, summed since the last bsg_profile_reset while
+ * profiling was enabled) of the site DP's planning phases: 0 row grouping
+ * and partition keys of every (j, left group, right group) combination
+ * (parallel), 1 new partition programs (serial), 2 per-site buckets
+ * (parallel), 3 the global bucket list, 4 bucket layout and remap,
+ * 5 program upload, 6 plan staging and the scatter/DP launches, 7 the
+ * whole of it.  n: entries to fill (8 covers every phase). */
+int bsg_profile_plan_phases(bsg_handle_t h, double* ms, int n);
+
 /* Hafnian DP launches since the last bsg_profile_reset while profiling was
  * enabled.  *n_rows = buckets seen; rows[6 r + f] (r < max_rows) = launch
  * (0 large-table, 1 small-table programs), 32-item chunks, classes k, F ring
@@ -334,6 +343,30 @@ int bsg_profile_build_timeline(bsg_handle_t h, double* ms, int n);
  * last entry collects larger counts).  rows / state_hist may be null. */
 int bsg_profile_dp_buckets(bsg_handle_t h, double* rows, int max_rows, int* n_rows, double* state_hist,
                            int hist_len);
+
+/* ---- covariance decomposition ---------------------------------------------
+ * The pure quantum part of a Gaussian covariance, replacing
+ * get_decomposition.py:16-29 (cvxpy/CVXOPT):
+ *   sq_cov = argmin tr X  s.t.  [[X, Omega], [-Omega, X]] >= 0,  cov - X >= 0,
+ * Omega = kron([[0, 1], [-1, 0]], I_M).  cov, sq_cov: device float64
+ * [2M, 2M] row-major, xxpp order.  An infeasible-start primal-dual
+ * interior-point method (HKM direction, Mehrotra predictor-corrector), all
+ * in FP64 on the device; the Schur complement takes (M (2M + 1))^2 * 8
+ * bytes (M <= 315; 0.2 GB at M = 50, 13.9 GB at M = 144).  Stops when the
+ * relative duality gap, primal and dual residuals are all below tol, or
+ * after max_iter (<= 1000) iterations (BSG_ERR_NO_CONVERGE; sq_cov then holds
+ * the last iterate).  info (host, may be NULL): [iterations, relative gap,
+ * primal residual, dual residual, primal objective tr X, dual objective].
+ * Synchronises `stream`. */
+int bsg_cov_decomposition(bsg_handle_t h, const double* cov, int M, double* sq_cov, double tol, int max_iter,
+                          double* info, bsg_stream_t stream);
+
+/* In-place lower Cholesky factor of a device float64 [n, n] row-major
+ * symmetric matrix (the decomposition's blocked factorisation, exposed for
+ * testing; the strict upper triangle is left as it was).  *info (host) = 0,
+ * or the 1-based column of the first non-positive pivot.  Synchronises
+ * `stream`. */
+int bsg_potrf_f64(bsg_handle_t h, double* A, int n, int* info, bsg_stream_t stream);
 
 /* ---- tuning knobs (no reference counterpart) ------------------------------
  * Launch parameters an autotuner may change per handle (bosonsupremacy_gb300

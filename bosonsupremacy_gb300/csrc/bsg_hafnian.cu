@@ -14,12 +14,16 @@
 #include <chrono>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <mutex>
 #include <thread>
 #include <cstring>
 #include <functional>
 #include <numeric>
 #include <type_traits>
 #include <vector>
+
+#include <unistd.h>
 
 #include "bsg_arith.cuh"
 #include "bsg_internal.h"
@@ -1117,21 +1121,86 @@ static int run_target_dp(bsg_handle_t h, int mode, const void* sig, int n_len, c
 // combinations with their partition keys.  Phase B (serial): generate the
 // programs of keys not seen before.  Phase C (parallel): map combinations to
 // per-site buckets.  Phase D (serial): concatenate the buckets of all sites.
+// Worker threads kept for the life of the process (planning runs several
+// parallel phases per call; starting threads each time cost more than the
+// phases on small builds).  One parallel_for at a time uses the pool; a call
+// that finds it busy (another handle planning on another thread) runs inline.
+class PlanPool {
+ public:
+  explicit PlanPool(int workers) : owner(getpid()) {
+    for (int t = 0; t < workers; ++t) th_.emplace_back([this] { work(); });
+  }
+  const pid_t owner;  // a forked child inherits this object but not its threads
+  ~PlanPool() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& x : th_) x.join();
+  }
+  std::mutex run_mutex;
+  // runs f(0..n-1) on the workers and the calling thread; returns when all are done
+  void run(int n, const std::function<void(int)>& f) {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      job_ = &f;
+      n_ = n;
+      next_.store(0);
+      busy_ = int(th_.size());
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (int i = next_++; i < n; i = next_++) f(i);
+    std::unique_lock<std::mutex> g(m_);
+    done_cv_.wait(g, [this] { return busy_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work() {
+    uint64_t seen = 0;
+    while (true) {
+      const std::function<void(int)>* job;
+      int n;
+      {
+        std::unique_lock<std::mutex> g(m_);
+        cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+        job = job_;
+        n = n_;
+      }
+      for (int i = next_++; i < n; i = next_++) (*job)(i);
+      std::lock_guard<std::mutex> g(m_);
+      if (--busy_ == 0) done_cv_.notify_one();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* job_ = nullptr;
+  int n_ = 0, busy_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+  std::atomic<int> next_{0};
+};
+
 template <class F>
 static void parallel_for(int n, F&& f) {
-  const int hw = std::max(1u, std::thread::hardware_concurrency());
-  const int nt = std::max(1, std::min(n, std::min(hw, 32)));
-  if (nt <= 1 || n < 4) {
+  static const int hw = int(std::max(1u, std::thread::hardware_concurrency()));
+  if (hw <= 1 || n < 4) {
     for (int i = 0; i < n; ++i) f(i);
     return;
   }
-  std::atomic<int> next(0);
-  std::vector<std::thread> th;
-  for (int t = 0; t < nt; ++t)
-    th.emplace_back([&] {
-      for (int i = next++; i < n; i = next++) f(i);
-    });
-  for (auto& x : th) x.join();
+  static PlanPool pool(std::min(hw, 32) - 1);
+  std::unique_lock<std::mutex> busy(pool.run_mutex, std::defer_lock);
+  if (pool.owner != getpid() || !busy.try_lock()) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  const std::function<void(int)> fn = [&f](int i) { f(i); };
+  pool.run(n, fn);
 }
 
 struct SiteCombos {

@@ -327,26 +327,21 @@ __device__ __forceinline__ int build_classes(const DPArgs& a, const SiteDesc* sd
   sig_base = 0;
   fac = 1.0;
   if (MODE == MODE_SITE) {
-    const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff, j = item & 0xff;
+    const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff;
     const int32_t* le = sd->l_ent + (size_t)beta * kMaxNnz;
     const int32_t* re = sd->r_ent + (size_t)alpha * kMaxNnz;
     const int nl = sd->l_nnz[beta], nr = sd->r_nnz[alpha];
     const int roff = sd->Mr;
     int il = 0, ir = 0, k = 0;
-    bool jpend = j > 0;
-    // three-way merge by multiplicity (j class first on ties)
-    while (jpend || il < nl || ir < nr) {
+    // left and right label classes merged by multiplicity (left first on
+    // ties), then the site class, which the site programs keep last
+    while (il < nl || ir < nr) {
       const int ml = il < nl ? (le[il] & 0xff) : 1 << 20;
       const int mr = ir < nr ? (re[ir] & 0xff) : 1 << 20;
-      if (jpend && j <= ml && j <= mr) {
-        cls[k++] = 0;
-        jpend = false;
-      } else if (ml <= mr) {
-        cls[k++] = 1 + (le[il++] >> 8);
-      } else {
-        cls[k++] = roff + (re[ir++] >> 8);
-      }
+      if (ml <= mr) cls[k++] = 1 + (le[il++] >> 8);
+      else cls[k++] = roff + (re[ir++] >> 8);
     }
+    cls[k++] = 0;
     return k;
   } else {
     const int n = a.n;
@@ -483,12 +478,43 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
     const char* cls_b = reinterpret_cast<const char*>(cls);
     const char* Fl = reinterpret_cast<const char*>(Fb + lane);
     auto F_at = [&](uint32_t w) -> CF { return *reinterpret_cast<const CF*>(Fl + ((w & ~511u) >> kFShift)); };
+    // site mode: Gamma entry (alpha, beta, j) of a root state (site multiplicity j)
+    auto emit_site = [&](int j, const CF& v) {
+      const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff;
+      const size_t o = ((size_t)alpha * sd->chi + beta) * sd->d + j;
+      if constexpr (std::is_same<P, PrecSplit>::value) {
+        if (!sd->out_c128) {
+          // epilogue on the FP32 pipe: (hi + lo) * sqrt(j!) * l_scale * r_rowfact as FP32 pairs
+          const float4 q = v;  // (re_h, im_h, re_l, im_l)
+          const float2 js = c_sqrt_fact2[j], ls = sd->l_scale2[beta], rs = sd->r_rowfact2[alpha];
+          float sh, sl, th, tl, re_h, re_l, im_h, im_l;
+          PrecSplit::mul(js.x, js.y, ls.x, ls.y, sh, sl);
+          PrecSplit::mul(sh, sl, rs.x, rs.y, th, tl);
+          PrecSplit::mul(q.x, q.z, th, tl, re_h, re_l);
+          PrecSplit::mul(q.y, q.w, th, tl, im_h, im_l);
+          __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(re_h + re_l, im_h + im_l));
+          return;
+        }
+      }
+      const double2 w = P::to_c128(v);
+      const double scale = c_sqrt_fact[j] * sd->l_scale[beta] * sd->r_rowfact[alpha];
+      if (sd->out_c128) {
+        __stcs(reinterpret_cast<double2*>(sd->gamma) + o, make_double2(w.x * scale, w.y * scale));
+      } else {
+        __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(float(w.x * scale), float(w.y * scale)));
+      }
+    };
     // run the program (the final coefficient stays in a register)
     Fb[lane] = P::one();
     CF fin = P::one();
+    if (MODE == MODE_SITE) {
+      // the empty state is a root only for j = 0 with empty labels
+      const uint32_t tag0 = __ldg(&a.prog.st_pack[so].y) >> 16;
+      if (tag0 && live) emit_site(int(tag0) - 1, fin);
+    }
     for (int s = 1; s < ns; ++s) {
       const uint4 pk = __ldg(a.prog.st_pack + so + s);
-      const int off = int(pk.x), cnt = int(pk.y & 0xffffu), ra = int(pk.y >> 16);
+      const int off = int(pk.x), cnt = int(pk.y & 0xffu), ra = int((pk.y >> 8) & 0xffu);
       const uint32_t ya = uint32_t(cls[pk.w]);
       done += cnt;
       auto A_at = [&](uint32_t w) -> CA {
@@ -534,36 +560,10 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
       }
       fin = P::finish(acc, ra, c_inv_d, c_inv_f);
       Fb[(size_t)pk.z * 32 + lane] = fin;
+      if (MODE == MODE_SITE && (pk.y >> 16) && live) emit_site(int(pk.y >> 16) - 1, fin);
     }
     if (!live) continue;
-    if (MODE == MODE_SITE) {
-      const int alpha = (item >> 20) & 0xfff, beta = (item >> 8) & 0xfff, j = item & 0xff;
-      const size_t o = ((size_t)alpha * sd->chi + beta) * sd->d + j;
-      bool done = false;
-      if constexpr (std::is_same<P, PrecSplit>::value) {
-        if (!sd->out_c128) {
-        // epilogue on the FP32 pipe: (hi + lo) * sqrt(j!) * l_scale * r_rowfact as FP32 pairs
-        const float4 q = fin;  // (re_h, im_h, re_l, im_l)
-        const float2 js = c_sqrt_fact2[j], ls = sd->l_scale2[beta], rs = sd->r_rowfact2[alpha];
-        float sh, sl, th, tl, re_h, re_l, im_h, im_l;
-        PrecSplit::mul(js.x, js.y, ls.x, ls.y, sh, sl);
-        PrecSplit::mul(sh, sl, rs.x, rs.y, th, tl);
-        PrecSplit::mul(q.x, q.z, th, tl, re_h, re_l);
-        PrecSplit::mul(q.y, q.w, th, tl, im_h, im_l);
-        __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(re_h + re_l, im_h + im_l));
-        done = true;
-        }
-      }
-      if (!done) {
-        const double2 v = P::to_c128(fin);
-        const double scale = c_sqrt_fact[j] * sd->l_scale[beta] * sd->r_rowfact[alpha];
-        if (sd->out_c128) {
-          __stcs(reinterpret_cast<double2*>(sd->gamma) + o, make_double2(v.x * scale, v.y * scale));
-        } else {
-          __stcs(reinterpret_cast<float2*>(sd->gamma) + o, make_float2(float(v.x * scale), float(v.y * scale)));
-        }
-      }
-    } else {
+    if (MODE != MODE_SITE) {
       const double2 v = P::to_c128(fin);
       double s = fac;
       if (a.den) s /= a.den[item];
@@ -1240,25 +1240,26 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
     sp.ngr = int(c.gk_r.size());
     c.keys.assign((size_t)d * sp.ngl * sp.ngr, ~0ull);
     c.prog.assign(c.keys.size(), -1);
-    // the program index is only read here (phase B adds to it afterwards)
-    for (int j = 0; j < d; ++j) {
-      const uint64_t kj = key_add_class(0, j);
-      for (int gl = 0; gl < sp.ngl; ++gl) {
-        const int nl = key_order(c.gk_l[gl]);
-        for (int gr = 0; gr < sp.ngr; ++gr) {
-          const int n = j + nl + key_order(c.gk_r[gr]);
-          if (n & 1) continue;
-          if (n > BSG_MAX_ORDER) {
-            c.err = 1;
-            continue;
-          }
-          const size_t o = ((size_t)j * sp.ngl + gl) * sp.ngr + gr;
-          const uint64_t k = kj + c.gk_l[gl] + c.gk_r[gr];
-          c.keys[o] = k;
-          auto it = ps.index.find(k);
-          if (it != ps.index.end()) c.prog[o] = it->second;
-          else c.missing.push_back(k);
+    // One site program per (left group, right group): its roots are the
+    // even orders j + n_l + n_r over j = jmax, jmax - 2, ... >= 0 (jmax the
+    // largest j < d of that parity), and its items carry j = jmax.  The
+    // program index is only read here (phase B adds to it afterwards).
+    for (int gl = 0; gl < sp.ngl; ++gl) {
+      const int nl = key_order(c.gk_l[gl]);
+      for (int gr = 0; gr < sp.ngr; ++gr) {
+        const int nlr = nl + key_order(c.gk_r[gr]);
+        const int jmax = (d - 1) - (((d - 1) + nlr) & 1);
+        if (jmax < 0) continue;  // d = 1 and an odd order: no even hafnian
+        if (jmax + nlr > BSG_MAX_ORDER) {
+          c.err = 1;
+          continue;
         }
+        const size_t o = ((size_t)jmax * sp.ngl + gl) * sp.ngr + gr;
+        const uint64_t k = key_site_roots(c.gk_l[gl] + c.gk_r[gr], jmax);
+        c.keys[o] = k;
+        auto it = ps.index.find(k);
+        if (it != ps.index.end()) c.prog[o] = it->second;
+        else c.missing.push_back(k);
       }
     }
   });

@@ -48,20 +48,25 @@ void set_error(const char* fmt, ...);
 // A "program" lists the reachable states of one multiplicity partition in
 // topological order with their transitions; every item whose target has that
 // multiplicity partition runs the same program, which makes warps uniform.
+// Site programs have several roots: the site mode is the last class, and the
+// hafnians with site multiplicity j = jmax, jmax - 2, ..., (one parity, the
+// Gamma entries (a, b, j) of one row pair) are all states of one program,
+// read out as the program reaches them (F_r does not depend on the root).
 struct ProgramSet {
   // host mirror
   std::vector<uint64_t> keys;          // partition key per program
   std::vector<int32_t> k;              // classes per program
   std::vector<int32_t> nstates;        // states per program (>= 1)
   std::vector<int32_t> state_off;      // first state (global index) per program
-  std::vector<int32_t> mult;           // [prog * BSG_MAX_CLASSES + c] ascending multiplicities
+  std::vector<int32_t> mult;           // [prog * BSG_MAX_CLASSES + c] multiplicities in class order
   // host-only per-state tables (planning, statistics); the device reads st_pack
   std::vector<int32_t> st_trans_off;   // per global state: first transition
   std::vector<int32_t> st_trans_cnt;   // per global state: number of transitions
   std::vector<int32_t> st_ra;          // per global state: r_a (0 for the empty state)
   std::vector<uint32_t> trans;         // packed (src F slot << 9) | (b << 2), b >= the state's class a
   std::vector<int32_t> fslots;         // F table entries per program (two levels of states)
-  std::vector<uint4> st_pack;          // per global state: {first transition, count | r_a << 16, F slot, a}
+  std::vector<uint4> st_pack;          // per global state: {first transition, count | r_a << 8 | (root j + 1) << 16,
+                                       //  F slot, a}; root j + 1 = 0 when the state is not a root
   std::unordered_map<uint64_t, int32_t> index;
   // device copies (valid when dev_valid)
   int32_t* d_k = nullptr;
@@ -82,6 +87,12 @@ constexpr int kKeyMaxMult = 10;
 inline uint64_t key_add_class(uint64_t key, int mult) {
   return mult <= 0 ? key : key + (uint64_t(1) << (kKeyBits * (mult - 1)));
 }
+// Site programs: the multiset X of the label classes plus a last class (the
+// site mode) with roots at multiplicities jmax, jmax - 2, ..., >= 0; the key
+// carries jmax + 1 in its top four bits.
+constexpr int kKeyRootShift = kKeyBits * kKeyMaxMult;
+static_assert(kKeyRootShift + 4 <= 64, "root field");
+inline uint64_t key_site_roots(uint64_t x_key, int jmax) { return x_key | (uint64_t(jmax + 1) << kKeyRootShift); }
 int key_order(uint64_t key);            // sum of multiplicities (hafnian order n)
 int key_classes(uint64_t key);          // number of classes
 

@@ -14,6 +14,7 @@ namespace bsg {
 // the source slot's [32 lanes] row.  Every transition of a state shares its
 // first class a, which the state's pack word carries.
 static_assert(BSG_MAX_CLASSES <= 32, "class byte offsets take bits 2..6 of a transition word");
+static_assert(BSG_MAX_CLASSES < 256 && kKeyMaxMult + 1 < 256, "transition counts and r_a take 8 bits of a pack word");
 static_assert(2 * BSG_MAX_STATES < (1 << 23), "F ring slots take 23 bits of a transition word");
 
 int key_order(uint64_t key) {
@@ -34,27 +35,37 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
     *prog_out = it->second;
     return BSG_OK;
   }
-  if (key >> (kKeyBits * kKeyMaxMult)) {
-    set_error("partition key 0x%llx uses a multiplicity above %d", (unsigned long long)key, kKeyMaxMult);
-    return BSG_ERR_LIMIT;
-  }
+  // site programs: jroot = jmax >= 0 (the site class last, roots at jmax, jmax - 2, ...)
+  const int jroot = int(key >> kKeyRootShift) - 1;
+  const uint64_t xkey = key & ((uint64_t(1) << kKeyRootShift) - 1);
   std::vector<int> mult;
   for (int v = 1; v <= kKeyMaxMult; ++v) {
-    int c = int((key >> (kKeyBits * (v - 1))) & 63);
+    int c = int((xkey >> (kKeyBits * (v - 1))) & 63);
     for (int i = 0; i < c; ++i) mult.push_back(v);
   }
+  if (jroot >= 0) mult.push_back(jroot);
   const int k = int(mult.size());
   if (k > BSG_MAX_CLASSES) {
     set_error("hafnian with %d distinct indices exceeds BSG_MAX_CLASSES=%d", k, BSG_MAX_CLASSES);
     return BSG_ERR_LIMIT;
   }
-  // Enumerate the states reachable from the full multiset.
+  // Enumerate the states reachable from the root(s).
   std::unordered_map<std::string, int> seen;
   std::vector<std::string> states;
   std::vector<std::string> stack;
   std::string full(k, '\0');
   for (int c = 0; c < k; ++c) full[c] = char(mult[c]);
-  stack.push_back(full);
+  std::unordered_map<std::string, int> root_j;  // root state -> its site multiplicity
+  if (jroot >= 0) {
+    for (int j = jroot; j >= 0; j -= 2) {
+      std::string r = full;
+      r[k - 1] = char(j);
+      root_j.emplace(r, j);
+      stack.push_back(r);
+    }
+  } else {
+    stack.push_back(full);
+  }
   while (!stack.empty()) {
     std::string s = std::move(stack.back());
     stack.pop_back();
@@ -63,7 +74,7 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
     states.push_back(s);
     if (int(states.size()) > BSG_MAX_STATES) {
       set_error("partition with %d classes (n=%d) needs more than BSG_MAX_STATES=%d DP states", k,
-                key_order(key), BSG_MAX_STATES);
+                key_order(xkey) + std::max(jroot, 0), BSG_MAX_STATES);
       return BSG_ERR_LIMIT;
     }
     int a = 0;
@@ -137,7 +148,10 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
     }
     ps.st_trans_cnt.push_back(cnt);
     ps.st_ra.push_back(a < k ? int(s[a]) : 0);
-    ps.st_pack.push_back(make_uint4(uint32_t(ps.st_trans_off.back()), uint32_t(cnt) | (uint32_t(a < k ? s[a] : 0) << 16),
+    auto rj = root_j.find(s);
+    const uint32_t tag = rj == root_j.end() ? 0u : uint32_t(rj->second + 1);
+    ps.st_pack.push_back(make_uint4(uint32_t(ps.st_trans_off.back()),
+                                    uint32_t(cnt) | (uint32_t(a < k ? s[a] : 0) << 8) | (tag << 16),
                                     uint32_t(slot[i]), uint32_t(a < k ? a : 0)));
   }
   ps.index.emplace(key, prog);

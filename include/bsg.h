@@ -62,7 +62,7 @@ typedef struct CUstream_st* bsg_stream_t; /* == cudaStream_t */
 /* documented limits */
 #define BSG_MAX_CLASSES 24     /* distinct Sigma indices in one hafnian            */
 #define BSG_MAX_ORDER 63       /* hafnian order n                                   */
-#define BSG_MAX_STATES 16384   /* states of one partition program                   */
+#define BSG_MAX_STATES 65536   /* states of one partition program                   */
 #define BSG_MAX_LABEL_NNZ 32   /* non-zero Fock entries in one Schmidt label row    */
 #define BSG_MAX_DD 16          /* sampler Fock cutoff after displacement (dd)       */
 

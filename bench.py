@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import os
 import statistics
@@ -166,8 +167,9 @@ def link_probe(dev_bufs, host_bufs, reps=2):
 
 def measure_contraction(args, lib, handle, peaks):
     """Bond contraction (amplitudes of all patterns with <= k photons) of a
-    freshly built MPS: split path (3xTF32 tcgen05 GEMMs) timed with CUDA
-    events on its stream, plain FP64 path once for the error."""
+    freshly built FP64 MPS: the sliced tensor-core path (FP64-accurate, the
+    parity path) and the fast approximate 3xTF32 path, each timed with CUDA
+    events on its stream; the plain FP64 CUDA-core path once for the error."""
     import numpy as np
     import torch
 
@@ -231,24 +233,34 @@ def measure_contraction(args, lib, handle, peaks):
     kern_ms = prof["ms"] / max(1, prof["launches"])
     tf32_peak = peaks.get("bf16_tflops")
     achieved = useful / (kern_ms / 1e3) / 1e12
+    bf16_peak = peaks.get("bf16_tflops")
+    sl_kern_ms = prof_sl["ms"] / max(1, prof_sl["launches"])
+    sl_achieved = sl_useful / (sl_kern_ms / 1e3) / 1e12
     return {
         "workload": cfg.label(), "patterns": int(pats.shape[0]), "max_photons": args.contract_photons,
-        "ms": ms, "patterns_per_s": pats.shape[0] / (ms / 1e3), "fp64_ms": t64, "speedup_vs_fp64": t64 / ms,
-        "prob_rel_err_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel))},
-        "sliced": {"ms": sl_ms, "patterns_per_s": pats.shape[0] / (sl_ms / 1e3), "speedup_vs_fp64": t64 / sl_ms,
-                   "prob_rel_err_vs_fp64": {"max": float(rel_sl.max()), "median": float(np.median(rel_sl))},
-                   "useful_tflops": sl_useful / (prof_sl["ms"] / max(1, prof_sl["launches"]) / 1e3) / 1e12,
-                   "note": "complex128 Gamma, FP64 environments; every level's complex GEMM as BF16 fixed-point "
-                           "slice products (tcgen05 kind::f16) summed exactly per slice level in TMEM; useful = 8 "
-                           "flops per complex MAC of the contraction over the contraction's CUDA-event time"},
-        "roofline": {"kernel": "umma_gemm_kernel (3xTF32 tcgen05) + gather/env kernels", "bound": "tensor",
-                     "achieved": achieved, "unit": "TFLOP/s",
-                     "peak": tf32_peak / 2 if tf32_peak else None,
-                     "frac": achieved / (tf32_peak / 2) if tf32_peak else None,
-                     "tensor_issue_frac": 3 * achieved / (tf32_peak / 2) if tf32_peak else None,
-                     "peak_source": "TF32 dense = half the measured cuBLAS bf16 burst rate (nominal ratio)",
-                     "work": "8 real flops per complex MAC of the trie contraction (useful; the 3xTF32 split "
-                             "issues 3 tensor products per useful one)"},
+        "path": "sliced: FP64-accurate tensor-core contraction (the parity path)",
+        "ms": sl_ms, "patterns_per_s": pats.shape[0] / (sl_ms / 1e3), "fp64_ms": t64, "speedup_vs_fp64": t64 / sl_ms,
+        "prob_rel_err_vs_fp64": {"max": float(rel_sl.max()), "median": float(np.median(rel_sl))},
+        "note": "complex128 Gamma, FP64 environments; every level's complex GEMM as BF16 fixed-point slice "
+                "products (tcgen05 kind::f16) summed exactly per slice level in TMEM",
+        "roofline": {"kernel": "sliced_gemm_kernel (BF16 slices, tcgen05) + slicing/env kernels", "bound": "tensor",
+                     "achieved": sl_achieved, "unit": "TFLOP/s", "peak": bf16_peak,
+                     "frac": sl_achieved / bf16_peak if bf16_peak else None,
+                     "peak_source": "measured cuBLAS bf16 burst rate (MEASURED_PEAKS.json)",
+                     "work": "8 real flops per complex MAC of the trie contraction (useful; each is S(S+1)/2 "
+                             "BF16 slice products, 28 at S = 7)"},
+        "tf32x3_fast": {
+            "ms": ms, "patterns_per_s": pats.shape[0] / (ms / 1e3), "speedup_vs_fp64": t64 / ms,
+            "prob_rel_err_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel))},
+            "note": "approximate: complex64 Gamma, 3xTF32 products accumulated in FP32 -- misses the 1e-6 "
+                    "probability tolerance, so it is not the parity path",
+            "roofline": {"kernel": "umma_gemm_kernel (3xTF32 tcgen05) + gather/env kernels", "bound": "tensor",
+                         "achieved": achieved, "unit": "TFLOP/s",
+                         "peak": tf32_peak / 2 if tf32_peak else None,
+                         "frac": achieved / (tf32_peak / 2) if tf32_peak else None,
+                         "peak_source": "TF32 dense = half the measured cuBLAS bf16 burst rate (nominal ratio)",
+                         "work": "8 real flops per complex MAC of the trie contraction (useful; the 3xTF32 split "
+                                 "issues 3 tensor products per useful one)"}},
     }
 
 
@@ -455,6 +467,7 @@ def measure_largest(args, lib, handle):
     # the FP64 build writes its first 32 sites to their own buffers and the
     # rest over the split build's (not compared)
     fp64 = [torch.empty(chi, chi, d, dtype=torch.complex64, device="cuda") for _ in range(n)] + split[n:]
+    timed("fp64", fp64)  # untimed: the FP64 DP kernel loaded, as the split build was warmed above
     ms64, _ = timed("fp64", fp64)
     g_err = [float((split[i] - fp64[i]).abs().max().item() / fp64[i].abs().max().item()) for i in range(n)]
     out = {"workload": cfg.label(), "build_ms": ms, "sites_per_s": M / (ms / 1e3), "fp64_build_ms": ms64,
@@ -579,16 +592,21 @@ def main():
     clocks.start()
     times = []
     stream = torch.cuda.current_stream()
-    for _ in range(args.steps):
-        flush.fill_(1.0)  # evict L2 between steps (outside the timed region)
-        torch.cuda.synchronize()
-        barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1))
+    gc.collect()
+    gc.disable()  # as timeit does: no collector pauses inside the timed steps
+    try:
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # evict L2 between steps (outside the timed region)
+            torch.cuda.synchronize()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            build_mps(sq_dev, d, chi, precision=args.precision, out=outs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    finally:
+        gc.enable()
     clk = clocks.stop()
     lib.bsg_profile_enable(handle.h, 0)
     prof = profile_read(lib, handle.h)
@@ -612,14 +630,19 @@ def main():
         torch.cuda.synchronize()
         link_before = link_probe(outs, host_out)
         et = []
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            barrier()
-            t0 = time.perf_counter()
-            build_mps_host(host_sq, d, chi, host_out, host_lam, precision=args.precision, device_out=outs)
-            torch.cuda.synchronize()
-            et.append(time.perf_counter() - t0)
+        gc.collect()
+        gc.disable()  # as timeit does: no collector pauses inside the timed steps
+        try:
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                barrier()
+                t0 = time.perf_counter()
+                build_mps_host(host_sq, d, chi, host_out, host_lam, precision=args.precision, device_out=outs)
+                torch.cuda.synchronize()
+                et.append(time.perf_counter() - t0)
+        finally:
+            gc.enable()
         es = statistics.mean(et)
         if ws > 1:
             t = torch.tensor([es], device=dev)
@@ -629,24 +652,32 @@ def main():
         d2h = int(sum(o.numel() * 8 for o in host_out) + host_lam.numel() * 8)
         e2e = {"value": ws * M / es, "unit": UNIT, "h2d_bytes_per_step": int(host_sq.numel() * 8),
                "d2h_bytes_per_step": d2h, "ms_per_step": es * 1e3,
-               "step_ms": {"min": min(et) * 1e3, "median": statistics.median(et) * 1e3, "max": max(et) * 1e3},
+               "step_ms": {"min": min(et) * 1e3, "median": statistics.median(et) * 1e3, "max": max(et) * 1e3,
+                           "all": [round(x * 1e3, 2) for x in et]},
                "link_d2h_gbs": {"before": link_before, "after": link_after,
                                 "note": "bare device-to-host copy of the same Gamma bytes into the same pinned "
                                         "buffers (one cudaMemcpyAsync per site), timed just before and after the "
                                         "e2e steps; the e2e floor is max(build, bytes / link rate)"},
                "pinned": "torch pin_memory buffers, one per site, touched by two untimed e2e builds"}
 
-    # plain-FP64 path of the same kernels, one build
+    # plain-FP64 path of the same kernels: one untimed build (its first DP
+    # launch loads the FP64 kernel), then warm builds timed like the split ones
     fp64 = None
     if not args.no_fp64 and args.precision != "fp64":
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
         build_mps(sq_dev, d, chi, precision="fp64", out=outs)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        t64 = e0.elapsed_time(e1)
-        fp64 = {"build_ms": t64, "sites_per_s": M / (t64 / 1e3), "split_speedup": t64 / ms}
+        t64s = []
+        for _ in range(2):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            build_mps(sq_dev, d, chi, precision="fp64", out=outs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t64s.append(e0.elapsed_time(e1))
+        t64 = statistics.mean(t64s)
+        fp64 = {"build_ms": t64, "sites_per_s": M / (t64 / 1e3), "split_speedup": t64 / ms,
+                "note": "mean of 2 warm builds after one untimed build, L2 flushed before each"}
         build_mps(sq_dev, d, chi, precision=args.precision, out=outs)  # restore outputs
 
     # first build on a fresh handle: partition programs generated, scratch

@@ -56,6 +56,115 @@ __device__ __forceinline__ double apply_L(const SigmaJob& jb, int r, int c, cons
 
 // One CTA per call: the whole Sigma construction of one site (the
 // descriptor travels as a kernel parameter, so no host-to-device copy).
+// In-place Gauss-Jordan with partial pivoting on G = [A' | I] (Mr x 2Mr
+// complex, leading dimension n2, global memory): the right half becomes
+// A'^-1 and sh.logdet log|det A'| (*status = 1 on a zero pivot).  A step
+// updates only the columns that can be non-zero in its pivot row -- the
+// columns of A' not yet eliminated and the columns of the inverse already
+// reached by earlier pivots (the original indices of the rows pivoted so
+// far) -- so a step costs Mr x Mr updates, not Mr x 2Mr; the pivot row and
+// the multipliers sit in shared memory and a warp updates one row.  Column
+// col is not written back (it is never read again).
+constexpr int kGJMaxModes = 1024;
+struct GJShared {
+  double2 f[kGJMaxModes];  // multipliers G[r][col] of this step
+  double2 v[kGJMaxModes];  // the scaled pivot row on the active columns
+  int cols[kGJMaxModes];   // the active columns
+  int orig[kGJMaxModes];   // original row of each row position (row swaps)
+  double val[32];
+  int idx[32];
+  double logdet;
+  int piv;
+};
+
+__device__ void gj_inverse(double2* G, int Mr, int n2, int* status, GJShared& sh) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int r = tid; r < Mr; r += nt) sh.orig[r] = r;
+  if (tid == 0) sh.logdet = 0.0;
+  __syncthreads();
+  for (int col = 0; col < Mr; ++col) {
+    double best = -1.0;
+    int bi = col;
+    for (int r = col + tid; r < Mr; r += nt) {
+      const double2 v = G[(size_t)r * n2 + col];
+      const double m = v.x * v.x + v.y * v.y;
+      if (m > best) {
+        best = m;
+        bi = r;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      sh.val[warp] = best;
+      sh.idx[warp] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double b = sh.val[0];
+      int i0 = sh.idx[0];
+      for (int w = 1; w < nw; ++w)
+        if (sh.val[w] > b || (sh.val[w] == b && sh.idx[w] < i0)) {
+          b = sh.val[w];
+          i0 = sh.idx[w];
+        }
+      sh.piv = i0;
+      if (!(b > 0.0)) *status = 1;
+      sh.logdet += 0.5 * log(b > 0.0 ? b : 1e-300);
+      if (i0 != col) {
+        const int t = sh.orig[i0];
+        sh.orig[i0] = sh.orig[col];
+        sh.orig[col] = t;
+      }
+    }
+    __syncthreads();
+    const int p = sh.piv;
+    if (p != col) {
+      for (int c = tid; c < n2; c += nt) {
+        const double2 t = G[(size_t)p * n2 + c];
+        G[(size_t)p * n2 + c] = G[(size_t)col * n2 + c];
+        G[(size_t)col * n2 + c] = t;
+      }
+    }
+    // active columns: A' columns col+1..Mr-1, then the inverse's columns Mr + orig[0..col]
+    const int nleft = Mr - col - 1;
+    for (int q = tid; q < Mr; q += nt) sh.cols[q] = q < nleft ? col + 1 + q : Mr + sh.orig[q - nleft];
+    __syncthreads();
+    const double2 pv = G[(size_t)col * n2 + col];
+    const double den = pv.x * pv.x + pv.y * pv.y;
+    const double2 inv = den > 0.0 ? make_double2(pv.x / den, -pv.y / den) : make_double2(0.0, 0.0);
+    for (int q = tid; q < Mr; q += nt) {
+      double2* cp = G + (size_t)col * n2 + sh.cols[q];
+      const double2 v = *cp;
+      const double2 w = make_double2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
+      *cp = w;
+      sh.v[q] = w;
+    }
+    for (int r = tid; r < Mr; r += nt) sh.f[r] = r == col ? make_double2(0.0, 0.0) : G[(size_t)r * n2 + col];
+    __syncthreads();
+    for (int r = warp; r < Mr; r += nw) {
+      const double2 f = sh.f[r];
+      if (f.x == 0.0 && f.y == 0.0) continue;
+      double2* row = G + (size_t)r * n2;
+      for (int q = lane; q < Mr; q += 32) {
+        const double2 v = sh.v[q];
+        double2* gp = row + sh.cols[q];
+        double2 g = *gp;
+        g.x -= f.x * v.x - f.y * v.y;
+        g.y -= f.x * v.y + f.y * v.x;
+        *gp = g;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob jb) {
   const int Mr = jb.Mr, n2 = 2 * Mr;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -63,10 +172,7 @@ __global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob jb) {
   double* T = P + (size_t)n2 * n2;                       // [n2, n2]
   double2* G = reinterpret_cast<double2*>(T + (size_t)n2 * n2);  // [Mr, 2Mr]  (conj A' | I)
   double2* Bm = G + (size_t)Mr * n2;                     // [Mr, Mr]
-  __shared__ double s_val[32];
-  __shared__ int s_idx[32];
-  __shared__ double s_logdet;
-  __shared__ int s_piv;
+  __shared__ GJShared sh;
 
   // P = L S_r (general) or L sq L^T (first)
   for (int i = tid; i < n2 * n2; i += nt) {
@@ -94,81 +200,8 @@ __global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob jb) {
     G[(size_t)r * n2 + Mr + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
     Bm[i] = make_double2(0.5 * (xx - pp), 0.5 * (px + xp));
   }
-  if (tid == 0) s_logdet = 0.0;
   __syncthreads();
-  // Gauss-Jordan with partial pivoting on G
-  for (int col = 0; col < Mr; ++col) {
-    double best = -1.0;
-    int bi = col;
-    for (int r = col + tid; r < Mr; r += nt) {
-      double2 v = G[(size_t)r * n2 + col];
-      double m = v.x * v.x + v.y * v.y;
-      if (m > best) {
-        best = m;
-        bi = r;
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      double ob = __shfl_down_sync(0xffffffffu, best, o);
-      int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) {
-        best = ob;
-        bi = oi;
-      }
-    }
-    if ((tid & 31) == 0) {
-      s_val[tid >> 5] = best;
-      s_idx[tid >> 5] = bi;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double b = s_val[0];
-      int i0 = s_idx[0];
-      for (int w = 1; w < (nt + 31) / 32; ++w)
-        if (s_val[w] > b || (s_val[w] == b && s_idx[w] < i0)) {
-          b = s_val[w];
-          i0 = s_idx[w];
-        }
-      s_piv = i0;
-      if (!(b > 0.0)) *jb.status = 1;
-      s_logdet += 0.5 * log(b > 0.0 ? b : 1e-300);
-    }
-    __syncthreads();
-    const int p = s_piv;
-    if (p != col) {
-      for (int c = tid; c < n2; c += nt) {
-        double2 t = G[(size_t)p * n2 + c];
-        G[(size_t)p * n2 + c] = G[(size_t)col * n2 + c];
-        G[(size_t)col * n2 + c] = t;
-      }
-    }
-    __syncthreads();
-    const double2 pv = G[(size_t)col * n2 + col];
-    const double den = pv.x * pv.x + pv.y * pv.y;
-    const double2 inv = den > 0.0 ? make_double2(pv.x / den, -pv.y / den) : make_double2(0.0, 0.0);
-    __syncthreads();
-    for (int c = tid; c < n2; c += nt) {
-      double2 v = G[(size_t)col * n2 + c];
-      G[(size_t)col * n2 + c] = make_double2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
-    }
-    __syncthreads();
-    for (int i = tid; i < Mr * n2; i += nt) {
-      int r = i / n2, c = i % n2;
-      if (r == col) continue;
-      double2 f = G[(size_t)r * n2 + col];
-      if (f.x == 0.0 && f.y == 0.0) continue;
-      if (c == col) continue;
-      double2 v = G[(size_t)col * n2 + c];
-      double2 g = G[i];
-      g.x -= f.x * v.x - f.y * v.y;
-      g.y -= f.x * v.y + f.y * v.x;
-      G[i] = g;
-    }
-    __syncthreads();
-    for (int r = tid; r < Mr; r += nt)
-      if (r != col) G[(size_t)r * n2 + col] = make_double2(0.0, 0.0);
-    __syncthreads();
-  }
+  gj_inverse(G, Mr, n2, jb.status, sh);
   // X = right half of G
   auto X = [&](int r, int c) { return G[(size_t)r * n2 + Mr + c]; };
   for (int i = tid; i < Mr * Mr; i += nt) {
@@ -197,7 +230,7 @@ __global__ void __launch_bounds__(1024) sigma_kernel(const SigmaJob jb) {
     }
   }
   if (tid == 0) {
-    double ld = s_logdet;  // log|det A'|
+    double ld = sh.logdet;  // log|det A'|
     *jb.Z = jb.first ? exp(0.25 * (ld - Mr * log(2.0))) : exp(0.5 * ld);
   }
 }
@@ -307,10 +340,7 @@ __global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restri
   double* P = jb.ws;
   double2* G = reinterpret_cast<double2*>(jb.ws + 2 * (size_t)n2 * n2);
   double2* Bm = G + (size_t)Mr * n2;
-  __shared__ double s_val[32];
-  __shared__ int s_idx[32];
-  __shared__ double s_logdet;
-  __shared__ int s_piv;
+  __shared__ GJShared sh;
   for (int i = tid; i < Mr * Mr; i += nt) {
     int r = i / Mr, c = i % Mr;
     double xx = P[(size_t)r * n2 + c], xp = P[(size_t)r * n2 + Mr + c];
@@ -321,80 +351,8 @@ __global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restri
     G[(size_t)r * n2 + Mr + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
     Bm[i] = make_double2(0.5 * (xx - pp), 0.5 * (px + xp));
   }
-  if (tid == 0) s_logdet = 0.0;
   __syncthreads();
-  for (int col = 0; col < Mr; ++col) {
-    double best = -1.0;
-    int bi = col;
-    for (int r = col + tid; r < Mr; r += nt) {
-      double2 v = G[(size_t)r * n2 + col];
-      double m = v.x * v.x + v.y * v.y;
-      if (m > best) {
-        best = m;
-        bi = r;
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      double ob = __shfl_down_sync(0xffffffffu, best, o);
-      int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) {
-        best = ob;
-        bi = oi;
-      }
-    }
-    if ((tid & 31) == 0) {
-      s_val[tid >> 5] = best;
-      s_idx[tid >> 5] = bi;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double b = s_val[0];
-      int i0 = s_idx[0];
-      for (int w = 1; w < (nt + 31) / 32; ++w)
-        if (s_val[w] > b || (s_val[w] == b && s_idx[w] < i0)) {
-          b = s_val[w];
-          i0 = s_idx[w];
-        }
-      s_piv = i0;
-      if (!(b > 0.0)) *jb.status = 1;
-      s_logdet += 0.5 * log(b > 0.0 ? b : 1e-300);
-    }
-    __syncthreads();
-    const int p = s_piv;
-    if (p != col) {
-      for (int c = tid; c < n2; c += nt) {
-        double2 t = G[(size_t)p * n2 + c];
-        G[(size_t)p * n2 + c] = G[(size_t)col * n2 + c];
-        G[(size_t)col * n2 + c] = t;
-      }
-    }
-    __syncthreads();
-    const double2 pv = G[(size_t)col * n2 + col];
-    const double den = pv.x * pv.x + pv.y * pv.y;
-    const double2 inv = den > 0.0 ? make_double2(pv.x / den, -pv.y / den) : make_double2(0.0, 0.0);
-    __syncthreads();
-    for (int c = tid; c < n2; c += nt) {
-      double2 v = G[(size_t)col * n2 + c];
-      G[(size_t)col * n2 + c] = make_double2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
-    }
-    __syncthreads();
-    for (int i = tid; i < Mr * n2; i += nt) {
-      int r = i / n2, c = i % n2;
-      if (r == col) continue;
-      double2 f = G[(size_t)r * n2 + col];
-      if (f.x == 0.0 && f.y == 0.0) continue;
-      if (c == col) continue;
-      double2 v = G[(size_t)col * n2 + c];
-      double2 g = G[i];
-      g.x -= f.x * v.x - f.y * v.y;
-      g.y -= f.x * v.y + f.y * v.x;
-      G[i] = g;
-    }
-    __syncthreads();
-    for (int r = tid; r < Mr; r += nt)
-      if (r != col) G[(size_t)r * n2 + col] = make_double2(0.0, 0.0);
-    __syncthreads();
-  }
+  gj_inverse(G, Mr, n2, jb.status, sh);
   for (int i = tid; i < Mr * Mr; i += nt) {
     const int r = i / Mr, c = i % Mr;
     if (jb.first) {
@@ -407,7 +365,7 @@ __global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restri
     }
   }
   if (tid == 0) {
-    double ld = s_logdet;  // log|det A'|
+    double ld = sh.logdet;  // log|det A'|
     *jb.Z = jb.first ? exp(0.25 * (ld - Mr * log(2.0))) : exp(0.5 * ld);
   }
 }

@@ -795,7 +795,7 @@ def main():
             "data": "synthetic (seeded lossy GBS covariance; independent instance per rank)",
             "config": {"workload": cfg.label(), "M": M, "d": d, "chi": chi, "precision": args.precision,
                        "gamma_dtype": "complex64", "l2": "flushed between steps (512 MiB write)"},
-            "clocks": clk, "gpu_launches": launches, "kernels": {k: {"ms": v["ms"], "launches": v["launches"]}
+            "step_ms_all": [round(t, 2) for t in times], "clocks": clk, "gpu_launches": launches, "kernels": {k: {"ms": v["ms"], "launches": v["launches"]}
                                                                  for k, v in prof.items()},
             "host": {k: {"ms": v["ms"], "calls": v["launches"]} for k, v in host_prof.items()},
             "roofline": roof, "fp64_path": fp64, "cold_build": cold, "e2e": e2e, "cpu_baseline": cpu, "contraction": contraction, "sampler": sampler,

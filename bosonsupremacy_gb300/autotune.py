@@ -35,6 +35,7 @@ KNOBS = {
     "factor_threads": _lib.TUNE_FACTOR_THREADS,
     "gemm_kernel": _lib.TUNE_GEMM_KERNEL,
     "dp_quantum": _lib.TUNE_DP_QUANTUM,
+    "dp_hold": _lib.TUNE_DP_HOLD,
 }
 
 

@@ -159,10 +159,171 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
   return -1;
 }
 
+// ---- double-float products for the eigenvector refinement ------------------
+// GB300's FP64 pipe runs ~1/73 of the FP32 rate, so the refinement's m x m
+// products run as double-float arithmetic on the FP32 pipe: each FP64
+// operand is split into an FP32 pair (hi + lo), each product term is formed
+// with an exact FP32 product error (fma) plus the cross terms, and the sum
+// is kept as an FP32 sum s with its exact rounding errors collected in t
+// (Dekker / Knuth two-sum).  A term carries ~2^-48 relative error, a sum of
+// m terms ~2^-48 sqrt(m) of sum |a b| -- ~1e-14 of the norm here, far below
+// what the refinement needs to stop (corrections <= 1e-8, clustered
+// numerators <= 1e-12 of the norm).
+constexpr int kDfTile = 32;
+constexpr size_t kDfSmemBytes = 2 * kDfTile * (kDfTile + 1) * sizeof(float2);
+
+// x = hi + lo from the IEEE bits on the integer pipe (FP64 conversions and
+// subtractions run on the narrow FP64 pipe): hi keeps the top 24 bits of the
+// significand (truncated), lo the next 29 rounded to 24, so hi + lo carries
+// ~48 bits; a lo below FP32's normal range (|x| < 2^-75) is dropped, and x
+// outside FP32's exponent range falls back to the FP64 split.
+__device__ __forceinline__ float2 df_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
+  const int e = int((hw >> 20) & 0x7ffu);  // biased double exponent
+  if (e == 0) return make_float2(0.f, 0.f);  // zero (or a double subnormal)
+  const int fe = e - 1023 + 127;
+  if (fe <= 0 || fe >= 255) {
+    const float h = float(x);
+    return make_float2(h, float(x - double(h)));
+  }
+  const unsigned sign = hw & 0x80000000u;
+  const float h = __uint_as_float(sign | (unsigned(fe) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  // the remaining 29 significand bits are r * 2^(e - 1023 - 52)
+  const int pe = e - 1075 + 127;
+  float l = 0.f;
+  if (pe > 0) l = __uint2float_rn(lw & 0x1fffffffu) * __uint_as_float(unsigned(pe) << 23);
+  return make_float2(h, sign ? -l : l);
+}
+
+// (s, t) += a b
+__device__ __forceinline__ void df_mac(float& s, float& t, float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float u = s + p;
+  const float bb = u - s;
+  t += e + ((s - (u - bb)) + (p - bb));
+  s = u;
+}
+
+// C[i][j] = add[i][j] + sign * sum_q A(i, q) B(q, j) (+ diag where i == j),
+// all m x m row-major, A(i, q) = ta ? A[q][i] : A[i][q], B(q, j) = tb ? B[j][q]
+// : B[q][j].  sym: the result is symmetric -- only tiles on or above the
+// diagonal are computed and mirrored.  C must not alias A, B or add unless
+// add == C (each entry of C is read before it is written, by the same
+// thread).  tiles: kDfSmemBytes of shared memory.  Block-wide (barriers).
+// PER: outputs per thread (1024, 512 or 256 threads)
+template <int PER>
+__device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B, bool tb, const double* add,
+                                       double sign, double diag, double* C, int m, bool sym, float2* tiles) {
+  float2 (*As)[kDfTile + 1] = reinterpret_cast<float2 (*)[kDfTile + 1]>(tiles);
+  float2 (*Bs)[kDfTile + 1] = reinterpret_cast<float2 (*)[kDfTile + 1]>(tiles + kDfTile * (kDfTile + 1));
+  const int tid = threadIdx.x, nt = blockDim.x;
+  constexpr int kOut = kDfTile * kDfTile;
+  const int nb = (m + kDfTile - 1) / kDfTile;
+  // element e of a tile: consecutive threads read consecutive addresses
+  // (the row index runs fastest for a transposed operand)
+  auto rc = [](bool tr, int e, int& r, int& c) {
+    if (tr) {
+      r = e % kDfTile;
+      c = e / kDfTile;
+    } else {
+      r = e / kDfTile;
+      c = e % kDfTile;
+    }
+  };
+  auto a_val = [&](int ti, int q0, int e) {
+    int r, c;
+    rc(ta, e, r, c);
+    const int ai = ti * kDfTile + r, aq = q0 + c;
+    if (ai >= m || aq >= m) return 0.0;
+    return ta ? A[(size_t)aq * m + ai] : A[(size_t)ai * m + aq];
+  };
+  auto b_val = [&](int tj, int q0, int e) {
+    int r, c;
+    rc(tb, e, r, c);
+    const int bq = q0 + r, bj = tj * kDfTile + c;
+    if (bq >= m || bj >= m) return 0.0;
+    return tb ? B[(size_t)bj * m + bq] : B[(size_t)bq * m + bj];
+  };
+  for (int ti = 0; ti < nb; ++ti)
+    for (int tj = sym ? ti : 0; tj < nb; ++tj) {
+      float s[PER], t[PER];
+#pragma unroll
+      for (int o = 0; o < PER; ++o) s[o] = t[o] = 0.f;
+      // the K chunk q0 is in registers while chunk q0 - 32 is multiplied
+      double pa[PER], pb[PER];
+#pragma unroll
+      for (int o = 0; o < PER; ++o) {
+        const int e = tid + o * nt;
+        pa[o] = (e < kOut) ? a_val(ti, 0, e) : 0.0;
+        pb[o] = (e < kOut) ? b_val(tj, 0, e) : 0.0;
+      }
+      for (int q0 = 0; q0 < m; q0 += kDfTile) {
+#pragma unroll
+        for (int o = 0; o < PER; ++o) {
+          const int e = tid + o * nt;
+          if (e < kOut) {
+            int r, cc;
+            rc(ta, e, r, cc);
+            As[r][cc] = df_split(pa[o]);
+            rc(tb, e, r, cc);
+            Bs[r][cc] = df_split(pb[o]);
+          }
+        }
+        __syncthreads();
+        if (q0 + kDfTile < m) {
+#pragma unroll
+          for (int o = 0; o < PER; ++o) {
+            const int e = tid + o * nt;
+            if (e < kOut) {
+              pa[o] = a_val(ti, q0 + kDfTile, e);
+              pb[o] = b_val(tj, q0 + kDfTile, e);
+            }
+          }
+        }
+#pragma unroll
+        for (int o = 0; o < PER; ++o) {
+          const int e = tid + o * nt;
+          if (e < kOut) {
+            const int r = e / kDfTile, c = e % kDfTile;
+#pragma unroll 8
+            for (int q = 0; q < kDfTile; ++q) df_mac(s[o], t[o], As[r][q], Bs[q][c]);
+          }
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int o = 0; o < PER; ++o) {
+        const int e = tid + o * nt;
+        if (e >= kOut) continue;
+        const int i = ti * kDfTile + e / kDfTile, j = tj * kDfTile + e % kDfTile;
+        if (i >= m || j >= m) continue;
+        double v = sign * (double(s[o]) + double(t[o]));
+        if (add) v += add[(size_t)i * m + j];
+        if (i == j) v += diag;
+        C[(size_t)i * m + j] = v;
+        // off-diagonal tiles are mirrored; a diagonal tile computes both halves itself
+        if (sym && tj != ti) C[(size_t)j * m + i] = v;
+      }
+    }
+  __syncthreads();
+}
+
+__device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, const double* add, double sign,
+                        double diag, double* C, int m, bool sym, float2* tiles) {
+  if (blockDim.x >= 1024) df_gemm_t<1>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  else if (blockDim.x >= 512) df_gemm_t<2>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  else df_gemm_t<4>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+}
+
 // Mixed-precision symmetric eigen-decomposition of the m x m matrix Hm with
 // eigenvector rows in QT: FP32 Jacobi sweeps on a rounded copy (the FP32
 // pipe is ~64x the FP64 one on GB300) until the off-diagonal is ~1e-5 of the
-// diagonal, then FP64 iterative refinement by matrix products only (Ogita &
+// diagonal, then iterative refinement by matrix products only -- double-float
+// products on the FP32 pipe (df_gemm), FP64 everywhere else (Ogita &
 // Aishima, "Iterative refinement for symmetric eigenvalue decomposition",
 // Japan J. Indust. Appl. Math. 35 (2018)).  With X the eigenvector columns
 // (X = QT^T):
@@ -176,21 +337,9 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
 // eigenvalues (the rest of Hm is overwritten).  s1, s2, s3: m*m doubles of
 // scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
 // the start tolerance of the refinement.
-// (i, j), i <= j, of entry p of an m x m upper triangle stored row by row
-// (row r holds m - r entries and starts at r m - r (r - 1) / 2)
-__device__ __forceinline__ void upper_index(int64_t p, int m, int& i, int& j) {
-  const double b = 2.0 * m + 1.0;
-  int r = int((b - sqrt(b * b - 8.0 * (double)p)) * 0.5);
-  auto start = [m](int64_t q) { return q * m - q * (q - 1) / 2; };
-  r = max(0, min(r, m - 1));
-  while (r > 0 && start(r) > p) --r;
-  while (r + 1 < m && start(r + 1) <= p) ++r;
-  i = r;
-  j = r + int(p - start(r));
-}
-
 __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
-                            double* cs, double* sn, int* pos, float* jsm, unsigned long long* sweep_log) {
+                            double* cs, double* sn, int* pos, float* jsm, float2* dft,
+                            unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t mm = (size_t)m * m;
   // the FP32 copies: in shared memory when the launch reserved room for them
@@ -224,39 +373,14 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
   // (relative gaps ~1e-6, near-vacuum modes of middle cuts) by a few percent,
   // which three fixed steps left at ~1e-6.
   constexpr int kRefineMax = 8;
-  const size_t tri = (size_t)m * (m + 1) / 2;  // entries of an upper triangle (diagonal included)
   int refined = 0;
   bool converged = false;
   for (int it = 0; it < kRefineMax; ++it) {
-    // s2 = T = Hm QT^T (all m^2 entries) and s1 = R = I - QT QT^T (symmetric:
-    // its upper triangle, mirrored), one pass over both index sets
-    for (size_t t = tid; t < mm + tri; t += nt) {
-      if (t < mm) {
-        const int i = int(t / m), j = int(t % m);
-        double h = 0.0;
-        for (int q = 0; q < m; ++q) h = fma(Hm[(size_t)i * m + q], QT[(size_t)j * m + q], h);
-        s2[t] = h;
-      } else {
-        int i, j;
-        upper_index(int64_t(t - mm), m, i, j);
-        double r = 0.0;
-        for (int q = 0; q < m; ++q) r = fma(QT[(size_t)i * m + q], QT[(size_t)j * m + q], r);
-        r = (i == j ? 1.0 : 0.0) - r;
-        s1[(size_t)i * m + j] = r;
-        s1[(size_t)j * m + i] = r;
-      }
-    }
-    __syncthreads();
-    // s3 = S = QT T = QT Hm QT^T (symmetric: its upper triangle, mirrored)
-    for (size_t t = tid; t < tri; t += nt) {
-      int i, j;
-      upper_index(int64_t(t), m, i, j);
-      double acc = 0.0;
-      for (int q = 0; q < m; ++q) acc = fma(QT[(size_t)i * m + q], s2[(size_t)q * m + j], acc);
-      s3[(size_t)i * m + j] = acc;
-      s3[(size_t)j * m + i] = acc;
-    }
-    __syncthreads();
+    // s2 = T = Hm QT^T, s1 = R = I - QT QT^T, s3 = S = QT T = QT Hm QT^T
+    // (double-float products on the FP32 pipe; R and S symmetric)
+    df_gemm(Hm, false, QT, true, nullptr, 1.0, 0.0, s2, m, false, dft);
+    df_gemm(QT, false, QT, true, nullptr, -1.0, 1.0, s1, m, true, dft);
+    df_gemm(QT, false, s2, false, nullptr, 1.0, 0.0, s3, m, true, dft);
     for (int i = tid; i < m; i += nt) lam[i] = s3[(size_t)i * m + i] / (1.0 - s1[(size_t)i * m + i]);
     __syncthreads();
     double so = 0.0, rr = 0.0;
@@ -286,13 +410,7 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     emax = block_max(emax, red);
     cnum = block_max(cnum, red);
     // s2 = QT + E^T QT, then QT = s2
-    for (size_t t = tid; t < mm; t += nt) {
-      const int i = int(t / m), j = int(t % m);
-      double acc = QT[t];
-      for (int q = 0; q < m; ++q) acc = fma(s1[(size_t)q * m + i], QT[(size_t)q * m + j], acc);
-      s2[t] = acc;
-    }
-    __syncthreads();
+    df_gemm(s1, true, QT, false, QT, 1.0, 0.0, s2, m, false, dft);
     for (size_t t = tid; t < mm; t += nt) QT[t] = s2[t];
     __syncthreads();
     refined = it + 1;
@@ -394,8 +512,10 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n (also Householder taus)
   double* vec = dots + 2 * kMaxCutModes;                               // n
   double* vec2 = vec + 2 * kMaxCutModes;                               // n
-  // FP32 Jacobi matrices (2 m^2 floats) when the launch reserved them
-  float* jsm = a.jac_smem_m > 0 ? reinterpret_cast<float*>(vec2 + 2 * kMaxCutModes) : nullptr;
+  // double-float product tiles, then the FP32 Jacobi matrices (2 m^2 floats)
+  // when the launch reserved them
+  float2* dft = reinterpret_cast<float2*>(vec2 + 2 * kMaxCutModes);
+  float* jsm = a.jac_smem_m > 0 ? reinterpret_cast<float*>(reinterpret_cast<char*>(dft) + kDfSmemBytes) : nullptr;
   __shared__ int s_flag;
   __shared__ double s_scalar;
 
@@ -463,7 +583,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     }
     __syncthreads();
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm,
+    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
@@ -563,7 +683,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     __syncthreads();
     // Gm is free in this path (G is applied through W = L^{-1}, which the pairing still needs)
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos, jsm,
+    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos, jsm, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
@@ -1067,7 +1187,7 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
   if (c1 <= c0) return BSG_OK;
   CutArgs a = args;
   a.c0 = c0;
-  size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
+  size_t wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8 + kDfSmemBytes;
   // eigen-problem size of cut c: 2 min(L, k) (full path m = 2k, low-rank path m = 2L)
   int m_max = 0;
   for (int c = c0; c < c1; ++c) {
@@ -1091,7 +1211,7 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
 // Dynamic shared memory of a Williamson launch whose largest eigen-problem
 // is m_max (the FP32 Jacobi matrices in shared memory when they fit).
 static int williamson_smem(bsg_handle_t h, int m_max, size_t* wsm, int* jac_m) {
-  *wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8;
+  *wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8 + kDfSmemBytes;
   int smem_optin = 0;
   BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
   const size_t jac = (size_t)2 * m_max * m_max * sizeof(float);
@@ -1196,7 +1316,7 @@ int cut_queue_status(const CutArgs& a, int c0, int c1, int* hst, cudaStream_t st
 // Decodes the status of cuts [c0, c1) and adds their Williamson FMA count
 // to the profiler.
 int cut_check_status(bsg_handle_t h, const CutArgs& a, int c0, int c1, const int* status) {
-  const int M = a.M, L0 = a.L0, n_cuts = a.n_cuts;
+  const int M = a.M, L0 = a.L0;
   // FP64 FMAs of the Williamson step: Cholesky n^3/3, L^-1 n^3/6, G n^3,
   // pairing ~n^3 (G x per pair, projections), S n^3/2; full path: H n^3 and
   // 12 n^3 for three refinement steps of the eigen-decomposition (its Jacobi

@@ -1140,21 +1140,22 @@ class PlanPool {
     for (auto& x : th_) x.join();
   }
   std::mutex run_mutex;
-  // runs f(0..n-1) on the workers and the calling thread; returns when all are done
+  // Runs f(0..n-1) on the workers and the calling thread; returns when every
+  // index is done.  It waits only for the workers that took the job: one that
+  // wakes late (descheduled on a busy host) finds the job withdrawn and skips it.
   void run(int n, const std::function<void(int)>& f) {
     {
       std::lock_guard<std::mutex> g(m_);
       job_ = &f;
       n_ = n;
       next_.store(0);
-      busy_ = int(th_.size());
       ++gen_;
     }
     cv_.notify_all();
     for (int i = next_++; i < n; i = next_++) f(i);
     std::unique_lock<std::mutex> g(m_);
-    done_cv_.wait(g, [this] { return busy_ == 0; });
-    job_ = nullptr;
+    job_ = nullptr;  // no worker takes it from now on
+    done_cv_.wait(g, [this] { return active_ == 0; });
   }
 
  private:
@@ -1170,17 +1171,19 @@ class PlanPool {
         seen = gen_;
         job = job_;
         n = n_;
+        if (!job) continue;  // already finished by the others
+        ++active_;
       }
       for (int i = next_++; i < n; i = next_++) (*job)(i);
       std::lock_guard<std::mutex> g(m_);
-      if (--busy_ == 0) done_cv_.notify_one();
+      if (--active_ == 0) done_cv_.notify_one();
     }
   }
   std::vector<std::thread> th_;
   std::mutex m_;
   std::condition_variable cv_, done_cv_;
   const std::function<void(int)>* job_ = nullptr;
-  int n_ = 0, busy_ = 0;
+  int n_ = 0, active_ = 0;
   uint64_t gen_ = 0;
   bool stop_ = false;
   std::atomic<int> next_{0};
@@ -1870,7 +1873,8 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // host (one event per group), then its Sigma; the middle group's labels and
   // Sigma also read the edge groups' boundary cuts
   const int ng = int(groups.size());
-  // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[4..9] = final joins,
+  // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[3] = the left group's
+  // Williamson done (BSG_TUNE_DP_HOLD), h->ev[4..9] = final joins,
   // h->ev[10..12] = Gammas final (pinned copies), h->ev[13..14] = copy-stream joins,
   // h->ev[16 + 3 g + q] (q < 3) = site part q of group g final (host outputs)
   cudaEvent_t ev_keys[3] = {}, ev_done[3] = {};
@@ -1893,6 +1897,7 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
     const int nc_g = G.c1 - G.c0;
     BSG_TRY(cut_launch_williamson(h, cuts, G.c0, G.c1, s2));
     if (tl0) BSG_CUDA(cudaEventRecord(tl[g][0], s2));
+    if (ng == 3 && g == 1 && h->tune[BSG_TUNE_DP_HOLD]) BSG_CUDA(cudaEventRecord(h->ev[3], s2));
     BSG_TRY(cut_launch_thermal(h, cuts, G.c0, G.c1, s2));
     BSG_TRY(cut_queue_status(cuts, G.c0, G.c1, hcut, s2));
     if (nc_g > 0) {
@@ -1991,6 +1996,9 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
       // the group's DP waits for its Sigma (and labels) on the group stream
       cudaError_t e = cudaEventRecord(ev_done[g], G.stream);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(G.dp_stream, ev_done[g], 0);
+      // the right group's DP held until the left group's Williamson is done
+      if (e == cudaSuccess && ng == 3 && g == 0 && h->tune[BSG_TUNE_DP_HOLD])
+        e = cudaStreamWaitEvent(G.dp_stream, h->ev[3], 0);
       if (e != cudaSuccess) {
         set_error("bsg_build_mps: %s", cudaGetErrorString(e));
         rc = BSG_ERR_CUDA;

@@ -386,7 +386,11 @@ int bsg_potrf_f64(bsg_handle_t h, double* A, int n, int* info, bsg_stream_t stre
 #define BSG_TUNE_DP_QUANTUM 8        /* hafnian DP: a warp leaves its launch after this many x 256 program
                                         transitions, so kernels on higher-priority streams get SMs; 0 keeps
                                         every DP block until the queue is empty (default 2) */
-#define BSG_TUNE_COUNT 9
+#define BSG_TUNE_DP_HOLD 9           /* pipelined build: 1 = the right group's DP waits until the left group's
+                                        Williamson kernel is done (the left group's factorisations, the
+                                        build's critical path, then run without the DP's memory traffic
+                                        beside them), 0 = it starts with its Sigma (default 0) */
+#define BSG_TUNE_COUNT 10
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

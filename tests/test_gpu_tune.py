@@ -42,7 +42,8 @@ def test_launch_split_bit_identical(cuda, golden, prec):
         for knobs in ({"small_entries": 0, "blocks_per_sm": 4, "dp_quantum": 0},
                       {"small_entries": 16, "small_blocks": 2, "scratch_mib": 64, "dp_quantum": 64},
                       {"small_entries": 4096, "small_blocks": 8, "dp_quantum": 1},
-                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 1 << 20}):
+                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 1 << 20},
+                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 2, "dp_hold": 1}):
             autotune.set_knobs(**knobs)
             mps = build_mps(t["sq_cov"], d, chi, precision=prec, out_dtype=torch.complex128)
             outs.append([g.cpu().numpy() for g in mps.Gammas])

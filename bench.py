@@ -32,10 +32,10 @@ if REPO not in sys.path:
 METRIC = "full-MPS build throughput (sites/s), split-precision batched kernels"
 UNIT = "sites/s"
 # DRAM bytes (read + write) per complex multiply-add of the split hafnian DP,
-# from the ncu capture of the M=50, d=6, chi=256 build's DP launches (725 MB
-# for 3.182e8 multiply-adds, profiles/dp_kernel_traffic_M50_d6_chi256.md),
+# from the ncu capture of the M=50, d=6, chi=256 build's DP launches (1001 MB
+# for 2.66e8 multiply-adds, profiles/dp_kernel_traffic_M50_d6_chi256.md),
 # scaled to each launch's work.
-DP_DRAM_BYTES_PER_CMAC = 725e6 / 3.182e8
+DP_DRAM_BYTES_PER_CMAC = 1001e6 / 2.66e8
 
 
 def parse():

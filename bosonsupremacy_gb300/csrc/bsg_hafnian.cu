@@ -218,8 +218,9 @@ struct SitePlanDev {
   const int32_t* grp_l;      // sorted position -> left key group
   const int32_t* perm_r;
   const int32_t* grp_r;
-  const int32_t* bucket_of;  // [d][ngl][ngr] -> global bucket or -1 (odd order)
-  const int32_t* combo_off;  // [d][ngl][ngr] -> first slot of the combination inside its bucket
+  const int32_t* bucket_of;  // [ngl][ngr] -> global bucket or -1 (no even order)
+  const int32_t* combo_off;  // [ngl][ngr] -> first slot of the combination inside its bucket
+  const int8_t* combo_j;     // [ngl][ngr] -> the site multiplicity jmax its items carry
   const int32_t* gstart_l;   // [ngl] sorted position of the group's first row
   const int32_t* gcnt_l;     // [ngl] rows of the group
   const int32_t* gstart_r;   // [ngr]
@@ -229,8 +230,8 @@ struct SitePlanDev {
 };
 
 // One launch per set of sites (blockIdx.y = site).  A thread takes one (right
-// row, left row) pair in key-sorted order and writes its even-order items
-// over j, so the row lookups happen once per pair.
+// row, left row) pair in key-sorted order and writes its item: one multi-root
+// program per pair evaluates every Gamma entry j of the pair's parity.
 __global__ void site_scatter_kernel(const SitePlanDev* __restrict__ plans) {
   const SitePlanDev p = plans[blockIdx.y];
   const int64_t total = (int64_t)p.kr * p.kl;
@@ -240,11 +241,9 @@ __global__ void site_scatter_kernel(const SitePlanDev* __restrict__ plans) {
     const int gl = p.grp_l[bs], gr = p.grp_r[as];
     const int32_t within = (as - p.gstart_r[gr]) * p.gcnt_l[gl] + (bs - p.gstart_l[gl]);
     const int32_t ab = (p.perm_r[as] << 20) | (p.perm_l[bs] << 8);
-    for (int j = 0; j < p.d; ++j) {
-      const size_t o = ((size_t)j * p.ngl + gl) * p.ngr + gr;
-      const int bucket = p.bucket_of[o];
-      if (bucket >= 0) p.items[p.bucket_off[bucket] + p.combo_off[o] + within] = ab | j;
-    }
+    const size_t o = (size_t)gl * p.ngr + gr;
+    const int bucket = p.bucket_of[o];
+    if (bucket >= 0) p.items[p.bucket_off[bucket] + p.combo_off[o] + within] = ab | int(p.combo_j[o]);
   }
 }
 
@@ -844,6 +843,7 @@ static int layout_buckets(const bsg::ProgramSet& ps, int small_entries, Buckets&
 struct SitePlanHost {
   int KL = 0, KR = 0, ngl = 0, ngr = 0, d = 0;
   std::vector<int32_t> perm_l, grp_l, perm_r, grp_r, bucket_of, combo_off, gstart_l, gcnt_l, gstart_r;
+  std::vector<int8_t> combo_j;
 };
 
 static void group_rows(const uint64_t* key, int rows, std::vector<int32_t>& perm, std::vector<int32_t>& grp,
@@ -1241,7 +1241,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
     group_rows(kr[s], KR[s], sp.perm_r, sp.grp_r, c.gk_r, c.gc_r);
     sp.ngl = int(c.gk_l.size());
     sp.ngr = int(c.gk_r.size());
-    c.keys.assign((size_t)d * sp.ngl * sp.ngr, ~0ull);
+    c.keys.assign((size_t)sp.ngl * sp.ngr, ~0ull);
     c.prog.assign(c.keys.size(), -1);
     // One site program per (left group, right group): its roots are the
     // even orders j + n_l + n_r over j = jmax, jmax - 2, ... >= 0 (jmax the
@@ -1257,7 +1257,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
           c.err = 1;
           continue;
         }
-        const size_t o = ((size_t)jmax * sp.ngl + gl) * sp.ngr + gr;
+        const size_t o = (size_t)gl * sp.ngr + gr;
         const uint64_t k = key_site_roots(c.gk_l[gl] + c.gk_r[gr], jmax);
         c.keys[o] = k;
         auto it = ps.index.find(k);
@@ -1288,6 +1288,7 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
     std::unordered_map<int32_t, int32_t> local;
     sp.bucket_of.assign(c.keys.size(), -1);
     sp.combo_off.assign(c.keys.size(), 0);
+    sp.combo_j.assign(c.keys.size(), 0);
     sp.gstart_l.assign(sp.ngl, 0);
     sp.gcnt_l.assign(sp.ngl, 0);
     sp.gstart_r.assign(sp.ngr, 0);
@@ -1296,27 +1297,27 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
       sp.gcnt_l[g] = int32_t(c.gc_l[g]);
     }
     for (int g = 0, at = 0; g < sp.ngr; at += int(c.gc_r[g]), ++g) sp.gstart_r[g] = at;
-    for (int j = 0; j < sp.d; ++j)
-      for (int gl = 0; gl < sp.ngl; ++gl)
-        for (int gr = 0; gr < sp.ngr; ++gr) {
-          const size_t o = ((size_t)j * sp.ngl + gl) * sp.ngr + gr;
-          const uint64_t k = c.keys[o];
-          if (k == ~0ull) continue;
-          const int32_t prog = c.prog[o] >= 0 ? c.prog[o] : ps.index.find(k)->second;
-          auto it = local.find(prog);
-          int32_t b;
-          if (it == local.end()) {
-            b = int32_t(lprog[s].size());
-            local.emplace(prog, b);
-            lprog[s].push_back(prog);
-            lcount[s].push_back(0);
-          } else {
-            b = it->second;
-          }
-          sp.combo_off[o] = int32_t(lcount[s][b]);
-          lcount[s][b] += c.gc_l[gl] * c.gc_r[gr];
-          sp.bucket_of[o] = b;
+    for (int gl = 0; gl < sp.ngl; ++gl)
+      for (int gr = 0; gr < sp.ngr; ++gr) {
+        const size_t o = (size_t)gl * sp.ngr + gr;
+        const uint64_t k = c.keys[o];
+        if (k == ~0ull) continue;
+        sp.combo_j[o] = int8_t(int(k >> kKeyRootShift) - 1);
+        const int32_t prog = c.prog[o] >= 0 ? c.prog[o] : ps.index.find(k)->second;
+        auto it = local.find(prog);
+        int32_t b;
+        if (it == local.end()) {
+          b = int32_t(lprog[s].size());
+          local.emplace(prog, b);
+          lprog[s].push_back(prog);
+          lcount[s].push_back(0);
+        } else {
+          b = it->second;
         }
+        sp.combo_off[o] = int32_t(lcount[s][b]);
+        lcount[s][b] += c.gc_l[gl] * c.gc_r[gr];
+        sp.bucket_of[o] = b;
+      }
   });
   if (ph) ph[2] += plan_ms_since(t_ph);
   // phase D: global bucket list
@@ -1399,8 +1400,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   const size_t o_desc = carve(sizeof(SiteDesc) * ns);
   const size_t o_lsj = carve(sizeof(LeftScaleJob) * ns);
   const size_t o_fs = carve(sizeof(FillSpan) * ns);  // Gamma clears
-  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns), o_co(ns), o_gsl(ns), o_gcl(ns), o_gsr(ns),
-      o_lsd(ns), o_lsf(ns);
+  std::vector<size_t> o_pl(ns), o_gl(ns), o_pr(ns), o_gr(ns), o_bo(ns), o_co(ns), o_cj(ns), o_gsl(ns), o_gcl(ns),
+      o_gsr(ns), o_lsd(ns), o_lsf(ns);
   int max_kl = 1;
   for (int s = 0; s < ns; ++s) {
     o_lsd[s] = carve((size_t)in[s].KL * 8);
@@ -1412,6 +1413,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     o_gr[s] = carve(plans[s].grp_r.size() * 4);
     o_bo[s] = carve(plans[s].bucket_of.size() * 4);
     o_co[s] = carve(plans[s].combo_off.size() * 4);
+    o_cj[s] = carve(plans[s].combo_j.size());
     o_gsl[s] = carve(plans[s].gstart_l.size() * 4);
     o_gcl[s] = carve(plans[s].gcnt_l.size() * 4);
     o_gsr[s] = carve(plans[s].gstart_r.size() * 4);
@@ -1474,6 +1476,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     std::memcpy(hp + o_gr[s], plans[s].grp_r.data(), plans[s].grp_r.size() * 4);
     std::memcpy(hp + o_bo[s], plans[s].bucket_of.data(), plans[s].bucket_of.size() * 4);
     std::memcpy(hp + o_co[s], plans[s].combo_off.data(), plans[s].combo_off.size() * 4);
+    std::memcpy(hp + o_cj[s], plans[s].combo_j.data(), plans[s].combo_j.size());
     std::memcpy(hp + o_gsl[s], plans[s].gstart_l.data(), plans[s].gstart_l.size() * 4);
     std::memcpy(hp + o_gcl[s], plans[s].gcnt_l.data(), plans[s].gcnt_l.size() * 4);
     std::memcpy(hp + o_gsr[s], plans[s].gstart_r.data(), plans[s].gstart_r.size() * 4);
@@ -1497,7 +1500,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     const SitePlanHost& p = plans[s];
     auto dptr = [&](size_t o) { return reinterpret_cast<int32_t*>(dp + o); };
     hsp[s] = SitePlanDev{dptr(o_pl[s]),  dptr(o_gl[s]),  dptr(o_pr[s]), dptr(o_gr[s]), dptr(o_bo[s]),
-                         dptr(o_co[s]),  dptr(o_gsl[s]), dptr(o_gcl[s]), dptr(o_gsr[s]), dptr(o_boff),
+                         dptr(o_co[s]),  reinterpret_cast<const int8_t*>(dp + o_cj[s]),
+                         dptr(o_gsl[s]), dptr(o_gcl[s]), dptr(o_gsr[s]), dptr(o_boff),
                          d_items,        p.ngl,          p.ngr,          p.KL,           p.KR,
                          p.d};
     max_pairs = std::max<int64_t>(max_pairs, (int64_t)p.KL * p.KR);
@@ -1517,7 +1521,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     const int64_t per_site = std::max<int64_t>(1, ((int64_t)h->num_sms * 8 + ns - 1) / ns);
     const int bx = int(std::max<int64_t>(1, std::min<int64_t>((max_pairs + 255) / 256, per_site)));
     double pairs = 0.0;
-    for (int s = 0; s < ns; ++s) pairs += (double)plans[s].KL * plans[s].KR * plans[s].d;
+    for (int s = 0; s < ns; ++s) pairs += (double)plans[s].KL * plans[s].KR;
     BSG_PROFILED(h, BSG_K_PREP, st, pairs,
                  (site_scatter_kernel<<<dim3(bx, ns), 256, 0, st>>>(reinterpret_cast<const SitePlanDev*>(dp + o_sp))));
   }
@@ -1874,7 +1878,8 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // Sigma also read the edge groups' boundary cuts
   const int ng = int(groups.size());
   // events: h->ev[g] = group g's Sigma done (its DP stream waits), h->ev[3] = the left group's
-  // Williamson done (BSG_TUNE_DP_HOLD), h->ev[4..9] = final joins,
+  // Williamson done (BSG_TUNE_DP_HOLD), h->ev[4..9] = final joins, h->ev[15] = the batched
+  // build's keys on the host,
   // h->ev[10..12] = Gammas final (pinned copies), h->ev[13..14] = copy-stream joins,
   // h->ev[16 + 3 g + q] (q < 3) = site part q of group g final (host outputs)
   cudaEvent_t ev_keys[3] = {}, ev_done[3] = {};
@@ -2302,6 +2307,9 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
     }
     BSG_CUDA(cudaMemcpyAsync(hbh, hb, hb_bytes, cudaMemcpyDeviceToHost, st));
   }
+  // the host plans as soon as the keys are here, while the GPU builds Sigma
+  BSG_TRY(h->ensure_aux());
+  BSG_CUDA(cudaEventRecord(h->ev[15], st));
   // 3. Sigma of every site of every instance in one set of launches
   SigmaJob* jobs = reinterpret_cast<SigmaJob*>(hs + h_jobs);
   for (int i = 0; i < n; ++i) {
@@ -2344,10 +2352,11 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
                                  (int64_t)(2 * Mr) * (2 * Mr)};
     }
   BSG_TRY(convert_many(h, conv, n_conv, wb + o_conv, precision, st));
-  // 4. one host wait: every instance's cut status, row counts and keys
+  // 4. one host wait: every instance's cut status, row counts and keys (the
+  // Sigma launches keep running; the DP launches queue behind them on st)
   {
     auto t_wait = clk::now();
-    BSG_CUDA(cudaStreamSynchronize(st));
+    BSG_CUDA(cudaEventSynchronize(h->ev[15]));
     h->prof.add_host(BSG_K_HOST_WAIT, ms_since(t_wait), 0.0);
   }
   auto t_plan = clk::now();

@@ -1506,6 +1506,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
                          p.d};
     max_pairs = std::max<int64_t>(max_pairs, (int64_t)p.KL * p.KR);
   }
+  if (ph) ph[6] += plan_ms_since(t_ph);
   BSG_CUDA(cudaMemcpyAsync(dp, hp, plan_bytes, cudaMemcpyHostToDevice, st));
   BSG_PROFILED(h, BSG_K_PREP, st, (double)ns * max_kl,
                (left_scale_kernel<<<dim3((max_kl + 127) / 128, ns), 128, 0, st>>>(
@@ -1536,7 +1537,7 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   a.sites = reinterpret_cast<SiteDesc*>(dp + o_desc);
   const int rc = launch_dp<MODE_SITE>(h, precision, a, bk, slot.scratch, st);
   if (ph) {
-    ph[6] += plan_ms_since(t_ph);
+    ph[5] += plan_ms_since(t_ph);
     ph[7] += std::chrono::duration<double, std::milli>(plan_clk::now() - t_all).count();
   }
   return rc;

@@ -114,7 +114,7 @@ def build_mps_batch(sq_covs, ds, chis, precision="split", out_dtype=torch.comple
         kh = kept_all[k0:k0 + nc]
         rh = res_all[r0:r0 + nc * c].reshape(nc, c)
         k0, r0 = k0 + nc, r0 + nc * c
-        left = np.array([int((rh[q, : kh[q]] > err_tol).sum()) for q in range(nc)])
+        left = ((rh > err_tol) & (np.arange(c)[None, :] < kh[:, None])).sum(axis=1)
         out.append(MPS(outs[i], lam[i], res[i], num[i], S[i], kh, left, t))
     return out
 

@@ -331,8 +331,9 @@ int bsg_profile_build_timeline(bsg_handle_t h, double* ms, int n);
  * and partition keys of every (j, left group, right group) combination
  * (parallel), 1 new partition programs (serial), 2 per-site buckets
  * (parallel), 3 the global bucket list, 4 bucket layout and remap,
- * 5 program upload, 6 plan staging and the scatter/DP launches, 7 the
- * whole of it.  n: entries to fill (8 covers every phase). */
+ * 5 program upload and the plan / scatter / DP launches, 6 plan staging
+ * (the host tables copied into the pinned plan buffer), 7 the whole of it.
+ * n: entries to fill (8 covers every phase). */
 int bsg_profile_plan_phases(bsg_handle_t h, double* ms, int n);
 
 /* Hafnian DP launches since the last bsg_profile_reset while profiling was

@@ -36,6 +36,8 @@ KNOBS = {
     "gemm_kernel": _lib.TUNE_GEMM_KERNEL,
     "dp_quantum": _lib.TUNE_DP_QUANTUM,
     "dp_hold": _lib.TUNE_DP_HOLD,
+    "right_pct": _lib.TUNE_RIGHT_PCT,
+    "left_pct": _lib.TUNE_LEFT_PCT,
 }
 
 

@@ -227,6 +227,8 @@ int bsg_tune_set(bsg_handle_t h, int key, int value) {
     BSG_CHECK_ARG(value == 256 || value == 512 || value == 1024, "bsg_tune_set: factor threads %d", value);
   if (key == BSG_TUNE_DP_SCRATCH_MIB)
     BSG_CHECK_ARG(value >= 64 && value <= 65536, "bsg_tune_set: DP scratch %d MiB", value);
+  if (key == BSG_TUNE_RIGHT_PCT || key == BSG_TUNE_LEFT_PCT)
+    BSG_CHECK_ARG(value == 0 || (value >= 5 && value <= 60), "bsg_tune_set: group share %d %%", value);
   if (key == BSG_TUNE_DP_HOLD) BSG_CHECK_ARG(value == 0 || value == 1, "bsg_tune_set: DP hold %d", value);
   if (key == BSG_TUNE_DP_QUANTUM)
     BSG_CHECK_ARG(value >= 0 && value <= (1 << 20), "bsg_tune_set: DP quantum %d", value);

@@ -154,7 +154,7 @@ __global__ void cut_rows_batch_kernel(const CutRowsJob* __restrict__ jobs, const
   }
   const unsigned bal = __ballot_sync(0xffffffffu, keep);
   if ((threadIdx.x & 31) == 0 && bal) atomicAdd(jb.above + c, __popc(bal));
-  const int rows = jb.kept[c];
+  const int rows = min(jb.kept[c], chi);  // a caller's kept count never indexes past the row tables
   if (blockIdx.x == 0 && threadIdx.x == 0) jb.cnt[c] = rows;
   if (r < rows)
     label_row(jb.num + ((size_t)c * chi + r) * jb.ld, jb.m0 - c, jb.t, (size_t)c * chi + r, jb.err);
@@ -1752,14 +1752,22 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // still in flight take SMs within about one quantum instead of waiting for
   // a whole DP launch.  No kernel waits on another; streams are ordered by
   // events only.
-  // Host outputs take a smaller left group (a quarter of the cuts instead of
-  // a third): it finishes last, and what it leaves to download after the
-  // build is the tail of the end-to-end time (M=144: 115.4 -> 113.5 ms, the
-  // device-resident build 108.3 -> 109.2 ms, so it keeps a third).
+  // The group boundaries T1 (left | middle) and T2 (middle | right) come
+  // from the tuned shares below; host outputs take a smaller left group (it
+  // finishes last, and what it leaves to download after the build is the
+  // tail of the end-to-end time).
   int T1 = 0, T2 = nc;
   if (nc >= 6) {
-    T1 = gammas_pinned ? nc / 4 : nc / 3;
-    T2 = nc - nc / 4;
+    // built-in shares (measured at M=144): right 33 % / left 33 % for the
+    // device-resident build (82.2 -> 80.0 ms against 25 / 33), right 40 % /
+    // left 30 % when Gamma goes to the host (e2e 98.8 -> 91.2 ms against
+    // 25 / 25): the right group's cuts are cheap, so a larger right group
+    // puts more of the build's work (and of the downloads) early
+    const int lp = h->tune[BSG_TUNE_LEFT_PCT] ? h->tune[BSG_TUNE_LEFT_PCT] : gammas_pinned ? 30 : 33;
+    const int rp = h->tune[BSG_TUNE_RIGHT_PCT] ? h->tune[BSG_TUNE_RIGHT_PCT] : gammas_pinned ? 40 : 33;
+    T1 = std::max(1, nc * lp / 100);
+    T2 = nc - std::max(1, nc * rp / 100);
+    if (T2 <= T1) T2 = T1 + 1;  // shares above 100 %: a middle group of one cut
   }
   struct Group {
     int c0, c1, s0, s1;

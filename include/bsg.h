@@ -391,7 +391,11 @@ int bsg_potrf_f64(bsg_handle_t h, double* A, int n, int* info, bsg_stream_t stre
                                         Williamson kernel is done (the left group's factorisations, the
                                         build's critical path, then run without the DP's memory traffic
                                         beside them), 0 = it starts with its Sigma (default 0) */
-#define BSG_TUNE_COUNT 10
+#define BSG_TUNE_RIGHT_PCT 10        /* pipelined build: percent of the cuts in the right group, 5..60,
+                                        0 = built-in (33; 40 when Gamma goes to the host) */
+#define BSG_TUNE_LEFT_PCT 11         /* pipelined build: percent of the cuts in the left group, 5..60,
+                                        0 = built-in (33; 30 when Gamma goes to the host) */
+#define BSG_TUNE_COUNT 12
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

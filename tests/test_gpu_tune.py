@@ -43,7 +43,8 @@ def test_launch_split_bit_identical(cuda, golden, prec):
                       {"small_entries": 16, "small_blocks": 2, "scratch_mib": 64, "dp_quantum": 64},
                       {"small_entries": 4096, "small_blocks": 8, "dp_quantum": 1},
                       {"small_entries": 64, "small_blocks": 8, "dp_quantum": 1 << 20},
-                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 2, "dp_hold": 1}):
+                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 2, "dp_hold": 1},
+                      {"small_entries": 64, "small_blocks": 8, "dp_quantum": 2, "right_pct": 50, "left_pct": 20}):
             autotune.set_knobs(**knobs)
             mps = build_mps(t["sq_cov"], d, chi, precision=prec, out_dtype=torch.complex128)
             outs.append([g.cpu().numpy() for g in mps.Gammas])

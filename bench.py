@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--no-sampler", action="store_true")
     p.add_argument("--no-decomp", action="store_true")
     p.add_argument("--decomp-M", type=int, default=50)
+    p.add_argument("--decomp-cpu-M", type=int, default=24)
     p.add_argument("--sampler-workload", default="M50_d6_chi256")
     p.add_argument("--sampler-n", type=int, default=100000)
     return p.parse_args()
@@ -414,6 +415,23 @@ def measure_decomposition(args):
         if name == "uniform_loss":
             r["rel_err_vs_closed_form"] = float(np.abs(X - sq_u).max() / np.abs(sq_u).max())
         out[name] = r
+    if not args.no_cpu:
+        # CPU leg: the oracle's interior-point restatement (numpy / LAPACK on
+        # the host's cores) against the GPU solver on one mode-dependent-loss
+        # covariance of a size the oracle solves in seconds
+        from oracle import decomposition as oracle_decomposition
+        Mc = args.decomp_cpu_M
+        cov_c = synthetic.nonuniform_lossy_covariance(Mc, seed=1)
+        t0 = time.perf_counter()
+        ref = oracle_decomposition.decompose(cov_c)
+        cpu_ms = 1e3 * (time.perf_counter() - t0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Xg, meta = decomposition.decompose(cov_c)
+        gpu_ms = 1e3 * (time.perf_counter() - t0)
+        out["cpu_baseline"] = {"M": Mc, "kind": "port", "cores": os.cpu_count(), "cpu_ms": cpu_ms,
+                               "cpu_iterations": ref.iterations, "gpu_ms": gpu_ms, "gpu_iterations": meta["iterations"],
+                               "max_abs_diff": float(np.abs(Xg - ref.X).max())}
     return out
 
 

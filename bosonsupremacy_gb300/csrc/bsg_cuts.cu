@@ -28,6 +28,7 @@
 #include <cstring>
 #include <vector>
 
+#include "bsg_df.cuh"
 #include "bsg_internal.h"
 
 namespace bsg {
@@ -171,42 +172,6 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
 // numerators <= 1e-12 of the norm).
 constexpr int kDfTile = 32;
 constexpr size_t kDfSmemBytes = 2 * kDfTile * (kDfTile + 1) * sizeof(float2);
-
-// x = hi + lo from the IEEE bits on the integer pipe (FP64 conversions and
-// subtractions run on the narrow FP64 pipe): hi keeps the top 24 bits of the
-// significand (truncated), lo the next 29 rounded to 24, so hi + lo carries
-// ~48 bits; a lo below FP32's normal range (|x| < 2^-75) is dropped, and x
-// outside FP32's exponent range falls back to the FP64 split.
-__device__ __forceinline__ float2 df_split(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
-  const int e = int((hw >> 20) & 0x7ffu);  // biased double exponent
-  if (e == 0) return make_float2(0.f, 0.f);  // zero (or a double subnormal)
-  const int fe = e - 1023 + 127;
-  if (fe <= 0 || fe >= 255) {
-    const float h = float(x);
-    return make_float2(h, float(x - double(h)));
-  }
-  const unsigned sign = hw & 0x80000000u;
-  const float h = __uint_as_float(sign | (unsigned(fe) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
-  // the remaining 29 significand bits are r * 2^(e - 1023 - 52)
-  const int pe = e - 1075 + 127;
-  float l = 0.f;
-  if (pe > 0) l = __uint2float_rn(lw & 0x1fffffffu) * __uint_as_float(unsigned(pe) << 23);
-  return make_float2(h, sign ? -l : l);
-}
-
-// (s, t) += a b
-__device__ __forceinline__ void df_mac(float& s, float& t, float2 a, float2 b) {
-  const float p = a.x * b.x;
-  float e = fmaf(a.x, b.x, -p);
-  e = fmaf(a.x, b.y, e);
-  e = fmaf(a.y, b.x, e);
-  const float u = s + p;
-  const float bb = u - s;
-  t += e + ((s - (u - bb)) + (p - bb));
-  s = u;
-}
 
 // C[i][j] = add[i][j] + sign * sum_q A(i, q) B(q, j) (+ diag where i == j),
 // all m x m row-major, A(i, q) = ta ? A[q][i] : A[i][q], B(q, j) = tb ? B[j][q]

@@ -1,0 +1,49 @@
+// Double-float arithmetic on the FP32 pipe (GB300's FP64 pipe runs ~1/73 of
+// the FP32 rate): an FP64 operand is split into an FP32 pair hi + lo, a
+// product term is formed with its exact FP32 rounding error (fma) plus the
+// cross terms, and a sum is kept as an FP32 sum s with its rounding errors
+// collected in t (Dekker's exact product, Knuth's two-sum).  A term carries
+// ~2^-48 relative error, a sum of m terms ~2^-48 sqrt(m) of sum |a b|.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace bsg {
+
+// x = hi + lo from the IEEE bits on the integer pipe (FP64 conversions and
+// subtractions run on the narrow FP64 pipe): hi keeps the top 24 bits of the
+// significand (truncated), lo the next 29 rounded to 24, so hi + lo carries
+// ~48 bits; a lo below FP32's normal range (|x| < 2^-75) is dropped, and x
+// outside FP32's exponent range falls back to the FP64 split.
+__device__ __forceinline__ float2 df_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
+  const int e = int((hw >> 20) & 0x7ffu);  // biased double exponent
+  if (e == 0) return make_float2(0.f, 0.f);  // zero (or a double subnormal)
+  const int fe = e - 1023 + 127;
+  if (fe <= 0 || fe >= 255) {
+    const float h = float(x);
+    return make_float2(h, float(x - double(h)));
+  }
+  const unsigned sign = hw & 0x80000000u;
+  const float h = __uint_as_float(sign | (unsigned(fe) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  // the remaining 29 significand bits are r * 2^(e - 1023 - 52)
+  const int pe = e - 1075 + 127;
+  float l = 0.f;
+  if (pe > 0) l = __uint2float_rn(lw & 0x1fffffffu) * __uint_as_float(unsigned(pe) << 23);
+  return make_float2(h, sign ? -l : l);
+}
+
+// (s, t) += a b
+__device__ __forceinline__ void df_mac(float& s, float& t, float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float u = s + p;
+  const float bb = u - s;
+  t += e + ((s - (u - bb)) + (p - bb));
+  s = u;
+}
+
+}  // namespace bsg

@@ -1936,7 +1936,8 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
       // their S (Sigma), Lambda and label tables (DP)
       for (int e = 0; e < ng - 1; ++e) BSG_CUDA(cudaStreamWaitEvent(s2, ev_keys[e], 0));
     }
-    BSG_TRY(launch_sigma_jobs(h, jobs + G.s0, G.s1 - G.s0, wb + o_jobs + sizeof(SigmaJob) * G.s0, s2));
+    BSG_TRY(launch_sigma_jobs(h, jobs + G.s0, G.s1 - G.s0, wb + o_jobs + sizeof(SigmaJob) * G.s0, s2,
+                              precision == BSG_PREC_SPLIT));
     for (int i = G.s0; i < G.s1; ++i) {
       const int Mr = i == 0 ? M : M - i;
       if (o_sigc[i] != o_sig[i])
@@ -2349,7 +2350,7 @@ static int build_mps_batch_impl(bsg_handle_t h, int n, const double* const* sq, 
       jobs[s] = jb;
     }
   }
-  BSG_TRY(launch_sigma_jobs(h, jobs, ns, wb + o_jobs, st));
+  BSG_TRY(launch_sigma_jobs(h, jobs, ns, wb + o_jobs, st, precision == BSG_PREC_SPLIT));
   // every site's Sigma into the DP's storage type, one launch
   ConvJob* conv = reinterpret_cast<ConvJob*>(hs + h_conv);
   int n_conv = 0;

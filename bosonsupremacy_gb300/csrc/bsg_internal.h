@@ -252,7 +252,10 @@ int sliced_slice_gamma(const double2* G, int chi, int d, bool left, int S, int b
 int sliced_gemm(bsg_handle_t h, const void* A, int a_rows, const int* ea, const void* B, int b_rows, const int* eb,
                 double* C, int M, int N, int K, int ldc, int S, int b, int* d_err, cudaStream_t st, bool profile,
                 const int4* mtiles, int n_mtiles);
-int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st);
+// df_products: the Sigma products in double-float on the FP32 pipe (the
+// split-precision build), else FP64.
+int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st,
+                      bool df_products);
 
 }  // namespace bsg
 

@@ -16,7 +16,9 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
+#include "bsg_df.cuh"
 #include "bsg_internal.h"
 
 namespace bsg {
@@ -74,6 +76,7 @@ struct GJShared {
   double val[32];
   int idx[32];
   double logdet;
+  float4 inv4;  // 1 / pivot, double-float (gj_inverse_df)
   int piv;
 };
 
@@ -271,9 +274,143 @@ __global__ void sigma_linv_kernel(const SigmaJob* __restrict__ jobs) {
   T[t] = v;
 }
 
+// Double-float complex entries of the Gauss-Jordan matrix: (re s, re t,
+// im s, im t), value s + t per part; s + t is renormalised to hi + lo on
+// every store (Knuth's two-sum).
+__device__ __forceinline__ float2 df_norm(float s, float t) {
+  const float h = s + t;
+  const float bb = h - s;
+  return make_float2(h, (s - (h - bb)) + (t - bb));
+}
+__device__ __forceinline__ float4 df_cnorm(float4 v) {
+  const float2 r = df_norm(v.x, v.y), i = df_norm(v.z, v.w);
+  return make_float4(r.x, r.y, i.x, i.y);
+}
+__device__ __forceinline__ double2 df_cval(float4 v) {
+  return make_double2(double(v.x) + double(v.y), double(v.z) + double(v.w));
+}
+__device__ __forceinline__ float4 df_csplit(double2 v) {
+  const float2 r = df_split(v.x), i = df_split(v.y);
+  return make_float4(r.x, r.y, i.x, i.y);
+}
+
+// gj_inverse with G in double-float (float4 entries, same layout and size as
+// double2): the pivot search, the row scaling and the rank-1 updates run on
+// the FP32 pipe (four exact products per complex multiply-add); the pivot's
+// reciprocal and log|pivot| in FP64.  Entries carry ~2^-48 relative error
+// per operation (A' is well conditioned: its singular values are the
+// cosh r_k of the site unitary's squeezing), which is what the
+// split-precision DP reads of Sigma (FP32 pairs).
+__device__ void gj_inverse_df(float4* G, int Mr, int n2, int* status, GJShared& sh) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  float4* f4 = reinterpret_cast<float4*>(sh.f);
+  float4* v4 = reinterpret_cast<float4*>(sh.v);
+  for (int r = tid; r < Mr; r += nt) sh.orig[r] = r;
+  if (tid == 0) sh.logdet = 0.0;
+  __syncthreads();
+  for (int col = 0; col < Mr; ++col) {
+    float best = -1.f;
+    int bi = col;
+    for (int r = col + tid; r < Mr; r += nt) {
+      const float4 v = G[(size_t)r * n2 + col];  // stored normalised: hi parts carry the magnitude
+      const float m = v.x * v.x + v.z * v.z;
+      if (m > best) {
+        best = m;
+        bi = r;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      sh.val[warp] = best;
+      sh.idx[warp] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double b = sh.val[0];
+      int i0 = sh.idx[0];
+      for (int w = 1; w < nw; ++w)
+        if (sh.val[w] > b || (sh.val[w] == b && sh.idx[w] < i0)) {
+          b = sh.val[w];
+          i0 = sh.idx[w];
+        }
+      sh.piv = i0;
+      const double2 pv = df_cval(G[(size_t)i0 * n2 + col]);
+      const double m = pv.x * pv.x + pv.y * pv.y;
+      if (!(m > 0.0)) *status = 1;
+      sh.logdet += 0.5 * log(m > 0.0 ? m : 1e-300);
+      // 1 / pivot, split: in f4[Mr] (no row index reaches Mr)
+      const double2 inv = m > 0.0 ? make_double2(pv.x / m, -pv.y / m) : make_double2(0.0, 0.0);
+      f4[kGJMaxModes - 1] = df_csplit(inv);
+      if (i0 != col) {
+        const int t = sh.orig[i0];
+        sh.orig[i0] = sh.orig[col];
+        sh.orig[col] = t;
+      }
+    }
+    __syncthreads();
+    const int p = sh.piv;
+    if (p != col) {
+      for (int c = tid; c < n2; c += nt) {
+        const float4 t = G[(size_t)p * n2 + c];
+        G[(size_t)p * n2 + c] = G[(size_t)col * n2 + c];
+        G[(size_t)col * n2 + c] = t;
+      }
+    }
+    const int nleft = Mr - col - 1;
+    for (int q = tid; q < Mr; q += nt) sh.cols[q] = q < nleft ? col + 1 + q : Mr + sh.orig[q - nleft];
+    __syncthreads();
+    const float4 iv = sh.inv4;
+    const float2 ir = make_float2(iv.x, iv.y), ii = make_float2(iv.z, iv.w);
+    for (int q = tid; q < Mr; q += nt) {
+      float4* cp = G + (size_t)col * n2 + sh.cols[q];
+      const float4 v = *cp;
+      const float2 vr = make_float2(v.x, v.y), vi = make_float2(v.z, v.w);
+      float sr = 0.f, tr = 0.f, si = 0.f, ti = 0.f;
+      df_mac(sr, tr, vr, ir);
+      df_mac(sr, tr, make_float2(-vi.x, -vi.y), ii);
+      df_mac(si, ti, vr, ii);
+      df_mac(si, ti, vi, ir);
+      const float4 w = df_cnorm(make_float4(sr, tr, si, ti));
+      *cp = w;
+      v4[q] = w;
+    }
+    for (int r = tid; r < Mr; r += nt) f4[r] = r == col ? make_float4(0.f, 0.f, 0.f, 0.f) : G[(size_t)r * n2 + col];
+    __syncthreads();
+    for (int r = warp; r < Mr; r += nw) {
+      const float4 f = f4[r];
+      if (f.x == 0.f && f.z == 0.f) continue;
+      const float2 nfr = make_float2(-f.x, -f.y), fi = make_float2(f.z, f.w), nfi = make_float2(-f.z, -f.w);
+      float4* row = G + (size_t)r * n2;
+      for (int q = lane; q < Mr; q += 32) {
+        const float4 v = v4[q];
+        const float2 vr = make_float2(v.x, v.y), vi = make_float2(v.z, v.w);
+        float4* gp = row + sh.cols[q];
+        float4 g = *gp;
+        // g -= f v: re -= fr vr - fi vi, im -= fr vi + fi vr
+        df_mac(g.x, g.y, nfr, vr);
+        df_mac(g.x, g.y, fi, vi);
+        df_mac(g.z, g.w, nfr, vi);
+        df_mac(g.z, g.w, nfi, vr);
+        *gp = df_cnorm(g);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // MODE 0: C = L B0 with B0 = S_r (C -> P) or, at site 0, B0 = sq (C -> G region);
 // MODE 1 (site 0 only): P = L C0^T with C0 = L sq.  64 x 64 tiles, 256 threads.
-template <int MODE>
+// DF: the products in double-float on the FP32 pipe (operands split once per
+// tile load; the split-precision build, whose DP reads Sigma as FP32 pairs),
+// else FP64.
+template <int MODE, bool DF>
 __global__ void __launch_bounds__(256) sigma_gemm_kernel(const SigmaJob* __restrict__ jobs) {
   const SigmaJob jb = jobs[blockIdx.y];
   if (MODE == 1 && !jb.first) return;
@@ -296,20 +433,29 @@ __global__ void __launch_bounds__(256) sigma_gemm_kernel(const SigmaJob* __restr
     bs1 = n2;
     C = jb.ws;
   }
-  __shared__ double As[16][65], Bs[16][65];
+  using E = typename std::conditional<DF, float2, double>::type;
+  __shared__ E As[16][65], Bs[16][65];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   double acc[4][4] = {};
+  float s[4][4] = {}, t[4][4] = {};
   for (int k0 = 0; k0 < n2; k0 += 16) {
     for (int e = threadIdx.x; e < 64 * 16; e += 256) {
       const int ii = e / 16, kk = e % 16, i = i0 + ii, k = k0 + kk;
-      As[kk][ii] = (i < n2 && k < n2) ? L[(size_t)i * n2 + k] : 0.0;
+      const double av = (i < n2 && k < n2) ? L[(size_t)i * n2 + k] : 0.0;
       const int kb = e / 64, jj = e % 64, j = j0 + jj, k2 = k0 + kb;
-      Bs[kb][jj] = (k2 < n2 && j < n2) ? B[(int64_t)k2 * bs0 + (int64_t)j * bs1] : 0.0;
+      const double bv = (k2 < n2 && j < n2) ? B[(int64_t)k2 * bs0 + (int64_t)j * bs1] : 0.0;
+      if constexpr (DF) {
+        As[kk][ii] = df_split(av);
+        Bs[kb][jj] = df_split(bv);
+      } else {
+        As[kk][ii] = av;
+        Bs[kb][jj] = bv;
+      }
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < 16; ++kk) {
-      double av[4], bv[4];
+      E av[4], bv[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         av[q] = As[kk][ty * 4 + q];
@@ -318,7 +464,10 @@ __global__ void __launch_bounds__(256) sigma_gemm_kernel(const SigmaJob* __restr
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
-        for (int w = 0; w < 4; ++w) acc[q][w] = fma(av[q], bv[w], acc[q][w]);
+        for (int w = 0; w < 4; ++w) {
+          if constexpr (DF) df_mac(s[q][w], t[q][w], av[q], bv[w]);
+          else acc[q][w] = fma(av[q], bv[w], acc[q][w]);
+        }
     }
     __syncthreads();
   }
@@ -327,18 +476,22 @@ __global__ void __launch_bounds__(256) sigma_gemm_kernel(const SigmaJob* __restr
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
       const int i = i0 + ty * 4 + q, j = j0 + tx * 4 + w;
-      if (i < n2 && j < n2) C[(size_t)i * n2 + j] = acc[q][w];
+      if (i < n2 && j < n2) C[(size_t)i * n2 + j] = DF ? double(s[q][w]) + double(t[q][w]) : acc[q][w];
     }
 }
 
 // One CTA per job: A', B from P, Gauss-Jordan for X = conj(A')^{-1}, Z, and
-// the X / X^T blocks of Sigma (zeros at site 0).
+// the X / X^T blocks of Sigma (zeros at site 0).  DF: the Gauss-Jordan in
+// double-float (gj_inverse_df); its inverse half is turned back into FP64
+// in place for the products that follow.
+template <bool DF>
 __global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restrict__ jobs) {
   const SigmaJob jb = jobs[blockIdx.x];
   const int Mr = jb.Mr, n2 = 2 * Mr;
   const int tid = threadIdx.x, nt = blockDim.x;
   double* P = jb.ws;
   double2* G = reinterpret_cast<double2*>(jb.ws + 2 * (size_t)n2 * n2);
+  float4* G4 = reinterpret_cast<float4*>(G);
   double2* Bm = G + (size_t)Mr * n2;
   __shared__ GJShared sh;
   for (int i = tid; i < Mr * Mr; i += nt) {
@@ -347,12 +500,28 @@ __global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restri
     double px = P[(size_t)(Mr + r) * n2 + c], pp = P[(size_t)(Mr + r) * n2 + Mr + c];
     double ar = 0.5 * (xx + pp), ai = 0.5 * (px - xp);
     if (jb.first && r == c) ar += 1.0;
-    G[(size_t)r * n2 + c] = make_double2(ar, -ai);
-    G[(size_t)r * n2 + Mr + c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+    const double2 a = make_double2(ar, -ai), e = make_double2(r == c ? 1.0 : 0.0, 0.0);
+    if (DF) {
+      G4[(size_t)r * n2 + c] = df_csplit(a);
+      G4[(size_t)r * n2 + Mr + c] = df_csplit(e);
+    } else {
+      G[(size_t)r * n2 + c] = a;
+      G[(size_t)r * n2 + Mr + c] = e;
+    }
     Bm[i] = make_double2(0.5 * (xx - pp), 0.5 * (px + xp));
   }
   __syncthreads();
-  gj_inverse(G, Mr, n2, jb.status, sh);
+  if (DF) {
+    gj_inverse_df(G4, Mr, n2, jb.status, sh);
+    for (int i = tid; i < Mr * Mr; i += nt) {
+      const size_t o = (size_t)(i / Mr) * n2 + Mr + i % Mr;
+      const float4 v = G4[o];
+      G[o] = df_cval(v);  // same 16 bytes, read before written by this thread
+    }
+    __syncthreads();
+  } else {
+    gj_inverse(G, Mr, n2, jb.status, sh);
+  }
   for (int i = tid; i < Mr * Mr; i += nt) {
     const int r = i / Mr, c = i % Mr;
     if (jb.first) {
@@ -371,7 +540,9 @@ __global__ void __launch_bounds__(1024) sigma_gj_kernel(const SigmaJob* __restri
 }
 
 // Sigma11 = B X (every site) and Sigma22 = -X conj(B) (blockIdx.z = 1, not at
-// site 0): complex products, 32 x 32 tiles, 256 threads with 2 x 2 outputs.
+// site 0): complex products, 32 x 32 tiles, 256 threads with 2 x 2 outputs;
+// DF as in sigma_gemm_kernel (each complex operand split into four floats).
+template <bool DF>
 __global__ void __launch_bounds__(256) sigma_cgemm_kernel(const SigmaJob* __restrict__ jobs) {
   const SigmaJob jb = jobs[blockIdx.y];
   const int z = blockIdx.z;
@@ -387,15 +558,25 @@ __global__ void __launch_bounds__(256) sigma_cgemm_kernel(const SigmaJob* __rest
     const double2 b = Bm[(size_t)k * Mr + j];
     return make_double2(b.x, -b.y);
   };
-  __shared__ double2 As[16][33], Bs[16][33];
+  using E = typename std::conditional<DF, float4, double2>::type;  // DF: (re hi, re lo, im hi, im lo)
+  auto put = [](double2 v) -> E {
+    if constexpr (DF) {
+      const float2 r = df_split(v.x), i = df_split(v.y);
+      return make_float4(r.x, r.y, i.x, i.y);
+    } else {
+      return v;
+    }
+  };
+  __shared__ E As[16][33], Bs[16][33];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   double2 acc[2][2] = {};
+  float sr[2][2] = {}, tr[2][2] = {}, si[2][2] = {}, ti[2][2] = {};
   for (int k0 = 0; k0 < Mr; k0 += 16) {
     for (int e = threadIdx.x; e < 32 * 16; e += 256) {
       const int ii = e / 16, kk = e % 16, i = i0 + ii, k = k0 + kk;
-      As[kk][ii] = (i < Mr && k < Mr) ? Aop(i, k) : make_double2(0.0, 0.0);
+      As[kk][ii] = put((i < Mr && k < Mr) ? Aop(i, k) : make_double2(0.0, 0.0));
       const int kb = e / 32, jj = e % 32, j = j0 + jj, k2 = k0 + kb;
-      Bs[kb][jj] = (k2 < Mr && j < Mr) ? Bop(k2, j) : make_double2(0.0, 0.0);
+      Bs[kb][jj] = put((k2 < Mr && j < Mr) ? Bop(k2, j) : make_double2(0.0, 0.0));
     }
     __syncthreads();
 #pragma unroll
@@ -404,9 +585,18 @@ __global__ void __launch_bounds__(256) sigma_cgemm_kernel(const SigmaJob* __rest
       for (int q = 0; q < 2; ++q)
 #pragma unroll
         for (int w = 0; w < 2; ++w) {
-          const double2 av = As[kk][ty * 2 + q], bv = Bs[kk][tx * 2 + w];
-          acc[q][w].x = fma(av.x, bv.x, fma(-av.y, bv.y, acc[q][w].x));
-          acc[q][w].y = fma(av.x, bv.y, fma(av.y, bv.x, acc[q][w].y));
+          const E av = As[kk][ty * 2 + q], bv = Bs[kk][tx * 2 + w];
+          if constexpr (DF) {
+            const float2 ar = make_float2(av.x, av.y), ai = make_float2(av.z, av.w);
+            const float2 br = make_float2(bv.x, bv.y), bi = make_float2(bv.z, bv.w);
+            df_mac(sr[q][w], tr[q][w], ar, br);
+            df_mac(sr[q][w], tr[q][w], make_float2(-ai.x, -ai.y), bi);
+            df_mac(si[q][w], ti[q][w], ar, bi);
+            df_mac(si[q][w], ti[q][w], ai, br);
+          } else {
+            acc[q][w].x = fma(av.x, bv.x, fma(-av.y, bv.y, acc[q][w].x));
+            acc[q][w].y = fma(av.x, bv.y, fma(av.y, bv.x, acc[q][w].y));
+          }
         }
     }
     __syncthreads();
@@ -417,13 +607,15 @@ __global__ void __launch_bounds__(256) sigma_cgemm_kernel(const SigmaJob* __rest
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
       const int i = i0 + ty * 2 + q, j = j0 + tx * 2 + w;
+      if (DF) acc[q][w] = make_double2(double(sr[q][w]) + double(tr[q][w]), double(si[q][w]) + double(ti[q][w]));
       if (i < Mr && j < Mr)
         jb.Sigma[(size_t)(z == 0 ? i : Mr + i) * n2 + (z == 0 ? j : Mr + j)] =
             make_double2(sg * acc[q][w].x, sg * acc[q][w].y);
     }
 }
 
-int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st) {
+int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, void* jobs_dev, cudaStream_t st,
+                      bool df_products) {
   if (n_jobs <= 0) return BSG_OK;
   BSG_CUDA(cudaMemcpyAsync(jobs_dev, jobs_host, sizeof(SigmaJob) * n_jobs, cudaMemcpyHostToDevice, st));
   double work = 0.0;
@@ -439,13 +631,19 @@ int launch_sigma_jobs(bsg_handle_t h, const SigmaJob* jobs_host, int n_jobs, voi
   cudaEvent_t ev = nullptr;
   if (h->prof.on) BSG_TRY(h->prof.begin(BSG_K_SIGMA, st, &ev));
   sigma_linv_kernel<<<dim3(unsigned((n2 * n2 + 255) / 256), n_jobs), 256, 0, st>>>(jd);
-  sigma_gemm_kernel<0><<<dim3(unsigned(tn * tn), n_jobs), 256, 0, st>>>(jd);
+  const dim3 g0(unsigned(tn * tn), n_jobs), gc(unsigned(tc * tc), n_jobs, 2);
+  if (df_products) sigma_gemm_kernel<0, true><<<g0, 256, 0, st>>>(jd);
+  else sigma_gemm_kernel<0, false><<<g0, 256, 0, st>>>(jd);
   if (first_mr) {
     const int64_t t1 = (2 * (int64_t)first_mr + 63) / 64;
-    sigma_gemm_kernel<1><<<dim3(unsigned(t1 * t1), n_jobs), 256, 0, st>>>(jd);
+    const dim3 g1(unsigned(t1 * t1), n_jobs);
+    if (df_products) sigma_gemm_kernel<1, true><<<g1, 256, 0, st>>>(jd);
+    else sigma_gemm_kernel<1, false><<<g1, 256, 0, st>>>(jd);
   }
-  sigma_gj_kernel<<<n_jobs, h->tune[BSG_TUNE_FACTOR_THREADS], 0, st>>>(jd);
-  sigma_cgemm_kernel<<<dim3(unsigned(tc * tc), n_jobs, 2), 256, 0, st>>>(jd);
+  if (df_products) sigma_gj_kernel<true><<<n_jobs, h->tune[BSG_TUNE_FACTOR_THREADS], 0, st>>>(jd);
+  else sigma_gj_kernel<false><<<n_jobs, h->tune[BSG_TUNE_FACTOR_THREADS], 0, st>>>(jd);
+  if (df_products) sigma_cgemm_kernel<true><<<gc, 256, 0, st>>>(jd);
+  else sigma_cgemm_kernel<false><<<gc, 256, 0, st>>>(jd);
   BSG_CUDA(cudaGetLastError());
   if (h->prof.on) BSG_TRY(h->prof.end(BSG_K_SIGMA, st, ev, work));
   return BSG_OK;
@@ -464,7 +662,7 @@ static int single_job(bsg_handle_t h, SigmaJob jb, cudaStream_t st) {
   // the staging owner (the next planning call synchronises the stream)
   BSG_CUDA(cudaStreamSynchronize(st));
   std::memcpy(h->host_stage.ptr, &jb, sizeof(SigmaJob));
-  return launch_sigma_jobs(h, reinterpret_cast<SigmaJob*>(h->host_stage.ptr), 1, jd, st);
+  return launch_sigma_jobs(h, reinterpret_cast<SigmaJob*>(h->host_stage.ptr), 1, jd, st, false);
 }
 
 }  // namespace bsg

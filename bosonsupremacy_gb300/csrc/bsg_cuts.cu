@@ -66,27 +66,29 @@ __device__ double block_sum(double v, double* red) {
   return red[32];
 }
 
-// Cyclic Jacobi on the symmetric m x m matrix Hm (global memory), rows of
-// QT accumulating the eigenvectors (QT <- J^T QT).  Round-robin order: n/2
-// disjoint rotations per step, each thread updating whole 2x2 blocks of
-// J1^T B J2 (and the transposed block), so a step needs two barriers.
-// Returns the number of sweeps, or -1 if max_sweeps did not converge.
+// Cyclic Jacobi on the symmetric m x m matrix Hm (shared or global memory),
+// rows of QT accumulating the eigenvectors (QT <- J^T QT).  Round-robin
+// order: n/2 disjoint rotations per step, each updating whole 2x2 blocks of
+// J1^T B J2 (and the transposed block), so a step needs two barriers.  The
+// rotation angles and the convergence sums run in T (FP32 for the FP32
+// sweeps); warps take rows of the pair triangle and of QT, lanes their
+// columns, so no thread divides an index.  Returns the number of sweeps, or
+// -1 if max_sweeps did not converge.
 template <class T>
 __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, double* red, T* cs, T* sn, int* pos) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const size_t mm = (size_t)m * m;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int P = m / 2;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-    double off = 0.0, dia = 0.0;
-    for (size_t t = tid; t < mm; t += nt) {
-      const int i = int(t / m), j = int(t % m);
-      const double h = double(Hm[t]);
-      if (i < j) off += h * h;
-      else if (i == j) dia += h * h;
-    }
-    off = block_sum(off, red);
-    dia = block_sum(dia, red);
-    if (off <= tol * dia) return sweep;
+    T off = T(0), dia = T(0);
+    for (int i = warp; i < m; i += nw)
+      for (int j = lane; j < m; j += 32) {
+        const T h = Hm[(size_t)i * m + j];
+        if (i < j) off += h * h;
+        else if (i == j) dia += h * h;
+      }
+    const double offs = block_sum(double(off), red);
+    const double dias = block_sum(double(dia), red);
+    if (offs <= tol * dias) return sweep;
     for (int step = 0; step < m - 1; ++step) {
       // round-robin pairing of this step: slot i holds index pos(i)
       auto pos_at = [&](int i) { return i == 0 ? 0 : ((i - 1 + step) % (m - 1)) + 1; };
@@ -97,62 +99,63 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
           p = q;
           q = x;
         }
-        const double hpq = double(Hm[(size_t)p * m + q]);
-        const double skip = sizeof(T) == 8 ? 1e-17 : 1e-8;
-        double c_ = 1.0, s_ = 0.0;
-        const double hpp = double(Hm[(size_t)p * m + p]), hqq = double(Hm[(size_t)q * m + q]);
-        if (fabs(hpq) > 1e-300 && fabs(hpq) > skip * sqrt(fabs(hpp * hqq))) {
-          const double th = (hqq - hpp) / (2.0 * hpq);
-          const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-          c_ = 1.0 / sqrt(tt * tt + 1.0);
+        const T hpq = Hm[(size_t)p * m + q];
+        const T skip = sizeof(T) == 8 ? T(1e-17) : T(1e-8);
+        T c_ = T(1), s_ = T(0);
+        const T hpp = Hm[(size_t)p * m + p], hqq = Hm[(size_t)q * m + q];
+        if (fabs(hpq) > T(1e-30) && fabs(hpq) > skip * sqrt(fabs(hpp * hqq))) {
+          const T th = (hqq - hpp) / (T(2) * hpq);
+          const T tt = (th >= T(0) ? T(1) : T(-1)) / (fabs(th) + sqrt(th * th + T(1)));
+          c_ = T(1) / sqrt(tt * tt + T(1));
           s_ = tt * c_;
         }
-        cs[q0] = T(c_);
-        sn[q0] = T(s_);
+        cs[q0] = c_;
+        sn[q0] = s_;
         pos[q0] = p;
         pos[P + q0] = q;
       }
       __syncthreads();
       // 2 x 2 blocks (m1 <= m2) of the two-sided update, upper triangle of pairs
-      const int PT = P * (P + 1) / 2;
-      for (int t = tid; t < PT; t += nt) {
-        // t -> (m1, m2), m1 <= m2: row m2 of the triangle starts at m2 (m2 + 1) / 2
-        int m2 = int((sqrtf(8.f * float(t) + 1.f) - 1.f) * 0.5f);
-        while (m2 * (m2 + 1) / 2 > t) --m2;
-        while ((m2 + 1) * (m2 + 2) / 2 <= t) ++m2;
-        const int m1 = t - m2 * (m2 + 1) / 2;
-        const int p1 = pos[m1], q1 = pos[P + m1], p2 = pos[m2], q2 = pos[P + m2];
-        const T c1 = cs[m1], s1 = sn[m1], c2 = cs[m2], s2 = sn[m2];
-        const T b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
-        const T b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
-        const T r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
-        const T r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
-        const T o00 = c2 * r00 - s2 * r01;
-        T o01 = s2 * r00 + c2 * r01;
-        T o10 = c2 * r10 - s2 * r11;
-        const T o11 = s2 * r10 + c2 * r11;
-        if (m1 == m2) {
-          o01 = T(0);
-          o10 = T(0);
-        }
-        Hm[(size_t)p1 * m + p2] = o00;
-        Hm[(size_t)p1 * m + q2] = o01;
-        Hm[(size_t)q1 * m + p2] = o10;
-        Hm[(size_t)q1 * m + q2] = o11;
-        if (m1 != m2) {
-          Hm[(size_t)p2 * m + p1] = o00;
-          Hm[(size_t)q2 * m + p1] = o01;
-          Hm[(size_t)p2 * m + q1] = o10;
-          Hm[(size_t)q2 * m + q1] = o11;
+      for (int m2 = warp; m2 < P; m2 += nw) {
+        const int p2 = pos[m2], q2 = pos[P + m2];
+        const T c2 = cs[m2], s2 = sn[m2];
+        for (int m1 = lane; m1 <= m2; m1 += 32) {
+          const int p1 = pos[m1], q1 = pos[P + m1];
+          const T c1 = cs[m1], s1 = sn[m1];
+          const T b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
+          const T b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
+          const T r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
+          const T r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
+          const T o00 = c2 * r00 - s2 * r01;
+          T o01 = s2 * r00 + c2 * r01;
+          T o10 = c2 * r10 - s2 * r11;
+          const T o11 = s2 * r10 + c2 * r11;
+          if (m1 == m2) {
+            o01 = T(0);
+            o10 = T(0);
+          }
+          Hm[(size_t)p1 * m + p2] = o00;
+          Hm[(size_t)p1 * m + q2] = o01;
+          Hm[(size_t)q1 * m + p2] = o10;
+          Hm[(size_t)q1 * m + q2] = o11;
+          if (m1 != m2) {
+            Hm[(size_t)p2 * m + p1] = o00;
+            Hm[(size_t)q2 * m + p1] = o01;
+            Hm[(size_t)p2 * m + q1] = o10;
+            Hm[(size_t)q2 * m + q1] = o11;
+          }
         }
       }
-      for (int t = tid; t < P * m; t += nt) {
-        const int q0 = t / m, j = t % m;
+      for (int q0 = warp; q0 < P; q0 += nw) {
         const int p = pos[q0], q = pos[P + q0];
         const T c_ = cs[q0], s_ = sn[q0];
-        const T hp = QT[(size_t)p * m + j], hq = QT[(size_t)q * m + j];
-        QT[(size_t)p * m + j] = c_ * hp - s_ * hq;
-        QT[(size_t)q * m + j] = s_ * hp + c_ * hq;
+        T* rp = QT + (size_t)p * m;
+        T* rq = QT + (size_t)q * m;
+        for (int j = lane; j < m; j += 32) {
+          const T hp = rp[j], hq = rq[j];
+          rp[j] = c_ * hp - s_ * hq;
+          rq[j] = s_ * hp + c_ * hq;
+        }
       }
       __syncthreads();
     }

@@ -345,9 +345,8 @@ __device__ void gj_inverse_df(float4* G, int Mr, int n2, int* status, GJShared& 
       const double m = pv.x * pv.x + pv.y * pv.y;
       if (!(m > 0.0)) *status = 1;
       sh.logdet += 0.5 * log(m > 0.0 ? m : 1e-300);
-      // 1 / pivot, split: in f4[Mr] (no row index reaches Mr)
       const double2 inv = m > 0.0 ? make_double2(pv.x / m, -pv.y / m) : make_double2(0.0, 0.0);
-      f4[kGJMaxModes - 1] = df_csplit(inv);
+      sh.inv4 = df_csplit(inv);  // 1 / pivot
       if (i0 != col) {
         const int t = sh.orig[i0];
         sh.orig[i0] = sh.orig[col];

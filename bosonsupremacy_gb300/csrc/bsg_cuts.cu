@@ -66,8 +66,9 @@ __device__ double block_sum(double v, double* red) {
   return red[32];
 }
 
-// Cyclic Jacobi on the symmetric m x m matrix Hm (shared or global memory),
-// rows of QT accumulating the eigenvectors (QT <- J^T QT).  Round-robin
+// Cyclic Jacobi on the symmetric m x m matrix Hm (shared or global memory;
+// row stride ld, odd in shared memory so that the scattered rows of a
+// rotation round fall in different banks), rows of QT accumulating the eigenvectors (QT <- J^T QT).  Round-robin
 // order: n/2 disjoint rotations per step, each updating whole 2x2 blocks of
 // J1^T B J2 (and the transposed block), so a step needs two barriers.  The
 // rotation angles and the convergence sums run in T (FP32 for the FP32
@@ -75,14 +76,15 @@ __device__ double block_sum(double v, double* red) {
 // columns, so no thread divides an index.  Returns the number of sweeps, or
 // -1 if max_sweeps did not converge.
 template <class T>
-__device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, double* red, T* cs, T* sn, int* pos) {
+__device__ __noinline__ int block_jacobi(T* Hm, int m, int ld, T* QT, int max_sweeps, double tol, double* red, T* cs, T* sn,
+                                         int* pos) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int P = m / 2;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     T off = T(0), dia = T(0);
     for (int i = warp; i < m; i += nw)
       for (int j = lane; j < m; j += 32) {
-        const T h = Hm[(size_t)i * m + j];
+        const T h = Hm[(size_t)i * ld + j];
         if (i < j) off += h * h;
         else if (i == j) dia += h * h;
       }
@@ -99,10 +101,10 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
           p = q;
           q = x;
         }
-        const T hpq = Hm[(size_t)p * m + q];
+        const T hpq = Hm[(size_t)p * ld + q];
         const T skip = sizeof(T) == 8 ? T(1e-17) : T(1e-8);
         T c_ = T(1), s_ = T(0);
-        const T hpp = Hm[(size_t)p * m + p], hqq = Hm[(size_t)q * m + q];
+        const T hpp = Hm[(size_t)p * ld + p], hqq = Hm[(size_t)q * ld + q];
         if (fabs(hpq) > T(1e-30) && fabs(hpq) > skip * sqrt(fabs(hpp * hqq))) {
           const T th = (hqq - hpp) / (T(2) * hpq);
           const T tt = (th >= T(0) ? T(1) : T(-1)) / (fabs(th) + sqrt(th * th + T(1)));
@@ -122,8 +124,8 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
         for (int m1 = lane; m1 <= m2; m1 += 32) {
           const int p1 = pos[m1], q1 = pos[P + m1];
           const T c1 = cs[m1], s1 = sn[m1];
-          const T b00 = Hm[(size_t)p1 * m + p2], b01 = Hm[(size_t)p1 * m + q2];
-          const T b10 = Hm[(size_t)q1 * m + p2], b11 = Hm[(size_t)q1 * m + q2];
+          const T b00 = Hm[(size_t)p1 * ld + p2], b01 = Hm[(size_t)p1 * ld + q2];
+          const T b10 = Hm[(size_t)q1 * ld + p2], b11 = Hm[(size_t)q1 * ld + q2];
           const T r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
           const T r10 = s1 * b00 + c1 * b10, r11 = s1 * b01 + c1 * b11;
           const T o00 = c2 * r00 - s2 * r01;
@@ -134,15 +136,15 @@ __device__ int block_jacobi(T* Hm, int m, T* QT, int max_sweeps, double tol, dou
             o01 = T(0);
             o10 = T(0);
           }
-          Hm[(size_t)p1 * m + p2] = o00;
-          Hm[(size_t)p1 * m + q2] = o01;
-          Hm[(size_t)q1 * m + p2] = o10;
-          Hm[(size_t)q1 * m + q2] = o11;
+          Hm[(size_t)p1 * ld + p2] = o00;
+          Hm[(size_t)p1 * ld + q2] = o01;
+          Hm[(size_t)q1 * ld + p2] = o10;
+          Hm[(size_t)q1 * ld + q2] = o11;
           if (m1 != m2) {
-            Hm[(size_t)p2 * m + p1] = o00;
-            Hm[(size_t)q2 * m + p1] = o01;
-            Hm[(size_t)p2 * m + q1] = o10;
-            Hm[(size_t)q2 * m + q1] = o11;
+            Hm[(size_t)p2 * ld + p1] = o00;
+            Hm[(size_t)q2 * ld + p1] = o01;
+            Hm[(size_t)p2 * ld + q1] = o10;
+            Hm[(size_t)q2 * ld + q1] = o11;
           }
         }
       }
@@ -305,7 +307,7 @@ __device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, cons
 // eigenvalues (the rest of Hm is overwritten).  s1, s2, s3: m*m doubles of
 // scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
 // the start tolerance of the refinement.
-__device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
+__device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
                             double* cs, double* sn, int* pos, float* jsm, float2* dft,
                             unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -313,16 +315,19 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
   // the FP32 copies: in shared memory when the launch reserved room for them
   // (the rotation rounds touch scattered rows and columns), else in s1
   float* H32 = jsm ? jsm : reinterpret_cast<float*>(s1);
-  float* Q32 = H32 + mm;  // 2 m^2 floats
-  for (size_t t = tid; t < mm; t += nt) {
-    H32[t] = float(Hm[t]);
-    Q32[t] = (t / m == t % m) ? 1.f : 0.f;
-  }
+  const int ld = jsm ? m + 1 : m;  // s1 holds 2 m^2 floats
+  float* Q32 = H32 + (size_t)m * ld;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int i = warp; i < m; i += nw)
+    for (int j = lane; j < m; j += 32) {
+      H32[(size_t)i * ld + j] = float(Hm[(size_t)i * m + j]);
+      Q32[(size_t)i * m + j] = i == j ? 1.f : 0.f;
+    }
   __syncthreads();
   unsigned long long t32 = 0;
   if (sweep_log && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t32));
   const int sw32 =
-      block_jacobi<float>(H32, m, Q32, 24, 1e-10, red, reinterpret_cast<float*>(cs), reinterpret_cast<float*>(sn), pos);
+      block_jacobi<float>(H32, m, ld, Q32, 24, 1e-10, red, reinterpret_cast<float*>(cs), reinterpret_cast<float*>(sn), pos);
   if (sweep_log && tid == 0) {
     unsigned long long t1;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
@@ -352,12 +357,13 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     for (int i = tid; i < m; i += nt) lam[i] = s3[(size_t)i * m + i] / (1.0 - s1[(size_t)i * m + i]);
     __syncthreads();
     double so = 0.0, rr = 0.0;
-    for (size_t t = tid; t < mm; t += nt) {
-      const int i = int(t / m), j = int(t % m);
-      const double d = s3[t] - (i == j ? lam[i] : 0.0);
-      so += d * d;
-      rr += s1[t] * s1[t];
-    }
+    for (int i = warp; i < m; i += nw)
+      for (int j = lane; j < m; j += 32) {
+        const size_t t = (size_t)i * m + j;
+        const double d = s3[t] - (i == j ? lam[i] : 0.0);
+        so += d * d;
+        rr += s1[t] * s1[t];
+      }
     so = block_sum(so, red);
     rr = block_sum(rr, red);
     const double delta = 2.0 * (sqrt(so) + anorm * sqrt(rr));
@@ -366,15 +372,16 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     // an exactly degenerate pair, about gap x mixing for distinct eigenvalues
     // the clustering leaves unresolved
     double emax = 0.0, cnum = 0.0;
-    for (size_t t = tid; t < mm; t += nt) {
-      const int i = int(t / m), j = int(t % m);
-      const double r = s1[t], gap = lam[j] - lam[i];
-      const bool sep = i != j && fabs(gap) > delta;
-      const double e = sep ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
-      s1[t] = e;
-      if (i != j) emax = fmax(emax, fabs(e));
-      if (i != j && !sep) cnum = fmax(cnum, fabs(s3[t] + lam[j] * r));
-    }
+    for (int i = warp; i < m; i += nw)
+      for (int j = lane; j < m; j += 32) {
+        const size_t t = (size_t)i * m + j;
+        const double r = s1[t], gap = lam[j] - lam[i];
+        const bool sep = i != j && fabs(gap) > delta;
+        const double e = sep ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
+        s1[t] = e;
+        if (i != j) emax = fmax(emax, fabs(e));
+        if (i != j && !sep) cnum = fmax(cnum, fabs(s3[t] + lam[j] * r));
+      }
     emax = block_max(emax, red);
     cnum = block_max(cnum, red);
     // s2 = QT + E^T QT, then QT = s2
@@ -398,7 +405,7 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
     // which resolve any gap above the FP64 rounding of Hm.
     for (size_t t = tid; t < mm; t += nt) QT[t] = (t / m == t % m) ? 1.0 : 0.0;
     __syncthreads();
-    const int sw64 = block_jacobi<double>(Hm, m, QT, 60, 1e-26, red, cs, sn, pos);
+    const int sw64 = block_jacobi<double>(Hm, m, m, QT, 60, 1e-26, red, cs, sn, pos);
     if (sweep_log && tid == 0) {
       sweep_log[0] = (unsigned long long)(sw32 < 0 ? 99 : sw32);
       sweep_log[1] = 100 + (unsigned long long)(sw64 < 0 ? 99 : sw64);  // 100 + FP64 sweeps: the restart
@@ -416,33 +423,40 @@ __device__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s
 }
 
 // In-place right-looking Cholesky of the m x m SPD matrix X (lower triangle,
-// upper zeroed).  Returns false if a pivot is not positive.
-__device__ bool block_cholesky(double* X, int m, int* s_flag, double* s_scalar) {
-  const int tid = threadIdx.x, nt = blockDim.x;
+// upper zeroed).  dinv, col: m doubles of shared memory each; dinv receives
+// 1 / L_jj, col holds the scaled column of the current step, which the
+// trailing update reads (warps take its rows, lanes their columns).
+// Returns false if a pivot is not positive.
+__device__ __noinline__ bool block_cholesky(double* X, int m, int* s_flag, double* dinv, double* col) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   if (tid == 0) *s_flag = 0;
   __syncthreads();
   for (int j = 0; j < m; ++j) {
     if (tid == 0) {
       const double djj = X[(size_t)j * m + j];
       if (!(djj > 0.0)) *s_flag = 1;
-      *s_scalar = djj > 0.0 ? sqrt(djj) : 1.0;
-      X[(size_t)j * m + j] = *s_scalar;
+      const double d = djj > 0.0 ? sqrt(djj) : 1.0;
+      X[(size_t)j * m + j] = d;
+      dinv[j] = 1.0 / d;
     }
     __syncthreads();
     if (*s_flag) return false;
-    const double dj = *s_scalar;
-    for (int i = j + 1 + tid; i < m; i += nt) X[(size_t)i * m + j] /= dj;
+    const double inv = dinv[j];
+    for (int i = j + 1 + tid; i < m; i += nt) {
+      const double v = X[(size_t)i * m + j] * inv;
+      X[(size_t)i * m + j] = v;
+      col[i] = v;
+    }
     __syncthreads();
-    const int r = m - j - 1;
-    for (size_t t = tid; t < (size_t)r * r; t += nt) {
-      const int i = j + 1 + int(t / r), l = j + 1 + int(t % r);
-      if (l > i) continue;
-      X[(size_t)i * m + l] -= X[(size_t)i * m + j] * X[(size_t)l * m + j];
+    for (int i = j + 1 + warp; i < m; i += nw) {
+      const double xij = col[i];
+      double* row = X + (size_t)i * m;
+      for (int l = j + 1 + lane; l <= i; l += 32) row[l] -= xij * col[l];
     }
     __syncthreads();
   }
-  for (size_t t = tid; t < (size_t)m * m; t += nt)
-    if (int(t % m) > int(t / m)) X[t] = 0.0;
+  for (int i = warp; i < m; i += nw)
+    for (int l = i + 1 + lane; l < m; l += 32) X[(size_t)i * m + l] = 0.0;
   __syncthreads();
   return true;
 }
@@ -480,7 +494,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n (also Householder taus)
   double* vec = dots + 2 * kMaxCutModes;                               // n
   double* vec2 = vec + 2 * kMaxCutModes;                               // n
-  // double-float product tiles, then the FP32 Jacobi matrices (2 m^2 floats)
+  // double-float product tiles, then the FP32 Jacobi matrices (m (2m + 1) floats)
   // when the launch reserved them
   float2* dft = reinterpret_cast<float2*>(vec2 + 2 * kMaxCutModes);
   float* jsm = a.jac_smem_m > 0 ? reinterpret_cast<float*>(reinterpret_cast<char*>(dft) + kDfSmemBytes) : nullptr;
@@ -505,22 +519,26 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   }
   phase_stamp(a, c, 1);
   // 2. Cholesky V = L L^T
-  if (!block_cholesky(A, n, &s_flag, &s_scalar)) {
+  if (!block_cholesky(A, n, &s_flag, vec, vec2)) {
     if (tid == 0) a.status[c] = 2;
     return;
   }
   phase_stamp(a, c, 2);
-  // 3. W = L^{-1}: forward substitution on all columns, row by row
-  for (size_t i = tid; i < nn; i += nt) W[i] = (i / n == i % n) ? 1.0 : 0.0;
+  // 3. W = L^{-1}: forward substitution on all columns, row by row (1 / L_rr
+  // in vec from the Cholesky; warps take rows, lanes columns)
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int i = warp; i < n; i += nw)
+    for (int q = lane; q < n; q += 32) W[(size_t)i * n + q] = i == q ? 1.0 : 0.0;
   __syncthreads();
   for (int r = 0; r < n; ++r) {
-    const double inv = 1.0 / A[(size_t)r * n + r];
+    const double inv = vec[r];
     for (int q = tid; q <= r; q += nt) W[(size_t)r * n + q] *= inv;
     __syncthreads();
-    const int m = n - r - 1;
-    for (size_t t = tid; t < (size_t)m * (r + 1); t += nt) {
-      const int i = r + 1 + int(t / (r + 1)), q = int(t % (r + 1));
-      W[(size_t)i * n + q] -= A[(size_t)i * n + r] * W[(size_t)r * n + q];
+    const double* wr = W + (size_t)r * n;
+    for (int i = r + 1 + warp; i < n; i += nw) {
+      const double lir = A[(size_t)i * n + r];
+      double* wi = W + (size_t)i * n;
+      for (int q = lane; q <= r; q += 32) wi[q] -= lir * wr[q];
     }
     __syncthreads();
   }
@@ -531,25 +549,18 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   const bool g_dense = nA >= n;
   double* EV = g_dense ? W : X1;  // eigenvector rows of H
   if (g_dense) {
-    // G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r]
-    for (size_t t = tid; t < nn; t += nt) {
-      const int i = int(t / n), j = int(t % n);
-      double s = 0.0;
-      for (int r = 0; r < k; ++r)
-        s += W[(size_t)i * n + r] * W[(size_t)j * n + r + k] - W[(size_t)i * n + r + k] * W[(size_t)j * n + r];
-      Gm[t] = s;
-    }
+    // G[i][j] = sum_{r<k} W[i][r] W[j][r+k] - W[i][r+k] W[j][r] = sum_q W[i][q] Wp[j][q]
+    // with Wp[j][q] = (Omega W^T)[q][j] = q < k ? W[j][q+k] : -W[j][q-k] (in X1),
+    // a double-float product
+    for (int i = warp; i < n; i += nw)
+      for (int q = lane; q < n; q += 32)
+        X1[(size_t)i * n + q] = q < k ? W[(size_t)i * n + q + k] : -W[(size_t)i * n + q - k];
     __syncthreads();
+    df_gemm(W, false, X1, true, nullptr, 1.0, 0.0, Gm, n, false, dft);
     phase_stamp(a, c, 4);
-    // 5a. full path: H = G^T G, Jacobi with eigenvector rows in W
-    for (size_t t = tid; t < nn; t += nt) {
-      const int i = int(t / n), j = int(t % n);
-      double s = 0.0;
-#pragma unroll 8
-      for (int r = 0; r < n; ++r) s += Gm[(size_t)r * n + i] * Gm[(size_t)r * n + j];
-      H[t] = s;
-    }
-    __syncthreads();
+    // 5a. full path: H = G^T G (double-float, symmetric), Jacobi with
+    // eigenvector rows in W
+    df_gemm(Gm, true, Gm, false, nullptr, 1.0, 0.0, H, n, true, dft);
     phase_stamp(a, c, 5);
     sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
@@ -571,19 +582,20 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       X2[t] = a.sq_cov[(size_t)gA(r) * (2 * M) + gidx(q)];  // C [nA, n]
     }
     __syncthreads();
-    if (!block_cholesky(X1, nA, &s_flag, &s_scalar)) {
+    if (!block_cholesky(X1, nA, &s_flag, vec, vec2)) {
       if (tid == 0) a.status[c] = 2;
       return;
     }
-    // X2 <- L_A^{-1} C (forward substitution over rows)
+    // X2 <- L_A^{-1} C (forward substitution over rows; 1 / L_A,rr in vec)
     for (int r = 0; r < nA; ++r) {
-      const double inv = 1.0 / X1[(size_t)r * nA + r];
+      const double inv = vec[r];
       for (int q = tid; q < n; q += nt) X2[(size_t)r * n + q] *= inv;
       __syncthreads();
-      const int m = nA - r - 1;
-      for (size_t t = tid; t < (size_t)m * n; t += nt) {
-        const int i = r + 1 + int(t / n), q = int(t % n);
-        X2[(size_t)i * n + q] -= X1[(size_t)i * nA + r] * X2[(size_t)r * n + q];
+      const double* xr = X2 + (size_t)r * n;
+      for (int i = r + 1 + warp; i < nA; i += nw) {
+        const double l = X1[(size_t)i * nA + r];
+        double* xi = X2 + (size_t)i * n;
+        for (int q = lane; q < n; q += 32) xi[q] -= l * xr[q];
       }
       __syncthreads();
     }
@@ -698,101 +710,119 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   // dimension (e.g. the nu = 1 vacuum modes) is always completed.  The
   // candidates' squared residuals are tracked in FP32 by subtraction (pivot
   // choice only); the chosen FP64 eigenvector (not its FP32 copy) is cleaned
-  // by one FP64 projection against the accepted vectors of the cluster.
+  // by one projection against the accepted vectors of the cluster.  The
+  // products (projections, G x, norms) run in double-float on the FP32 pipe:
+  // the accepted vectors are kept as FP32 pairs and the operator of G x (G,
+  // or W = L^{-1} in the low-rank path) is split once; S below reads the
+  // vectors back in FP64.
   // 1/nu of each pair is |G x| (x a unit eigenvector: |G x|^2 = mu).
-  double* Xacc = H;  // accepted vectors as rows
+  float2* Xacc2 = reinterpret_cast<float2*>(H);        // accepted vectors as rows
   float* c32 = reinterpret_cast<float*>(X2 + nn);       // FP32 candidates of the cluster
   float* r32 = reinterpret_cast<float*>(X2 + 2 * nn);   // their squared residuals
   float* xy32 = r32 + n;                                 // FP32 copies of x and y
-  double* tv = X2;                                       // 2n doubles: W^T x and Omega W^T x
+  float2* tv = reinterpret_cast<float2*>(X2);           // 2n: W^T x and Omega W^T x
+  float2* dots2 = reinterpret_cast<float2*>(dots);      // projection coefficients (negated)
   // The triangular W^T x and the projection update are sums per output of up
   // to n terms: with one thread per output only n of the CTA's threads would
   // work, so each sum is split into `segs` ranges whose partial sums (part,
-  // segs x n doubles after tv in X2) are added in range order.
+  // segs x n pairs after tv in X2) are added in range order.
   const int segs = n >= 6 ? max(1, min(4, nt / n)) : 1;
-  double* part = X2 + 2 * (size_t)n;
+  float2* part = tv + 2 * (size_t)n;
+  // the operator of G x, split once: G in place (full path) or W into Gm
+  // (free in the low-rank path)
+  float2* Gop = reinterpret_cast<float2*>(Gm);
+  {
+    const double* src = g_dense ? Gm : W;
+    for (size_t t = tid; t < nn; t += nt) Gop[t] = df_split(src[t]);  // in place: one element per thread
+  }
   for (int i = tid; i < n; i += nt) vec2[i] = MU[order[i]];
   __syncthreads();
   int* used = reinterpret_cast<int*>(vec);  // n flags (vec reused as int storage)
   for (int i = tid; i < n; i += nt) used[i] = 0;
   __syncthreads();
   // y = G x with G = W Omega W^T
-  auto apply_G = [&](const double* x, double* y) {
+  auto apply_G = [&](const float2* x, float2* y) {
     if (g_dense) {
-      for (int i = tid >> 5; i < n; i += nt >> 5) {
-        double s = 0.0;
-        for (int j = tid & 31; j < n; j += 32) s = fma(Gm[(size_t)i * n + j], x[j], s);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((tid & 31) == 0) y[i] = s;
+      for (int i = warp; i < n; i += nw) {
+        float s = 0.f, t = 0.f;
+        for (int j = lane; j < n; j += 32) df_mac(s, t, Gop[(size_t)i * n + j], x[j]);
+        df_warp_sum(s, t);
+        if (lane == 0) y[i] = df_norm(s, t);
       }
     } else {
       for (int u = tid; u < n * segs; u += nt) {  // t = W^T x (W lower triangular)
         const int j = u % n, g = u / n;
         const int len = (n - j + segs - 1) / segs, i0 = j + g * len, i1 = min(n, i0 + len);
-        double s = 0.0;
-        // unrolled: the FMA chain is serial, so the loads of the next 8
-        // terms must be in flight (the workspace lives in L2 / DRAM while the
-        // DP runs)
+        float s = 0.f, t = 0.f;
 #pragma unroll 8
-        for (int i = i0; i < i1; ++i) s = fma(W[(size_t)i * n + j], x[i], s);
-        if (segs == 1) tv[j] = s;
-        else part[(size_t)g * n + j] = s;
+        for (int i = i0; i < i1; ++i) df_mac(s, t, Gop[(size_t)i * n + j], x[i]);
+        if (segs == 1) tv[j] = df_norm(s, t);
+        else part[(size_t)g * n + j] = df_norm(s, t);
       }
       __syncthreads();
       if (segs > 1) {
         for (int j = tid; j < n; j += nt) {
-          double s = part[j];
-          for (int g = 1; g < segs; ++g) s += part[(size_t)g * n + j];
+          float2 s = part[j];
+          for (int g = 1; g < segs; ++g) s = df_add(s, part[(size_t)g * n + j]);
           tv[j] = s;
         }
         __syncthreads();
       }
-      for (int j = tid; j < n; j += nt) tv[n + j] = j < k ? tv[j + k] : -tv[j - k];  // Omega t
+      for (int j = tid; j < n; j += nt) {  // Omega t
+        const float2 v = j < k ? tv[j + k] : tv[j - k];
+        tv[n + j] = j < k ? v : make_float2(-v.x, -v.y);
+      }
       __syncthreads();
-      for (int i = tid >> 5; i < n; i += nt >> 5) {  // y = W (Omega t)
-        double s = 0.0;
-        for (int j = tid & 31; j <= i; j += 32) s = fma(W[(size_t)i * n + j], tv[n + j], s);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((tid & 31) == 0) y[i] = s;
+      for (int i = warp; i < n; i += nw) {  // y = W (Omega t)
+        float s = 0.f, t = 0.f;
+        for (int j = lane; j <= i; j += 32) df_mac(s, t, Gop[(size_t)i * n + j], tv[n + j]);
+        df_warp_sum(s, t);
+        if (lane == 0) y[i] = df_norm(s, t);
       }
     }
     __syncthreads();
   };
   // v -= sum over accepted rows [a0, a1) of (row . v) row, one pass
-  auto project_out = [&](double* v, int a0, int a1) {
-    for (int t = tid; t < (a1 - a0) * 32; t += nt) {
-      const int av = a0 + (t >> 5);
-      double s = 0.0;
-      for (int i = t & 31; i < n; i += 32) s = fma(Xacc[(size_t)av * n + i], v[i], s);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if ((t & 31) == 0) dots[av - a0] = s;
+  auto project_out = [&](float2* v, int a0, int a1) {
+    for (int t0 = tid; t0 < (a1 - a0) * 32; t0 += nt) {  // one warp per accepted row
+      const int av = a0 + (t0 >> 5);
+      float s = 0.f, t = 0.f;
+      for (int i = t0 & 31; i < n; i += 32) df_mac(s, t, Xacc2[(size_t)av * n + i], v[i]);
+      df_warp_sum(s, t);
+      if ((t0 & 31) == 0) dots2[av - a0] = df_norm(-s, -t);
     }
     __syncthreads();
     if (segs == 1) {
       for (int i = tid; i < n; i += nt) {
-        double s = v[i];
+        float s = v[i].x, t = v[i].y;
 #pragma unroll 8
-        for (int av = a0; av < a1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
-        v[i] = s;
+        for (int av = a0; av < a1; ++av) df_mac(s, t, dots2[av - a0], Xacc2[(size_t)av * n + i]);
+        v[i] = df_norm(s, t);
       }
     } else {
       const int len = (a1 - a0 + segs - 1) / segs;
       for (int u = tid; u < n * segs; u += nt) {
         const int i = u % n, g = u / n;
         const int b0 = a0 + g * len, b1 = min(a1, b0 + len);
-        double s = 0.0;
+        float s = 0.f, t = 0.f;
 #pragma unroll 8
-        for (int av = b0; av < b1; ++av) s = fma(-dots[av - a0], Xacc[(size_t)av * n + i], s);
-        part[(size_t)g * n + i] = s;
+        for (int av = b0; av < b1; ++av) df_mac(s, t, dots2[av - a0], Xacc2[(size_t)av * n + i]);
+        part[(size_t)g * n + i] = df_norm(s, t);
       }
       __syncthreads();
       for (int i = tid; i < n; i += nt) {
-        double s = v[i];
-        for (int g = 0; g < segs; ++g) s += part[(size_t)g * n + i];
+        float2 s = v[i];
+        for (int g = 0; g < segs; ++g) s = df_add(s, part[(size_t)g * n + i]);
         v[i] = s;
       }
     }
     __syncthreads();
+  };
+  // |v|^2 over the block (FP64 total of the threads' double-float sums)
+  auto norm2 = [&](const float2* v) {
+    float s = 0.f, t = 0.f;
+    for (int i = tid; i < n; i += nt) df_mac(s, t, v[i], v[i]);
+    return block_sum(double(s) + double(t), red);
   };
   int acc = 0;
   int cb = 0;
@@ -843,19 +873,16 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
         if (tid == 0) a.status[c] = 4;
         return;
       }
-      double* x = Xacc + (size_t)acc * n;
-      double* y = Xacc + (size_t)(acc + 1) * n;
+      float2* x = Xacc2 + (size_t)acc * n;
+      float2* y = Xacc2 + (size_t)(acc + 1) * n;
       // x: the FP64 eigenvector itself (an FP32-rounded copy would leave the
       // eigenspace by ~1e-7), one projection pass (its residual is the
       // largest of the cluster, so one pass keeps orthogonality at rounding)
-      for (int i = tid; i < n; i += nt) x[i] = EV[(size_t)order[cb + best] * n + i];
+      for (int i = tid; i < n; i += nt) x[i] = df_split(EV[(size_t)order[cb + best] * n + i]);
       __syncthreads();
       project_out(x, acc0, acc);
-      double nx = 0.0;
-      for (int i = tid; i < n; i += nt) nx += x[i] * x[i];
-      nx = block_sum(nx, red);
-      const double ix = 1.0 / sqrt(nx);
-      for (int i = tid; i < n; i += nt) x[i] *= ix;
+      const float2 ix = df_split(1.0 / sqrt(norm2(x)));
+      for (int i = tid; i < n; i += nt) x[i] = df_mul(x[i], ix);
       __syncthreads();
       // y = G x / |G x| needs no projection: G maps the span of the accepted
       // pairs into itself (G x_j = |G x_j| y_j, G y_j = -|G x_j| x_j for
@@ -863,17 +890,13 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       // orthogonal to it up to rounding (checked to 1e-10 on every kind of
       // cut by the symplectic tests)
       apply_G(x, y);
-      double gx = 0.0;
-      for (int i = tid; i < n; i += nt) gx += y[i] * y[i];
-      gx = block_sum(gx, red);  // |G x|^2 = 1/nu^2
-      double ny = 0.0;
-      for (int i = tid; i < n; i += nt) ny += y[i] * y[i];
-      ny = block_sum(ny, red);
-      const double iy = ny > 0.0 ? 1.0 / sqrt(ny) : 0.0;
+      const double gx = norm2(y);  // |G x|^2 = 1/nu^2
+      const float2 iy = df_split(gx > 0.0 ? 1.0 / sqrt(gx) : 0.0);
       for (int i = tid; i < n; i += nt) {
-        y[i] *= iy;
-        xy32[i] = float(x[i]);
-        xy32[n + i] = float(y[i] );
+        const float2 yi = df_mul(y[i], iy);
+        y[i] = yi;
+        xy32[i] = x[i].x;
+        xy32[n + i] = yi.x;
       }
       // 1/nu of pair acc/2 (MU no longer needed by candidates): |G x| in the
       // full path; in the low-rank path the eigenvalue of K = I - R R^T
@@ -908,6 +931,10 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     if (tid == 0) a.status[c] = 4;
     return;
   }
+  // the accepted vectors back to FP64 for S (in place: one element per thread)
+  double* Xacc = H;
+  for (size_t t = tid; t < nn; t += nt) Xacc[t] = df_val(Xacc2[t]);
+  __syncthreads();
   phase_stamp(a, c, 9);
   // 9. S = L [y | x] nu^{-1/2}, nbar = max(0, (nu - 1)/2)
   for (int pi = 0; pi < k; ++pi) {
@@ -1164,7 +1191,7 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
   }
   int smem_optin = 0;
   BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-  const size_t jac = (size_t)2 * m_max * m_max * sizeof(float);
+  const size_t jac = (size_t)m_max * (2 * m_max + 1) * sizeof(float);
   a.jac_smem_m = 0;
   if (wsm + jac <= (size_t)smem_optin) {
     a.jac_smem_m = m_max;
@@ -1182,7 +1209,7 @@ static int williamson_smem(bsg_handle_t h, int m_max, size_t* wsm, int* jac_m) {
   *wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8 + kDfSmemBytes;
   int smem_optin = 0;
   BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-  const size_t jac = (size_t)2 * m_max * m_max * sizeof(float);
+  const size_t jac = (size_t)m_max * (2 * m_max + 1) * sizeof(float);
   *jac_m = 0;
   if (*wsm + jac <= (size_t)smem_optin) {
     *jac_m = m_max;

@@ -46,4 +46,40 @@ __device__ __forceinline__ void df_mac(float& s, float& t, float2 a, float2 b) {
   s = u;
 }
 
+// s + t renormalised to hi + lo (Knuth's two-sum)
+__device__ __forceinline__ float2 df_norm(float s, float t) {
+  const float h = s + t;
+  const float bb = h - s;
+  return make_float2(h, (s - (h - bb)) + (t - bb));
+}
+
+// a + b, renormalised
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = a.x + b.x;
+  const float bb = s - a.x;
+  const float e = (a.x - (s - bb)) + (b.x - bb);
+  return df_norm(s, e + (a.y + b.y));
+}
+
+// a b, renormalised
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  float s = 0.f, t = 0.f;
+  df_mac(s, t, a, b);
+  return df_norm(s, t);
+}
+
+__device__ __forceinline__ double df_val(float2 a) { return double(a.x) + double(a.y); }
+
+// (s, t) summed over the warp (every lane gets the sum)
+__device__ __forceinline__ void df_warp_sum(float& s, float& t) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    const float t2 = __shfl_xor_sync(0xffffffffu, t, o);
+    const float u = s + s2;
+    const float bb = u - s;
+    t += t2 + ((s - (u - bb)) + (s2 - bb));
+    s = u;
+  }
+}
+
 }  // namespace bsg

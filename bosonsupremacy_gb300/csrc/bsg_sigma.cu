@@ -277,11 +277,6 @@ __global__ void sigma_linv_kernel(const SigmaJob* __restrict__ jobs) {
 // Double-float complex entries of the Gauss-Jordan matrix: (re s, re t,
 // im s, im t), value s + t per part; s + t is renormalised to hi + lo on
 // every store (Knuth's two-sum).
-__device__ __forceinline__ float2 df_norm(float s, float t) {
-  const float h = s + t;
-  const float bb = h - s;
-  return make_float2(h, (s - (h - bb)) + (t - bb));
-}
 __device__ __forceinline__ float4 df_cnorm(float4 v) {
   const float2 r = df_norm(v.x, v.y), i = df_norm(v.z, v.w);
   return make_float4(r.x, r.y, i.x, i.y);

@@ -176,7 +176,8 @@ __device__ __noinline__ int block_jacobi(T* Hm, int m, int ld, T* QT, int max_sw
 // what the refinement needs to stop (corrections <= 1e-8, clustered
 // numerators <= 1e-12 of the norm).
 constexpr int kDfTile = 32;
-constexpr size_t kDfSmemBytes = 2 * kDfTile * (kDfTile + 1) * sizeof(float2);
+constexpr int kDfLd = kDfTile + 2;  // float2 row stride of the tiles (16-byte aligned rows)
+constexpr size_t kDfSmemBytes = 2 * kDfTile * kDfLd * sizeof(float2);
 
 // C[i][j] = add[i][j] + sign * sum_q A(i, q) B(q, j) (+ diag where i == j),
 // all m x m row-major, A(i, q) = ta ? A[q][i] : A[i][q], B(q, j) = tb ? B[j][q]
@@ -184,109 +185,137 @@ constexpr size_t kDfSmemBytes = 2 * kDfTile * (kDfTile + 1) * sizeof(float2);
 // diagonal are computed and mirrored.  C must not alias A, B or add unless
 // add == C (each entry of C is read before it is written, by the same
 // thread).  tiles: kDfSmemBytes of shared memory.  Block-wide (barriers).
-// PER: outputs per thread (1024, 512 or 256 threads)
-template <int PER>
+// NT threads (256, 512 or 1024): 32 x 32 output tiles, each thread a 2 x 2
+// block of one of NT / 256 K groups (so every shared-memory load feeds two
+// products and four accumulations run side by side); the groups' partial
+// sums are added in a tree through shared memory at the end of a tile.
+template <int NT>
 __device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B, bool tb, const double* add,
                                        double sign, double diag, double* C, int m, bool sym, float2* tiles) {
-  float2 (*As)[kDfTile + 1] = reinterpret_cast<float2 (*)[kDfTile + 1]>(tiles);
-  float2 (*Bs)[kDfTile + 1] = reinterpret_cast<float2 (*)[kDfTile + 1]>(tiles + kDfTile * (kDfTile + 1));
-  const int tid = threadIdx.x, nt = blockDim.x;
-  constexpr int kOut = kDfTile * kDfTile;
+  constexpr int G = NT / 256, KG = kDfTile / G, PER = kDfTile * kDfTile / NT;
+  float2 (*As)[kDfLd] = reinterpret_cast<float2 (*)[kDfLd]>(tiles);  // [k][row]
+  float2 (*Bs)[kDfLd] = reinterpret_cast<float2 (*)[kDfLd]>(tiles + kDfTile * kDfLd);  // [k][col]
+  const int tid = threadIdx.x, g = tid >> 8, l = tid & 255, tx = l & 15, ty = l >> 4;
   const int nb = (m + kDfTile - 1) / kDfTile;
-  // element e of a tile: consecutive threads read consecutive addresses
-  // (the row index runs fastest for a transposed operand)
-  auto rc = [](bool tr, int e, int& r, int& c) {
-    if (tr) {
+  // element e of a chunk: (row or column r, k c), consecutive threads along
+  // the operand's contiguous index
+  auto a_at = [&](int ti, int q0, int e, int& r, int& c) {
+    if (ta) {
       r = e % kDfTile;
       c = e / kDfTile;
     } else {
       r = e / kDfTile;
       c = e % kDfTile;
     }
-  };
-  auto a_val = [&](int ti, int q0, int e) {
-    int r, c;
-    rc(ta, e, r, c);
     const int ai = ti * kDfTile + r, aq = q0 + c;
     if (ai >= m || aq >= m) return 0.0;
     return ta ? A[(size_t)aq * m + ai] : A[(size_t)ai * m + aq];
   };
-  auto b_val = [&](int tj, int q0, int e) {
-    int r, c;
-    rc(tb, e, r, c);
-    const int bq = q0 + r, bj = tj * kDfTile + c;
+  auto b_at = [&](int tj, int q0, int e, int& r, int& c) {
+    if (tb) {
+      c = e % kDfTile;
+      r = e / kDfTile;
+    } else {
+      c = e / kDfTile;
+      r = e % kDfTile;
+    }
+    const int bq = q0 + c, bj = tj * kDfTile + r;
     if (bq >= m || bj >= m) return 0.0;
     return tb ? B[(size_t)bj * m + bq] : B[(size_t)bq * m + bj];
   };
   for (int ti = 0; ti < nb; ++ti)
     for (int tj = sym ? ti : 0; tj < nb; ++tj) {
-      float s[PER], t[PER];
-#pragma unroll
-      for (int o = 0; o < PER; ++o) s[o] = t[o] = 0.f;
+      float s[4] = {0.f, 0.f, 0.f, 0.f}, t[4] = {0.f, 0.f, 0.f, 0.f};
       // the K chunk q0 is in registers while chunk q0 - 32 is multiplied
       double pa[PER], pb[PER];
+      int r, c;
 #pragma unroll
       for (int o = 0; o < PER; ++o) {
-        const int e = tid + o * nt;
-        pa[o] = (e < kOut) ? a_val(ti, 0, e) : 0.0;
-        pb[o] = (e < kOut) ? b_val(tj, 0, e) : 0.0;
+        pa[o] = a_at(ti, 0, tid + o * NT, r, c);
+        pb[o] = b_at(tj, 0, tid + o * NT, r, c);
       }
       for (int q0 = 0; q0 < m; q0 += kDfTile) {
 #pragma unroll
         for (int o = 0; o < PER; ++o) {
-          const int e = tid + o * nt;
-          if (e < kOut) {
-            int r, cc;
-            rc(ta, e, r, cc);
-            As[r][cc] = df_split(pa[o]);
-            rc(tb, e, r, cc);
-            Bs[r][cc] = df_split(pb[o]);
+          const int e = tid + o * NT;
+          if (ta) {
+            r = e % kDfTile;
+            c = e / kDfTile;
+          } else {
+            r = e / kDfTile;
+            c = e % kDfTile;
           }
+          As[c][r] = df_split(pa[o]);
+          if (tb) {
+            c = e % kDfTile;
+            r = e / kDfTile;
+          } else {
+            c = e / kDfTile;
+            r = e % kDfTile;
+          }
+          Bs[c][r] = df_split(pb[o]);
         }
         __syncthreads();
         if (q0 + kDfTile < m) {
 #pragma unroll
           for (int o = 0; o < PER; ++o) {
-            const int e = tid + o * nt;
-            if (e < kOut) {
-              pa[o] = a_val(ti, q0 + kDfTile, e);
-              pb[o] = b_val(tj, q0 + kDfTile, e);
-            }
+            pa[o] = a_at(ti, q0 + kDfTile, tid + o * NT, r, c);
+            pb[o] = b_at(tj, q0 + kDfTile, tid + o * NT, r, c);
           }
         }
 #pragma unroll
-        for (int o = 0; o < PER; ++o) {
-          const int e = tid + o * nt;
-          if (e < kOut) {
-            const int r = e / kDfTile, c = e % kDfTile;
-#pragma unroll 8
-            for (int q = 0; q < kDfTile; ++q) df_mac(s[o], t[o], As[r][q], Bs[q][c]);
-          }
+        for (int kk = g * KG; kk < (g + 1) * KG; ++kk) {
+          const float4 a = *reinterpret_cast<const float4*>(&As[kk][2 * ty]);
+          const float4 b = *reinterpret_cast<const float4*>(&Bs[kk][2 * tx]);
+          const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+          const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
+          df_mac(s[0], t[0], a0, b0);
+          df_mac(s[1], t[1], a0, b1);
+          df_mac(s[2], t[2], a1, b0);
+          df_mac(s[3], t[3], a1, b1);
         }
         __syncthreads();
       }
+      // K groups: tree sum through shared memory (the tiles are free now)
+      float2* red = tiles;
 #pragma unroll
-      for (int o = 0; o < PER; ++o) {
-        const int e = tid + o * nt;
-        if (e >= kOut) continue;
-        const int i = ti * kDfTile + e / kDfTile, j = tj * kDfTile + e % kDfTile;
-        if (i >= m || j >= m) continue;
-        double v = sign * (double(s[o]) + double(t[o]));
-        if (add) v += add[(size_t)i * m + j];
-        if (i == j) v += diag;
-        C[(size_t)i * m + j] = v;
-        // off-diagonal tiles are mirrored; a diagonal tile computes both halves itself
-        if (sym && tj != ti) C[(size_t)j * m + i] = v;
+      for (int step = G / 2; step >= 1; step /= 2) {
+        if (g >= step && g < 2 * step)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) red[((g - step) * 256 + l) * 4 + u] = df_norm(s[u], t[u]);
+        __syncthreads();
+        if (g < step)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float2 v = red[(g * 256 + l) * 4 + u];
+            const float w = s[u] + v.x;
+            const float bb = w - s[u];
+            t[u] += v.y + ((s[u] - (w - bb)) + (v.x - bb));
+            s[u] = w;
+          }
+        __syncthreads();
       }
+      if (g == 0)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = ti * kDfTile + 2 * ty + (u >> 1), j = tj * kDfTile + 2 * tx + (u & 1);
+          if (i >= m || j >= m) continue;
+          double v = sign * (double(s[u]) + double(t[u]));
+          if (add) v += add[(size_t)i * m + j];
+          if (i == j) v += diag;
+          C[(size_t)i * m + j] = v;
+          // off-diagonal tiles are mirrored; a diagonal tile computes both halves itself
+          if (sym && tj != ti) C[(size_t)j * m + i] = v;
+        }
     }
   __syncthreads();
 }
 
 __device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, const double* add, double sign,
                         double diag, double* C, int m, bool sym, float2* tiles) {
-  if (blockDim.x >= 1024) df_gemm_t<1>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
-  else if (blockDim.x >= 512) df_gemm_t<2>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
-  else df_gemm_t<4>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  if (blockDim.x >= 1024) df_gemm_t<1024>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  else if (blockDim.x >= 512) df_gemm_t<512>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  else df_gemm_t<256>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
 }
 
 // Mixed-precision symmetric eigen-decomposition of the m x m matrix Hm with
@@ -348,12 +377,22 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
   constexpr int kRefineMax = 8;
   int refined = 0;
   bool converged = false;
+  // profiling: time in the refinement's products and in the whole refinement
+  unsigned long long t_ref0 = 0, t_gemm = 0, t_g0 = 0;
+  auto stamp = [&]() {
+    unsigned long long t = 0;
+    if (sweep_log && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+  };
+  t_ref0 = stamp();
   for (int it = 0; it < kRefineMax; ++it) {
     // s2 = T = Hm QT^T, s1 = R = I - QT QT^T, s3 = S = QT T = QT Hm QT^T
     // (double-float products on the FP32 pipe; R and S symmetric)
+    t_g0 = stamp();
     df_gemm(Hm, false, QT, true, nullptr, 1.0, 0.0, s2, m, false, dft);
     df_gemm(QT, false, QT, true, nullptr, -1.0, 1.0, s1, m, true, dft);
     df_gemm(QT, false, s2, false, nullptr, 1.0, 0.0, s3, m, true, dft);
+    t_gemm += stamp() - t_g0;
     for (int i = tid; i < m; i += nt) lam[i] = s3[(size_t)i * m + i] / (1.0 - s1[(size_t)i * m + i]);
     __syncthreads();
     double so = 0.0, rr = 0.0;
@@ -385,7 +424,9 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     emax = block_max(emax, red);
     cnum = block_max(cnum, red);
     // s2 = QT + E^T QT, then QT = s2
+    t_g0 = stamp();
     df_gemm(s1, true, QT, false, QT, 1.0, 0.0, s2, m, false, dft);
+    t_gemm += stamp() - t_g0;
     for (size_t t = tid; t < mm; t += nt) QT[t] = s2[t];
     __syncthreads();
     refined = it + 1;
@@ -393,6 +434,10 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
       converged = cnum <= 1e-12 * anorm;
       break;
     }
+  }
+  if (sweep_log && tid == 0) {
+    sweep_log[3] = t_gemm;
+    sweep_log[4] = stamp() - t_ref0;
   }
   if (!converged) {
     // Eigenvalues closer than the FP32 start can separate (gaps ~1e-7 of the
@@ -599,29 +644,34 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       }
       __syncthreads();
     }
-    // F = W (L_A^{-1} C)^T  [n, nA] into H.  The lanes of a warp take
-    // consecutive j, so L_A^{-1} C is read through its transpose (in Gm, free
-    // in this path) to keep the loads coalesced; same products, same order.
-    double* X2T = Gm;  // [n, nA]
-    for (size_t t = tid; t < (size_t)n * nA; t += nt) {
-      const int r = int(t / nA), j = int(t % nA);
-      X2T[t] = X2[(size_t)j * n + r];
-    }
+    // F = W (L_A^{-1} C)^T [n, nA], stored transposed: row j of FT (in H,
+    // row stride n) is column j of F, so the Householder QR and the
+    // back-transformation below read and update contiguous rows.
+    // FT[j][i] = sum_{r <= i} X2[j][r] W[i][r], with W read through its
+    // transpose (in Gm, free in this path) for the i-consecutive lanes.
+    double* WT = Gm;
+    for (int r = warp; r < n; r += nw)
+      for (int i = lane; i < n; i += 32) WT[(size_t)r * n + i] = W[(size_t)i * n + r];
     __syncthreads();
-    for (size_t t = tid; t < (size_t)n * nA; t += nt) {
-      const int i = int(t / nA), j = int(t % nA);
-      double s = 0.0;
+    double* FT = H;
+    for (int j = warp; j < nA; j += nw) {
+      const double* xj = X2 + (size_t)j * n;
+      for (int i = lane; i < n; i += 32) {
+        double s = 0.0;
 #pragma unroll 8
-      for (int r = 0; r <= i; ++r) s += W[(size_t)i * n + r] * X2T[(size_t)r * nA + j];
-      H[t] = s;
+        for (int r = 0; r <= i; ++r) s += WT[(size_t)r * n + i] * xj[r];
+        FT[(size_t)j * n + i] = s;
+      }
     }
     __syncthreads();
-    // Householder QR of F (n x nA, row stride nA); taus in dots[]
+    // Householder QR of F (columns = rows of FT); taus in dots[], the current
+    // reflector v (v_j = 1) staged in vec
     for (int j = 0; j < nA; ++j) {
+      double* fj = FT + (size_t)j * n;
       double s2 = 0.0;
-      for (int i = j + 1 + tid; i < n; i += nt) s2 += H[(size_t)i * nA + j] * H[(size_t)i * nA + j];
+      for (int i = j + 1 + tid; i < n; i += nt) s2 += fj[i] * fj[i];
       s2 = block_sum(s2, red);
-      const double x0 = H[(size_t)j * nA + j];
+      const double x0 = fj[j];
       double beta = x0, tau = 0.0, scale = 0.0;
       if (s2 > 0.0) {
         beta = -copysign(sqrt(x0 * x0 + s2), x0);
@@ -629,37 +679,37 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
         scale = 1.0 / (x0 - beta);
       }
       __syncthreads();
-      for (int i = j + 1 + tid; i < n; i += nt) H[(size_t)i * nA + j] *= scale;
+      for (int i = j + 1 + tid; i < n; i += nt) {
+        const double v = fj[i] * scale;
+        fj[i] = v;
+        vec[i] = v;
+      }
       if (tid == 0) {
-        H[(size_t)j * nA + j] = beta;
+        fj[j] = beta;
         dots[j] = tau;
+        vec[j] = 1.0;
       }
       __syncthreads();
-      // apply to the trailing columns: one warp per column
-      for (int col = j + 1 + (tid >> 5); col < nA; col += nt >> 5) {
+      // apply to the trailing columns: one warp per column (row of FT)
+      for (int col = j + 1 + warp; col < nA; col += nw) {
+        double* fc = FT + (size_t)col * n;
         double d = 0.0;
-        for (int i = j + (tid & 31); i < n; i += 32) d += (i == j ? 1.0 : H[(size_t)i * nA + j]) * H[(size_t)i * nA + col];
+        for (int i = j + lane; i < n; i += 32) d += vec[i] * fc[i];
         for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         d *= tau;
-        for (int i = j + (tid & 31); i < n; i += 32) H[(size_t)i * nA + col] -= d * (i == j ? 1.0 : H[(size_t)i * nA + j]);
+        for (int i = j + lane; i < n; i += 32) fc[i] -= d * vec[i];
       }
       __syncthreads();
     }
-    // K = I - R R^T into X1, eigenvector rows of K (identity) into X2; R is
-    // read through its transpose (in Gm) for the j-consecutive lanes
-    double* RT = Gm;  // [nA, nA]
-    for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
-      const int q = int(t / nA), j = int(t % nA);
-      RT[t] = H[(size_t)j * nA + q];
-    }
-    __syncthreads();
-    for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
-      const int i = int(t / nA), j = int(t % nA);
-      double s = 0.0;
+    // K = I - R R^T into X1 (R[i][q] = FT[q][i], q >= i), eigenvector rows of
+    // K (identity) into X2
+    for (int i = warp; i < nA; i += nw)
+      for (int j = lane; j < nA; j += 32) {
+        double s = 0.0;
 #pragma unroll 8
-      for (int q = (i > j ? i : j); q < nA; ++q) s += H[(size_t)i * nA + q] * RT[(size_t)q * nA + j];
-      X1[t] = (i == j ? 1.0 : 0.0) - s;
-    }
+        for (int q = (i > j ? i : j); q < nA; ++q) s += FT[(size_t)q * n + i] * FT[(size_t)q * n + j];
+        X1[(size_t)i * nA + j] = (i == j ? 1.0 : 0.0) - s;
+      }
     __syncthreads();
     // Gm is free in this path (G is applied through W = L^{-1}, which the pairing still needs)
     phase_stamp(a, c, 5);
@@ -670,16 +720,18 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     __syncthreads();
     // eigenvector rows of H in the full space: u_i = Q z_i, z_i = [K eigvec; 0] or e_i
     // (into X1, so that W = L^{-1} survives for applying G)
-    for (int i = (tid >> 5); i < n; i += nt >> 5) {
+    // (reflector j is row j of FT from column j + 1 on, with v_j = 1)
+    for (int i = warp; i < n; i += nw) {
       double* z = EV + (size_t)i * n;
-      for (int t = tid & 31; t < n; t += 32) z[t] = i < nA ? (t < nA ? X2[(size_t)i * nA + t] : 0.0) : (t == i ? 1.0 : 0.0);
+      for (int t = lane; t < n; t += 32) z[t] = i < nA ? (t < nA ? X2[(size_t)i * nA + t] : 0.0) : (t == i ? 1.0 : 0.0);
       __syncwarp();
       for (int j = nA - 1; j >= 0; --j) {
+        const double* vj = FT + (size_t)j * n;
         double d = 0.0;
-        for (int t = j + (tid & 31); t < n; t += 32) d += (t == j ? 1.0 : H[(size_t)t * nA + j]) * z[t];
+        for (int t = j + lane; t < n; t += 32) d += (t == j ? 1.0 : vj[t]) * z[t];
         for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         d *= dots[j];
-        for (int t = j + (tid & 31); t < n; t += 32) z[t] -= d * (t == j ? 1.0 : H[(size_t)t * nA + j]);
+        for (int t = j + lane; t < n; t += 32) z[t] -= d * (t == j ? 1.0 : vj[t]);
         __syncwarp();
       }
     }
@@ -740,15 +792,30 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   int* used = reinterpret_cast<int*>(vec);  // n flags (vec reused as int storage)
   for (int i = tid; i < n; i += nt) used[i] = 0;
   __syncthreads();
+  // out[r - r0] = sign * (row r of M) . x over columns [0, min(n, r + 1) if
+  // tri else n) for rows r in [r0, r1): each warp takes four rows at a time
+  // (four independent sums per lane), lanes the columns
+  auto rows_dot = [&](const float2* Mr, int r0, int r1, const float2* x, float2* out, bool tri, float sign) {
+    for (int rb = r0 + 4 * warp; rb < r1; rb += 4 * nw) {
+      float s[4] = {0.f, 0.f, 0.f, 0.f}, t[4] = {0.f, 0.f, 0.f, 0.f};
+      const int jend = tri ? min(n, rb + 4) : n;
+      for (int j = lane; j < jend; j += 32) {
+        const float2 xj = x[j];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (rb + u < r1 && (!tri || j <= rb + u)) df_mac(s[u], t[u], Mr[(size_t)(rb + u) * n + j], xj);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        df_warp_sum(s[u], t[u]);
+        if (lane == 0 && rb + u < r1) out[rb + u - r0] = df_norm(sign * s[u], sign * t[u]);
+      }
+    }
+  };
   // y = G x with G = W Omega W^T
   auto apply_G = [&](const float2* x, float2* y) {
     if (g_dense) {
-      for (int i = warp; i < n; i += nw) {
-        float s = 0.f, t = 0.f;
-        for (int j = lane; j < n; j += 32) df_mac(s, t, Gop[(size_t)i * n + j], x[j]);
-        df_warp_sum(s, t);
-        if (lane == 0) y[i] = df_norm(s, t);
-      }
+      rows_dot(Gop, 0, n, x, y, false, 1.f);
     } else {
       for (int u = tid; u < n * segs; u += nt) {  // t = W^T x (W lower triangular)
         const int j = u % n, g = u / n;
@@ -773,24 +840,13 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
         tv[n + j] = j < k ? v : make_float2(-v.x, -v.y);
       }
       __syncthreads();
-      for (int i = warp; i < n; i += nw) {  // y = W (Omega t)
-        float s = 0.f, t = 0.f;
-        for (int j = lane; j <= i; j += 32) df_mac(s, t, Gop[(size_t)i * n + j], tv[n + j]);
-        df_warp_sum(s, t);
-        if (lane == 0) y[i] = df_norm(s, t);
-      }
+      rows_dot(Gop, 0, n, tv + n, y, true, 1.f);  // y = W (Omega t)
     }
     __syncthreads();
   };
   // v -= sum over accepted rows [a0, a1) of (row . v) row, one pass
   auto project_out = [&](float2* v, int a0, int a1) {
-    for (int t0 = tid; t0 < (a1 - a0) * 32; t0 += nt) {  // one warp per accepted row
-      const int av = a0 + (t0 >> 5);
-      float s = 0.f, t = 0.f;
-      for (int i = t0 & 31; i < n; i += 32) df_mac(s, t, Xacc2[(size_t)av * n + i], v[i]);
-      df_warp_sum(s, t);
-      if ((t0 & 31) == 0) dots2[av - a0] = df_norm(-s, -t);
-    }
+    rows_dot(Xacc2, a0, a1, v, dots2, false, -1.f);  // negated coefficients
     __syncthreads();
     if (segs == 1) {
       for (int i = tid; i < n; i += nt) {
@@ -818,11 +874,24 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     }
     __syncthreads();
   };
-  // |v|^2 over the block (FP64 total of the threads' double-float sums)
-  auto norm2 = [&](const float2* v) {
+  // |v|^2 over the block into *q (warp sums in double-float, the 32 warp
+  // totals in FP64 by thread 0) and 1/|v| split, for every thread: thread 0
+  // alone takes the FP64 square root and reciprocal (the FP64 pipe is narrow)
+  auto norm_inv = [&](const float2* v, double* q) {
     float s = 0.f, t = 0.f;
     for (int i = tid; i < n; i += nt) df_mac(s, t, v[i], v[i]);
-    return block_sum(double(s) + double(t), red);
+    df_warp_sum(s, t);
+    if (lane == 0) red[warp] = double(s) + double(t);
+    __syncthreads();
+    if (tid == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < nw; ++w) tot += red[w];
+      red[32] = tot;
+      red[33] = tot > 0.0 ? 1.0 / sqrt(tot) : 0.0;
+    }
+    __syncthreads();
+    *q = red[32];
+    return df_split(red[33]);
   };
   int acc = 0;
   int cb = 0;
@@ -881,7 +950,8 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       for (int i = tid; i < n; i += nt) x[i] = df_split(EV[(size_t)order[cb + best] * n + i]);
       __syncthreads();
       project_out(x, acc0, acc);
-      const float2 ix = df_split(1.0 / sqrt(norm2(x)));
+      double nx;
+      const float2 ix = norm_inv(x, &nx);
       for (int i = tid; i < n; i += nt) x[i] = df_mul(x[i], ix);
       __syncthreads();
       // y = G x / |G x| needs no projection: G maps the span of the accepted
@@ -890,8 +960,8 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       // orthogonal to it up to rounding (checked to 1e-10 on every kind of
       // cut by the symplectic tests)
       apply_G(x, y);
-      const double gx = norm2(y);  // |G x|^2 = 1/nu^2
-      const float2 iy = df_split(gx > 0.0 ? 1.0 / sqrt(gx) : 0.0);
+      double gx;  // |G x|^2 = 1/nu^2
+      const float2 iy = norm_inv(y, &gx);
       for (int i = tid; i < n; i += nt) {
         const float2 yi = df_mul(y[i], iy);
         y[i] = yi;
@@ -908,19 +978,31 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       // FP32 tracking: the candidates stay as they are (orthonormal); a
       // candidate's squared residual against the accepted orthonormal pairs
       // is |u|^2 - sum (a . u)^2, so each step subtracts (x . u)^2 + (y . u)^2
-      for (int r = tid >> 5; r < C; r += nt >> 5) {
-        if (used[cb + r]) continue;
-        const float* w = c32 + (size_t)r * n;
-        float sx = 0.f, sy = 0.f;
-        for (int i = tid & 31; i < n; i += 32) {
-          sx = fmaf(xy32[i], w[i], sx);
-          sy = fmaf(xy32[n + i], w[i], sy);
+      // (two candidates per warp step: four independent sums per lane)
+      for (int rb = 2 * warp; rb < C; rb += 2 * nw) {
+        const bool u0 = !used[cb + rb], u1 = rb + 1 < C && !used[cb + rb + 1];
+        if (!u0 && !u1) continue;
+        const float* w0 = c32 + (size_t)rb * n;
+        const float* w1 = w0 + n;
+        float sx0 = 0.f, sy0 = 0.f, sx1 = 0.f, sy1 = 0.f;
+        for (int i = lane; i < n; i += 32) {
+          const float xi = xy32[i], yi = xy32[n + i];
+          const float a0 = w0[i], a1 = u1 ? w1[i] : 0.f;
+          sx0 = fmaf(xi, a0, sx0);
+          sy0 = fmaf(yi, a0, sy0);
+          sx1 = fmaf(xi, a1, sx1);
+          sy1 = fmaf(yi, a1, sy1);
         }
         for (int o = 16; o > 0; o >>= 1) {
-          sx += __shfl_xor_sync(0xffffffffu, sx, o);
-          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+          sx0 += __shfl_xor_sync(0xffffffffu, sx0, o);
+          sy0 += __shfl_xor_sync(0xffffffffu, sy0, o);
+          sx1 += __shfl_xor_sync(0xffffffffu, sx1, o);
+          sy1 += __shfl_xor_sync(0xffffffffu, sy1, o);
         }
-        if ((tid & 31) == 0) r32[r] -= sx * sx + sy * sy;
+        if (lane == 0) {
+          if (u0) r32[rb] -= sx0 * sx0 + sy0 * sy0;
+          if (u1) r32[rb + 1] -= sx1 * sx1 + sy1 * sy1;
+        }
       }
       __syncthreads();
       acc += 2;
@@ -1296,7 +1378,7 @@ int cut_read_phases(bsg_handle_t h, const CutArgs& a, cudaStream_t st) {
     }
     for (int i = kCutTimedPhases; i < kCutPhases; ++i)
       h->prof.cut_phases[(size_t)c * kCutPhases + i] = double(t[(size_t)c * kCutPhases + i]);
-    h->prof.cut_phases[(size_t)c * kCutPhases + kCutPhases - 1] *= 1e-6;  // ns -> ms
+    for (int i = kCutPhases - 3; i < kCutPhases; ++i) h->prof.cut_phases[(size_t)c * kCutPhases + i] *= 1e-6;  // ns -> ms
   }
   return BSG_OK;
 }

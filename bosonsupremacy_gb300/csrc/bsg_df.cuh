@@ -10,27 +10,33 @@
 
 namespace bsg {
 
-// x = hi + lo from the IEEE bits on the integer pipe (FP64 conversions and
-// subtractions run on the narrow FP64 pipe): hi keeps the top 24 bits of the
-// significand (truncated), lo the next 29 rounded to 24, so hi + lo carries
-// ~48 bits; a lo below FP32's normal range (|x| < 2^-75) is dropped, and x
-// outside FP32's exponent range falls back to the FP64 split.
+// x = hi + lo from the IEEE bits, with integer and FP32 operations only
+// (FP64 and integer-to-float conversions run on GB300's narrow FP64-rate
+// units): hi keeps the top 24 bits of the significand (truncated), lo the
+// next 29 rounded to nearest to 24, so hi + lo carries ~48 bits.  The 29-bit
+// remainder becomes a float through its two halves, each exact as
+// (2^23 + v) - 2^23, and one fma that rounds once.  A lo below FP32's
+// normal range (|x| < 2^-75) is dropped; x outside FP32's exponent range
+// becomes 0 (|x| < 2^-126) or +-inf (|x| >= 2^128).  No FP64 instruction, so
+// none can be predicated into a caller's hot loop.
 __device__ __forceinline__ float2 df_split(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
   const int e = int((hw >> 20) & 0x7ffu);  // biased double exponent
-  if (e == 0) return make_float2(0.f, 0.f);  // zero (or a double subnormal)
   const int fe = e - 1023 + 127;
-  if (fe <= 0 || fe >= 255) {
-    const float h = float(x);
-    return make_float2(h, float(x - double(h)));
-  }
   const unsigned sign = hw & 0x80000000u;
+  if (fe <= 0) return make_float2(0.f, 0.f);  // zero, double subnormal or below FP32's range
+  if (fe >= 255) return make_float2(__uint_as_float(sign | 0x7f800000u), 0.f);
   const float h = __uint_as_float(sign | (unsigned(fe) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
   // the remaining 29 significand bits are r * 2^(e - 1023 - 52)
   const int pe = e - 1075 + 127;
   float l = 0.f;
-  if (pe > 0) l = __uint2float_rn(lw & 0x1fffffffu) * __uint_as_float(unsigned(pe) << 23);
+  if (pe > 0) {
+    const unsigned r = lw & 0x1fffffffu;
+    const float rh = __uint_as_float(0x4B000000u | (r >> 14)) - 8388608.f;      // r >> 14 < 2^15
+    const float rl = __uint_as_float(0x4B000000u | (r & 0x3fffu)) - 8388608.f;  // < 2^14
+    l = fmaf(rh, 16384.f, rl) * __uint_as_float(unsigned(pe) << 23);
+  }
   return make_float2(h, sign ? -l : l);
 }
 

@@ -179,7 +179,7 @@ struct CutArgs {
   unsigned long long* phase_t;  // [n_cuts, kCutPhases] phase timestamps (profiling) or null
 };
 constexpr int kCutTimedPhases = 11;  // stamps 0..10
-constexpr int kCutPhases = 14;       // + FP32 sweeps, FP64 refinement steps, FP32 sweep time (ns)
+constexpr int kCutPhases = 16;       // + FP32 sweeps, refinement steps, FP32 sweep / refinement product / refinement times (ns)
 
 // A byte range to set to one byte value; many of them are cleared by one
 // launch (fill_spans).

@@ -315,8 +315,9 @@ int bsg_gemm_tf32x3(bsg_handle_t h, const float* A, const float* B, float* C, in
  * for phases 1 load + symmetry check, 2 Cholesky, 3 L^-1, 4 G, 5 H = G^T G
  * (full path) or F, QR and K (low-rank path), 6 Jacobi, 7 back-transform,
  * 8 ordering, 9 pairing, 10 S and nbar; columns 11 and 12 are the FP32 Jacobi
- * sweeps and the FP64 refinement steps (counts, not times), column 13 the
- * ms of the FP32 sweeps inside phase 6.  Pass ms = NULL to query the sizes. */
+ * sweeps and the refinement steps (counts, not times), columns 13, 14 and 15
+ * the ms of the FP32 sweeps, of the refinement's products and of the whole
+ * refinement inside phase 6.  Pass ms = NULL to query the sizes. */
 int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* ms);
 
 /* Milestones of the last bsg_build_mps made while profiling was enabled, in

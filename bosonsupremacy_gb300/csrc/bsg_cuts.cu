@@ -93,7 +93,11 @@ __device__ __noinline__ int block_jacobi(T* Hm, int m, int ld, T* QT, int max_sw
     if (offs <= tol * dias) return sweep;
     for (int step = 0; step < m - 1; ++step) {
       // round-robin pairing of this step: slot i holds index pos(i)
-      auto pos_at = [&](int i) { return i == 0 ? 0 : ((i - 1 + step) % (m - 1)) + 1; };
+      auto pos_at = [&](int i) {  // (i - 1 + step) mod (m - 1), both terms below m - 1
+        if (i == 0) return 0;
+        const int v = i - 1 + step;
+        return (v >= m - 1 ? v - (m - 1) : v) + 1;
+      };
       for (int q0 = tid; q0 < P; q0 += nt) {
         int p = pos_at(q0), q = pos_at(m - 1 - q0);
         if (p > q) {
@@ -550,13 +554,14 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   phase_stamp(a, c, 0);
   // 1. V and the symmetry check of the reference (norm(V - V^T) < 1e-11)
   double asym = 0.0;
-  for (size_t i = tid; i < nn; i += nt) {
-    const int r = int(i / n), q = int(i % n);
-    const double v = a.sq_cov[(size_t)gidx(r) * (2 * M) + gidx(q)];
-    const double vt = a.sq_cov[(size_t)gidx(q) * (2 * M) + gidx(r)];
-    A[i] = v;
-    asym += (v - vt) * (v - vt);
-  }
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int r = warp; r < n; r += nw)
+    for (int q = lane; q < n; q += 32) {
+      const double v = a.sq_cov[(size_t)gidx(r) * (2 * M) + gidx(q)];
+      const double vt = a.sq_cov[(size_t)gidx(q) * (2 * M) + gidx(r)];
+      A[(size_t)r * n + q] = v;
+      asym += (v - vt) * (v - vt);
+    }
   asym = block_sum(asym, red);
   if (asym >= 1e-22) {
     if (tid == 0) a.status[c] = 1;
@@ -571,7 +576,6 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   phase_stamp(a, c, 2);
   // 3. W = L^{-1}: forward substitution on all columns, row by row (1 / L_rr
   // in vec from the Cholesky; warps take rows, lanes columns)
-  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int i = warp; i < n; i += nw)
     for (int q = lane; q < n; q += 32) W[(size_t)i * n + q] = i == q ? 1.0 : 0.0;
   __syncthreads();
@@ -618,13 +622,9 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     // so the non-trivial spectrum lives in range(F): QR of F, Jacobi on the
     // nA x nA matrix I - R R^T, and the complement of range(F) is the nu = 1 space.
     auto gA = [&](int i) { return i < L ? i : M + (i - L); };
-    for (size_t t = tid; t < (size_t)nA * nA; t += nt) {
-      const int r = int(t / nA), q = int(t % nA);
-      X1[t] = a.sq_cov[(size_t)gA(r) * (2 * M) + gA(q)];
-    }
-    for (size_t t = tid; t < (size_t)nA * n; t += nt) {
-      const int r = int(t / n), q = int(t % n);
-      X2[t] = a.sq_cov[(size_t)gA(r) * (2 * M) + gidx(q)];  // C [nA, n]
+    for (int r = warp; r < nA; r += nw) {
+      for (int q = lane; q < nA; q += 32) X1[(size_t)r * nA + q] = a.sq_cov[(size_t)gA(r) * (2 * M) + gA(q)];
+      for (int q = lane; q < n; q += 32) X2[(size_t)r * n + q] = a.sq_cov[(size_t)gA(r) * (2 * M) + gidx(q)];  // C [nA, n]
     }
     __syncthreads();
     if (!block_cholesky(X1, nA, &s_flag, vec, vec2)) {
@@ -780,6 +780,10 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   // segs x n pairs after tv in X2) are added in range order.
   const int segs = n >= 6 ? max(1, min(4, nt / n)) : 1;
   float2* part = tv + 2 * (size_t)n;
+  // item u of the segmented sums is (column u % n, range u / n): with segs > 1
+  // there are n * segs <= nt items, so u = tid, mapped once; with segs = 1 it
+  // is (u, 0) (no integer division in the pair loop)
+  const int my_j = tid % n, my_g = tid / n;
   // the operator of G x, split once: G in place (full path) or W into Gm
   // (free in the low-rank path)
   float2* Gop = reinterpret_cast<float2*>(Gm);
@@ -818,7 +822,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       rows_dot(Gop, 0, n, x, y, false, 1.f);
     } else {
       for (int u = tid; u < n * segs; u += nt) {  // t = W^T x (W lower triangular)
-        const int j = u % n, g = u / n;
+        const int j = segs == 1 ? u : my_j, g = segs == 1 ? 0 : my_g;
         const int len = (n - j + segs - 1) / segs, i0 = j + g * len, i1 = min(n, i0 + len);
         float s = 0.f, t = 0.f;
 #pragma unroll 8
@@ -858,7 +862,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     } else {
       const int len = (a1 - a0 + segs - 1) / segs;
       for (int u = tid; u < n * segs; u += nt) {
-        const int i = u % n, g = u / n;
+        const int i = segs == 1 ? u : my_j, g = segs == 1 ? 0 : my_g;
         const int b0 = a0 + g * len, b1 = min(a1, b0 + len);
         float s = 0.f, t = 0.f;
 #pragma unroll 8
@@ -901,9 +905,9 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     if (ce > n) ce = n;
     const int acc0 = acc, C = ce - cb;
     // FP32 copies of the cluster's candidates and their squared norms
-    for (size_t t = tid; t < (size_t)C * n; t += nt) {
-      const int r = int(t / n), i = int(t % n);
-      c32[t] = float(EV[(size_t)order[cb + r] * n + i]);
+    for (int r = warp; r < C; r += nw) {
+      const double* ev = EV + (size_t)order[cb + r] * n;
+      for (int i = lane; i < n; i += 32) c32[(size_t)r * n + i] = df_split(ev[i]).x;  // no FP64 conversion
     }
     __syncthreads();
     for (int r = tid >> 5; r < C; r += nt >> 5) {
@@ -1078,9 +1082,18 @@ __device__ __forceinline__ void thermal_cut(const CutArgs& a, const int c) {
       t[n] = 1.0 / (x + 1.0) * pow(x / (x + 1.0), (double)n);
     }
     __syncthreads();
-    for (int u = tid; u < d * K; u += nt) {
-      int n = u / K, i = u % K;
+    // item u = n * K + i (consecutive threads on consecutive candidates of one
+    // column); (n, i) advance by (dn, di) per stride, so only the first item
+    // of a thread and the stride take an integer division
+    const int dn = nt / K, di = nt - dn * K, n0 = tid / K, i0 = tid - n0 * K;
+    for (int u = tid, n = n0, i = i0; u < d * K; u += nt) {
       prod[(size_t)n * chi + i] = dbits(cur[i] * t[n]);
+      n += dn;
+      i += di;
+      if (i >= K) {
+        i -= K;
+        ++n;
+      }
     }
     if (tid == 0) s_valid = 0;
     __syncthreads();
@@ -1099,8 +1112,11 @@ __device__ __forceinline__ void thermal_cut(const CutArgs& a, const int c) {
     __syncthreads();
     const int Kn = min(chi, s_valid);
     uint32_t* rs = rec + (size_t)s * chi;
-    for (int u = tid; u < d * K; u += nt) {
-      const int n = u / K, i = u % K;
+    for (int u = tid, n = n0, i = i0; u < d * K; u += nt, n += dn, i += di) {
+      if (i >= K) {
+        i -= K;
+        ++n;
+      }
       const unsigned long long v = prod[(size_t)n * chi + i];
       if (v <= tol) continue;
       int rank = 0;

@@ -341,15 +341,18 @@ __device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, cons
 // scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
 // the start tolerance of the refinement.
 __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
-                            double* cs, double* sn, int* pos, float* jsm, float2* dft,
+                            double* cs, double* sn, int* pos, float* jsm, bool q_smem, float2* dft,
                             unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t mm = (size_t)m * m;
   // the FP32 copies: in shared memory when the launch reserved room for them
   // (the rotation rounds touch scattered rows and columns), else in s1
+  // (the scattered 2 x 2 blocks of a rotation round are the shared-memory
+  // win; the eigenvector rows are updated row-wise, coalesced, so for large
+  // m only the matrix stays in shared memory)
   float* H32 = jsm ? jsm : reinterpret_cast<float*>(s1);
   const int ld = jsm ? m + 1 : m;  // s1 holds 2 m^2 floats
-  float* Q32 = H32 + (size_t)m * ld;
+  float* Q32 = jsm ? (q_smem ? H32 + (size_t)m * ld : reinterpret_cast<float*>(s1)) : H32 + mm;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int i = warp; i < m; i += nw)
     for (int j = lane; j < m; j += 32) {
@@ -380,7 +383,12 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
   // which three fixed steps left at ~1e-6.
   constexpr int kRefineMax = 8;
   int refined = 0;
-  bool converged = false;
+  bool converged = false, settled = false;
+  // pairs closer than tau_gap stay clustered (the FP32 start cannot separate
+  // them, and a Newton step on an O(1) mixing diverges); unresolved clusters
+  // are diagonalised at the end in FP64 on their own small blocks
+  const double tau_gap = 1e-6 * anorm;
+  double delta_last = 0.0;
   // profiling: time in the refinement's products and in the whole refinement
   unsigned long long t_ref0 = 0, t_gemm = 0, t_g0 = 0;
   auto stamp = [&]() {
@@ -410,6 +418,7 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     so = block_sum(so, red);
     rr = block_sum(rr, red);
     const double delta = 2.0 * (sqrt(so) + anorm * sqrt(rr));
+    delta_last = delta;
     // s1 <- E (in place: E_ij reads s1_ij and s3_ij only).  cnum: the largest
     // numerator s_ij + lambda_j r_ij of a clustered pair -- rounding level for
     // an exactly degenerate pair, about gap x mixing for distinct eigenvalues
@@ -419,7 +428,7 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
       for (int j = lane; j < m; j += 32) {
         const size_t t = (size_t)i * m + j;
         const double r = s1[t], gap = lam[j] - lam[i];
-        const bool sep = i != j && fabs(gap) > delta;
+        const bool sep = i != j && fabs(gap) > fmax(delta, tau_gap);
         const double e = sep ? (s3[t] + lam[j] * r) / gap : 0.5 * r;
         s1[t] = e;
         if (i != j) emax = fmax(emax, fabs(e));
@@ -435,9 +444,83 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     __syncthreads();
     refined = it + 1;
     if (emax <= 1e-8) {  // the remaining error is ~emax^2
+      settled = true;
       converged = cnum <= 1e-12 * anorm;
       break;
     }
+  }
+  if (settled && !converged && m <= kMaxCutModes) {  // (lam fills cs; sn is free for the small Jacobi)
+    // Clusters (eigenvalues chained by gaps <= max(delta, tau_gap), in sorted
+    // order) whose vectors are an orthonormal basis of their eigenspace but
+    // still mixed: for each, S_c = QT_c Hm QT_c^T in FP64 (p x p), cyclic
+    // FP64 Jacobi on it, QT_c <- R QT_c and its eigenvalues.  The rotation
+    // scratch of the small Jacobi is sn / pos + 256, so lam (cs) and the
+    // sorted order (pos) survive.
+    __shared__ int s_g0, s_g1;
+    int* ord = pos;
+    for (int i = tid; i < m; i += nt) {
+      const double li = lam[i];
+      int r = 0;
+      for (int j = 0; j < m; ++j) r += (lam[j] < li) || (lam[j] == li && j < i);
+      ord[r] = i;
+    }
+    if (tid == 0) s_g1 = 0;
+    __syncthreads();
+    const double chain = fmax(delta_last, tau_gap);
+    bool ok = true;
+    while (true) {
+      __syncthreads();  // every thread has read the previous cluster's bounds
+      if (tid == 0) {
+        int g0 = s_g1, g1 = g0 + 1;
+        while (g1 < m && lam[ord[g1]] - lam[ord[g1 - 1]] <= chain) ++g1;
+        s_g0 = g0;
+        s_g1 = g1;
+      }
+      __syncthreads();
+      const int g0 = s_g0, g1 = s_g1, p = g1 - g0;
+      if (g0 >= m) break;
+      if (p >= 2) {
+        // U = QT_c Hm (p x m, in s2), S_c = U QT_c^T (p x p, in s3), R = I (s1)
+        for (int a = warp; a < p; a += nw) {
+          const double* qa = QT + (size_t)ord[g0 + a] * m;
+          for (int j = lane; j < m; j += 32) {
+            double u = 0.0;
+            for (int i = 0; i < m; ++i) u = fma(qa[i], Hm[(size_t)i * m + j], u);
+            s2[(size_t)a * m + j] = u;
+          }
+        }
+        __syncthreads();
+        for (int t = warp; t < p * p; t += nw) {
+          const int a = t / p, b2 = t - a * p;
+          const double* qb = QT + (size_t)ord[g0 + b2] * m;
+          double u = 0.0;
+          for (int j = lane; j < m; j += 32) u = fma(s2[(size_t)a * m + j], qb[j], u);
+          for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+          if (lane == 0) {
+            s3[t] = u;
+            s1[t] = a == b2 ? 1.0 : 0.0;
+          }
+        }
+        __syncthreads();
+        const int swc = block_jacobi<double>(s3, p, p, s1, 60, 1e-26, red, sn, sn + kMaxCutModes / 2, pos + 256);
+        if (swc < 0) ok = false;
+        // QT_c <- R QT_c (through s2), eigenvalues from the diagonal
+        for (int a = warp; a < p; a += nw)
+          for (int j = lane; j < m; j += 32) {
+            double u = 0.0;
+            for (int b2 = 0; b2 < p; ++b2) u = fma(s1[(size_t)a * p + b2], QT[(size_t)ord[g0 + b2] * m + j], u);
+            s2[(size_t)a * m + j] = u;
+          }
+        __syncthreads();
+        for (int a = warp; a < p; a += nw) {
+          double* qa = QT + (size_t)ord[g0 + a] * m;
+          for (int j = lane; j < m; j += 32) qa[j] = s2[(size_t)a * m + j];
+          if (lane == 0) lam[ord[g0 + a]] = s3[(size_t)a * p + a];
+        }
+        __syncthreads();
+      }
+    }
+    converged = ok;
   }
   if (sweep_log && tid == 0) {
     sweep_log[3] = t_gemm;
@@ -451,8 +534,11 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     // delta drops below their gap, or the mixed pair keeps delta above its
     // gap and stays a cluster (cnum above rounding).  Such a cut restarts from
     // the identity with FP64 Jacobi sweeps on Hm (still the input matrix),
-    // which resolve any gap above the FP64 rounding of Hm.
-    for (size_t t = tid; t < mm; t += nt) QT[t] = (t / m == t % m) ? 1.0 : 0.0;
+    // which resolve any gap above the FP64 rounding of Hm.  (The refined
+    // vectors are no start for it: a refinement that stopped converging has
+    // left them far from orthonormal.)
+    for (int i = warp; i < m; i += nw)
+      for (int j = lane; j < m; j += 32) QT[(size_t)i * m + j] = i == j ? 1.0 : 0.0;
     __syncthreads();
     const int sw64 = block_jacobi<double>(Hm, m, m, QT, 60, 1e-26, red, cs, sn, pos);
     if (sweep_log && tid == 0) {
@@ -543,12 +629,15 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   double* dots = reinterpret_cast<double*>(order + 2 * kMaxCutModes);  // n (also Householder taus)
   double* vec = dots + 2 * kMaxCutModes;                               // n
   double* vec2 = vec + 2 * kMaxCutModes;                               // n
-  // double-float product tiles, then the FP32 Jacobi matrices (m (2m + 1) floats)
+  // double-float product tiles, then the FP32 Jacobi matrix (m (m + 1) floats)
+  // and, with jac_q_smem, its eigenvector rows (m^2 floats)
   // when the launch reserved them
   float2* dft = reinterpret_cast<float2*>(vec2 + 2 * kMaxCutModes);
   float* jsm = a.jac_smem_m > 0 ? reinterpret_cast<float*>(reinterpret_cast<char*>(dft) + kDfSmemBytes) : nullptr;
   __shared__ int s_flag;
   __shared__ double s_scalar;
+  __shared__ int s_pick[4], s_nb;  // blocked vacuum pairing: the block's candidates
+  __shared__ float s_pickv[4];
 
   auto gidx = [&](int i) { return i < k ? L + i : M + L + (i - k); };
   phase_stamp(a, c, 0);
@@ -611,7 +700,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     // eigenvector rows in W
     df_gemm(Gm, true, Gm, false, nullptr, 1.0, 0.0, H, n, true, dft);
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm, dft,
+    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm, a.jac_q_smem != 0, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
@@ -713,7 +802,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     __syncthreads();
     // Gm is free in this path (G is applied through W = L^{-1}, which the pairing still needs)
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos, jsm, dft,
+    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos, jsm, a.jac_q_smem != 0, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
@@ -784,6 +873,21 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   // there are n * segs <= nt items, so u = tid, mapped once; with segs = 1 it
   // is (u, 0) (no integer division in the pair loop)
   const int my_j = tid % n, my_g = tid / n;
+  // profiling: time in six parts of the pairing (cluster setup, pivots and
+  // candidate loads, projections, G products, in-block Gram-Schmidt or
+  // normalisation, residual tracking), accumulated by thread 0
+  unsigned long long* pst = a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 16 : nullptr;
+  auto pstamp = [&]() {
+    unsigned long long t = 0;
+    if (pst && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+  };
+  auto pacc = [&](int part, unsigned long long t0) {
+    if (pst && tid == 0) pst[part] += pstamp() - t0;
+  };
+  if (pst && tid == 0)
+    for (int i = 0; i < 6; ++i) pst[i] = 0;
+  unsigned long long tp = 0;
   // the operator of G x, split once: G in place (full path) or W into Gm
   // (free in the low-rank path)
   float2* Gop = reinterpret_cast<float2*>(Gm);
@@ -904,6 +1008,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     while (ce < n && !(vec2[ce] - vec2[ce - 1] > 1e-9 * fmax(fabs(vec2[ce]), 1e-300))) ce += 2;
     if (ce > n) ce = n;
     const int acc0 = acc, C = ce - cb;
+    tp = pstamp();
     // FP32 copies of the cluster's candidates and their squared norms
     for (int r = warp; r < C; r += nw) {
       const double* ev = EV + (size_t)order[cb + r] * n;
@@ -917,6 +1022,301 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       if ((tid & 31) == 0) r32[r] = s;
     }
     __syncthreads();
+    // The exact nu = 1 block of the low-rank path (every mu exactly 1: the
+    // complement of range(F)) is paired four candidates at a time: G maps it
+    // onto itself with G^2 = -I, so after G is applied to the block's four
+    // projected candidates at once, the in-block Gram-Schmidt needs no further
+    // G products (G y_p = -x_p).  Per pair this reads W, the accepted
+    // vectors and the FP32 candidates a quarter as often and takes ~6 block
+    // barriers instead of ~16.
+    bool vac = !g_dense && n >= 64 && C >= 8;
+    for (int r = 0; r < C && vac; ++r) vac = vec2[cb + r] == 1.0;
+    pacc(0, tp);
+    if (vac) {
+      float2* dotsb = tv + 6 * (size_t)n;   // [accepted row][4] negated projections
+      float2* tvb = dotsb + 4 * (size_t)n;  // [q][2n]: W^T x_q and Omega W^T x_q
+      float2* partb = tvb + 8 * (size_t)n;  // [range][q][n] partial sums
+      float2* bred = dots2;                 // [warp][8] partial dots, then [8] totals at 256
+      while (acc - acc0 < C) {
+        tp = pstamp();
+        // 1. up to four unused candidates with the largest residuals (the
+        // first must exist; the others must keep a residual above 0.05)
+        if (tid < 32) {
+          const int want = min(4, (C - (acc - acc0)) / 2);
+          int taken = 0;
+          for (int q = 0; q < want; ++q) {
+            float bv = -1.f;
+            int best = -1;
+            for (int r = lane; r < C; r += 32)
+              if (!used[cb + r] && r32[r] > bv) {
+                bv = r32[r];
+                best = r;
+              }
+            for (int o = 16; o > 0; o >>= 1) {
+              const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+              const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+              if (ov > bv || (ov == bv && ob >= 0 && (best < 0 || ob < best))) {
+                bv = ov;
+                best = ob;
+              }
+            }
+            if (best < 0 || !(bv > (q == 0 ? 1e-6f : 0.05f))) break;
+            if (lane == 0) {
+              used[cb + best] = 1;
+              s_pick[q] = best;
+              s_pickv[q] = bv;
+            }
+            __syncwarp();
+            ++taken;
+          }
+          if (lane == 0) s_nb = taken;
+        }
+        __syncthreads();
+        const int nb = s_nb;
+        if (nb == 0) {
+          if (tid == 0) a.status[c] = 4;
+          return;
+        }
+        // 2. the candidates (FP64 eigenvectors, split) into the x rows acc + 2q
+        for (int q = 0; q < nb; ++q) {
+          float2* xq = Xacc2 + (size_t)(acc + 2 * q) * n;
+          const double* ev = EV + (size_t)order[cb + s_pick[q]] * n;
+          for (int i = tid; i < n; i += nt) xq[i] = df_split(ev[i]);
+        }
+        __syncthreads();
+        pacc(1, tp);
+        tp = pstamp();
+        // the block's x rows; q >= nb repeats the last one (results dropped), so
+        // the loops below carry no per-iteration guard and unroll, keeping
+        // several loads per warp in flight (these loops are L2-latency bound)
+        const float2* xr0 = Xacc2 + (size_t)acc * n;
+        const float2* xr1 = Xacc2 + (size_t)(acc + 2 * min(1, nb - 1)) * n;
+        const float2* xr2 = Xacc2 + (size_t)(acc + 2 * min(2, nb - 1)) * n;
+        const float2* xr3 = Xacc2 + (size_t)(acc + 2 * min(3, nb - 1)) * n;
+        // 3. project the block against the accepted vectors of the cluster
+        if (acc > acc0) {
+          for (int av = acc0 + warp; av < acc; av += nw) {
+            float ss[4] = {0.f, 0.f, 0.f, 0.f}, tt[4] = {0.f, 0.f, 0.f, 0.f};
+            const float2* ra = Xacc2 + (size_t)av * n;
+#pragma unroll 3
+            for (int i = lane; i < n; i += 32) {
+              const float2 r = ra[i];
+              df_mac(ss[0], tt[0], r, xr0[i]);
+              df_mac(ss[1], tt[1], r, xr1[i]);
+              df_mac(ss[2], tt[2], r, xr2[i]);
+              df_mac(ss[3], tt[3], r, xr3[i]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              if (q >= nb) break;
+              df_warp_sum(ss[q], tt[q]);
+              if (lane == 0) dotsb[(size_t)(av - acc0) * 4 + q] = df_norm(-ss[q], -tt[q]);
+            }
+          }
+          __syncthreads();
+          const int len = (acc - acc0 + segs - 1) / segs;
+          for (int u = tid; u < n * segs; u += nt) {
+            const int i = segs == 1 ? u : my_j, g = segs == 1 ? 0 : my_g;
+            const int b0 = acc0 + g * len, b1 = min(acc, b0 + len);
+            float ss[4] = {0.f, 0.f, 0.f, 0.f}, tt[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+            for (int av = b0; av < b1; ++av) {
+              const float2 r = Xacc2[(size_t)av * n + i];
+              const float4 d01 = *reinterpret_cast<const float4*>(dotsb + (size_t)(av - acc0) * 4);
+              const float4 d23 = *reinterpret_cast<const float4*>(dotsb + (size_t)(av - acc0) * 4 + 2);
+              df_mac(ss[0], tt[0], make_float2(d01.x, d01.y), r);
+              df_mac(ss[1], tt[1], make_float2(d01.z, d01.w), r);
+              df_mac(ss[2], tt[2], make_float2(d23.x, d23.y), r);
+              df_mac(ss[3], tt[3], make_float2(d23.z, d23.w), r);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (q < nb) partb[((size_t)g * 4 + q) * n + i] = df_norm(ss[q], tt[q]);
+          }
+          __syncthreads();
+          for (int q = 0; q < nb; ++q) {
+            float2* xq = Xacc2 + (size_t)(acc + 2 * q) * n;
+            for (int i = tid; i < n; i += nt) {
+              float2 v = xq[i];
+              for (int g = 0; g < segs; ++g) v = df_add(v, partb[((size_t)g * 4 + q) * n + i]);
+              xq[i] = v;
+            }
+          }
+          __syncthreads();
+        }
+        pacc(2, tp);
+        tp = pstamp();
+        // 4. z_q = G x_q = W (Omega (W^T x_q)), one pass over W per product
+        for (int u = tid; u < n * segs; u += nt) {
+          const int j = segs == 1 ? u : my_j, g = segs == 1 ? 0 : my_g;
+          const int len = (n - j + segs - 1) / segs, i0 = j + g * len, i1 = min(n, i0 + len);
+          float ss[4] = {0.f, 0.f, 0.f, 0.f}, tt[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+          for (int i = i0; i < i1; ++i) {
+            const float2 w = Gop[(size_t)i * n + j];
+            df_mac(ss[0], tt[0], w, xr0[i]);
+            df_mac(ss[1], tt[1], w, xr1[i]);
+            df_mac(ss[2], tt[2], w, xr2[i]);
+            df_mac(ss[3], tt[3], w, xr3[i]);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (q < nb) partb[((size_t)g * 4 + q) * n + j] = df_norm(ss[q], tt[q]);
+        }
+        __syncthreads();
+        for (int q = 0; q < nb; ++q)
+          for (int j = tid; j < n; j += nt) {
+            float2 v = partb[(size_t)q * n + j];
+            for (int g = 1; g < segs; ++g) v = df_add(v, partb[((size_t)g * 4 + q) * n + j]);
+            tvb[(size_t)q * 2 * n + j] = v;
+          }
+        __syncthreads();
+        for (int q = 0; q < nb; ++q)
+          for (int j = tid; j < n; j += nt) {  // Omega t
+            const float2 v = j < k ? tvb[(size_t)q * 2 * n + j + k] : tvb[(size_t)q * 2 * n + j - k];
+            tvb[(size_t)q * 2 * n + n + j] = j < k ? v : make_float2(-v.x, -v.y);
+          }
+        __syncthreads();
+        const float2* ot0 = tvb + n;
+        const float2* ot1 = tvb + (size_t)min(1, nb - 1) * 2 * n + n;
+        const float2* ot2 = tvb + (size_t)min(2, nb - 1) * 2 * n + n;
+        const float2* ot3 = tvb + (size_t)min(3, nb - 1) * 2 * n + n;
+        for (int i = warp; i < n; i += nw) {
+          float ss[4] = {0.f, 0.f, 0.f, 0.f}, tt[4] = {0.f, 0.f, 0.f, 0.f};
+          const float2* wi = Gop + (size_t)i * n;
+#pragma unroll 3
+          for (int j = lane; j <= i; j += 32) {
+            const float2 w = wi[j];
+            df_mac(ss[0], tt[0], w, ot0[j]);
+            df_mac(ss[1], tt[1], w, ot1[j]);
+            df_mac(ss[2], tt[2], w, ot2[j]);
+            df_mac(ss[3], tt[3], w, ot3[j]);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (q >= nb) break;
+            df_warp_sum(ss[q], tt[q]);
+            if (lane == 0) Xacc2[(size_t)(acc + 2 * q + 1) * n + i] = df_norm(ss[q], tt[q]);
+          }
+        }
+        __syncthreads();
+        pacc(3, tp);
+        tp = pstamp();
+        // 5. in-block Gram-Schmidt: x_q against the pairs accepted before it
+        // (dots and |x_q|^2 in one reduction; |x_q - proj|^2 = |x_q|^2 -
+        // sum of the squared coefficients), z_q with the same coefficients
+        // through G x_p = y_p, G y_p = -x_p, both scaled by 1 / |x_q - proj|
+        // (|G x| = |x| on this block); a candidate left with less than a
+        // quarter of its residual goes back to the pool
+        int nacc = 0;
+        for (int q = 0; q < nb; ++q) {
+          const float2* xq = Xacc2 + (size_t)(acc + 2 * q) * n;
+          const float2* zq = xq + n;
+          const int nd = 2 * nacc + 1;  // dots x_p . x_q, y_p . x_q (p < nacc), then |x_q|^2
+          float ss[7], tt[7];
+#pragma unroll
+          for (int e = 0; e < 7; ++e) ss[e] = tt[e] = 0.f;
+          for (int i = tid; i < n; i += nt) {
+            const float2 v = xq[i];
+#pragma unroll
+            for (int e = 0; e < 6; ++e)
+              if (e < nd - 1) df_mac(ss[e], tt[e], Xacc2[(size_t)(acc + e) * n + i], v);
+            df_mac(ss[6], tt[6], v, v);
+          }
+#pragma unroll
+          for (int e = 0; e < 7; ++e) {
+            if (e < nd - 1 || e == 6) {
+              df_warp_sum(ss[e], tt[e]);
+              if (lane == 0) bred[warp * 8 + e] = df_norm(ss[e], tt[e]);
+            }
+          }
+          __syncthreads();
+          if (tid < 7 && (tid < nd - 1 || tid == 6)) {
+            float2 v = bred[tid];
+            for (int w = 1; w < nw; ++w) v = df_add(v, bred[w * 8 + tid]);
+            bred[256 + tid] = v;
+          }
+          __syncthreads();
+          double rem = df_val(bred[256 + 6]);
+          for (int e = 0; e < nd - 1; ++e) {
+            const double cc = df_val(bred[256 + e]);
+            rem -= cc * cc;
+          }
+          if (nacc > 0 && !(rem > 0.25 * double(s_pickv[q]))) {  // block-uniform: back to the pool
+            if (tid == 0) used[cb + s_pick[q]] = 0;
+            __syncthreads();
+            continue;
+          }
+          if (!(rem > 0.0)) {  // the block's first candidate has no residual left
+            if (tid == 0) a.status[c] = 4;
+            return;
+          }
+          if (tid == 0) red[34] = 1.0 / sqrt(rem);
+          __syncthreads();
+          const float2 inv = df_split(red[34]);
+          float2 cf[6];
+#pragma unroll
+          for (int e = 0; e < 6; ++e) cf[e] = e < nd - 1 ? bred[256 + e] : make_float2(0.f, 0.f);
+          float2* xo = Xacc2 + (size_t)(acc + 2 * nacc) * n;  // compacted slot (nacc <= q)
+          float2* yo = xo + n;
+          for (int i = tid; i < n; i += nt) {
+            float sx = xq[i].x, tx = xq[i].y, sz = zq[i].x, tz = zq[i].y;
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+              if (p >= nacc) break;
+              const float2 xp = Xacc2[(size_t)(acc + 2 * p) * n + i], yp = Xacc2[(size_t)(acc + 2 * p + 1) * n + i];
+              const float2 c1 = make_float2(-cf[2 * p].x, -cf[2 * p].y), c2 = make_float2(-cf[2 * p + 1].x, -cf[2 * p + 1].y);
+              // x -= c1 x_p + c2 y_p;  z -= c1 y_p - c2 x_p
+              df_mac(sx, tx, c1, xp);
+              df_mac(sx, tx, c2, yp);
+              df_mac(sz, tz, c1, yp);
+              df_mac(sz, tz, cf[2 * p + 1], xp);
+            }
+            const float2 xn = df_mul(df_norm(sx, tx), inv), zn = df_mul(df_norm(sz, tz), inv);
+            xo[i] = xn;  // xo is row x_q itself or an earlier, unread (rejected) slot
+            yo[i] = zn;
+          }
+          __syncthreads();
+          if (tid == 0) MU[(acc + 2 * nacc) / 2] = sqrt(vec2[cb + s_pick[q]]);
+          ++nacc;
+        }
+        pacc(4, tp);
+        tp = pstamp();
+        // 6. FP32 residual tracking for the accepted pairs of this block
+        for (int e = 0; e < 2 * nacc; ++e) {
+          const float2* v = Xacc2 + (size_t)(acc + e) * n;
+          for (int i = tid; i < n; i += nt) xy32[(size_t)e * n + i] = v[i].x;
+        }
+        __syncthreads();
+        for (int r = warp; r < C; r += nw) {
+          if (used[cb + r]) continue;
+          const float* w = c32 + (size_t)r * n;
+          float sd[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) sd[e] = 0.f;
+          for (int i = lane; i < n; i += 32) {
+            const float wi = w[i];
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+              if (e < 2 * nacc) sd[e] = fmaf(xy32[(size_t)e * n + i], wi, sd[e]);
+          }
+          float sub = 0.f;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            if (e >= 2 * nacc) break;
+            float v = sd[e];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            sub += v * v;
+          }
+          if (lane == 0) r32[r] -= sub;
+        }
+        __syncthreads();
+        pacc(5, tp);
+        acc += 2 * nacc;
+      }
+      cb = ce;
+      continue;
+    }
     for (int pi = 0; pi < C / 2; ++pi) {
       if (tid < 32) {  // pivot: the unused candidate with the largest residual
         float bv = -1.f;
@@ -1289,11 +1689,16 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
   }
   int smem_optin = 0;
   BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-  const size_t jac = (size_t)m_max * (2 * m_max + 1) * sizeof(float);
+  const size_t jac = (size_t)m_max * (2 * m_max + 1) * sizeof(float), jac_h = (size_t)m_max * (m_max + 1) * sizeof(float);
   a.jac_smem_m = 0;
+  a.jac_q_smem = 0;
   if (wsm + jac <= (size_t)smem_optin) {
     a.jac_smem_m = m_max;
+    a.jac_q_smem = 1;
     wsm += jac;
+  } else if (wsm + jac_h <= (size_t)smem_optin) {
+    a.jac_smem_m = m_max;
+    wsm += jac_h;
   }
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
   BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0,
@@ -1303,15 +1708,20 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
 
 // Dynamic shared memory of a Williamson launch whose largest eigen-problem
 // is m_max (the FP32 Jacobi matrices in shared memory when they fit).
-static int williamson_smem(bsg_handle_t h, int m_max, size_t* wsm, int* jac_m) {
+static int williamson_smem(bsg_handle_t h, int m_max, size_t* wsm, int* jac_m, int* jac_q) {
   *wsm = (40 + 2 * kMaxCutModes) * 8 + 4 * kMaxCutModes * 4 + 6 * kMaxCutModes * 8 + kDfSmemBytes;
   int smem_optin = 0;
   BSG_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-  const size_t jac = (size_t)m_max * (2 * m_max + 1) * sizeof(float);
+  const size_t jac = (size_t)m_max * (2 * m_max + 1) * sizeof(float), jac_h = (size_t)m_max * (m_max + 1) * sizeof(float);
   *jac_m = 0;
+  *jac_q = 0;
   if (*wsm + jac <= (size_t)smem_optin) {
     *jac_m = m_max;
+    *jac_q = 1;
     *wsm += jac;
+  } else if (*wsm + jac_h <= (size_t)smem_optin) {
+    *jac_m = m_max;
+    *wsm += jac_h;
   }
   return BSG_OK;
 }
@@ -1342,9 +1752,12 @@ int cut_launch_batch(bsg_handle_t h, CutArgs* args, int n, void* dev, void* stag
   }
   if (total == 0) return BSG_OK;
   size_t wsm = 0;
-  int jac_m = 0;
-  BSG_TRY(williamson_smem(h, m_max, &wsm, &jac_m));
-  for (int i = 0; i < n; ++i) args[i].jac_smem_m = jac_m;
+  int jac_m = 0, jac_q = 0;
+  BSG_TRY(williamson_smem(h, m_max, &wsm, &jac_m, &jac_q));
+  for (int i = 0; i < n; ++i) {
+    args[i].jac_smem_m = jac_m;
+    args[i].jac_q_smem = jac_q;
+  }
   char* hs = reinterpret_cast<char*>(stage);
   std::memcpy(hs, args, sizeof(CutArgs) * n);
   int2* map = reinterpret_cast<int2*>(hs + al256(sizeof(CutArgs) * n));
@@ -1394,7 +1807,7 @@ int cut_read_phases(bsg_handle_t h, const CutArgs& a, cudaStream_t st) {
     }
     for (int i = kCutTimedPhases; i < kCutPhases; ++i)
       h->prof.cut_phases[(size_t)c * kCutPhases + i] = double(t[(size_t)c * kCutPhases + i]);
-    for (int i = kCutPhases - 3; i < kCutPhases; ++i) h->prof.cut_phases[(size_t)c * kCutPhases + i] *= 1e-6;  // ns -> ms
+    for (int i = kCutTimedPhases + 2; i < kCutPhases; ++i) h->prof.cut_phases[(size_t)c * kCutPhases + i] *= 1e-6;  // ns -> ms
   }
   return BSG_OK;
 }

@@ -175,11 +175,12 @@ struct CutArgs {
   double* mu;          // [n_cuts, 2 kmax] eigenvalues of G^T G, then 1/nu per pair
   int max_sweeps;
   int c0;              // first cut of this launch (block b handles cut c0 + b)
-  int jac_smem_m;      // > 0: the FP32 Jacobi matrices of eigen-problems up to this size live in shared memory
+  int jac_smem_m;      // > 0: the FP32 Jacobi matrix (and, with jac_q_smem, its eigenvectors) of eigen-problems up to this size live in shared memory
+  int jac_q_smem;      // 1: the FP32 eigenvector rows in shared memory too
   unsigned long long* phase_t;  // [n_cuts, kCutPhases] phase timestamps (profiling) or null
 };
 constexpr int kCutTimedPhases = 11;  // stamps 0..10
-constexpr int kCutPhases = 16;       // + FP32 sweeps, refinement steps, FP32 sweep / refinement product / refinement times (ns)
+constexpr int kCutPhases = 22;       // + FP32 sweeps, refinement steps, FP32 sweep / refinement product / refinement times, six pairing parts (ns)
 
 // A byte range to set to one byte value; many of them are cleared by one
 // launch (fill_spans).

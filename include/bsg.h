@@ -317,7 +317,10 @@ int bsg_gemm_tf32x3(bsg_handle_t h, const float* A, const float* B, float* C, in
  * 8 ordering, 9 pairing, 10 S and nbar; columns 11 and 12 are the FP32 Jacobi
  * sweeps and the refinement steps (counts, not times), columns 13, 14 and 15
  * the ms of the FP32 sweeps, of the refinement's products and of the whole
- * refinement inside phase 6.  Pass ms = NULL to query the sizes. */
+ * refinement inside phase 6, columns 16-21 the ms of six parts of the
+ * pairing (cluster setup, pivots and loads, projections, G products,
+ * in-block Gram-Schmidt, residual tracking; the blocked vacuum pairing).
+ * Pass ms = NULL to query the sizes. */
 int bsg_profile_cut_phases(bsg_handle_t h, int* n_cuts, int* n_phases, double* ms);
 
 /* Milestones of the last bsg_build_mps made while profiling was enabled, in

@@ -1517,6 +1517,9 @@ __device__ __forceinline__ void thermal_cut(const CutArgs& a, const int c) {
         i -= K;
         ++n;
       }
+      // the (i + 1)(n + 1) - 1 candidates (i' <= i, n' <= n) are >= v and come
+      // first on ties (flattened order), so rank >= (i + 1)(n + 1) - 1
+      if ((i + 1) * (n + 1) > Kn) continue;
       const unsigned long long v = prod[(size_t)n * chi + i];
       if (v <= tol) continue;
       int rank = 0;

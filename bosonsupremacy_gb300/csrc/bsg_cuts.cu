@@ -315,6 +315,89 @@ __device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B
   __syncthreads();
 }
 
+// The same tiling in FP64 (2 x 2 blocks per thread, NT / 256 K groups; the
+// tiles hold doubles): for the few products whose results must keep FP64
+// accuracy.
+template <int NT>
+__device__ __noinline__ void f64_gemm_t(const double* A, bool ta, const double* B, bool tb, const double* add,
+                                        double sign, double diag, double* C, int m, bool sym, float2* tiles) {
+  constexpr int G = NT / 256, KG = kDfTile / G, PER = kDfTile * kDfTile / NT;
+  double (*As)[kDfLd] = reinterpret_cast<double (*)[kDfLd]>(tiles);
+  double (*Bs)[kDfLd] = reinterpret_cast<double (*)[kDfLd]>(tiles + kDfTile * kDfLd);
+  double* red = reinterpret_cast<double*>(tiles);
+  const int tid = threadIdx.x, g = tid >> 8, l = tid & 255, tx = l & 15, ty = l >> 4;
+  const int nb = (m + kDfTile - 1) / kDfTile;
+  for (int ti = 0; ti < nb; ++ti)
+    for (int tj = sym ? ti : 0; tj < nb; ++tj) {
+      double sd[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int q0 = 0; q0 < m; q0 += kDfTile) {
+#pragma unroll
+        for (int o = 0; o < PER; ++o) {
+          const int e = tid + o * NT;
+          int r, c;
+          if (ta) {
+            r = e % kDfTile;
+            c = e / kDfTile;
+          } else {
+            r = e / kDfTile;
+            c = e % kDfTile;
+          }
+          const int ai = ti * kDfTile + r, aq = q0 + c;
+          As[c][r] = (ai < m && aq < m) ? (ta ? A[(size_t)aq * m + ai] : A[(size_t)ai * m + aq]) : 0.0;
+          if (tb) {
+            c = e % kDfTile;
+            r = e / kDfTile;
+          } else {
+            c = e / kDfTile;
+            r = e % kDfTile;
+          }
+          const int bq = q0 + c, bj = tj * kDfTile + r;
+          Bs[c][r] = (bq < m && bj < m) ? (tb ? B[(size_t)bj * m + bq] : B[(size_t)bq * m + bj]) : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = g * KG; kk < (g + 1) * KG; ++kk) {
+          const double a0 = As[kk][2 * ty], a1 = As[kk][2 * ty + 1], b0 = Bs[kk][2 * tx], b1 = Bs[kk][2 * tx + 1];
+          sd[0] = fma(a0, b0, sd[0]);
+          sd[1] = fma(a0, b1, sd[1]);
+          sd[2] = fma(a1, b0, sd[2]);
+          sd[3] = fma(a1, b1, sd[3]);
+        }
+        __syncthreads();
+      }
+      for (int gg = 1; gg < G; ++gg) {  // K groups added in group order
+        if (g == gg)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) red[l * 4 + u] = sd[u];
+        __syncthreads();
+        if (g == 0)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) sd[u] += red[l * 4 + u];
+        __syncthreads();
+      }
+      if (g == 0)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = ti * kDfTile + 2 * ty + (u >> 1), j = tj * kDfTile + 2 * tx + (u & 1);
+          if (i >= m || j >= m) continue;
+          double v = sign * sd[u];
+          if (add) v += add[(size_t)i * m + j];
+          if (i == j) v += diag;
+          C[(size_t)i * m + j] = v;
+          if (sym && tj != ti) C[(size_t)j * m + i] = v;
+        }
+    }
+  __syncthreads();
+}
+
+// The same block-wide product in FP64 (tiles: kDfSmemBytes, holding doubles).
+__device__ void f64_gemm(const double* A, bool ta, const double* B, bool tb, const double* add, double sign,
+                         double diag, double* C, int m, bool sym, float2* tiles) {
+  if (blockDim.x >= 1024) f64_gemm_t<1024>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  else if (blockDim.x >= 512) f64_gemm_t<512>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+  else f64_gemm_t<256>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+}
+
 __device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, const double* add, double sign,
                         double diag, double* C, int m, bool sym, float2* tiles) {
   if (blockDim.x >= 1024) df_gemm_t<1024>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
@@ -452,10 +535,13 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
   if (settled && !converged && m <= kMaxCutModes) {  // (lam fills cs; sn is free for the small Jacobi)
     // Clusters (eigenvalues chained by gaps <= max(delta, tau_gap), in sorted
     // order) whose vectors are an orthonormal basis of their eigenspace but
-    // still mixed: for each, S_c = QT_c Hm QT_c^T in FP64 (p x p), cyclic
-    // FP64 Jacobi on it, QT_c <- R QT_c and its eigenvalues.  The rotation
-    // scratch of the small Jacobi is sn / pos + 256, so lam (cs) and the
-    // sorted order (pos) survive.
+    // still mixed.  S = QT Hm QT^T once (FP64, tiled);
+    // for each cluster its p x p block (shared memory, odd stride, when it
+    // fits in the FP32 Jacobi area: free now) by cyclic FP64 Jacobi, the
+    // rotations gathered into a block-diagonal R (identity outside the
+    // clusters) and QT <- R QT in one product.  The rotation scratch of the
+    // small Jacobi is sn / pos + 256, so lam (cs) and the sorted order (pos)
+    // survive.
     __shared__ int s_g0, s_g1;
     int* ord = pos;
     for (int i = tid; i < m; i += nt) {
@@ -465,8 +551,17 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
       ord[r] = i;
     }
     if (tid == 0) s_g1 = 0;
+    // S in FP64: the eigenvalues of a cluster of K near 1 carry a small nbar
+    // in 1 - mu, which double-float products would blur
+    f64_gemm(Hm, false, QT, true, nullptr, 1.0, 0.0, s2, m, false, dft);  // T = Hm QT^T
+    f64_gemm(QT, false, s2, false, nullptr, 1.0, 0.0, s3, m, true, dft);  // S = QT T
+    for (int i = warp; i < m; i += nw)
+      for (int j = lane; j < m; j += 32) s2[(size_t)i * m + j] = i == j ? 1.0 : 0.0;  // R
     __syncthreads();
     const double chain = fmax(delta_last, tau_gap);
+    const size_t jsm_bytes = jsm ? (size_t)m * (m + 1) * sizeof(float) : 0;  // the FP32 matrix area
+    double* sblk = reinterpret_cast<double*>(jsm);
+    double* rblk = s1;
     bool ok = true;
     while (true) {
       __syncthreads();  // every thread has read the previous cluster's bounds
@@ -479,46 +574,31 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
       __syncthreads();
       const int g0 = s_g0, g1 = s_g1, p = g1 - g0;
       if (g0 >= m) break;
-      if (p >= 2) {
-        // U = QT_c Hm (p x m, in s2), S_c = U QT_c^T (p x p, in s3), R = I (s1)
-        for (int a = warp; a < p; a += nw) {
-          const double* qa = QT + (size_t)ord[g0 + a] * m;
-          for (int j = lane; j < m; j += 32) {
-            double u = 0.0;
-            for (int i = 0; i < m; ++i) u = fma(qa[i], Hm[(size_t)i * m + j], u);
-            s2[(size_t)a * m + j] = u;
-          }
-        }
-        __syncthreads();
-        for (int t = warp; t < p * p; t += nw) {
-          const int a = t / p, b2 = t - a * p;
-          const double* qb = QT + (size_t)ord[g0 + b2] * m;
-          double u = 0.0;
-          for (int j = lane; j < m; j += 32) u = fma(s2[(size_t)a * m + j], qb[j], u);
-          for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
-          if (lane == 0) {
-            s3[t] = u;
-            s1[t] = a == b2 ? 1.0 : 0.0;
-          }
-        }
-        __syncthreads();
-        const int swc = block_jacobi<double>(s3, p, p, s1, 60, 1e-26, red, sn, sn + kMaxCutModes / 2, pos + 256);
-        if (swc < 0) ok = false;
-        // QT_c <- R QT_c (through s2), eigenvalues from the diagonal
-        for (int a = warp; a < p; a += nw)
-          for (int j = lane; j < m; j += 32) {
-            double u = 0.0;
-            for (int b2 = 0; b2 < p; ++b2) u = fma(s1[(size_t)a * p + b2], QT[(size_t)ord[g0 + b2] * m + j], u);
-            s2[(size_t)a * m + j] = u;
-          }
-        __syncthreads();
-        for (int a = warp; a < p; a += nw) {
-          double* qa = QT + (size_t)ord[g0 + a] * m;
-          for (int j = lane; j < m; j += 32) qa[j] = s2[(size_t)a * m + j];
-          if (lane == 0) lam[ord[g0 + a]] = s3[(size_t)a * p + a];
-        }
-        __syncthreads();
+      if (p < 2) continue;
+      const bool in_smem = (size_t)p * (p + 1) * sizeof(double) <= jsm_bytes;
+      const int ldb = in_smem ? p + 1 : p;
+      double* sb = in_smem ? sblk : s1 + (size_t)p * p;  // s1 holds 2 p^2 when p^2 <= m^2 / 2
+      if (!in_smem && 2 * (size_t)p * p > (size_t)m * m) {  // no room: leave it to the restart
+        ok = false;
+        break;
       }
+      for (int a = warp; a < p; a += nw)
+        for (int b2 = lane; b2 < p; b2 += 32) {
+          sb[(size_t)a * ldb + b2] = s3[(size_t)ord[g0 + a] * m + ord[g0 + b2]];
+          rblk[(size_t)a * p + b2] = a == b2 ? 1.0 : 0.0;
+        }
+      __syncthreads();
+      if (block_jacobi<double>(sb, p, ldb, rblk, 60, 1e-26, red, sn, sn + kMaxCutModes / 2, pos + 256) < 0) ok = false;
+      for (int a = warp; a < p; a += nw) {
+        for (int b2 = lane; b2 < p; b2 += 32) s2[(size_t)ord[g0 + a] * m + ord[g0 + b2]] = rblk[(size_t)a * p + b2];
+        if (lane == 0) lam[ord[g0 + a]] = sb[(size_t)a * ldb + a];
+      }
+    }
+    __syncthreads();
+    if (ok) {
+      df_gemm(s2, false, QT, false, nullptr, 1.0, 0.0, s3, m, false, dft);  // R QT
+      for (size_t t = tid; t < mm; t += nt) QT[t] = s3[t];
+      __syncthreads();
     }
     converged = ok;
   }

@@ -17,6 +17,7 @@
 #include <condition_variable>
 #include <mutex>
 #include <thread>
+#include <unordered_set>
 #include <cstring>
 #include <functional>
 #include <numeric>
@@ -1272,12 +1273,24 @@ static int plan_sites_parallel(bsg::ProgramSet& ps, const uint64_t* const* kl, c
       return BSG_ERR_LIMIT;
     }
   if (ph) ph[0] += plan_ms_since(t_ph);
-  // phase B: new programs, serially (only the keys phase A did not find)
-  for (int s = 0; s < ns; ++s)
-    for (uint64_t k : cb[s].missing) {
-      int32_t prog;
-      BSG_TRY(program_for_key(ps, k, &prog));
+  // phase B: new programs (only the keys phase A did not find), built in
+  // parallel and appended in site / key order
+  {
+    std::vector<uint64_t> uniq;
+    std::unordered_set<uint64_t> seen_k;
+    for (int s = 0; s < ns; ++s)
+      for (uint64_t k : cb[s].missing)
+        if (!ps.index.count(k) && seen_k.insert(k).second) uniq.push_back(k);
+    std::vector<ProgramBuild> built(uniq.size());
+    parallel_for(int(uniq.size()), [&](int i) { build_program(uniq[i], built[i]); });
+    for (size_t i = 0; i < uniq.size(); ++i) {
+      if (built[i].err != BSG_OK) {
+        set_error("%s", built[i].msg.c_str());
+        return built[i].err;
+      }
+      append_program(ps, uniq[i], built[i]);
     }
+  }
   if (ph) ph[1] += plan_ms_since(t_ph);
   // phase C: per-site buckets (read-only program index)
   std::vector<std::vector<int32_t>> lprog(ns);

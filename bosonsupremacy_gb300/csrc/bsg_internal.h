@@ -99,6 +99,16 @@ int key_classes(uint64_t key);          // number of classes
 // Returns the program index for `key` (generating it on first use), or a
 // negative status.
 int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out);
+// A program built apart from the set (thread-safe) and its serial append.
+struct ProgramBuild {
+  int k = 0, nstates = 0, fslots = 1, err = 0;
+  std::string msg;
+  std::vector<int> mult, st_trans_off, st_trans_cnt, st_ra;
+  std::vector<uint32_t> trans;
+  std::vector<uint4> st_pack;
+};
+int build_program(uint64_t key, ProgramBuild& b);
+int append_program(ProgramSet& ps, uint64_t key, const ProgramBuild& b);
 int programs_upload(ProgramSet& ps, cudaStream_t stream);
 void programs_free(ProgramSet& ps);
 

@@ -29,25 +29,27 @@ int key_classes(uint64_t key) {
   return k;
 }
 
-int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
-  auto it = ps.index.find(key);
-  if (it != ps.index.end()) {
-    *prog_out = it->second;
-    return BSG_OK;
-  }
+// The program of one key, built apart from the program set (thread-safe:
+// the planner builds the new keys of a build in parallel and appends them in
+// a fixed order).  On failure b.err holds the status and b.msg the message.
+int build_program(uint64_t key, ProgramBuild& b) {
   // site programs: jroot = jmax >= 0 (the site class last, roots at jmax, jmax - 2, ...)
   const int jroot = int(key >> kKeyRootShift) - 1;
   const uint64_t xkey = key & ((uint64_t(1) << kKeyRootShift) - 1);
-  std::vector<int> mult;
+  std::vector<int>& mult = b.mult;
+  mult.clear();
   for (int v = 1; v <= kKeyMaxMult; ++v) {
     int c = int((xkey >> (kKeyBits * (v - 1))) & 63);
     for (int i = 0; i < c; ++i) mult.push_back(v);
   }
   if (jroot >= 0) mult.push_back(jroot);
   const int k = int(mult.size());
+  b.k = k;
   if (k > BSG_MAX_CLASSES) {
-    set_error("hafnian with %d distinct indices exceeds BSG_MAX_CLASSES=%d", k, BSG_MAX_CLASSES);
-    return BSG_ERR_LIMIT;
+    b.err = BSG_ERR_LIMIT;
+    b.msg = "hafnian with " + std::to_string(k) + " distinct indices exceeds BSG_MAX_CLASSES=" +
+            std::to_string(BSG_MAX_CLASSES);
+    return b.err;
   }
   // Enumerate the states reachable from the root(s).
   std::unordered_map<std::string, int> seen;
@@ -67,31 +69,33 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
     stack.push_back(full);
   }
   while (!stack.empty()) {
-    std::string s = std::move(stack.back());
+    std::string st = std::move(stack.back());
     stack.pop_back();
-    if (seen.count(s)) continue;
-    seen.emplace(s, int(states.size()));
-    states.push_back(s);
+    if (seen.count(st)) continue;
+    seen.emplace(st, int(states.size()));
+    states.push_back(st);
     if (int(states.size()) > BSG_MAX_STATES) {
-      set_error("partition with %d classes (n=%d) needs more than BSG_MAX_STATES=%d DP states", k,
-                key_order(xkey) + std::max(jroot, 0), BSG_MAX_STATES);
-      return BSG_ERR_LIMIT;
+      b.err = BSG_ERR_LIMIT;
+      b.msg = "partition with " + std::to_string(k) + " classes (n=" +
+              std::to_string(key_order(xkey) + std::max(jroot, 0)) + ") needs more than BSG_MAX_STATES=" +
+              std::to_string(BSG_MAX_STATES) + " DP states";
+      return b.err;
     }
     int a = 0;
-    while (a < k && s[a] == 0) ++a;
+    while (a < k && st[a] == 0) ++a;
     if (a == k) continue;
-    for (int b = a; b < k; ++b) {
-      if (s[b] == 0 || (b == a && s[a] < 2)) continue;
-      std::string t = s;
+    for (int c = a; c < k; ++c) {
+      if (st[c] == 0 || (c == a && st[a] < 2)) continue;
+      std::string t = st;
       t[a]--;
-      t[b]--;
+      t[c]--;
       if (!seen.count(t)) stack.push_back(t);
     }
   }
   // Topological order: ascending total (every transition removes two units).
-  auto total = [](const std::string& s) {
+  auto total = [](const std::string& x) {
     int t = 0;
-    for (char c : s) t += c;
+    for (char c : x) t += c;
     return t;
   };
   std::vector<int> order(states.size());
@@ -120,45 +124,81 @@ int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
       slot[i] = (lv & 1) * width + pos[i];
     }
   }
-
-  const int prog = int(ps.keys.size());
-  const int base = int(ps.st_trans_off.size());
-  ps.keys.push_back(key);
-  ps.k.push_back(k);
-  ps.nstates.push_back(int(states.size()));
-  ps.state_off.push_back(base);
-  ps.fslots.push_back(states.size() > 1 ? 2 * width : 1);
-  for (int c = 0; c < BSG_MAX_CLASSES; ++c) ps.mult.push_back(c < k ? mult[c] : 0);
+  b.nstates = int(states.size());
+  b.fslots = states.size() > 1 ? 2 * width : 1;
+  b.trans.clear();
+  b.st_trans_off.clear();
+  b.st_trans_cnt.clear();
+  b.st_ra.clear();
+  b.st_pack.clear();
   for (size_t i = 0; i < order.size(); ++i) {
-    const std::string& s = states[order[i]];
-    ps.st_trans_off.push_back(int(ps.trans.size()));
+    const std::string& st = states[order[i]];
+    b.st_trans_off.push_back(int(b.trans.size()));  // relative to the program's first transition
     int a = 0;
-    while (a < k && s[a] == 0) ++a;
+    while (a < k && st[a] == 0) ++a;
     int cnt = 0;
     if (a < k) {
-      for (int b = a; b < k; ++b) {
-        if (s[b] == 0 || (b == a && s[a] < 2)) continue;
-        std::string t = s;
+      for (int c = a; c < k; ++c) {
+        if (st[c] == 0 || (c == a && st[a] < 2)) continue;
+        std::string t = st;
         t[a]--;
-        t[b]--;
+        t[c]--;
         const uint32_t src = uint32_t(slot[local[seen.at(t)]]);
-        ps.trans.push_back((src << 9) | (uint32_t(b) << 2));
+        b.trans.push_back((src << 9) | (uint32_t(c) << 2));
         ++cnt;
       }
     }
-    ps.st_trans_cnt.push_back(cnt);
-    ps.st_ra.push_back(a < k ? int(s[a]) : 0);
-    auto rj = root_j.find(s);
+    b.st_trans_cnt.push_back(cnt);
+    b.st_ra.push_back(a < k ? int(st[a]) : 0);
+    auto rj = root_j.find(st);
     const uint32_t tag = rj == root_j.end() ? 0u : uint32_t(rj->second + 1);
-    ps.st_pack.push_back(make_uint4(uint32_t(ps.st_trans_off.back()),
-                                    uint32_t(cnt) | (uint32_t(a < k ? s[a] : 0) << 8) | (tag << 16),
-                                    uint32_t(slot[i]), uint32_t(a < k ? a : 0)));
+    b.st_pack.push_back(make_uint4(uint32_t(b.st_trans_off.back()),
+                                   uint32_t(cnt) | (uint32_t(a < k ? st[a] : 0) << 8) | (tag << 16),
+                                   uint32_t(slot[i]), uint32_t(a < k ? a : 0)));
   }
+  b.err = BSG_OK;
+  return BSG_OK;
+}
+
+// Appends a built program to the set (serial); returns its index.
+int append_program(ProgramSet& ps, uint64_t key, const ProgramBuild& b) {
+  const int prog = int(ps.keys.size());
+  const int base = int(ps.st_trans_off.size());
+  const uint32_t toff = uint32_t(ps.trans.size());
+  ps.keys.push_back(key);
+  ps.k.push_back(b.k);
+  ps.nstates.push_back(b.nstates);
+  ps.state_off.push_back(base);
+  ps.fslots.push_back(b.fslots);
+  for (int c = 0; c < BSG_MAX_CLASSES; ++c) ps.mult.push_back(c < b.k ? b.mult[c] : 0);
+  for (int i = 0; i < b.nstates; ++i) {
+    ps.st_trans_off.push_back(int(toff) + b.st_trans_off[i]);
+    ps.st_trans_cnt.push_back(b.st_trans_cnt[i]);
+    ps.st_ra.push_back(b.st_ra[i]);
+    uint4 pk = b.st_pack[i];
+    pk.x += toff;
+    ps.st_pack.push_back(pk);
+  }
+  ps.trans.insert(ps.trans.end(), b.trans.begin(), b.trans.end());
   ps.index.emplace(key, prog);
-  ps.max_states = std::max(ps.max_states, int(states.size()));
-  ps.max_k = std::max(ps.max_k, k);
+  ps.max_states = std::max(ps.max_states, b.nstates);
+  ps.max_k = std::max(ps.max_k, b.k);
   ps.dev_valid = false;
-  *prog_out = prog;
+  return prog;
+}
+
+int program_for_key(ProgramSet& ps, uint64_t key, int32_t* prog_out) {
+  auto it = ps.index.find(key);
+  if (it != ps.index.end()) {
+    *prog_out = it->second;
+    return BSG_OK;
+  }
+  ProgramBuild b;
+  if (build_program(key, b) != BSG_OK) {
+    set_error("%s", b.msg.c_str());
+    return b.err;
+  }
+  *prog_out = append_program(ps, key, b);
   return BSG_OK;
 }
 

@@ -38,6 +38,7 @@ KNOBS = {
     "dp_hold": _lib.TUNE_DP_HOLD,
     "right_pct": _lib.TUNE_RIGHT_PCT,
     "left_pct": _lib.TUNE_LEFT_PCT,
+    "factor_dual": _lib.TUNE_FACTOR_DUAL,
 }
 
 

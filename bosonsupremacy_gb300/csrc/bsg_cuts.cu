@@ -1783,9 +1783,18 @@ int cut_launch_williamson(bsg_handle_t h, const CutArgs& args, int c0, int c1, c
     a.jac_smem_m = m_max;
     wsm += jac_h;
   }
+  // two CTAs of half the threads per SM when two fit in its shared memory
+  // (small eigen-problems): the factorisation steps are latency-bound, so
+  // each SM serves two cuts for little more than one cut's time
+  int threads = h->tune[BSG_TUNE_FACTOR_THREADS];
+  if (h->tune[BSG_TUNE_FACTOR_DUAL] && threads >= 512) {
+    int smem_sm = 0, reserved = 0;
+    BSG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device));
+    BSG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, h->device));
+    if (2 * (wsm + (size_t)reserved + 64) <= (size_t)smem_sm) threads /= 2;
+  }
   BSG_CUDA(cudaFuncSetAttribute(williamson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0,
-               (williamson_kernel<<<c1 - c0, h->tune[BSG_TUNE_FACTOR_THREADS], wsm, st>>>(a)));
+  BSG_PROFILED(h, BSG_K_WILLIAMSON, st, 0.0, (williamson_kernel<<<c1 - c0, threads, wsm, st>>>(a)));
   return BSG_OK;
 }
 

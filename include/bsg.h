@@ -399,7 +399,10 @@ int bsg_potrf_f64(bsg_handle_t h, double* A, int n, int* info, bsg_stream_t stre
                                         0 = built-in (33; 40 when Gamma goes to the host) */
 #define BSG_TUNE_LEFT_PCT 11         /* pipelined build: percent of the cuts in the left group, 5..60,
                                         0 = built-in (33; 30 when Gamma goes to the host) */
-#define BSG_TUNE_COUNT 12
+#define BSG_TUNE_FACTOR_DUAL 12       /* Williamson launches: 1 = two CTAs of half the threads per SM when two fit
+                                        in shared memory (the launches of small eigen-problems), 0 = one CTA of
+                                        BSG_TUNE_FACTOR_THREADS (default 0) */
+#define BSG_TUNE_COUNT 13
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

@@ -259,6 +259,21 @@ __global__ void pad_items_kernel(const int32_t* __restrict__ bucket_end, const i
   if (slot < (int64_t)bucket_chunk[b + 1] * 32) items[slot] = -1;
 }
 
+// The bucket of each chunk (the last b with bucket_chunk[b] <= c), so that a
+// DP warp finds its chunk's bucket with one load.
+__global__ void chunk_bucket_kernel(const int32_t* __restrict__ bucket_chunk, int nb, int64_t n_chunks,
+                                    int32_t* __restrict__ out) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_chunks) return;
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((int64_t)bucket_chunk[mid] <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  out[c] = lo;
+}
+
 // ---------------------------------------------------------------------------
 // The DP kernel
 // ---------------------------------------------------------------------------
@@ -296,6 +311,7 @@ struct DPArgs {
   const int32_t* items;
   // chunks (32 item slots) of bucket b are [bucket_chunk[b], bucket_chunk[b+1])
   const int32_t* bucket_chunk;  // [nb + 1]
+  const int32_t* chunk_bucket;  // [chunks] the bucket of each chunk, or null (binary search in bucket_chunk)
   const int32_t* bucket_prog;   // [nb]
   const int32_t* bucket_site;   // [nb] (site mode)
   int nb;
@@ -433,12 +449,18 @@ __global__ void __launch_bounds__(kDPThreads, 1280 / kDPThreads) dp_kernel(DPArg
     c = __shfl_sync(0xffffffffu, c, 0);
     if ((int64_t)c >= a.n_chunks) break;
     c += (unsigned long long)a.chunk_base;
-    // bucket of chunk c: the last b with bucket_chunk[b] <= c
-    int lo = 0, hi = a.nb - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if ((unsigned long long)a.bucket_chunk[mid] <= c) lo = mid;
-      else hi = mid - 1;
+    // bucket of chunk c: the last b with bucket_chunk[b] <= c (one load from
+    // the per-chunk table where the plan has one, else a binary search)
+    int lo = 0;
+    if (a.chunk_bucket) {
+      lo = __ldg(a.chunk_bucket + c);
+    } else {
+      int hi = a.nb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((unsigned long long)a.bucket_chunk[mid] <= c) lo = mid;
+        else hi = mid - 1;
+      }
     }
     const int prog = a.bucket_prog[lo];
     const SiteDesc* sd = MODE == MODE_SITE ? a.sites + a.bucket_site[lo] : nullptr;
@@ -1434,6 +1456,8 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
   const size_t o_boff = carve((size_t)nb * 4 + 4), o_bend = carve((size_t)nb * 4 + 4);
   const size_t o_bch = carve((size_t)nb * 4 + 4), o_bpr = carve((size_t)nb * 4 + 4),
                o_bsi = carve((size_t)nb * 4 + 4), o_ctr = carve(16), o_sp = carve(sizeof(SitePlanDev) * ns);
+  const int64_t n_chunks = nb ? bk.chunk_start[nb] : 0;
+  const size_t o_cbk = carve((size_t)n_chunks * 4 + 4);
   const size_t plan_bytes = off;
   BSG_TRY(slot.plan.ensure(plan_bytes));
   BSG_TRY(slot.stage.ensure(plan_bytes));
@@ -1539,10 +1563,16 @@ static int run_sites(bsg_handle_t h, const std::vector<SiteInput>& in, int d, in
     BSG_PROFILED(h, BSG_K_PREP, st, pairs,
                  (site_scatter_kernel<<<dim3(bx, ns), 256, 0, st>>>(reinterpret_cast<const SitePlanDev*>(dp + o_sp))));
   }
+  int32_t* d_cbk = reinterpret_cast<int32_t*>(dp + o_cbk);
+  if (n_chunks > 0)
+    BSG_PROFILED(h, BSG_K_PREP, st, (double)n_chunks,
+                 (chunk_bucket_kernel<<<unsigned((n_chunks + 255) / 256), 256, 0, st>>>(
+                     reinterpret_cast<const int32_t*>(dp + o_bch), nb, n_chunks, d_cbk)));
   DPArgs a{};
   a.prog = prog_dev(ps);
   a.items = d_items;
   a.bucket_chunk = reinterpret_cast<int32_t*>(dp + o_bch);
+  a.chunk_bucket = d_cbk;
   a.bucket_prog = reinterpret_cast<int32_t*>(dp + o_bpr);
   a.bucket_site = reinterpret_cast<int32_t*>(dp + o_bsi);
   a.nb = nb;

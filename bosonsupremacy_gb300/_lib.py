@@ -24,7 +24,7 @@ HOST_CLASSES = {K_HOST_PLAN: "host_plan", K_HOST_WAIT: "host_wait"}
 OUT_C64, OUT_C128 = 0, 1
 (TUNE_DP_BLOCKS_PER_SM, TUNE_DP_L1_CARVEOUT, TUNE_DP_SMALL_ENTRIES, TUNE_DP_SMALL_BLOCKS, TUNE_DP_SCRATCH_MIB,
  TUNE_DP_FP64_BLOCKS, TUNE_FACTOR_THREADS, TUNE_GEMM_KERNEL, TUNE_DP_QUANTUM, TUNE_DP_HOLD, TUNE_RIGHT_PCT,
- TUNE_LEFT_PCT, TUNE_FACTOR_DUAL) = range(13)
+ TUNE_LEFT_PCT, TUNE_FACTOR_DUAL, TUNE_DP_ORDER) = range(14)
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "input not positive definite",
           -4: "no convergence", -5: "size limit exceeded", -6: "allocation failed"}

@@ -39,6 +39,7 @@ KNOBS = {
     "right_pct": _lib.TUNE_RIGHT_PCT,
     "left_pct": _lib.TUNE_LEFT_PCT,
     "factor_dual": _lib.TUNE_FACTOR_DUAL,
+    "dp_order": _lib.TUNE_DP_ORDER,
 }
 
 

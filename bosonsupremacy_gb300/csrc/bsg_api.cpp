@@ -231,6 +231,7 @@ int bsg_tune_set(bsg_handle_t h, int key, int value) {
     BSG_CHECK_ARG(value == 0 || (value >= 5 && value <= 60), "bsg_tune_set: group share %d %%", value);
   if (key == BSG_TUNE_DP_HOLD) BSG_CHECK_ARG(value == 0 || value == 1, "bsg_tune_set: DP hold %d", value);
   if (key == BSG_TUNE_FACTOR_DUAL) BSG_CHECK_ARG(value == 0 || value == 1, "bsg_tune_set: factor dual %d", value);
+  if (key == BSG_TUNE_DP_ORDER) BSG_CHECK_ARG(value >= 0 && value <= 3, "bsg_tune_set: DP order %d", value);
   if (key == BSG_TUNE_DP_QUANTUM)
     BSG_CHECK_ARG(value >= 0 && value <= (1 << 20), "bsg_tune_set: DP quantum %d", value);
   h->tune[key] = value;

@@ -1821,9 +1821,14 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   std::vector<Group> groups;
   if (T1 > 0) {
     BSG_TRY(h->ensure_aux());
-    groups.push_back(Group{T2, nc, T2 + 1, M, h->grp[0], h->dp_lo[0], 2});
-    groups.push_back(Group{0, T1, 0, T1, h->grp[1], h->dp_lo[1], 1});
-    groups.push_back(Group{T1, T2, T1, T2 + 1, h->grp[2], h->dp_lo[2], 0});
+    // DP streams by priority: dp_lo[0] > dp_lo[2] > dp_lo[1]; the order of the
+    // groups (right, left, middle) over them is a tuning knob
+    cudaStream_t hi = h->dp_lo[0], mid = h->dp_lo[2], lo = h->dp_lo[1];
+    cudaStream_t ds[4][3] = {{hi, lo, mid}, {mid, hi, lo}, {lo, hi, mid}, {lo, mid, hi}};
+    const int order = h->tune[BSG_TUNE_DP_ORDER];
+    groups.push_back(Group{T2, nc, T2 + 1, M, h->grp[0], ds[order][0], 2});
+    groups.push_back(Group{0, T1, 0, T1, h->grp[1], ds[order][1], 1});
+    groups.push_back(Group{T1, T2, T1, T2 + 1, h->grp[2], ds[order][2], 0});
   } else {
     groups.push_back(Group{0, nc, 0, M, st, st, 0});
   }

@@ -308,7 +308,7 @@ struct bsg_handle_s {
     bsg::DevBuf plan, items, scratch;
     bsg::HostBuf stage;
   } slot[12];
-  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1, 2, 0, 0, 0, 0};
+  int tune[BSG_TUNE_COUNT] = {8, 0, 64, 8, 8192, 0, 1024, 1, 2, 0, 0, 0, 0, 0};
 };
 
 // Brackets a kernel launch with profiler events when profiling is on.

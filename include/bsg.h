@@ -402,7 +402,10 @@ int bsg_potrf_f64(bsg_handle_t h, double* A, int n, int* info, bsg_stream_t stre
 #define BSG_TUNE_FACTOR_DUAL 12       /* Williamson launches: 1 = two CTAs of half the threads per SM when two fit
                                         in shared memory (the launches of small eigen-problems), 0 = one CTA of
                                         BSG_TUNE_FACTOR_THREADS (default 0) */
-#define BSG_TUNE_COUNT 13
+#define BSG_TUNE_DP_ORDER 13         /* pipelined build: priority order of the groups' DP streams, 0 = right >
+                                        middle > left, 1 = left > right > middle, 2 = left > middle > right,
+                                        3 = middle > left > right (default 0) */
+#define BSG_TUNE_COUNT 14
 int bsg_tune_set(bsg_handle_t h, int key, int value);
 int bsg_tune_get(bsg_handle_t h, int key, int* value);
 

@@ -835,30 +835,35 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     __syncthreads();
     // Householder QR of F (columns = rows of FT); taus in dots[], the current
     // reflector v (v_j = 1) staged in vec
+    // (the reflector of a column by warp 0 alone: two block barriers per
+    // column instead of five)
     for (int j = 0; j < nA; ++j) {
       double* fj = FT + (size_t)j * n;
-      double s2 = 0.0;
-      for (int i = j + 1 + tid; i < n; i += nt) s2 += fj[i] * fj[i];
-      s2 = block_sum(s2, red);
-      const double x0 = fj[j];
-      double beta = x0, tau = 0.0, scale = 0.0;
-      if (s2 > 0.0) {
-        beta = -copysign(sqrt(x0 * x0 + s2), x0);
-        tau = (beta - x0) / beta;
-        scale = 1.0 / (x0 - beta);
+      if (warp == 0) {
+        double s2 = 0.0;
+        for (int i = j + 1 + lane; i < n; i += 32) s2 += fj[i] * fj[i];
+        for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        const double x0 = fj[j];
+        double beta = x0, tau = 0.0, scale = 0.0;
+        if (s2 > 0.0) {
+          beta = -copysign(sqrt(x0 * x0 + s2), x0);
+          tau = (beta - x0) / beta;
+          scale = 1.0 / (x0 - beta);
+        }
+        for (int i = j + 1 + lane; i < n; i += 32) {
+          const double v = fj[i] * scale;
+          fj[i] = v;
+          vec[i] = v;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          fj[j] = beta;
+          dots[j] = tau;
+          vec[j] = 1.0;
+        }
       }
       __syncthreads();
-      for (int i = j + 1 + tid; i < n; i += nt) {
-        const double v = fj[i] * scale;
-        fj[i] = v;
-        vec[i] = v;
-      }
-      if (tid == 0) {
-        fj[j] = beta;
-        dots[j] = tau;
-        vec[j] = 1.0;
-      }
-      __syncthreads();
+      const double tau = dots[j];
       // apply to the trailing columns: one warp per column (row of FT)
       for (int col = j + 1 + warp; col < nA; col += nw) {
         double* fc = FT + (size_t)col * n;

@@ -186,7 +186,9 @@ constexpr size_t kDfSmemBytes = 2 * kDfTile * kDfLd * sizeof(float2);
 // C[i][j] = add[i][j] + sign * sum_q A(i, q) B(q, j) (+ diag where i == j),
 // all m x m row-major, A(i, q) = ta ? A[q][i] : A[i][q], B(q, j) = tb ? B[j][q]
 // : B[q][j].  sym: the result is symmetric -- only tiles on or above the
-// diagonal are computed and mirrored.  C must not alias A, B or add unless
+// diagonal are computed and mirrored.  b_upper: B(q, j) = 0 for q > j (B is
+// the transpose of a lower-triangular factor), so the K loop of a column
+// tile stops after its diagonal tile.  C must not alias A, B or add unless
 // add == C (each entry of C is read before it is written, by the same
 // thread).  tiles: kDfSmemBytes of shared memory.  Block-wide (barriers).
 // NT threads (256, 512 or 1024): 32 x 32 output tiles, each thread a 2 x 2
@@ -195,7 +197,8 @@ constexpr size_t kDfSmemBytes = 2 * kDfTile * kDfLd * sizeof(float2);
 // sums are added in a tree through shared memory at the end of a tile.
 template <int NT>
 __device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B, bool tb, const double* add,
-                                       double sign, double diag, double* C, int m, bool sym, float2* tiles) {
+                                       double sign, double diag, double* C, int m, bool sym, float2* tiles,
+                                       bool b_upper) {
   constexpr int G = NT / 256, KG = kDfTile / G, PER = kDfTile * kDfTile / NT;
   float2 (*As)[kDfLd] = reinterpret_cast<float2 (*)[kDfLd]>(tiles);  // [k][row]
   float2 (*Bs)[kDfLd] = reinterpret_cast<float2 (*)[kDfLd]>(tiles + kDfTile * kDfLd);  // [k][col]
@@ -230,6 +233,7 @@ __device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B
   for (int ti = 0; ti < nb; ++ti)
     for (int tj = sym ? ti : 0; tj < nb; ++tj) {
       float s[4] = {0.f, 0.f, 0.f, 0.f}, t[4] = {0.f, 0.f, 0.f, 0.f};
+      const int qend = b_upper ? min(m, (tj + 1) * kDfTile) : m;
       // the K chunk q0 is in registers while chunk q0 - 32 is multiplied
       double pa[PER], pb[PER];
       int r, c;
@@ -238,7 +242,7 @@ __device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B
         pa[o] = a_at(ti, 0, tid + o * NT, r, c);
         pb[o] = b_at(tj, 0, tid + o * NT, r, c);
       }
-      for (int q0 = 0; q0 < m; q0 += kDfTile) {
+      for (int q0 = 0; q0 < qend; q0 += kDfTile) {
 #pragma unroll
         for (int o = 0; o < PER; ++o) {
           const int e = tid + o * NT;
@@ -260,7 +264,7 @@ __device__ __noinline__ void df_gemm_t(const double* A, bool ta, const double* B
           Bs[c][r] = df_split(pb[o]);
         }
         __syncthreads();
-        if (q0 + kDfTile < m) {
+        if (q0 + kDfTile < qend) {
 #pragma unroll
           for (int o = 0; o < PER; ++o) {
             pa[o] = a_at(ti, q0 + kDfTile, tid + o * NT, r, c);
@@ -399,10 +403,10 @@ __device__ void f64_gemm(const double* A, bool ta, const double* B, bool tb, con
 }
 
 __device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, const double* add, double sign,
-                        double diag, double* C, int m, bool sym, float2* tiles) {
-  if (blockDim.x >= 1024) df_gemm_t<1024>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
-  else if (blockDim.x >= 512) df_gemm_t<512>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
-  else df_gemm_t<256>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles);
+                        double diag, double* C, int m, bool sym, float2* tiles, bool b_upper = false) {
+  if (blockDim.x >= 1024) df_gemm_t<1024>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles, b_upper);
+  else if (blockDim.x >= 512) df_gemm_t<512>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles, b_upper);
+  else df_gemm_t<256>(A, ta, B, tb, add, sign, diag, C, m, sym, tiles, b_upper);
 }
 
 // Mixed-precision symmetric eigen-decomposition of the m x m matrix Hm with
@@ -676,14 +680,28 @@ __device__ __noinline__ bool block_cholesky(double* X, int m, int* s_flag, doubl
   return true;
 }
 
-// Phase timestamps of the Williamson kernel (profiling only): thread 0 of
-// each cut's CTA writes the global nanosecond timer at each phase boundary.
+// Phase timestamps of the Williamson kernel (profiling only): the global
+// nanosecond timer at each phase boundary, taken as the latest of the warps'
+// readings (lane 0 of each warp reads the timer and takes the maximum in
+// shared memory before a barrier).  One thread's reading after a barrier
+// does not mark the barrier: the compiler may schedule the timer read
+// before it, so a thread that finished its share of a phase early would
+// stamp the phase's end while other warps are still in it.  Called by every
+// thread of the CTA (block-uniform; it holds a barrier when profiling).
 __device__ __forceinline__ void phase_stamp(const CutArgs& a, int c, int i) {
-  if (a.phase_t && threadIdx.x == 0) {
+  if (!a.phase_t) return;
+  __shared__ unsigned long long s_pt[kCutTimedPhases];
+  if (i == 0) {
+    if (threadIdx.x < kCutTimedPhases) s_pt[threadIdx.x] = 0;
+    __syncthreads();
+  }
+  if ((threadIdx.x & 31) == 0) {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    a.phase_t[(size_t)c * kCutPhases + i] = t;
+    atomicMax(&s_pt[i], t);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) a.phase_t[(size_t)c * kCutPhases + i] = s_pt[i];
 }
 
 // The Williamson decomposition of cut c of `a` by the whole CTA.
@@ -1507,27 +1525,28 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   for (size_t t = tid; t < nn; t += nt) Xacc[t] = df_val(Xacc2[t]);
   __syncthreads();
   phase_stamp(a, c, 9);
-  // 9. S = L [y | x] nu^{-1/2}, nbar = max(0, (nu - 1)/2)
-  for (int pi = 0; pi < k; ++pi) {
-    const double* x = Xacc + (size_t)(2 * pi) * n;
-    const double* y = Xacc + (size_t)(2 * pi + 1) * n;
+  // 9. S = L [y | x] nu^{-1/2}, nbar = max(0, (nu - 1)/2).  The products
+  // R = Xacc L^T (row 2p of R is L x_p, row 2p + 1 is L y_p) run as one
+  // double-float product on the FP32 pipe (the accepted vectors are
+  // double-float values already; L is split), skipping the zero upper
+  // triangle of L: k n^2 FP64 multiply-adds were ~5 ms of one CTA at n = 286.
+  double* R = Gm;  // free after the pairing
+  double* scl = vec;  // nu^{-1/2} per pair
+  for (int pi = tid; pi < k; pi += nt) {
     const double s = MU[pi];  // 1/nu
-    const double nu = 1.0 / s;
-    const double sc = sqrt(s);  // nu^{-1/2}
-    for (int i = tid; i < n; i += nt) {
-      double ly = 0.0, lx = 0.0;
-      for (int j = 0; j <= i; ++j) {
-        const double l = A[(size_t)i * n + j];
-        ly += l * y[j];
-        lx += l * x[j];
+    const double nb = (1.0 / s - 1.0) / 2.0;
+    scl[pi] = sqrt(s);
+    a.nbar[(size_t)c * a.kmax + pi] = nb > 0.0 ? nb : 0.0;
+  }
+  df_gemm(Xacc, false, A, true, nullptr, 1.0, 0.0, R, n, false, dft, true);
+  {
+    double* Sc = a.S + (size_t)c * a.ldS * a.ldS;
+    for (int i = warp; i < n; i += nw)
+      for (int col = lane; col < n; col += 32) {
+        const int pi = col < k ? col : col - k;
+        const int src = col < k ? 2 * pi + 1 : 2 * pi;
+        Sc[(size_t)i * a.ldS + col] = R[(size_t)src * n + i] * scl[pi];
       }
-      a.S[(size_t)c * a.ldS * a.ldS + (size_t)i * a.ldS + pi] = ly * sc;
-      a.S[(size_t)c * a.ldS * a.ldS + (size_t)i * a.ldS + pi + k] = lx * sc;
-    }
-    if (tid == 0) {
-      const double nb = (nu - 1.0) / 2.0;
-      a.nbar[(size_t)c * a.kmax + pi] = nb > 0.0 ? nb : 0.0;
-    }
   }
   __syncthreads();
   phase_stamp(a, c, 10);

@@ -719,6 +719,26 @@ static int convert_many(bsg_handle_t h, const ConvJob* jobs_host, int n_jobs, vo
   return BSG_OK;
 }
 
+// The small device-to-host transfers of the whole-MPS build (cut status,
+// label keys, row counts, flags) written by a kernel into the pinned staging
+// buffer through its device mapping.  Copy-engine copies would queue behind
+// the Gamma downloads of the host-output build: a group's label keys (which
+// its host planning waits for) arrived ~10 ms late there.
+constexpr int kHostCopyJobs = 6;
+struct HostCopyJobs {
+  uint32_t* dst[kHostCopyJobs];  // device addresses of pinned host words
+  const uint32_t* src[kHostCopyJobs];
+  int64_t words[kHostCopyJobs];
+  int n;
+};
+__global__ void host_copy_kernel(const __grid_constant__ HostCopyJobs j) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int q = 0; q < j.n; ++q)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < j.words[q]; i += stride)
+      j.dst[q][i] = j.src[q][i];
+  __threadfence_system();
+}
+
 // Span y of the list is set to its byte value: the 16-byte-aligned body by
 // vector stores (blocks along x stride over it), the unaligned head and tail
 // bytes by the first threads.
@@ -1801,13 +1821,12 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   // tail of the end-to-end time).
   int T1 = 0, T2 = nc;
   if (nc >= 6) {
-    // built-in shares (measured at M=144): right 33 % / left 33 % for the
-    // device-resident build (82.2 -> 80.0 ms against 25 / 33), right 40 % /
-    // left 30 % when Gamma goes to the host (e2e 98.8 -> 91.2 ms against
-    // 25 / 25): the right group's cuts are cheap, so a larger right group
-    // puts more of the build's work (and of the downloads) early
-    const int lp = h->tune[BSG_TUNE_LEFT_PCT] ? h->tune[BSG_TUNE_LEFT_PCT] : gammas_pinned ? 30 : 33;
-    const int rp = h->tune[BSG_TUNE_RIGHT_PCT] ? h->tune[BSG_TUNE_RIGHT_PCT] : gammas_pinned ? 40 : 33;
+    // built-in shares (measured at M=144): right 33 % / left 33 %, for the
+    // device-resident build (82.2 -> 80.0 ms against 25 / 33) and when Gamma
+    // goes to the host (e2e 78.2 -> 76.9 ms against right 40 % / left 30 %,
+    // which led while the left group's factorisation ended ~10 ms later)
+    const int lp = h->tune[BSG_TUNE_LEFT_PCT] ? h->tune[BSG_TUNE_LEFT_PCT] : 33;
+    const int rp = h->tune[BSG_TUNE_RIGHT_PCT] ? h->tune[BSG_TUNE_RIGHT_PCT] : 33;
     T1 = std::max(1, nc * lp / 100);
     T2 = nc - std::max(1, nc * rp / 100);
     if (T2 <= T1) T2 = T1 + 1;  // shares above 100 %: a middle group of one cut
@@ -1880,6 +1899,11 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
   int32_t* hcnt = reinterpret_cast<int32_t*>(hkeys + (size_t)nc * chi);
   int32_t* habove = hcnt + nc;
   int* herr = habove + nc;  // one flag per group
+  // the staging buffer's device address (pinned memory is mapped under
+  // unified addressing; the small transfers below are kernel stores to it)
+  char* hs_dev = nullptr;
+  BSG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&hs_dev), hs, 0));
+  auto to_dev = [&](const void* hp) { return reinterpret_cast<uint32_t*>(hs_dev + (reinterpret_cast<const char*>(hp) - hs)); };
   {
     // empty row: nnz 0, rowfact 1 (and as the FP32 pair (1, 0))
     std::vector<char> e(kMaxNnz * 4 + 64, 0);
@@ -1961,7 +1985,16 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
     if (tl0) BSG_CUDA(cudaEventRecord(tl[g][0], s2));
     if (ng == 3 && g == 1 && h->tune[BSG_TUNE_DP_HOLD]) BSG_CUDA(cudaEventRecord(h->ev[3], s2));
     BSG_TRY(cut_launch_thermal(h, cuts, G.c0, G.c1, s2));
-    BSG_TRY(cut_queue_status(cuts, G.c0, G.c1, hcut, s2));
+    HostCopyJobs hj{};
+    auto add_copy = [&](void* hdst, const void* dsrc, int64_t bytes) {
+      hj.dst[hj.n] = to_dev(hdst);
+      hj.src[hj.n] = reinterpret_cast<const uint32_t*>(dsrc);
+      hj.words[hj.n] = bytes / 4;
+      ++hj.n;
+    };
+    // cut status and Jacobi sweeps (as cut_queue_status)
+    add_copy(hcut + G.c0, cuts.status + G.c0, (int64_t)nc_g * 4);
+    add_copy(hcut + cuts.n_cuts + G.c0, cuts.sweeps + G.c0, (int64_t)nc_g * 4);
     if (nc_g > 0) {
       BSG_PROFILED(h, BSG_K_PREP, s2, (double)nc_g * chi,
                    (lambda_kernel<<<nc_g, 256, 0, s2>>>(res + (size_t)G.c0 * chi, chi, site_tol,
@@ -1970,12 +2003,13 @@ static int build_mps_impl(bsg_handle_t h, const double* sq_cov, int M, int d, in
                    (label_rows_kernel<<<dim3((chi + 127) / 128, nc_g), 128, 0, s2>>>(
                        num + (size_t)G.c0 * chi * (M - 1), (int64_t)chi * (M - 1), M - 1, kept + G.c0,
                        M - 1 - G.c0, 1, chi, cut_table(G.c0), d_err + 4 * g)));
-      BSG_CUDA(cudaMemcpyAsync(hkeys + (size_t)G.c0 * chi, tab.key + (size_t)G.c0 * chi, (size_t)nc_g * chi * 8,
-                               cudaMemcpyDeviceToHost, s2));
-      BSG_CUDA(cudaMemcpyAsync(hcnt + G.c0, kept + G.c0, (size_t)nc_g * 4, cudaMemcpyDeviceToHost, s2));
-      BSG_CUDA(cudaMemcpyAsync(habove + G.c0, d_above + G.c0, (size_t)nc_g * 4, cudaMemcpyDeviceToHost, s2));
+      add_copy(hkeys + (size_t)G.c0 * chi, tab.key + (size_t)G.c0 * chi, (int64_t)nc_g * chi * 8);
+      add_copy(hcnt + G.c0, kept + G.c0, (int64_t)nc_g * 4);
+      add_copy(habove + G.c0, d_above + G.c0, (int64_t)nc_g * 4);
     }
-    BSG_CUDA(cudaMemcpyAsync(herr + g, d_err + 4 * g, 4, cudaMemcpyDeviceToHost, s2));
+    add_copy(herr + g, d_err + 4 * g, 4);
+    host_copy_kernel<<<8, 256, 0, s2>>>(hj);
+    BSG_CUDA(cudaGetLastError());
     BSG_CUDA(cudaEventCreateWithFlags(&ev_keys[g], cudaEventDisableTiming));
     BSG_CUDA(cudaEventRecord(ev_keys[g], s2));
     if (tl0) BSG_CUDA(cudaEventRecord(tl[g][1], s2));

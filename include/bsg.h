@@ -396,9 +396,9 @@ int bsg_potrf_f64(bsg_handle_t h, double* A, int n, int* info, bsg_stream_t stre
                                         build's critical path, then run without the DP's memory traffic
                                         beside them), 0 = it starts with its Sigma (default 0) */
 #define BSG_TUNE_RIGHT_PCT 10        /* pipelined build: percent of the cuts in the right group, 5..60,
-                                        0 = built-in (33; 40 when Gamma goes to the host) */
+                                        0 = built-in (33) */
 #define BSG_TUNE_LEFT_PCT 11         /* pipelined build: percent of the cuts in the left group, 5..60,
-                                        0 = built-in (33; 30 when Gamma goes to the host) */
+                                        0 = built-in (33) */
 #define BSG_TUNE_FACTOR_DUAL 12       /* Williamson launches: 1 = two CTAs of half the threads per SM when two fit
                                         in shared memory (the launches of small eigen-problems), 0 = one CTA of
                                         BSG_TUNE_FACTOR_THREADS (default 0) */

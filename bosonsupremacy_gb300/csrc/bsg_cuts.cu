@@ -121,13 +121,19 @@ __device__ __noinline__ int block_jacobi(T* Hm, int m, int ld, T* QT, int max_sw
         pos[P + q0] = q;
       }
       __syncthreads();
-      // 2 x 2 blocks (m1 <= m2) of the two-sided update, upper triangle of pairs
+      // 2 x 2 blocks (m1 <= m2) of the two-sided update, upper triangle of
+      // pairs.  A pair whose rotation was skipped (c = 1, s = 0) leaves its
+      // rows and columns unchanged (exactly), so a block of two such pairs is
+      // not touched: once only the clustered pairs still rotate, a round
+      // costs their rows and columns only.  The diagonal block of every pair
+      // is written (a skipped pair's negligible h_pq becomes 0).
       for (int m2 = warp; m2 < P; m2 += nw) {
         const int p2 = pos[m2], q2 = pos[P + m2];
         const T c2 = cs[m2], s2 = sn[m2];
         for (int m1 = lane; m1 <= m2; m1 += 32) {
-          const int p1 = pos[m1], q1 = pos[P + m1];
           const T c1 = cs[m1], s1 = sn[m1];
+          if (s1 == T(0) && s2 == T(0) && m1 != m2) continue;
+          const int p1 = pos[m1], q1 = pos[P + m1];
           const T b00 = Hm[(size_t)p1 * ld + p2], b01 = Hm[(size_t)p1 * ld + q2];
           const T b10 = Hm[(size_t)q1 * ld + p2], b11 = Hm[(size_t)q1 * ld + q2];
           const T r00 = c1 * b00 - s1 * b10, r01 = c1 * b01 - s1 * b11;
@@ -153,8 +159,9 @@ __device__ __noinline__ int block_jacobi(T* Hm, int m, int ld, T* QT, int max_sw
         }
       }
       for (int q0 = warp; q0 < P; q0 += nw) {
-        const int p = pos[q0], q = pos[P + q0];
         const T c_ = cs[q0], s_ = sn[q0];
+        if (s_ == T(0)) continue;  // the identity
+        const int p = pos[q0], q = pos[P + q0];
         T* rp = QT + (size_t)p * m;
         T* rq = QT + (size_t)q * m;
         for (int j = lane; j < m; j += 32) {
@@ -427,8 +434,8 @@ __device__ void df_gemm(const double* A, bool ta, const double* B, bool tb, cons
 // eigenvalues (the rest of Hm is overwritten).  s1, s2, s3: m*m doubles of
 // scratch each.  Returns the FP32 sweeps used, or -1 if they did not reach
 // the start tolerance of the refinement.
-__device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* red,
-                            double* cs, double* sn, int* pos, float* jsm, bool q_smem, float2* dft,
+__device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* s1, double* s2, double* s3, double* s4,
+                            double* red, double* cs, double* sn, int* pos, float* jsm, bool q_smem, float2* dft,
                             unsigned long long* sweep_log) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t mm = (size_t)m * m;
@@ -456,7 +463,11 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
     sweep_log[2] = t1 - t32;
   }
-  for (size_t t = tid; t < mm; t += nt) QT[t] = double(Q32[t]);
+  for (size_t t = tid; t < mm; t += nt) {
+    const double q = double(Q32[t]);
+    QT[t] = q;
+    s4[t] = q;  // kept for an FP64 restart
+  }
   __syncthreads();
   double* lam = reinterpret_cast<double*>(cs);  // m doubles (cs and sn are adjacent: 2 kMaxCutModes)
   double anorm = 0.0;
@@ -616,13 +627,29 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     // couples, e.g. the banded M=216 workload's cuts 12 and up) come out of
     // the FP32 sweeps mixed by O(1): either the steps stop converging once
     // delta drops below their gap, or the mixed pair keeps delta above its
-    // gap and stays a cluster (cnum above rounding).  Such a cut restarts from
-    // the identity with FP64 Jacobi sweeps on Hm (still the input matrix),
-    // which resolve any gap above the FP64 rounding of Hm.  (The refined
-    // vectors are no start for it: a refinement that stopped converging has
-    // left them far from orthonormal.)
-    for (int i = warp; i < m; i += nw)
-      for (int j = lane; j < m; j += 32) QT[(size_t)i * m + j] = i == j ? 1.0 : 0.0;
+    // gap and stays a cluster (cnum above rounding).  Such a cut restarts
+    // with FP64 Jacobi sweeps, which resolve any gap above the FP64 rounding
+    // of Hm (still the input matrix), from the FP32 sweeps' eigenvector rows
+    // X (s4) rather than the identity: X is made orthonormal to rounding by
+    // two Newton-Schulz steps X <- (3 I - X X^T) X / 2 (its rows are
+    // orthonormal to FP32 rounding, so each step squares ~1e-7), and the
+    // sweeps run on X Hm X^T, whose off-diagonal is at FP32 rounding outside
+    // the mixed clusters: ~4 sweeps instead of ~16 from the identity.  The
+    // rotations act on X's rows, so QT ends as the eigenvector rows of Hm.
+    // (The refined vectors are no start: a refinement that stopped
+    // converging has left them far from orthonormal.)
+    for (int it = 0; it < 2; ++it) {
+      f64_gemm(s4, false, s4, true, nullptr, -0.5, 1.5, s1, m, true, dft);  // (3 I - X X^T) / 2
+      f64_gemm(s1, false, s4, false, nullptr, 1.0, 0.0, s2, m, false, dft);
+      for (size_t t = tid; t < mm; t += nt) s4[t] = s2[t];
+      __syncthreads();
+    }
+    f64_gemm(Hm, false, s4, true, nullptr, 1.0, 0.0, s2, m, false, dft);  // Hm X^T
+    f64_gemm(s4, false, s2, false, nullptr, 1.0, 0.0, s3, m, true, dft);  // X Hm X^T
+    for (size_t t = tid; t < mm; t += nt) {
+      Hm[t] = s3[t];
+      QT[t] = s4[t];
+    }
     __syncthreads();
     const int sw64 = block_jacobi<double>(Hm, m, m, QT, 60, 1e-26, red, cs, sn, pos);
     if (sweep_log && tid == 0) {
@@ -716,7 +743,8 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   double* H = Gm + nn;   // H (full path) / F and its reflectors (low-rank path) / accepted vectors
   double* X1 = H + nn;   // low-rank path: V_A -> L_A, then K = I - R R^T
   double* X2 = X1 + nn;  // low-rank path: L_A^{-1} C, then eigenvector rows of K
-  // (X2 + nn, X2 + 2 nn: two more n^2 blocks of eigen-solver scratch)
+  // (X2 + nn, X2 + 2 nn: two more n^2 blocks of eigen-solver scratch; X2 + 3 nn:
+  // the FP32 sweeps' eigenvectors, the start of an FP64 restart)
   double* MU = a.mu + (size_t)c * (2 * a.kmax);
   extern __shared__ double sm[];
   double* red = sm;                   // 33
@@ -798,7 +826,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     // eigenvector rows in W
     df_gemm(Gm, true, Gm, false, nullptr, 1.0, 0.0, H, n, true, dft);
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, red, cs, sn, pos, jsm, a.jac_q_smem != 0, dft,
+    sweeps = mixed_jacobi(H, n, W, X1, X2, X2 + nn, X2 + 3 * nn, red, cs, sn, pos, jsm, a.jac_q_smem != 0, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = H[(size_t)i * n + i];
@@ -905,7 +933,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     __syncthreads();
     // Gm is free in this path (G is applied through W = L^{-1}, which the pairing still needs)
     phase_stamp(a, c, 5);
-    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, red, cs, sn, pos, jsm, a.jac_q_smem != 0, dft,
+    sweeps = mixed_jacobi(X1, nA, X2, Gm, X2 + nn, X2 + 2 * nn, X2 + 3 * nn, red, cs, sn, pos, jsm, a.jac_q_smem != 0, dft,
                           a.phase_t ? a.phase_t + (size_t)c * kCutPhases + 11 : nullptr);
     phase_stamp(a, c, 6);
     for (int i = tid; i < n; i += nt) MU[i] = i < nA ? X1[(size_t)i * nA + i] : 1.0;
@@ -1701,10 +1729,14 @@ namespace bsg {
 
 static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// n^2 blocks of FP64 workspace per cut: V / L, L^-1, G, H, X1, X2 and three
+// eigen-solver scratch blocks after X2
+constexpr size_t kCutWsBlocks = 9;
+
 // Bytes of cut workspace for n_cuts cuts of an M-mode state (cut_prepare_at).
 size_t cut_ws_bytes(int M, int L0, int n_cuts, int chi) {
   const int kmax = M - L0, nmax = 2 * kmax;
-  return al256((size_t)8 * nmax * nmax * 8 * n_cuts) + al256((size_t)n_cuts * kmax * 8) +
+  return al256((size_t)kCutWsBlocks * nmax * nmax * 8 * n_cuts) + al256((size_t)n_cuts * kmax * 8) +
          al256((size_t)n_cuts * kmax * chi * 4) + al256((size_t)n_cuts * 8) + al256((size_t)n_cuts * 2 * kmax * 8) +
          al256((size_t)n_cuts * kCutPhases * 8);
 }
@@ -1741,7 +1773,7 @@ int cut_prepare_at(bsg_handle_t h, char* base, const double* sq_cov, int M, int 
   a.d = d;
   a.chi = chi;
   a.err_tol = err_tol;
-  a.ws_stride = (size_t)8 * nmax * nmax;
+  a.ws_stride = (size_t)kCutWsBlocks * nmax * nmax;
   a.S = S;
   a.ldS = 2 * (M - 1);
   a.kmax = kmax;

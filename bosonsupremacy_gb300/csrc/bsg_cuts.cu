@@ -603,7 +603,7 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
           rblk[(size_t)a * p + b2] = a == b2 ? 1.0 : 0.0;
         }
       __syncthreads();
-      if (block_jacobi<double>(sb, p, ldb, rblk, 60, 1e-26, red, sn, sn + kMaxCutModes / 2, pos + 256) < 0) ok = false;
+      if (block_jacobi<double>(sb, p, ldb, rblk, 60, 1e-30, red, sn, sn + kMaxCutModes / 2, pos + 256) < 0) ok = false;
       for (int a = warp; a < p; a += nw) {
         for (int b2 = lane; b2 < p; b2 += 32) s2[(size_t)ord[g0 + a] * m + ord[g0 + b2]] = rblk[(size_t)a * p + b2];
         if (lane == 0) lam[ord[g0 + a]] = sb[(size_t)a * ldb + a];
@@ -651,7 +651,7 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
       QT[t] = s4[t];
     }
     __syncthreads();
-    const int sw64 = block_jacobi<double>(Hm, m, m, QT, 60, 1e-26, red, cs, sn, pos);
+    const int sw64 = block_jacobi<double>(Hm, m, m, QT, 60, 1e-30, red, cs, sn, pos);
     if (sweep_log && tid == 0) {
       sweep_log[0] = (unsigned long long)(sw32 < 0 ? 99 : sw32);
       sweep_log[1] = 100 + (unsigned long long)(sw64 < 0 ? 99 : sw64);  // 100 + FP64 sweeps: the restart
@@ -982,7 +982,8 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
   // dimension (e.g. the nu = 1 vacuum modes) is always completed.  The
   // candidates' squared residuals are tracked in FP32 by subtraction (pivot
   // choice only); the chosen FP64 eigenvector (not its FP32 copy) is cleaned
-  // by one projection against the accepted vectors of the cluster.  The
+  // by one projection against the accepted vectors of the cluster and of the
+  // clusters whose mu is within 1e-4 of it.  The
   // products (projections, G x, norms) run in double-float on the FP32 pipe:
   // the accepted vectors are kept as FP32 pairs and the operator of G x (G,
   // or W = L^{-1} in the low-rank path) is split once; S below reads the
@@ -1139,6 +1140,13 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
     while (ce < n && !(vec2[ce] - vec2[ce - 1] > 1e-9 * fmax(fabs(vec2[ce]), 1e-300))) ce += 2;
     if (ce > n) ce = n;
     const int acc0 = acc, C = ce - cb;
+    // accepted rows of earlier clusters whose mu lies within 1e-4 of this
+    // cluster's: the eigen-solver leaves eigenvectors of such close
+    // eigenvalues mixed by (its residual) / gap, ~1e-7 at gaps just above the
+    // clustering threshold, so the new x are projected against them too
+    // (accepted row r belongs to the cluster of sorted candidate r)
+    int an = acc0;
+    while (an > 0 && vec2[cb] - vec2[an - 1] <= 1e-4 * fabs(vec2[cb])) --an;
     tp = pstamp();
     // FP32 copies of the cluster's candidates and their squared norms
     for (int r = warp; r < C; r += nw) {
@@ -1225,8 +1233,9 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
         const float2* xr2 = Xacc2 + (size_t)(acc + 2 * min(2, nb - 1)) * n;
         const float2* xr3 = Xacc2 + (size_t)(acc + 2 * min(3, nb - 1)) * n;
         // 3. project the block against the accepted vectors of the cluster
-        if (acc > acc0) {
-          for (int av = acc0 + warp; av < acc; av += nw) {
+        // and of the clusters within 1e-4 below it (rows an .. acc0)
+        if (acc > an) {
+          for (int av = an + warp; av < acc; av += nw) {
             float ss[4] = {0.f, 0.f, 0.f, 0.f}, tt[4] = {0.f, 0.f, 0.f, 0.f};
             const float2* ra = Xacc2 + (size_t)av * n;
 #pragma unroll 3
@@ -1241,20 +1250,20 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
             for (int q = 0; q < 4; ++q) {
               if (q >= nb) break;
               df_warp_sum(ss[q], tt[q]);
-              if (lane == 0) dotsb[(size_t)(av - acc0) * 4 + q] = df_norm(-ss[q], -tt[q]);
+              if (lane == 0) dotsb[(size_t)(av - an) * 4 + q] = df_norm(-ss[q], -tt[q]);
             }
           }
           __syncthreads();
-          const int len = (acc - acc0 + segs - 1) / segs;
+          const int len = (acc - an + segs - 1) / segs;
           for (int u = tid; u < n * segs; u += nt) {
             const int i = segs == 1 ? u : my_j, g = segs == 1 ? 0 : my_g;
-            const int b0 = acc0 + g * len, b1 = min(acc, b0 + len);
+            const int b0 = an + g * len, b1 = min(acc, b0 + len);
             float ss[4] = {0.f, 0.f, 0.f, 0.f}, tt[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
             for (int av = b0; av < b1; ++av) {
               const float2 r = Xacc2[(size_t)av * n + i];
-              const float4 d01 = *reinterpret_cast<const float4*>(dotsb + (size_t)(av - acc0) * 4);
-              const float4 d23 = *reinterpret_cast<const float4*>(dotsb + (size_t)(av - acc0) * 4 + 2);
+              const float4 d01 = *reinterpret_cast<const float4*>(dotsb + (size_t)(av - an) * 4);
+              const float4 d23 = *reinterpret_cast<const float4*>(dotsb + (size_t)(av - an) * 4 + 2);
               df_mac(ss[0], tt[0], make_float2(d01.x, d01.y), r);
               df_mac(ss[1], tt[1], make_float2(d01.z, d01.w), r);
               df_mac(ss[2], tt[2], make_float2(d23.x, d23.y), r);
@@ -1484,7 +1493,7 @@ __device__ __forceinline__ void williamson_cut(const CutArgs& a, const int c) {
       // largest of the cluster, so one pass keeps orthogonality at rounding)
       for (int i = tid; i < n; i += nt) x[i] = df_split(EV[(size_t)order[cb + best] * n + i]);
       __syncthreads();
-      project_out(x, acc0, acc);
+      project_out(x, an, acc);
       double nx;
       const float2 ix = norm_inv(x, &nx);
       for (int i = tid; i < n; i += nt) x[i] = df_mul(x[i], ix);

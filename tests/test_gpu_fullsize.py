@@ -174,3 +174,36 @@ def test_williamson_symplectics_at_full_size(full_builds, cut):
     pair_err = np.abs(dg[k:] - nu).max() / nu.max()
     assert pair_err <= 1e-9, pair_err
     assert nu.min() >= 1.0 - 1e-9, nu.min()
+
+
+@pytest.mark.parametrize("cut", [20, 31, 107, 160])
+def test_williamson_restart_symplectics_M216(cuda, golden, cut):
+    """Cuts of the banded M=216 workload whose refinement does not settle
+    (near-vacuum modes ~1e-7 of the norm apart, mixed by the FP32 sweeps):
+    they take the FP64 Jacobi restart from the FP32 sweeps' eigenvectors
+    (cuts 20 and 31: the low-rank core; 107 and 160: the full matrix).  Their
+    symplectics satisfy S Omega S^T = Omega and S^-1 V S^-T = diag(nu, nu)
+    with nu >= 1 as the refined cuts of the M=144 build do."""
+    from bosonsupremacy_gb300 import ops, synthetic
+    cfg = synthetic.LARGEST
+    sq = golden("largest_M216.npz")["sq_cov"]
+    M = cfg.M
+    L = cut + 1
+    k = M - L
+    _, _, S_all, _ = ops.cut_spectra(sq, cfg.d, cfg.chi, L0=L, n_cuts=1)
+    S = S_all[0, : 2 * k, : 2 * k].cpu().numpy()
+    sel = np.concatenate([np.arange(L, M), np.arange(L, M) + M])
+    V = sq[np.ix_(sel, sel)]
+    om = np.block([[np.zeros((k, k)), np.eye(k)], [-np.eye(k), np.zeros((k, k))]])
+    scale = max(1.0, np.abs(S).max() ** 2)
+    sym_err = np.abs(S @ om @ S.T - om).max() / scale
+    assert sym_err <= 1e-10, sym_err
+    Si = -om @ S.T @ om
+    D = Si @ V @ Si.T
+    dg = np.diag(D)
+    nu = dg[:k]
+    off = np.abs(D - np.diag(dg)) / np.sqrt(np.outer(np.abs(dg), np.abs(dg)))
+    assert off.max() <= 1e-9, off.max()
+    pair_err = np.abs(dg[k:] - nu).max() / nu.max()
+    assert pair_err <= 1e-9, pair_err
+    assert nu.min() >= 1.0 - 1e-9, nu.min()

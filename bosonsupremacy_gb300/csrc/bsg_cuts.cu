@@ -638,9 +638,11 @@ __device__ __noinline__ int mixed_jacobi(double* Hm, int m, double* QT, double* 
     // rotations act on X's rows, so QT ends as the eigenvector rows of Hm.
     // (The refined vectors are no start: a refinement that stopped
     // converging has left them far from orthonormal.)
+    // (the steps in double-float: orthonormal to ~1e-14, far below the
+    // pairing's tolerances; X Hm X^T below stays FP64 for the small nbar)
     for (int it = 0; it < 2; ++it) {
-      f64_gemm(s4, false, s4, true, nullptr, -0.5, 1.5, s1, m, true, dft);  // (3 I - X X^T) / 2
-      f64_gemm(s1, false, s4, false, nullptr, 1.0, 0.0, s2, m, false, dft);
+      df_gemm(s4, false, s4, true, nullptr, -0.5, 1.5, s1, m, true, dft);  // (3 I - X X^T) / 2
+      df_gemm(s1, false, s4, false, nullptr, 1.0, 0.0, s2, m, false, dft);
       for (size_t t = tid; t < mm; t += nt) s4[t] = s2[t];
       __syncthreads();
     }
